@@ -1,0 +1,182 @@
+/*
+ * tbgpu.h -- C-ABI of the GB300 k-mesh engine for Rustb tight-binding models.
+ *
+ * Every entry point replaces one method on Rustb's k-mesh hot path.  The
+ * reference interface each one stands in for is cited beside it (paths are
+ * relative to the Rustb crate root).  Layout conventions follow Rustb/ndarray:
+ *
+ *   - all arrays are C (row-major) contiguous;
+ *   - a complex number is two doubles {re, im} (binary layout of
+ *     num_complex::Complex<f64>);
+ *   - k-points are fractional coordinates, shape (nk, dim);
+ *   - hamR is int64 (isize on 64-bit targets), shape (nR, dim);
+ *   - ham is complex, shape (nR, nsta, nsta), ham[r][i][j] = <i,0|H|j,R_r>;
+ *   - orb is (norb, dim) fractional, lat is (dim, dim) with lattice vectors
+ *     as rows (src/model.rs:150-158).
+ *
+ * All pointers are HOST pointers.  Outputs are caller-allocated.  Each call is
+ * synchronous: on return the outputs are written.  Calls on different models
+ * (or the same model) from different host threads are safe.
+ *
+ * Every function returns a status (enum tbg_status).  On failure the message
+ * of the most recent error of the calling thread is available through
+ * tbg_last_error().
+ */
+#ifndef TBGPU_H
+#define TBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Codes 1..9 map 1:1 onto TbError variants (src/error.rs). */
+enum tbg_status {
+    TBG_OK = 0,
+    TBG_E_KVECTOR_LENGTH = 1,             /* TbError::KVectorLengthMismatch */
+    TBG_E_DIMENSION_MISMATCH = 2,         /* TbError::DimensionMismatch */
+    TBG_E_INVALID_RESPONSE_PARAMETER = 3, /* TbError::InvalidResponseParameter */
+    TBG_E_SPIN_NOT_ALLOWED = 4,           /* TbError::SpinNotAllowed */
+    TBG_E_INVALID_KMESH = 5,              /* TbError::InvalidKmeshDimensions */
+    TBG_E_LINALG = 6,                     /* TbError::Linalg (singular lattice) */
+    TBG_E_INVALID_DIMENSION = 7,          /* TbError::InvalidDimension */
+    TBG_E_INVALID_MODEL = 8,              /* TbError::InvalidModelInvariant */
+    TBG_E_INVALID_ARGUMENT = 9,           /* conditions on which Rustb panics */
+    TBG_E_CUDA = 20,                      /* CUDA runtime failure */
+    TBG_E_NOCONV = 21,                    /* eigensolver did not converge */
+    TBG_E_TIMEOUT = 22,                   /* a bounded device wait ran out */
+    TBG_E_OOM = 23,                       /* device allocation failed */
+    TBG_E_UNSUPPORTED = 24                /* size or option not supported */
+};
+
+/* Gauge (src/model.rs:449-452). */
+enum tbg_gauge { TBG_GAUGE_LATTICE = 0, TBG_GAUGE_ATOM = 1 };
+
+/* Spin-current polarisation (src/model.rs:470-474); -1 = None (charge current). */
+enum tbg_spin { TBG_SPIN_NONE = -1, TBG_SPIN_X = 0, TBG_SPIN_Y = 1, TBG_SPIN_Z = 2 };
+
+/* Arithmetic of tbg_hall_conductivity / tbg_berry_curvature. */
+enum tbg_precision {
+    TBG_PREC_FP64 = 0,  /* plain: FP64 end to end (the drop-in) */
+    TBG_PREC_MIXED = 1  /* FP32 eigensolve + FP64 eigenpair refinement */
+};
+
+typedef struct tbg_model tbg_model;
+
+/* Per-call report filled by tbg_hall_conductivity (may be NULL). */
+typedef struct tbg_report {
+    int64_t nk;              /* k-points processed */
+    int64_t nsta;            /* bands per k-point */
+    int32_t precision;       /* tbg_precision used */
+    int32_t fourier_mode;    /* 0 = direct phase x hop contraction, 1 = separable mesh transform */
+    int64_t kernel_launches; /* device kernels launched by the call */
+    double device_ms;        /* device time of the call (CUDA events) */
+    double eig_ms;           /* device time spent in the eigensolver kernels */
+    int64_t refine_clusters; /* near-degenerate clusters handled by the refinement */
+} tbg_report;
+
+/* ---------------------------------------------------------------- model --- */
+
+/* Upload a model and keep it resident on the device.
+ * Replaces: the Model<SPIN,DIM,R> value every hot-path method borrows
+ * (src/model.rs:150-158); validation mirrors Model::validate (src/model.rs:564).
+ * spin != 0 means nsta = 2*norb (spinful basis [up 0..norb, down norb..2norb]). */
+int tbg_model_create(int dim, int spin, int64_t norb, int64_t nR,
+                     const int64_t* hamR, const double* ham,
+                     const double* orb, const double* lat, tbg_model** out);
+
+/* Attach a position matrix (HasRMatrix models): rmatrix has shape
+ * (n_rmat, dim, nsta, nsta) complex, Cartesian; its rows pair with the first
+ * n_rmat rows of hamR.  Replaces: RMatrixData / HasRMatrix (src/model.rs:18-76)
+ * as read by gen_v (src/velocity.rs:377-401) and gen_v_projected
+ * (src/velocity.rs:627-668). */
+int tbg_model_set_rmatrix(tbg_model* m, int64_t n_rmat, const double* rmatrix);
+
+int tbg_model_destroy(tbg_model* m);
+
+int tbg_model_info(const tbg_model* m, int* dim, int* spin, int64_t* norb,
+                   int64_t* nsta, int64_t* nR);
+
+/* ------------------------------------------------------- per-k primitives --- */
+
+/* H(k) for nk k-points -> H_out (nk, nsta, nsta) complex.
+ * Replaces: Model::gen_ham (src/model_physics.rs:43-148). */
+int tbg_gen_ham(const tbg_model* m, int64_t nk, const double* k, int gauge,
+                double* H_out);
+
+/* Velocity along every Cartesian direction -> V_out (nk, dim, nsta, nsta),
+ * H_out (nk, nsta, nsta) (H_out may be NULL).
+ * Replaces: Velocity::gen_v (src/velocity.rs:214-441). */
+int tbg_gen_v(const tbg_model* m, int64_t nk, const double* k, int gauge,
+              double* V_out, double* H_out);
+
+/* Direction-projected velocity: dirs (n_proj, dim) -> V_out (nk, n_proj, nsta,
+ * nsta), H_out (nk, nsta, nsta) (may be NULL).
+ * Replaces: Model::gen_v_projected (src/velocity.rs:470-731). */
+int tbg_gen_v_projected(const tbg_model* m, int64_t nk, const double* k,
+                        int gauge, int64_t n_proj, const double* dirs,
+                        double* V_out, double* H_out);
+
+/* Band energies (ascending) -> E_out (nk, nsta).
+ * Replaces: Solve::solve_band_onek / solve_band_all / solve_band_all_parallel
+ * (src/solve_ham.rs:52-107; LAPACK zheev via eigvalsh_v,
+ * src/ndarray_lapack.rs:412-448). */
+int tbg_solve_band(const tbg_model* m, int64_t nk, const double* k,
+                   double* E_out);
+
+/* Energies and eigenvectors -> E_out (nk, nsta), U_out (nk, nsta, nsta).
+ * evec_rows != 0: U_out[k][n][:] is the n-th eigenvector (the layout of
+ * Solve::solve_onek / solve_all_parallel, src/solve_ham.rs:110-184);
+ * evec_rows == 0: eigenvectors in columns.  The phase of each eigenvector is
+ * arbitrary, as with LAPACK. */
+int tbg_solve(const tbg_model* m, int64_t nk, const double* k, double* E_out,
+              double* U_out, int evec_rows);
+
+/* ----------------------------------------------------------- response --- */
+
+/* Band-resolved Berry curvature at nk k-points: dirs2 (2, dim) rows = the two
+ * tensor indices, spin = tbg_spin, eta >= 0.  Omega_out, E_out (nk, nsta).
+ * Replaces: BerryCurvature::berry_curvature_at (src/response/traits.rs:60-78,
+ * kernel berry_curvature_at_impl traits.rs:160-200). */
+int tbg_berry_curvature(const tbg_model* m, int64_t nk, const double* k,
+                        const double* dirs2, int spin, double eta,
+                        int precision, double* Omega_out, double* E_out);
+
+/* Occupation-weighted Berry curvature sum_n Omega_n f(E_n, mu) per k-point.
+ * T in kelvin (0 = step function with f(mu) = 1/2).
+ * Replaces: BerryCurvature::occupied_berry_curvature_on
+ * (src/response/traits.rs:104-150). */
+int tbg_occupied_berry_curvature(const tbg_model* m, int64_t nk,
+                                 const double* k, const double* dirs2, int spin,
+                                 double eta, double T, double mu, int precision,
+                                 double* out);
+
+/* Anomalous / spin Hall conductivity, Direct integration over the uniform
+ * mesh kmesh[dim]: sigma_out[j] = sum_k sum_n Omega_n f(E_n, mu_j) / nk / det(lat).
+ * Replaces: Model::hall_conductivity with Integration::Direct
+ * (src/response/linear/mod.rs:160-225). */
+int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh,
+                          const double* dirs2, int64_t nmu, const double* mu,
+                          double T, double eta, int spin, int precision,
+                          double* sigma_out, tbg_report* report);
+
+/* ------------------------------------------------------------- utility --- */
+
+/* Copy the calling thread's last error message into buf (always NUL-terminated).
+ * Returns the status of that error. */
+int tbg_last_error(char* buf, size_t len);
+
+/* Library version string, e.g. "tbgpu 0.1.0 sm_103a". */
+const char* tbg_version(void);
+
+/* Number of tbgpu kernels launched by the calling thread since the last reset
+ * (reset != 0 zeroes the counter after reading). */
+int64_t tbg_kernel_launch_count(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TBGPU_H */

@@ -1,0 +1,312 @@
+"""CPU oracle for the Rustb k-mesh hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module restates, in numpy, the algorithm of Rustb's k-mesh path so that
+the GPU library can be checked against it.  It is imported only by the tests,
+by ``__graft_entry__.smoke()`` and by ``bench.py``'s CPU-baseline leg, always
+as the checker; the product (``rustb_gb300``) never calls it.
+
+Parity anchor.  Rustb is Rust and cannot be built here (no cargo/rustc), so
+the oracle is pinned against the known answers held by Rustb's own tests
+(``src/lib.rs``: ``test_gen_v`` golden velocity matrices and Gamma/K
+eigenvalues, ``evec_transform_sanity``, ``Haldan_model`` C = 1,
+``conductivity_test`` Kubo vs Wilson loop, ``hall_conductivity_ec_tr``
+antisymmetry, ``hall_conductivity_ec_3d_qwz`` plateau); see
+``tests/test_oracle_golden.py``.  The eigensolver is LAPACK ``zheev`` (scipy's
+bundled OpenBLAS), the routine Rustb's openblas backend reaches through
+ndarray-linalg ``Eigh`` (``src/response/traits.rs:168``).
+
+Functions cite the reference file:line they follow.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+from scipy.linalg import lapack
+
+TWO_PI = 2.0 * np.pi
+BOLTZMANN_CONSTANT_EV_PER_K = 8.617333262145e-5  # src/thermodynamics.rs:10
+
+
+# --------------------------------------------------------------------------
+# k-mesh and phases
+# --------------------------------------------------------------------------
+
+def gen_kmesh(kmesh) -> np.ndarray:
+    """``gen_kmesh`` (src/kpoints.rs:49-87): k = (i/N1, j/N2, l/N3) with the
+    first dimension outermost; row index = i*N2*N3 + j*N3 + l."""
+    kmesh = [int(n) for n in kmesh]
+    axes = [np.arange(n, dtype=np.float64) / float(n) for n in kmesh]
+    grids = np.meshgrid(*axes, indexing="ij")
+    return np.stack([g.reshape(-1) for g in grids], axis=1)
+
+
+def phases(k: np.ndarray, hamR: np.ndarray) -> np.ndarray:
+    """exp(i 2 pi k.R) for every R (src/model_physics.rs:58-90)."""
+    kr = np.atleast_2d(k) @ hamR.T.astype(np.float64)
+    return np.exp(1j * TWO_PI * kr)
+
+
+def orb_phase(k: np.ndarray, orb_sta: np.ndarray) -> np.ndarray:
+    """exp(i 2 pi k.tau) per state (src/model_physics.rs:103-128)."""
+    return np.exp(1j * TWO_PI * (np.atleast_2d(k) @ orb_sta.T))
+
+
+def orb_states(model) -> np.ndarray:
+    """Orbital positions per state; spinful duplicates tau
+    (src/model_physics.rs:131-137, src/velocity.rs:546-550)."""
+    return np.concatenate([model.orb, model.orb], axis=0) if model.spin else model.orb
+
+
+# --------------------------------------------------------------------------
+# H(k) and velocity
+# --------------------------------------------------------------------------
+
+def gen_ham(model, k, gauge: int = 1) -> np.ndarray:
+    """``gen_ham`` (src/model_physics.rs:43-148) for one k-point.
+    gauge: 0 = Lattice, 1 = Atom."""
+    return gen_ham_batch(model, np.atleast_2d(k), gauge)[0]
+
+
+def gen_ham_batch(model, k: np.ndarray, gauge: int = 1) -> np.ndarray:
+    """Batched ``gen_ham``: H_lat(k) = sum_R ham[R] e^{2 pi i k.R}
+    (zaxpy loop, model_physics.rs:92-96), then for the Atom gauge
+    H[m,n] *= conj(phi_m) phi_n (model_physics.rs:138-146)."""
+    nsta = model.nsta
+    u = phases(k, model.hamR)                                   # (nk, nR)
+    H = (u @ model.ham.reshape(model.nR, nsta * nsta)).reshape(-1, nsta, nsta)
+    if gauge == 1:
+        phi = orb_phase(k, orb_states(model))                   # (nk, nsta)
+        H = H * np.conj(phi)[:, :, None] * phi[:, None, :]
+    return H
+
+
+def gen_v_projected(model, k, gauge: int, directions) -> tuple[np.ndarray, np.ndarray]:
+    """``gen_v_projected`` (src/velocity.rs:470-731) for one k-point.
+
+    v_p = sum_R i (w_p . R_cart) ham[R] e^{2 pi i k.R}             (587-599)
+    Atom gauge: v_p[m,n] = (v_p[m,n] + i (w_p.tau_n - w_p.tau_m) H_lat[m,n])
+                           * conj(phi_m) phi_n                       (602-610)
+    and H -> conj(phi_m) H phi_n                                    (616-622).
+    Returns (v_proj (n_proj, nsta, nsta), H).
+    """
+    V, H = gen_v_projected_batch(model, np.atleast_2d(k), gauge, directions)
+    return V[0], H[0]
+
+
+def gen_v_projected_batch(model, k: np.ndarray, gauge: int, directions):
+    directions = np.atleast_2d(np.asarray(directions, dtype=np.float64))
+    nsta = model.nsta
+    nk = k.shape[0]
+    u = phases(k, model.hamR)                                   # (nk, nR)
+    hop = model.ham.reshape(model.nR, nsta * nsta)
+    R_cart = model.hamR.astype(np.float64) @ model.lat          # velocity.rs:530-531
+    H = (u @ hop).reshape(nk, nsta, nsta)
+    V = np.empty((nk, directions.shape[0], nsta, nsta), dtype=np.complex128)
+    for p, w in enumerate(directions):
+        coef = 1j * (R_cart @ w)                                # i (w . R_cart)
+        V[:, p] = ((u * coef[None, :]) @ hop).reshape(nk, nsta, nsta)
+    if gauge == 1:
+        orb_sta = orb_states(model)
+        phi = orb_phase(k, orb_sta)                             # (nk, nsta)
+        tau_proj = directions @ (orb_sta @ model.lat).T         # (n_proj, nsta)
+        g = np.conj(phi)[:, :, None] * phi[:, None, :]          # (nk, m, n)
+        for p in range(directions.shape[0]):
+            diff = tau_proj[p][None, :] - tau_proj[p][:, None]  # [m,n] = tau_n - tau_m
+            V[:, p] = (V[:, p] + 1j * diff[None] * H) * g
+        H = H * g
+    if getattr(model, "rmatrix", None) is not None:
+        V = V + _rmatrix_term(model, k, gauge, directions, H, u)
+    return V, H
+
+
+def _rmatrix_term(model, k, gauge, directions, Hk, u):
+    """i [H, A_w] position-matrix term (src/velocity.rs:627-668): A_w is the
+    direction-weighted Fourier sum of rmatrix over its first n_rmat R rows; in
+    the Atom gauge it is gauge-transformed and its diagonal zeroed."""
+    rm = model.rmatrix                                          # (n_rmat, dim, nsta, nsta)
+    n_rmat = rm.shape[0]
+    nsta = model.nsta
+    nk = k.shape[0]
+    out = np.zeros((nk, directions.shape[0], nsta, nsta), dtype=np.complex128)
+    rk = np.einsum("kr,rdij->kdij", u[:, :n_rmat], rm)          # (nk, dim, nsta, nsta)
+    if gauge == 1:
+        phi = orb_phase(k, orb_states(model))
+        g = np.conj(phi)[:, :, None] * phi[:, None, :]
+    for p, w in enumerate(directions):
+        a = np.einsum("d,kdij->kij", w, rk)
+        if gauge == 1:
+            a = a * g
+            idx = np.arange(nsta)
+            a[:, idx, idx] = 0.0
+        out[:, p] = 1j * (Hk @ a - a @ Hk)
+    return out
+
+
+def gen_v(model, k, gauge: int = 1):
+    """``gen_v`` (src/velocity.rs:236-441): the projected velocity with the
+    Cartesian unit vectors as directions."""
+    return gen_v_projected(model, k, gauge, np.eye(model.dim))
+
+
+# --------------------------------------------------------------------------
+# eigensolver
+# --------------------------------------------------------------------------
+
+def eigh(H: np.ndarray):
+    """LAPACK zheev with JOBZ='V' (src/response/traits.rs:168 via ndarray-linalg,
+    src/ndarray_lapack.rs:412-448).  Returns ascending E and eigenvectors in the
+    COLUMNS of W with H W = W diag(E)."""
+    w, v, info = lapack.zheev(np.asarray(H, dtype=np.complex128), compute_v=1, lower=1)
+    if info != 0:
+        raise RuntimeError(f"zheev info={info}")  # ndarray_lapack.rs:446 panics
+    return w, v
+
+
+def eigvalsh(H: np.ndarray) -> np.ndarray:
+    w, _, info = lapack.zheev(np.asarray(H, dtype=np.complex128), compute_v=0, lower=0)
+    if info != 0:
+        raise RuntimeError(f"zheev info={info}")
+    return w
+
+
+def solve_band_all(model, k: np.ndarray) -> np.ndarray:
+    """``solve_band_all_parallel`` (src/solve_ham.rs:94-107)."""
+    Hs = gen_ham_batch(model, np.atleast_2d(k), 1)
+    return np.stack([eigvalsh(H) for H in Hs])
+
+
+def solve_all(model, k: np.ndarray):
+    """``solve_all_parallel`` (src/solve_ham.rs:168-184); eigenvectors as ROWS
+    (solve_onek conj-transposes, solve_ham.rs:122-128)."""
+    Hs = gen_ham_batch(model, np.atleast_2d(k), 1)
+    E, U = [], []
+    for H in Hs:
+        w, v = eigh(H)
+        E.append(w)
+        U.append(v.T)  # row n = eigenvector n
+    return np.stack(E), np.stack(U)
+
+
+# --------------------------------------------------------------------------
+# Berry curvature and Hall conductivity
+# --------------------------------------------------------------------------
+
+def spin_matrix(norb: int, spin: int) -> np.ndarray:
+    """``build_spin_matrix`` (src/response/helpers.rs:11-40): sigma (x) I / 2."""
+    nsta = 2 * norb
+    m = np.zeros((nsta, nsta), dtype=np.complex128)
+    i = np.arange(norb)
+    if spin == 0:
+        m[i, i + norb] = 0.5
+        m[i + norb, i] = 0.5
+    elif spin == 1:
+        m[i, i + norb] = -0.5j
+        m[i + norb, i] = 0.5j
+    elif spin == 2:
+        m[i, i] = 0.5
+        m[i + norb, i + norb] = -0.5
+    else:
+        m = np.eye(nsta, dtype=np.complex128)
+    return m
+
+
+def berry_curvature_at(model, k, directions, spin: int = -1, eta: float = 1e-3):
+    """``berry_curvature_at_impl`` (src/response/traits.rs:160-200).
+
+    (V, H) = gen_v_projected(k, Atom, direction)                      :166
+    (E, U) = eigh(H)                                                  :168
+    J = 1/2 {S, V_0} if spin else V_0                                 :170-175
+    Jb = U^T J U*, Vb = U^T V_1 U* (eigenvectors of H in columns of U*) :177-180
+    K = Jb o Vb^T;  Omega_n = sum_{m != n} -2 Im K_nm / ((E_n-E_m)^2 + eta^2)  :181-195
+    Returns (Omega, E).
+    """
+    V, H = gen_v_projected(model, np.asarray(k, dtype=np.float64), 1, directions)
+    E, W = eigh(H)
+    J = V[0]
+    if model.spin and spin is not None and spin >= 0:
+        S = spin_matrix(model.norb, spin)
+        J = 0.5 * (S @ J + J @ S)                                # math.rs anti_comm
+    Jb = W.conj().T @ J @ W
+    Vb = W.conj().T @ V[1] @ W
+    K = Jb * Vb.T
+    dE = E[:, None] - E[None, :]
+    den = dE * dE + eta * eta
+    term = -2.0 * K.imag / den
+    np.fill_diagonal(term, 0.0)
+    return term.sum(axis=1), E
+
+
+def fermi(energy, mu: float, width: float):
+    """``fermi_from_width`` (src/thermodynamics.rs:100-118): step with 1/2 at
+    E == mu when width == 0; else 1/(1+e^x) clamped at |x| > 50."""
+    energy = np.asarray(energy, dtype=np.float64)
+    if width == 0.0:
+        return np.where(energy < mu, 1.0, np.where(energy > mu, 0.0, 0.5))
+    x = (energy - mu) / width
+    with np.errstate(over="ignore"):
+        f = 1.0 / (1.0 + np.exp(np.clip(x, -50.0, 50.0)))
+    f = np.where(x > 50.0, 0.0, np.where(x < -50.0, 1.0, f))
+    return f
+
+
+def occupation_width(T: float) -> float:
+    """``parameters_occupation`` (src/response/config.rs:173-181)."""
+    return 0.0 if T <= 0.0 else T * BOLTZMANN_CONSTANT_EV_PER_K
+
+
+def berry_on(model, k_list, directions, spin=-1, eta=1e-3):
+    """Band-resolved Omega and E on a k-list (berry_curvature_at per k)."""
+    k_list = np.atleast_2d(np.asarray(k_list, dtype=np.float64))
+    Om = np.empty((k_list.shape[0], model.nsta))
+    E = np.empty_like(Om)
+    for i, k in enumerate(k_list):
+        Om[i], E[i] = berry_curvature_at(model, k, directions, spin, eta)
+    return Om, E
+
+
+def occupied_berry_curvature_on(model, k_list, directions, mu: float, T=0.0, spin=-1, eta=1e-3):
+    """``occupied_berry_curvature_on`` (src/response/traits.rs:104-150)."""
+    Om, E = berry_on(model, k_list, directions, spin, eta)
+    return (Om * fermi(E, mu, occupation_width(T))).sum(axis=1)
+
+
+def hall_from_bands(Om, E, mu_list, T, nk, det):
+    """Direct-integration reduction (src/response/linear/mod.rs:204-223):
+    sigma(mu) = sum_k sum_n Omega_n f(E_n, mu) / nk / det(lat)."""
+    width = occupation_width(T)
+    out = np.empty(len(mu_list))
+    for j, mu in enumerate(mu_list):
+        per_k = (Om * fermi(E, float(mu), width)).sum(axis=1)
+        out[j] = per_k.sum() / nk / det
+    return out
+
+
+def hall_conductivity(model, kmesh, directions, mu_list, T=0.0, eta=1e-3, spin=-1):
+    """``hall_conductivity`` with Integration::Direct
+    (src/response/linear/mod.rs:160-225); det is the signed lattice
+    determinant (:188)."""
+    k = gen_kmesh(kmesh)
+    Om, E = berry_on(model, k, directions, spin, eta)
+    det = float(np.linalg.det(model.lat))
+    return hall_from_bands(Om, E, np.atleast_1d(mu_list), T, k.shape[0], det)
+
+
+# --------------------------------------------------------------------------
+# Wilson loop (used only to pin the Kubo formula, src/geometry.rs:156-215)
+# --------------------------------------------------------------------------
+
+def berry_loop(model, k_loop, occ):
+    """Berry phase of the occupied bands ``occ`` around a closed k-loop
+    (``berry_loop``, src/geometry.rs:156-215): -Im log det prod of overlap
+    matrices in the Atom gauge, with the loop's last point identified with its
+    first."""
+    k_loop = np.atleast_2d(np.asarray(k_loop, dtype=np.float64))
+    vecs = []
+    for k in k_loop[:-1]:
+        _, W = eigh(gen_ham(model, k, 1))
+        vecs.append(W[:, occ])
+    vecs.append(vecs[0])
+    prod = np.eye(len(occ), dtype=np.complex128)
+    for a, b in zip(vecs[:-1], vecs[1:]):
+        prod = prod @ (a.conj().T @ b)
+    return -np.angle(np.linalg.det(prod))

@@ -1,0 +1,691 @@
+// C-ABI entry points of libtbgpu (include/tbgpu.h).
+//
+// Each call runs on its own CUDA stream, allocates its device workspace from
+// the stream-ordered pool, processes the k-points in chunks sized to a device
+// memory budget, and synchronises before returning.  Validation mirrors the
+// reference's error behaviour (src/response/config.rs:183-303,
+// src/response/traits.rs:60-150, src/response/linear/mod.rs:160-188).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tbgpu_internal.cuh"
+
+struct tbg_model {
+    tbg::ModelDev d;
+};
+
+namespace tbg {
+
+static thread_local std::string g_err;
+static thread_local int g_code = 0;
+static thread_local int64_t g_launches = 0;
+
+int set_error(int code, const std::string& msg) {
+    g_code = code;
+    g_err = msg;
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char* where) {
+    const int code = (e == cudaErrorMemoryAllocation) ? TBG_E_OOM : TBG_E_CUDA;
+    cudaGetLastError();  // clear a non-sticky error
+    return set_error(code, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+void count_launch(int n) { g_launches += n; }
+
+int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* A, int64_t sA, const zc* B,
+                  int64_t sB, zc* C, int64_t sC);
+int berry_from_bands(cudaStream_t st, int N, int64_t batch, const zc* Bx, const zc* By, int64_t ldB,
+                     const double* E, double eta, double* Omega);
+int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
+                    size_t work_bytes, int* status_d);
+
+namespace {
+
+std::once_flag g_pool_once;
+
+void configure_pool() {
+    std::call_once(g_pool_once, [] {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+}
+
+// Per-call context: stream + stream-ordered allocations released at the end.
+struct Ctx {
+    cudaStream_t st = nullptr;
+    std::vector<void*> bufs;
+    int rc = TBG_OK;
+    Ctx() {
+        configure_pool();
+        cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) rc = cuda_error(e, "cudaStreamCreate");
+    }
+    template <typename T>
+    T* alloc(size_t count) {
+        if (rc != TBG_OK) return nullptr;
+        void* p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), st);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "cudaMallocAsync");
+            return nullptr;
+        }
+        bufs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    int sync(const char* where) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess && rc == TBG_OK) rc = cuda_error(e, where);
+        return rc;
+    }
+    ~Ctx() {
+        if (st) {
+            for (void* p : bufs) cudaFreeAsync(p, st);
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    }
+};
+
+int64_t chunk_budget_bytes() {
+    const char* s = std::getenv("TBG_CHUNK_BYTES");
+    if (s) {
+        const long long v = std::atoll(s);
+        if (v > 0) return v;
+    }
+    return 6LL << 30;
+}
+
+int64_t choose_chunk(int64_t nk, int64_t per_k_bytes) {
+    int64_t c = std::max<int64_t>(1, chunk_budget_bytes() / std::max<int64_t>(per_k_bytes, 1));
+    c = std::min<int64_t>(c, 65535);
+    const char* s = std::getenv("TBG_MAX_CHUNK");
+    if (s && std::atoll(s) > 0) c = std::min<int64_t>(c, std::atoll(s));
+    return std::max<int64_t>(1, std::min(c, nk));
+}
+
+__global__ void kmesh_kernel(int64_t k0, int64_t nk, int dim, int64_t n0, int64_t n1, int64_t n2,
+                             double* __restrict__ k) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t idx = k0 + t;
+        // gen_kmesh (src/kpoints.rs:49-87): first dimension outermost
+        if (dim == 1) {
+            k[t] = (double)idx / (double)n0;
+        } else if (dim == 2) {
+            k[2 * t] = (double)(idx / n1) / (double)n0;
+            k[2 * t + 1] = (double)(idx % n1) / (double)n1;
+        } else {
+            k[3 * t] = (double)(idx / (n1 * n2)) / (double)n0;
+            k[3 * t + 1] = (double)((idx / n2) % n1) / (double)n1;
+            k[3 * t + 2] = (double)(idx % n2) / (double)n2;
+        }
+    }
+}
+
+__global__ void transpose_kernel(int N, int64_t batch, const zc* __restrict__ U, zc* __restrict__ Ut) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < batch * NN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = idx / NN;
+        const int e = (int)(idx % NN), r = e / N, c = e % N;
+        Ut[b * NN + (int64_t)c * N + r] = U[idx];
+    }
+}
+
+inline unsigned blocks_for(int64_t total) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152LL * 64));
+}
+
+bool all_finite(const double* p, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+int check_model(const tbg_model* m) {
+    if (!m || !m->d.ham) return set_error(TBG_E_INVALID_ARGUMENT, "null or destroyed model handle");
+    if (cudaSetDevice(m->d.device) != cudaSuccess) return set_error(TBG_E_CUDA, "cudaSetDevice failed");
+    return TBG_OK;
+}
+
+// validate_direction_matrix (config.rs:202-233) for n rows of length dim
+int check_dirs(const double* dirs, int64_t rows, int dim, int64_t expect_rows) {
+    if (!dirs) return set_error(TBG_E_INVALID_ARGUMENT, "null direction matrix");
+    if (expect_rows >= 0 && rows != expect_rows)
+        return set_error(TBG_E_DIMENSION_MISMATCH, "direction: expected " + std::to_string(expect_rows) +
+                                                       ", found " + std::to_string(rows));
+    for (int64_t r = 0; r < rows; ++r) {
+        bool nz = false;
+        for (int d = 0; d < dim; ++d) {
+            const double v = dirs[r * dim + d];
+            if (!std::isfinite(v))
+                return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "direction: all components must be finite");
+            nz |= (v != 0.0);
+        }
+        if (!nz)
+            return set_error(TBG_E_INVALID_RESPONSE_PARAMETER,
+                             "direction: each direction row must not be the zero vector");
+    }
+    return TBG_OK;
+}
+
+int check_k(const double* k, int64_t nk, int dim) {
+    if (nk < 0) return set_error(TBG_E_INVALID_ARGUMENT, "negative number of k-points");
+    if (nk > 0 && !k) return set_error(TBG_E_INVALID_ARGUMENT, "null k-point array");
+    (void)dim;
+    return TBG_OK;
+}
+
+int check_eta(double eta) {
+    if (!std::isfinite(eta) || eta < 0.0)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "broadening: must be finite and non-negative");
+    return TBG_OK;
+}
+
+int check_spin(const tbg_model* m, int spin) {
+    if (spin < -1 || spin > 2) return set_error(TBG_E_INVALID_ARGUMENT, "spin must be -1 (None), 0, 1 or 2");
+    if (spin >= 0 && !m->d.spin)
+        return set_error(TBG_E_SPIN_NOT_ALLOWED, "Spin direction is invalid for a model without spin.");
+    return TBG_OK;
+}
+
+int check_status(int* status_d, cudaStream_t st) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, status_d, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "status readback");
+    if (h & 1) return set_error(TBG_E_NOCONV, "eigensolver input contains NaN or Inf");
+    return TBG_OK;
+}
+
+double lattice_det(const std::vector<double>& lat, int dim) {
+    if (dim == 1) return lat[0];
+    if (dim == 2) return lat[0] * lat[3] - lat[1] * lat[2];
+    return lat[0] * (lat[4] * lat[8] - lat[5] * lat[7]) - lat[1] * (lat[3] * lat[8] - lat[5] * lat[6]) +
+           lat[2] * (lat[3] * lat[7] - lat[4] * lat[6]);
+}
+
+// Shared per-chunk response pipeline: (k on device) -> Omega, E.
+struct BerryJob {
+    const ModelDev* m;
+    int spin;
+    double eta;
+    int precision;
+    const double* dirs_d;  // (2, dim)
+    int64_t chunk;
+    // buffers
+    double* k_d;
+    zc *H, *V, *U, *scratch, *Hcopy;
+    double *E, *Om;
+    int* status_d;
+    void* work;
+    size_t work_bytes;
+    cc* U32;
+};
+
+int alloc_berry(Ctx& ctx, BerryJob& J) {
+    const int N = (int)J.m->nsta;
+    const int64_t NN = (int64_t)N * N, c = J.chunk;
+    J.k_d = ctx.alloc<double>(c * J.m->dim);
+    J.H = ctx.alloc<zc>(c * NN);
+    J.V = ctx.alloc<zc>(2 * c * NN);
+    J.U = ctx.alloc<zc>(c * NN);
+    J.scratch = ctx.alloc<zc>(c * NN);
+    J.E = ctx.alloc<double>(c * N);
+    J.Om = ctx.alloc<double>(c * N);
+    J.status_d = ctx.alloc<int>(1);
+    J.Hcopy = nullptr;
+    J.U32 = nullptr;
+    J.work = nullptr;
+    J.work_bytes = 0;
+    if (J.precision == TBG_PREC_MIXED) {
+        J.work_bytes = std::max(mixed_workspace_bytes(N, c), eig_workspace_bytes(N, c, 1));
+        J.work = J.work_bytes ? ctx.alloc<unsigned char>(J.work_bytes) : nullptr;
+    }
+    if (ctx.rc == TBG_OK) {
+        cudaError_t e = cudaMemsetAsync(J.status_d, 0, sizeof(int), ctx.st);
+        if (e != cudaSuccess) ctx.rc = cuda_error(e, "memset status");
+    }
+    return ctx.rc;
+}
+
+int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
+    const ModelDev& m = *J.m;
+    const int N = (int)m.nsta;
+    const int64_t NN = (int64_t)N * N;
+    int rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
+    if (rc) return rc;
+    if (m.n_rmat > 0) {
+        rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
+        if (rc) return rc;
+    }
+    if (J.spin >= 0) {
+        rc = spin_dress(ctx.st, N, m.norb, nkc, J.spin, J.V, 2 * NN, J.scratch);
+        if (rc) return rc;
+    }
+    if (J.precision == TBG_PREC_MIXED) {
+        rc = mixed_eig_refine(ctx.st, N, nkc, J.H, J.E, J.U, J.work, J.work_bytes, J.status_d, clusters_d);
+    } else {
+        rc = eig_batched(ctx.st, N, nkc, J.H, J.E, J.U, nullptr, 0, J.status_d);
+    }
+    if (rc) return rc;
+    return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch);
+}
+
+}  // namespace
+}  // namespace tbg
+
+using namespace tbg;
+
+extern "C" {
+
+const char* tbg_version(void) { return "tbgpu 0.1.0 sm_103a"; }
+
+int64_t tbg_kernel_launch_count(int reset) {
+    const int64_t v = g_launches;
+    if (reset) g_launches = 0;
+    return v;
+}
+
+int tbg_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_err.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+    return g_code;
+}
+
+int tbg_model_create(int dim, int spin, int64_t norb, int64_t nR, const int64_t* hamR, const double* ham,
+                     const double* orb, const double* lat, tbg_model** out) {
+    if (!out) return set_error(TBG_E_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (dim < 1 || dim > 3) return set_error(TBG_E_INVALID_DIMENSION, "dim must be 1, 2 or 3");
+    if (norb < 1) return set_error(TBG_E_INVALID_MODEL, "model has no orbitals");
+    if (nR < 1) return set_error(TBG_E_INVALID_MODEL, "hamR must hold at least the R = 0 block");
+    if (!hamR || !ham || !orb || !lat) return set_error(TBG_E_INVALID_ARGUMENT, "null model array");
+    const int64_t nsta = spin ? 2 * norb : norb;
+    if (nsta > 4096) return set_error(TBG_E_UNSUPPORTED, "nsta > 4096 is not supported");
+    if (!all_finite(lat, (size_t)dim * dim) || !all_finite(orb, (size_t)norb * dim))
+        return set_error(TBG_E_INVALID_MODEL, "finite_geometry: lattice and orbital positions must be finite");
+    // every R needs its Hermitian partner -R (model_build.rs:430-440)
+    for (int64_t r = 0; r < nR; ++r) {
+        bool found = false;
+        for (int64_t q = 0; q < nR && !found; ++q) {
+            bool eq = true;
+            for (int d = 0; d < dim; ++d) eq &= (hamR[q * dim + d] == -hamR[r * dim + d]);
+            found = eq;
+        }
+        if (!found)
+            return set_error(TBG_E_INVALID_MODEL,
+                             "Hopping for vector R exists, but its Hermitian conjugate for -R does not");
+        for (int d = 0; d < dim; ++d)
+            if (std::llabs(hamR[r * dim + d]) > (1LL << 30))
+                return set_error(TBG_E_INVALID_MODEL, "R component out of range");
+    }
+    tbg_model* m = new tbg_model();
+    ModelDev& M = m->d;
+    cudaGetDevice(&M.device);
+    M.dim = dim;
+    M.spin = spin ? 1 : 0;
+    M.norb = norb;
+    M.nsta = nsta;
+    M.nR = nR;
+    M.hamR.assign(hamR, hamR + nR * dim);
+    M.orb.assign(orb, orb + norb * dim);
+    M.lat.assign(lat, lat + dim * dim);
+    std::vector<int> hr(nR * 3, 0);
+    std::vector<double> rc(nR * 3, 0.0), tau(nsta * 3, 0.0), tc(nsta * 3, 0.0);
+    for (int64_t r = 0; r < nR; ++r) {
+        for (int d = 0; d < dim; ++d) hr[r * 3 + d] = (int)hamR[r * dim + d];
+        for (int c = 0; c < dim; ++c) {
+            double s = 0.0;  // R_cart = hamR . lat (velocity.rs:530-531)
+            for (int d = 0; d < dim; ++d) s += (double)hamR[r * dim + d] * lat[d * dim + c];
+            rc[r * 3 + c] = s;
+        }
+    }
+    for (int64_t s = 0; s < nsta; ++s) {
+        const int64_t o = s % norb;  // spinful basis duplicates tau (velocity.rs:546-550)
+        for (int d = 0; d < dim; ++d) tau[s * 3 + d] = orb[o * dim + d];
+        for (int c = 0; c < dim; ++c) {
+            double v = 0.0;
+            for (int d = 0; d < dim; ++d) v += orb[o * dim + d] * lat[d * dim + c];
+            tc[s * 3 + c] = v;
+        }
+    }
+    const size_t hb = sizeof(zc) * (size_t)nR * nsta * nsta;
+    cudaError_t e = cudaMalloc(&M.ham, hb);
+    if (e == cudaSuccess) e = cudaMemcpy(M.ham, ham, hb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&M.hamR_d, sizeof(int) * hr.size());
+    if (e == cudaSuccess) e = cudaMemcpy(M.hamR_d, hr.data(), sizeof(int) * hr.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&M.Rcart_d, sizeof(double) * rc.size());
+    if (e == cudaSuccess) e = cudaMemcpy(M.Rcart_d, rc.data(), sizeof(double) * rc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&M.tau_d, sizeof(double) * tau.size());
+    if (e == cudaSuccess) e = cudaMemcpy(M.tau_d, tau.data(), sizeof(double) * tau.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&M.taucart_d, sizeof(double) * tc.size());
+    if (e == cudaSuccess) e = cudaMemcpy(M.taucart_d, tc.data(), sizeof(double) * tc.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        const int code = cuda_error(e, "tbg_model_create upload");
+        tbg_model_destroy(m);
+        return code;
+    }
+    *out = m;
+    return TBG_OK;
+}
+
+int tbg_model_set_rmatrix(tbg_model* m, int64_t n_rmat, const double* rmatrix) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    if (n_rmat < 0 || n_rmat > m->d.nR) return set_error(TBG_E_INVALID_MODEL, "n_rmat must be in [0, nR]");
+    if (n_rmat > 0 && !rmatrix) return set_error(TBG_E_INVALID_ARGUMENT, "null rmatrix");
+    if (m->d.rmatrix) {
+        cudaFree(m->d.rmatrix);
+        m->d.rmatrix = nullptr;
+    }
+    m->d.n_rmat = 0;
+    if (n_rmat == 0) return TBG_OK;
+    const size_t bytes = sizeof(zc) * (size_t)n_rmat * m->d.dim * m->d.nsta * m->d.nsta;
+    cudaError_t e = cudaMalloc(&m->d.rmatrix, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(m->d.rmatrix, rmatrix, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "tbg_model_set_rmatrix");
+    m->d.n_rmat = n_rmat;
+    return TBG_OK;
+}
+
+int tbg_model_destroy(tbg_model* m) {
+    if (!m) return TBG_OK;
+    ModelDev& M = m->d;
+    cudaSetDevice(M.device);
+    cudaFree(M.ham);
+    cudaFree(M.hamR_d);
+    cudaFree(M.Rcart_d);
+    cudaFree(M.tau_d);
+    cudaFree(M.taucart_d);
+    cudaFree(M.rmatrix);
+    cudaFree(M.box);
+    M.ham = nullptr;
+    delete m;
+    return TBG_OK;
+}
+
+int tbg_model_info(const tbg_model* m, int* dim, int* spin, int64_t* norb, int64_t* nsta, int64_t* nR) {
+    if (!m) return set_error(TBG_E_INVALID_ARGUMENT, "null model handle");
+    if (dim) *dim = m->d.dim;
+    if (spin) *spin = m->d.spin;
+    if (norb) *norb = m->d.norb;
+    if (nsta) *nsta = m->d.nsta;
+    if (nR) *nR = m->d.nR;
+    return TBG_OK;
+}
+
+int tbg_gen_v_projected(const tbg_model* m, int64_t nk, const double* k, int gauge, int64_t n_proj,
+                        const double* dirs, double* V_out, double* H_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    if ((rc = check_k(k, nk, M.dim))) return rc;
+    if (gauge != TBG_GAUGE_ATOM && gauge != TBG_GAUGE_LATTICE) return set_error(TBG_E_INVALID_ARGUMENT, "bad gauge");
+    if (n_proj < 0 || (n_proj > 0 && (!dirs || !V_out))) return set_error(TBG_E_INVALID_ARGUMENT, "bad projections");
+    if (nk == 0) return TBG_OK;
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    Ctx ctx;
+    const int64_t chunk = choose_chunk(nk, sizeof(zc) * NN * (2 + n_proj) + 64);
+    double* k_d = ctx.alloc<double>(chunk * M.dim);
+    zc* H = ctx.alloc<zc>(chunk * NN);
+    zc* V = n_proj ? ctx.alloc<zc>(chunk * n_proj * NN) : nullptr;
+    double* dirs_d = n_proj ? ctx.alloc<double>(n_proj * M.dim) : nullptr;
+    if (ctx.rc) return ctx.rc;
+    if (n_proj) TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs, sizeof(double) * n_proj * M.dim, cudaMemcpyHostToDevice, ctx.st));
+    for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
+        const int64_t nkc = std::min(chunk, nk - c0);
+        TBG_CUDA(cudaMemcpyAsync(k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
+        rc = fourier_direct(M, ctx.st, nkc, k_d, gauge, (int)n_proj, dirs_d, H, V, NN, n_proj * NN);
+        if (rc) return rc;
+        if (M.n_rmat > 0 && n_proj > 0) {
+            rc = rmatrix_term(M, ctx.st, nkc, k_d, gauge, (int)n_proj, dirs_d, H, V, nullptr);
+            if (rc) return rc;
+        }
+        if (H_out)
+            TBG_CUDA(cudaMemcpyAsync(H_out + c0 * NN * 2, H, sizeof(zc) * nkc * NN, cudaMemcpyDeviceToHost, ctx.st));
+        if (n_proj)
+            TBG_CUDA(cudaMemcpyAsync(V_out + c0 * n_proj * NN * 2, V, sizeof(zc) * nkc * n_proj * NN,
+                                     cudaMemcpyDeviceToHost, ctx.st));
+        if (ctx.sync("tbg_gen_v_projected")) return ctx.rc;
+    }
+    return ctx.sync("tbg_gen_v_projected");
+}
+
+int tbg_gen_ham(const tbg_model* m, int64_t nk, const double* k, int gauge, double* H_out) {
+    if (!H_out && nk > 0) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    return tbg_gen_v_projected(m, nk, k, gauge, 0, nullptr, nullptr, H_out);
+}
+
+int tbg_gen_v(const tbg_model* m, int64_t nk, const double* k, int gauge, double* V_out, double* H_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const int dim = m->d.dim;
+    std::vector<double> eye(dim * dim, 0.0);
+    for (int d = 0; d < dim; ++d) eye[d * dim + d] = 1.0;
+    return tbg_gen_v_projected(m, nk, k, gauge, dim, eye.data(), V_out, H_out);
+}
+
+static int solve_impl(const tbg_model* m, int64_t nk, const double* k, double* E_out, double* U_out, int rows) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    if ((rc = check_k(k, nk, M.dim))) return rc;
+    if (nk > 0 && !E_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    if (nk == 0) return TBG_OK;
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    Ctx ctx;
+    const int64_t chunk = choose_chunk(nk, sizeof(zc) * NN * (U_out ? 3 : 1) + 64);
+    double* k_d = ctx.alloc<double>(chunk * M.dim);
+    zc* H = ctx.alloc<zc>(chunk * NN);
+    zc* U = U_out ? ctx.alloc<zc>(chunk * NN) : nullptr;
+    zc* Ut = (U_out && rows) ? ctx.alloc<zc>(chunk * NN) : nullptr;
+    double* E = ctx.alloc<double>(chunk * N);
+    int* status_d = ctx.alloc<int>(1);
+    if (ctx.rc) return ctx.rc;
+    TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
+    for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
+        const int64_t nkc = std::min(chunk, nk - c0);
+        TBG_CUDA(cudaMemcpyAsync(k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
+        rc = fourier_direct(M, ctx.st, nkc, k_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0);
+        if (rc) return rc;
+        rc = eig_batched(ctx.st, N, nkc, H, E, U, nullptr, 0, status_d);
+        if (rc) return rc;
+        TBG_CUDA(cudaMemcpyAsync(E_out + c0 * N, E, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+        if (U_out) {
+            const zc* src = U;
+            if (rows) {
+                transpose_kernel<<<blocks_for(nkc * NN), 256, 0, ctx.st>>>(N, nkc, U, Ut);
+                TBG_LAUNCHED("transpose_kernel");
+                src = Ut;
+            }
+            TBG_CUDA(cudaMemcpyAsync(U_out + c0 * NN * 2, src, sizeof(zc) * nkc * NN, cudaMemcpyDeviceToHost, ctx.st));
+        }
+        if (ctx.sync("tbg_solve")) return ctx.rc;
+    }
+    if ((rc = check_status(status_d, ctx.st))) return rc;
+    return ctx.sync("tbg_solve");
+}
+
+int tbg_solve_band(const tbg_model* m, int64_t nk, const double* k, double* E_out) {
+    return solve_impl(m, nk, k, E_out, nullptr, 0);
+}
+
+int tbg_solve(const tbg_model* m, int64_t nk, const double* k, double* E_out, double* U_out, int evec_rows) {
+    if (!U_out && nk > 0) return set_error(TBG_E_INVALID_ARGUMENT, "null eigenvector output");
+    return solve_impl(m, nk, k, E_out, U_out, evec_rows);
+}
+
+static int berry_common(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, int spin, double eta,
+                        int precision, double* Omega_out, double* E_out, int nmu, const double* mu, double T,
+                        double* occ_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    if ((rc = check_k(k, nk, M.dim))) return rc;
+    if ((rc = check_dirs(dirs2, 2, M.dim, 2))) return rc;
+    if ((rc = check_eta(eta))) return rc;
+    if ((rc = check_spin(m, spin))) return rc;
+    if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
+        return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
+    if (nk == 0) return TBG_OK;
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    Ctx ctx;
+    BerryJob J;
+    J.m = &M;
+    J.spin = spin;
+    J.eta = eta;
+    J.precision = precision;
+    J.chunk = choose_chunk(nk, sizeof(zc) * NN * 5 + 64 * N);
+    double* dirs_d = ctx.alloc<double>(2 * M.dim);
+    J.dirs_d = dirs_d;
+    double* mu_d = (nmu > 0) ? ctx.alloc<double>(nmu) : nullptr;
+    double* S = (nmu > 0) ? ctx.alloc<double>(J.chunk * nmu) : nullptr;
+    if (ctx.rc) return ctx.rc;
+    if ((rc = alloc_berry(ctx, J))) return rc;
+    TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
+    if (nmu > 0) TBG_CUDA(cudaMemcpyAsync(mu_d, mu, sizeof(double) * nmu, cudaMemcpyHostToDevice, ctx.st));
+    const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
+    for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
+        const int64_t nkc = std::min(J.chunk, nk - c0);
+        TBG_CUDA(cudaMemcpyAsync(J.k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
+        if ((rc = run_berry_chunk(ctx, J, nkc, nullptr))) return rc;
+        if (Omega_out)
+            TBG_CUDA(cudaMemcpyAsync(Omega_out + c0 * N, J.Om, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+        if (E_out)
+            TBG_CUDA(cudaMemcpyAsync(E_out + c0 * N, J.E, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+        if (occ_out) {
+            if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, nmu, mu_d, width, S))) return rc;
+            TBG_CUDA(cudaMemcpyAsync(occ_out + c0, S, sizeof(double) * nkc, cudaMemcpyDeviceToHost, ctx.st));
+        }
+        if (ctx.sync("berry")) return ctx.rc;
+    }
+    if ((rc = check_status(J.status_d, ctx.st))) return rc;
+    return ctx.sync("berry");
+}
+
+int tbg_berry_curvature(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, int spin, double eta,
+                        int precision, double* Omega_out, double* E_out) {
+    return berry_common(m, nk, k, dirs2, spin, eta, precision, Omega_out, E_out, 0, nullptr, 0.0, nullptr);
+}
+
+int tbg_occupied_berry_curvature(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, int spin,
+                                 double eta, double T, double mu, int precision, double* out) {
+    if (!std::isfinite(mu))
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "chemical_potentials: all values must be finite");
+    if (!std::isfinite(T) || T < 0.0)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "T: all values must be finite and non-negative");
+    if (!out && nk > 0) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    return berry_common(m, nk, k, dirs2, spin, eta, precision, nullptr, nullptr, 1, &mu, T, out);
+}
+
+int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double* dirs2, int64_t nmu,
+                          const double* mu, double T, double eta, int spin, int precision, double* sigma_out,
+                          tbg_report* report) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    // validate_rank2 (config.rs:141-147) order: k-mesh, direction, mu, eta, T
+    if (!kmesh) return set_error(TBG_E_INVALID_ARGUMENT, "null k-mesh");
+    int64_t nk = 1;
+    for (int d = 0; d < M.dim; ++d) {
+        if (kmesh[d] <= 0) return set_error(TBG_E_INVALID_KMESH, "Invalid k-point mesh dimensions");
+        nk *= kmesh[d];
+    }
+    if ((rc = check_dirs(dirs2, 2, M.dim, 2))) return rc;
+    if (nmu < 1 || !mu)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "chemical_potentials: must contain at least one value");
+    for (int64_t j = 0; j < nmu; ++j)
+        if (!std::isfinite(mu[j]))
+            return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "chemical_potentials: all values must be finite");
+    if ((rc = check_eta(eta))) return rc;
+    if (!std::isfinite(T) || T < 0.0)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "T: all values must be finite and non-negative");
+    if ((rc = check_spin(m, spin))) return rc;
+    if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
+        return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
+    if (!sigma_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    const double det = lattice_det(M.lat, M.dim);
+    if (det == 0.0 || !std::isfinite(det))
+        return set_error(TBG_E_LINALG, "Linear algebra operation failed: singular lattice");
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    const int64_t launches0 = g_launches;
+    Ctx ctx;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, ctx.st);
+    BerryJob J;
+    J.m = &M;
+    J.spin = spin;
+    J.eta = eta;
+    J.precision = precision;
+    J.chunk = choose_chunk(nk, sizeof(zc) * NN * 5 + 64 * N + 8 * nmu);
+    double* dirs_d = ctx.alloc<double>(2 * M.dim);
+    J.dirs_d = dirs_d;
+    double* mu_d = ctx.alloc<double>(nmu);
+    double* S = ctx.alloc<double>(J.chunk * nmu);
+    double* acc = ctx.alloc<double>(2 * nmu);
+    int64_t* clusters_d = ctx.alloc<int64_t>(1);
+    if (ctx.rc) return ctx.rc;
+    if ((rc = alloc_berry(ctx, J))) return rc;
+    TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
+    TBG_CUDA(cudaMemcpyAsync(mu_d, mu, sizeof(double) * nmu, cudaMemcpyHostToDevice, ctx.st));
+    TBG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 2 * nmu, ctx.st));
+    TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
+    const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
+    const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
+    for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
+        const int64_t nkc = std::min(J.chunk, nk - c0);
+        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, M.dim, n0, n1, n2, J.k_d);
+        TBG_LAUNCHED("kmesh_kernel");
+        if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
+        if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
+        if ((rc = kahan_column_sums(ctx.st, nkc, (int)nmu, S, acc))) return rc;
+    }
+    std::vector<double> acc_h(2 * nmu);
+    int64_t clusters_h = 0;
+    TBG_CUDA(cudaMemcpyAsync(acc_h.data(), acc, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, ctx.st));
+    TBG_CUDA(cudaMemcpyAsync(&clusters_h, clusters_d, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.st));
+    cudaEventRecord(ev1, ctx.st);
+    if (ctx.sync("tbg_hall_conductivity")) return ctx.rc;
+    if ((rc = check_status(J.status_d, ctx.st))) return rc;
+    for (int64_t j = 0; j < nmu; ++j) sigma_out[j] = (acc_h[2 * j] - acc_h[2 * j + 1]) / (double)nk / det;
+    if (report) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        report->nk = nk;
+        report->nsta = N;
+        report->precision = precision;
+        report->fourier_mode = 0;
+        report->kernel_launches = g_launches - launches0;
+        report->device_ms = ms;
+        report->eig_ms = 0.0;
+        report->refine_clusters = clusters_h;
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    return TBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,557 @@
+// Batched Hermitian eigensolver: one CTA per matrix.
+//
+// Replaces LAPACK zheev as reached from Rustb (src/response/traits.rs:168 via
+// ndarray-linalg Eigh; src/ndarray_lapack.rs:412-448).  Algorithm per matrix:
+//
+//   1. Householder reduction to real symmetric tridiagonal form T = Q^H A Q
+//      (unblocked, full storage).  The reflector H_j = I - tau_j v_j v_j^H is
+//      chosen so that H_j^H [alpha; x] = [beta; 0] with real beta of sign
+//      opposite to Re(alpha) (no cancellation).  v_j is kept in row j of A.
+//   2. Eigenvalues of T by Sturm-count bisection, one thread per eigenvalue
+//      (ascending by construction, absolute accuracy ~ eps * ||T||).
+//   3. Eigenvectors of T by inverse iteration (tridiagonal LU with partial
+//      pivoting, three iterations), eigenvalues closer than 1e-3 ||T|| form a
+//      cluster whose vectors are computed by one thread with modified
+//      Gram-Schmidt against the earlier members.
+//   4. Back-transformation U = H_0 H_1 ... H_{N-2} Z in column panels.
+//
+// Output: E ascending (double), U with eigenvectors in columns (row-major).
+// Precision T = double (plain path; A stays in global memory, L2-resident)
+// or float (mixed path; A in shared memory when it fits).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "tbgpu_internal.cuh"
+
+namespace tbg {
+namespace {
+
+template <typename T>
+struct Lim;
+template <>
+struct Lim<double> {
+    static __device__ __forceinline__ double eps() { return DBL_EPSILON; }
+    static __device__ __forceinline__ double tiny() { return DBL_MIN; }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+};
+template <>
+struct Lim<float> {
+    static __device__ __forceinline__ float eps() { return FLT_EPSILON; }
+    static __device__ __forceinline__ float tiny() { return FLT_MIN; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum of one or two values; red must hold 2*32 T.  Ends with a barrier.
+template <typename T>
+__device__ __forceinline__ void block_sum2(T& a, T& b, T* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    __syncthreads();
+    if (lane == 0) {
+        red[warp] = a;
+        red[32 + warp] = b;
+    }
+    __syncthreads();
+    T sa = 0, sb = 0;
+    for (int w = 0; w < nw; ++w) {
+        sa += red[w];
+        sb += red[32 + w];
+    }
+    a = sa;
+    b = sb;
+    __syncthreads();
+}
+
+__device__ __forceinline__ unsigned hash32(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+// Number of eigenvalues of the tridiagonal (d, e2 = e^2) strictly below x.
+template <typename T>
+__device__ __forceinline__ int sturm_count(int N, const T* __restrict__ d, const T* __restrict__ e2, T x,
+                                           T pivmin) {
+    int cnt = 0;
+    T q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += (q < 0);
+    for (int i = 1; i < N; ++i) {
+        q = (d[i] - x) - Lim<T>::div(e2[i - 1], q);
+        if (fabs(q) < pivmin) q = -pivmin;
+        cnt += (q < 0);
+    }
+    return cnt;
+}
+
+// One inverse-iteration solve (T - lam I) y = x on the tridiagonal (d, e),
+// in place on x (stride G in the per-thread scratch).  u0/u1/u2 hold the
+// rows of the pivoted U factor.
+template <typename T>
+__device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ e, T lam, T pert,
+                          T* __restrict__ x, T* __restrict__ u0, T* __restrict__ u1, T* __restrict__ u2,
+                          int G) {
+    // forward elimination with partial pivoting, applied to the RHS on the fly
+    T cd = d[0] - lam;   // current row: entry at column i
+    T cs = (N > 1) ? e[0] : T(0);  // entry at column i+1
+    T cr = x[0];         // current row RHS
+    for (int i = 0; i < N - 1; ++i) {
+        const T b = e[i];                 // next row, column i
+        const T a1 = d[i + 1] - lam;      // next row, column i+1
+        const T b1 = (i + 2 < N) ? e[i + 1] : T(0);  // next row, column i+2
+        const T xn = x[(i + 1) * G];
+        if (fabs(cd) >= fabs(b)) {
+            T piv = cd;
+            if (fabs(piv) < pert) piv = (piv < 0) ? -pert : pert;
+            const T mlt = b / piv;
+            u0[i * G] = piv;
+            u1[i * G] = cs;
+            u2[i * G] = 0;
+            x[i * G] = cr;
+            cd = a1 - mlt * cs;
+            cs = b1;
+            cr = xn - mlt * cr;
+        } else {
+            const T mlt = cd / b;
+            u0[i * G] = b;
+            u1[i * G] = a1;
+            u2[i * G] = b1;
+            x[i * G] = xn;
+            const T ncd = cs - mlt * a1;
+            const T ncs = -mlt * b1;
+            cr = cr - mlt * xn;
+            cd = ncd;
+            cs = ncs;
+        }
+    }
+    if (fabs(cd) < pert) cd = (cd < 0) ? -pert : pert;
+    u0[(N - 1) * G] = cd;
+    x[(N - 1) * G] = cr;
+    // back substitution
+    T y2 = 0, y1 = 0;
+    for (int i = N - 1; i >= 0; --i) {
+        T r = x[i * G];
+        if (i + 1 < N) r -= u1[i * G] * y1;
+        if (i + 2 < N) r -= u2[i * G] * y2;
+        const T yi = r / u0[i * G];
+        x[i * G] = yi;
+        y2 = y1;
+        y1 = yi;
+    }
+}
+
+template <typename T>
+struct EigShared {
+    cx<T>* A;   // N*N (shared or global)
+    T* d;       // N
+    T* e;       // N
+    T* e2;      // N
+    T* lam;     // N
+    cx<T>* tau; // N
+    cx<T>* v;   // N
+    cx<T>* w;   // N
+    T* red;     // 64
+    T* scratch; // inverse iteration: 4*N*G ; back-transform panel: N*PB complex
+    int* flags; // 4
+};
+
+template <typename T>
+__host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB) {
+    size_t b = 0;
+    if (a_smem) b += sizeof(cx<T>) * (size_t)N * N;
+    b += sizeof(T) * 4 * (size_t)N;
+    b += sizeof(cx<T>) * 3 * (size_t)N;
+    b += sizeof(T) * 64;
+    size_t s1 = sizeof(T) * 4 * (size_t)N * G;
+    size_t s2 = sizeof(cx<T>) * (size_t)N * PB;
+    b += std::max(s1, s2);
+    b += 16;
+    return b;
+}
+
+// Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
+// input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
+template <typename T, bool A_SMEM, int G, int PB>
+__global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
+                                                   double* __restrict__ Eout, cx<T>* __restrict__ Uout,
+                                                   cx<T>* __restrict__ Awork, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    EigShared<T> sh;
+    {
+        unsigned char* p = smem_raw;
+        if (A_SMEM) {
+            sh.A = reinterpret_cast<cx<T>*>(p);
+            p += sizeof(cx<T>) * (size_t)N * N;
+        }
+        sh.tau = reinterpret_cast<cx<T>*>(p);
+        p += sizeof(cx<T>) * N;
+        sh.v = reinterpret_cast<cx<T>*>(p);
+        p += sizeof(cx<T>) * N;
+        sh.w = reinterpret_cast<cx<T>*>(p);
+        p += sizeof(cx<T>) * N;
+        sh.d = reinterpret_cast<T*>(p);
+        p += sizeof(T) * N;
+        sh.e = reinterpret_cast<T*>(p);
+        p += sizeof(T) * N;
+        sh.e2 = reinterpret_cast<T*>(p);
+        p += sizeof(T) * N;
+        sh.lam = reinterpret_cast<T*>(p);
+        p += sizeof(T) * N;
+        sh.red = reinterpret_cast<T*>(p);
+        p += sizeof(T) * 64;
+        sh.scratch = reinterpret_cast<T*>(p);
+        size_t s1 = sizeof(T) * 4 * (size_t)N * G;
+        size_t s2 = sizeof(cx<T>) * (size_t)N * PB;
+        p += std::max(s1, s2);
+        sh.flags = reinterpret_cast<int*>(p);
+    }
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    const size_t NN = (size_t)N * N;
+
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        cx<T>* A;
+        if (A_SMEM) {
+            A = sh.A;
+        } else if (sizeof(T) == sizeof(double)) {
+            A = reinterpret_cast<cx<T>*>(Hin + b * NN);
+        } else {
+            A = Awork + (size_t)blockIdx.x * NN;
+        }
+        // ---------------------------------------------------------- load --
+        if (A_SMEM || sizeof(T) != sizeof(double)) {
+            const zc* src = Hin + b * NN;
+            for (size_t idx = tid; idx < NN; idx += nthr) {
+                zc h = src[idx];
+                A[idx] = mk<T>((T)h.re, (T)h.im);
+            }
+        }
+        if (tid == 0) sh.flags[0] = 0;
+        __syncthreads();
+
+        // ------------------------------------------------- tridiagonalise --
+        for (int j = 0; j < N - 1; ++j) {
+            const int m = N - 1 - j;
+            cx<T>* rowj = A + (size_t)j * N + (j + 1);  // row j, columns j+1.. = conj(column j)
+            T part = 0, dummy = 0;
+            for (int i = 1 + tid; i < m; i += nthr) part += abs2(rowj[i]);
+            block_sum2(part, dummy, sh.red);
+            if (tid == 0) {
+                const cx<T> alpha = conj(rowj[0]);
+                const T xnorm2 = part;
+                cx<T> tau, scal;
+                T beta;
+                if (xnorm2 == T(0) && alpha.im == T(0)) {
+                    tau = mk<T>(0, 0);
+                    scal = mk<T>(0, 0);
+                    beta = alpha.re;
+                } else {
+                    const T nrm = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xnorm2);
+                    beta = (alpha.re >= T(0)) ? -nrm : nrm;
+                    tau = mk<T>((beta - alpha.re) / beta, -alpha.im / beta);
+                    const cx<T> den = mk<T>(alpha.re - beta, alpha.im);
+                    const T dd = den.re * den.re + den.im * den.im;
+                    scal = mk<T>(den.re / dd, -den.im / dd);
+                }
+                sh.tau[j] = tau;
+                sh.w[0] = scal;  // broadcast slot, read before w is overwritten
+                sh.e[j] = beta;
+                sh.d[j] = A[(size_t)j * N + j].re;
+            }
+            __syncthreads();
+            const cx<T> tau = sh.tau[j];
+            const cx<T> scal = sh.w[0];
+            __syncthreads();
+            for (int i = tid; i < m; i += nthr) {
+                cx<T> vi = (i == 0) ? mk<T>(1, 0) : conj(rowj[i]) * scal;
+                sh.v[i] = vi;
+                rowj[i] = vi;  // keep v_j in row j for the back-transformation
+            }
+            __syncthreads();
+            if (tau.re == T(0) && tau.im == T(0)) continue;
+            // w = tau * A22 v  (warp per row)
+            for (int i = warp; i < m; i += nwarps) {
+                const cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
+                cx<T> acc = mk<T>(0, 0);
+                for (int l = lane; l < m; l += 32) fma_cx(acc, row[l], sh.v[l]);
+                acc.re = warp_sum(acc.re);
+                acc.im = warp_sum(acc.im);
+                if (lane == 0) sh.w[i] = tau * acc;
+            }
+            __syncthreads();
+            // alpha2 = -1/2 tau (w^H v); w += alpha2 v
+            cx<T> dp = mk<T>(0, 0);
+            for (int i = tid; i < m; i += nthr) fma_cjx(dp, sh.w[i], sh.v[i]);
+            block_sum2(dp.re, dp.im, sh.red);
+            const cx<T> alpha2 = T(-0.5) * (tau * dp);
+            for (int i = tid; i < m; i += nthr) sh.w[i] = sh.w[i] + alpha2 * sh.v[i];
+            __syncthreads();
+            // A22 -= v w^H + w v^H
+            for (int i = warp; i < m; i += nwarps) {
+                cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
+                const cx<T> vi = sh.v[i], wi = sh.w[i];
+                for (int l = lane; l < m; l += 32) {
+                    cx<T> a = row[l];
+                    const cx<T> vl = sh.v[l], wl = sh.w[l];
+                    a = a - mulc(vi, wl) - mulc(wi, vl);
+                    row[l] = a;
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            sh.d[N - 1] = A[(size_t)(N - 1) * N + (N - 1)].re;
+            sh.e[N - 1] = 0;
+        }
+        __syncthreads();
+        for (int i = tid; i < N; i += nthr) sh.e2[i] = sh.e[i] * sh.e[i];
+        __syncthreads();
+
+        // ------------------------------------------------------ bisection --
+        T lo_g, hi_g, tnorm, pivmin;
+        {
+            T lo = INFINITY, hi = -INFINITY, em = 0;
+            for (int i = tid; i < N; i += nthr) {
+                const T r = ((i > 0) ? fabs(sh.e[i - 1]) : T(0)) + ((i < N - 1) ? fabs(sh.e[i]) : T(0));
+                lo = min(lo, sh.d[i] - r);
+                hi = max(hi, sh.d[i] + r);
+                em = max(em, sh.e2[i]);
+            }
+            lo = -warp_max(-lo);
+            hi = warp_max(hi);
+            em = warp_max(em);
+            if (lane == 0) {
+                sh.red[warp] = lo;
+                sh.red[32 + warp] = hi;
+            }
+            if (lane == 0) sh.scratch[warp] = em;
+            __syncthreads();
+            lo = INFINITY;
+            hi = -INFINITY;
+            em = 0;
+            for (int w2 = 0; w2 < nwarps; ++w2) {
+                lo = min(lo, sh.red[w2]);
+                hi = max(hi, sh.red[32 + w2]);
+                em = max(em, sh.scratch[w2]);
+            }
+            __syncthreads();
+            tnorm = max(fabs(lo), fabs(hi));
+            if (!(tnorm == tnorm) || isinf(tnorm)) {
+                if (tid == 0) sh.flags[0] = 1;  // NaN/Inf input
+                tnorm = 1;
+                lo = -1;
+                hi = 1;
+            }
+            pivmin = Lim<T>::tiny() * max(T(1), em);
+            const T pad = T(2) * Lim<T>::eps() * tnorm + T(4) * pivmin;
+            lo_g = lo - pad - T(2) * Lim<T>::eps() * tnorm;
+            hi_g = hi + pad + T(2) * Lim<T>::eps() * tnorm;
+            if (tnorm == T(0)) {
+                lo_g = -pivmin;
+                hi_g = pivmin;
+            }
+        }
+        const T atol = T(2) * Lim<T>::eps() * tnorm + T(2) * pivmin;
+        for (int i = tid; i < N; i += nthr) {
+            T a = lo_g, c = hi_g;
+            for (int it = 0; it < 200; ++it) {
+                const T mid = T(0.5) * (a + c);
+                if (c - a <= atol + T(2) * Lim<T>::eps() * max(fabs(a), fabs(c))) break;
+                if (sturm_count<T>(N, sh.d, sh.e2, mid, pivmin) <= i)
+                    a = mid;
+                else
+                    c = mid;
+            }
+            sh.lam[i] = T(0.5) * (a + c);
+        }
+        __syncthreads();
+        if (Eout) {
+            for (int i = tid; i < N; i += nthr) Eout[b * N + i] = (double)sh.lam[i];
+        }
+        if (Uout == nullptr) {
+            __syncthreads();
+            continue;
+        }
+
+        // ------------------------------------------- inverse iteration --
+        cx<T>* U = Uout + b * NN;
+        const T ctol = T(1e-3) * max(tnorm, Lim<T>::tiny());
+        const T pert = max(Lim<T>::eps() * tnorm, pivmin);
+        for (int g0 = 0; g0 < N; g0 += G) {
+            const int t = tid;
+            if (t < G && g0 + t < N) {
+                const int i = g0 + t;
+                const bool first = (i == 0) || (sh.lam[i] - sh.lam[i - 1] > ctol);
+                if (first) {
+                    int c1 = i;
+                    while (c1 + 1 < N && sh.lam[c1 + 1] - sh.lam[c1] <= ctol) ++c1;
+                    T* x = sh.scratch + t;
+                    T* u0 = x + (size_t)N * G;
+                    T* u1 = u0 + (size_t)N * G;
+                    T* u2 = u1 + (size_t)N * G;
+                    T shift_prev = -INFINITY;
+                    for (int jj = i; jj <= c1; ++jj) {
+                        T shift = sh.lam[jj];
+                        // separate coincident shifts inside a cluster
+                        const T pertol = T(10) * Lim<T>::eps() * max(fabs(shift), tnorm * T(1e-3));
+                        if (jj > i && shift - shift_prev < pertol) shift = shift_prev + pertol;
+                        shift_prev = shift;
+                        for (int r = 0; r < N; ++r) {
+                            const unsigned h = hash32((unsigned)(r * 7919 + jj * 104729 + 12345));
+                            x[(size_t)r * G] = T(1) + T(0.5) * ((T)(h & 0xffff) / T(65535) - T(0.5));
+                        }
+                        for (int iter = 0; iter < 3; ++iter) {
+                            tri_solve<T>(N, sh.d, sh.e, shift, pert, x, u0, u1, u2, G);
+                            // Gram-Schmidt against earlier cluster members (stored in U, real parts)
+                            for (int pp = i; pp < jj; ++pp) {
+                                T dot = 0;
+                                for (int r = 0; r < N; ++r) dot += U[(size_t)r * N + pp].re * x[(size_t)r * G];
+                                for (int r = 0; r < N; ++r) x[(size_t)r * G] -= dot * U[(size_t)r * N + pp].re;
+                            }
+                            T nrm = 0, amax = 0;
+                            for (int r = 0; r < N; ++r) amax = max(amax, fabs(x[(size_t)r * G]));
+                            if (!(amax > T(0)) || isinf(amax)) {
+                                for (int r = 0; r < N; ++r) x[(size_t)r * G] = (r == (jj % N)) ? T(1) : T(0);
+                                amax = 1;
+                            }
+                            const T sc = T(1) / amax;
+                            for (int r = 0; r < N; ++r) {
+                                const T xv = x[(size_t)r * G] * sc;
+                                x[(size_t)r * G] = xv;
+                                nrm += xv * xv;
+                            }
+                            const T inv = T(1) / sqrt(nrm);
+                            for (int r = 0; r < N; ++r) x[(size_t)r * G] *= inv;
+                        }
+                        for (int r = 0; r < N; ++r) U[(size_t)r * N + jj] = mk<T>(x[(size_t)r * G], T(0));
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        __threadfence_block();
+        __syncthreads();
+
+        // ----------------------------------------------- back-transform --
+        // Panel P holds PB columns of U, column-major (P[c*N + r]).
+        cx<T>* P = reinterpret_cast<cx<T>*>(sh.scratch);
+        for (int c0 = 0; c0 < N; c0 += PB) {
+            const int pw = min(PB, N - c0);
+            for (int idx = tid; idx < N * pw; idx += nthr) {
+                const int r = idx / pw, c = idx % pw;
+                P[(size_t)c * N + r] = U[(size_t)r * N + c0 + c];
+            }
+            __syncthreads();
+            for (int j = N - 2; j >= 0; --j) {
+                const cx<T> tau = sh.tau[j];
+                if (tau.re == T(0) && tau.im == T(0)) continue;
+                const int m = N - 1 - j;
+                const cx<T>* vj = A + (size_t)j * N + (j + 1);
+                // s_c = tau * sum_i conj(v_i) P[c][j+1+i]: one warp per column
+                for (int c = warp; c < pw; c += nwarps) {
+                    const cx<T>* pc = P + (size_t)c * N + (j + 1);
+                    cx<T> acc = mk<T>(0, 0);
+                    for (int i = lane; i < m; i += 32) fma_cjx(acc, vj[i], pc[i]);
+                    acc.re = warp_sum(acc.re);
+                    acc.im = warp_sum(acc.im);
+                    if (lane == 0) sh.w[c] = tau * acc;
+                }
+                __syncthreads();
+                for (int c = warp; c < pw; c += nwarps) {
+                    cx<T>* pc = P + (size_t)c * N + (j + 1);
+                    const cx<T> sc = sh.w[c];
+                    for (int i = lane; i < m; i += 32) pc[i] = pc[i] - vj[i] * sc;
+                }
+                __syncthreads();
+            }
+            for (int idx = tid; idx < N * pw; idx += nthr) {
+                const int r = idx / pw, c = idx % pw;
+                U[(size_t)r * N + c0 + c] = P[(size_t)c * N + r];
+            }
+            __syncthreads();
+        }
+        if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
+        __syncthreads();
+    }
+}
+
+template <typename T, bool A_SMEM, int G, int PB>
+int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
+                size_t work_bytes, int* status_d, const char* name) {
+    const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
+    auto kern = heev_kernel<T, A_SMEM, G, PB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
+    int dev = 0, nsm = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = (N <= 32) ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
+    if (e != cudaSuccess || perSM < 1) perSM = 1;
+    int64_t grid = (int64_t)nsm * perSM;
+    const bool needs_work = !A_SMEM && sizeof(T) != sizeof(double);
+    if (needs_work) {
+        const int64_t per = (int64_t)sizeof(cx<T>) * N * N;
+        const int64_t cap = (int64_t)(work_bytes / (size_t)per);
+        if (cap < 1) return set_error(TBG_E_OOM, "eigensolver workspace too small");
+        grid = std::min(grid, cap);
+    }
+    grid = std::min<int64_t>(grid, batch);
+    if (grid < 1) return TBG_OK;
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d);
+    TBG_LAUNCHED(name);
+    return TBG_OK;
+}
+
+}  // namespace
+
+size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
+    if (precision == 0) return 0;
+    const size_t smem = eig_smem_bytes<float>(N, true, 32, 32);
+    if (smem <= 200 * 1024) return 0;
+    return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
+}
+
+// FP64 driver (plain path): A destroyed, U complex<double>.
+int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
+                size_t work_bytes, int* status_d) {
+    if (batch <= 0) return TBG_OK;
+    return launch_heev<double, false, 16, 16>(st, N, batch, A, E, U, work, work_bytes, status_d,
+                                              "heev_kernel<double>");
+}
+
+// FP32 driver (mixed path): H preserved, U complex<float>.
+int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
+                    size_t work_bytes, int* status_d) {
+    if (batch <= 0) return TBG_OK;
+    const size_t smem = eig_smem_bytes<float>(N, true, 32, 32);
+    if (smem <= 200 * 1024)
+        return launch_heev<float, true, 32, 32>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                "heev_kernel<float,smem>");
+    return launch_heev<float, false, 32, 32>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                             "heev_kernel<float,global>");
+}
+
+}  // namespace tbg

@@ -1,0 +1,392 @@
+// Bloch Fourier sum H(k) and direction-projected velocities, direct form.
+//
+// Replaces the zaxpy loops of Model::gen_ham (src/model_physics.rs:92-96) and
+// Model::gen_v_projected (src/velocity.rs:538-541, 581-613):
+//
+//   H_lat(k)[e] = sum_R u(k,R) ham[R][e],                u = e^{2 pi i k.R}
+//   V_p(k)[e]   = i sum_R (w_p . R_cart) u(k,R) ham[R][e]
+//   Atom gauge:   H[m,n] = conj(phi_m) H_lat[m,n] phi_n,       phi = e^{2 pi i k.tau}
+//                 V_p[m,n] = (V_p[m,n] + i (w_p.tau_n - w_p.tau_m) H_lat[m,n]) conj(phi_m) phi_n
+//
+// As a contraction this is phase[nk x nR] . hop[nR x N^2] for H and the same
+// with the phase column scaled by w_p.R_cart for each V_p.  The kernel stages
+// tiles of the hop table and of the phases in shared memory and keeps one
+// complex accumulator per output in registers; the gauge / tau epilogue is
+// fused.  FP64 throughout (plain path).
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "tbgpu_internal.cuh"
+
+namespace tbg {
+namespace {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+// u(k,R) = exp(2 pi i k.R) for R rows [0, nR); phi(k,s) = exp(2 pi i k.tau_s).
+__global__ void phases_kernel(int64_t nk, int dim, const double* __restrict__ k, int nR,
+                              const int* __restrict__ hamR, int nsta, const double* __restrict__ tau,
+                              zc* __restrict__ ph, zc* __restrict__ orbph) {
+    const int64_t total = nk * (int64_t)(nR + nsta);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / (nR + nsta);
+        const int j = (int)(idx % (nR + nsta));
+        const double* kv = k + kk * dim;
+        double s = 0.0;
+        if (j < nR) {
+            const int* r = hamR + 3 * j;
+            // same operation order as the reference: r0*k0 + r1*k1 + r2*k2
+            s = (double)r[0] * kv[0];
+            if (dim > 1) s += (double)r[1] * kv[1];
+            if (dim > 2) s += (double)r[2] * kv[2];
+            double sn, cs;
+            sincos(kTwoPi * s, &sn, &cs);
+            ph[kk * nR + j] = mk(cs, sn);
+        } else {
+            const double* t = tau + 3 * (j - nR);
+            s = t[0] * kv[0];
+            if (dim > 1) s += t[1] * kv[1];
+            if (dim > 2) s += t[2] * kv[2];
+            double sn, cs;
+            sincos(kTwoPi * s, &sn, &cs);
+            orbph[kk * nsta + (j - nR)] = mk(cs, sn);
+        }
+    }
+}
+
+constexpr int TK = 32;   // k-points per tile
+constexpr int TE = 64;   // matrix elements per tile
+constexpr int RC = 8;    // R rows per shared-memory stage
+
+// NP velocity projections (0..3).  coef: (NP, nR) = w_p . R_cart.
+// taup: (NP, N) = w_p . tau_cart (Atom gauge only).
+template <int NP>
+__global__ void __launch_bounds__(256) fourier_gemm_kernel(
+    int64_t nk, int nR, int ldph, int N, const zc* __restrict__ ph, const zc* __restrict__ hop,
+    const double* __restrict__ coef, const zc* __restrict__ orbph, const double* __restrict__ taup,
+    int gauge, zc* __restrict__ H, int64_t ldH, zc* __restrict__ V, int64_t ldV) {
+    __shared__ zc s_hop[RC][TE];
+    __shared__ zc s_ph[RC][TK];
+    __shared__ double s_coef[NP > 0 ? NP : 1][RC];
+    const int tid = threadIdx.x;
+    const int te = tid & 15;  // element lane: e = te + 16 j
+    const int tk = tid >> 4;  // k lane: k = tk + 16 i
+    const int64_t NN = (int64_t)N * N;
+    const int64_t e0 = (int64_t)blockIdx.x * TE;
+    const int64_t k0 = (int64_t)blockIdx.y * TK;
+
+    zc accH[2][4];
+    zc accV[NP > 0 ? NP : 1][2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            accH[i][j] = mk(0.0, 0.0);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) accV[p][i][j] = mk(0.0, 0.0);
+        }
+
+    for (int r0 = 0; r0 < nR; r0 += RC) {
+        for (int idx = tid; idx < RC * TE; idx += 256) {
+            const int r = idx / TE, e = idx % TE;
+            zc h = mk(0.0, 0.0);
+            if (r0 + r < nR && e0 + e < NN) h = hop[(int64_t)(r0 + r) * NN + e0 + e];
+            s_hop[r][e] = h;
+        }
+        {
+            const int r = tid / TK, kk = tid % TK;  // 256 == RC*TK
+            zc u = mk(0.0, 0.0);
+            if (r0 + r < nR && k0 + kk < nk) u = ph[(k0 + kk) * ldph + r0 + r];
+            s_ph[r][kk] = u;
+        }
+        if (NP > 0 && tid < NP * RC) {
+            const int p = tid / RC, r = tid % RC;
+            s_coef[p][r] = (r0 + r < nR) ? coef[(int64_t)p * nR + r0 + r] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {
+            zc h[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) h[j] = s_hop[r][te + 16 * j];
+            double c[NP > 0 ? NP : 1];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) c[p] = s_coef[p][r];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const zc u = s_ph[r][tk + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const zc t = u * h[j];
+                    accH[i][j].re += t.re;
+                    accH[i][j].im += t.im;
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        accV[p][i][j].re = fma(c[p], t.re, accV[p][i][j].re);
+                        accV[p][i][j].im = fma(c[p], t.im, accV[p][i][j].im);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int64_t kk = k0 + tk + 16 * i;
+        if (kk >= nk) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t e = e0 + te + 16 * j;
+            if (e >= NN) continue;
+            const int mrow = (int)(e / N), ncol = (int)(e % N);
+            const zc hl = accH[i][j];
+            zc g = mk(1.0, 0.0);
+            if (gauge == TBG_GAUGE_ATOM) g = cmul(orbph[kk * N + mrow], orbph[kk * N + ncol]);
+            if (H) H[kk * ldH + e] = hl * g;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                // i * acc
+                zc v = mk(-accV[p][i][j].im, accV[p][i][j].re);
+                if (gauge == TBG_GAUGE_ATOM) {
+                    const double diff = taup[p * N + ncol] - taup[p * N + mrow];
+                    v.re -= diff * hl.im;
+                    v.im += diff * hl.re;
+                    v = v * g;
+                }
+                V[kk * ldV + p * NN + e] = v;
+            }
+        }
+    }
+}
+
+// coef[p][r] = w_p . R_cart[r];  taup[p][s] = w_p . tau_cart[s]
+__global__ void proj_coef_kernel(int nproj, int dim, const double* __restrict__ dirs, int nR,
+                                 const double* __restrict__ Rcart, int nsta, const double* __restrict__ taucart,
+                                 double* __restrict__ coef, double* __restrict__ taup) {
+    const int total = nproj * (nR + nsta);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int p = idx / (nR + nsta), j = idx % (nR + nsta);
+        const double* w = dirs + p * dim;
+        if (j < nR) {
+            const double* r = Rcart + 3 * j;
+            double s = w[0] * r[0];
+            if (dim > 1) s += w[1] * r[1];
+            if (dim > 2) s += w[2] * r[2];
+            coef[p * nR + j] = s;
+        } else {
+            const double* t = taucart + 3 * (j - nR);
+            double s = w[0] * t[0];
+            if (dim > 1) s += w[1] * t[1];
+            if (dim > 2) s += w[2] * t[2];
+            taup[p * nsta + (j - nR)] = s;
+        }
+    }
+}
+
+template <int NP>
+int launch_gemm(cudaStream_t st, int64_t nk, int nR, int ldph, int N, const zc* ph, const zc* hop,
+                const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH,
+                zc* V, int64_t ldV) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t kb = 0; kb < nk; kb += (int64_t)TK * 65535) {
+        const int64_t nkb = std::min<int64_t>(nk - kb, (int64_t)TK * 65535);
+        dim3 grid((unsigned)((NN + TE - 1) / TE), (unsigned)((nkb + TK - 1) / TK));
+        fourier_gemm_kernel<NP><<<grid, 256, 0, st>>>(nkb, nR, ldph, N, ph + kb * ldph, hop, coef,
+                                                        orbph + kb * N, taup, gauge,
+                                                        H ? H + kb * ldH : nullptr, ldH,
+                                                        V ? V + kb * ldV : nullptr, ldV);
+        TBG_LAUNCHED("fourier_gemm_kernel");
+    }
+    return TBG_OK;
+}
+
+int dispatch_gemm(cudaStream_t st, int np, int64_t nk, int nR, int ldph, int N, const zc* ph, const zc* hop,
+                  const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH,
+                  zc* V, int64_t ldV) {
+    switch (np) {
+        case 0: return launch_gemm<0>(st, nk, nR, ldph, N, ph, hop, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        case 1: return launch_gemm<1>(st, nk, nR, ldph, N, ph, hop, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        case 2: return launch_gemm<2>(st, nk, nR, ldph, N, ph, hop, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        default: return launch_gemm<3>(st, nk, nR, ldph, N, ph, hop, coef, orbph, taup, gauge, H, ldH, V, ldV);
+    }
+}
+
+// Gauge transform + zeroed diagonal of the rmatrix Fourier sum (Atom gauge),
+// velocity.rs:646-656.
+__global__ void rmat_gauge_kernel(int64_t nk, int N, const zc* __restrict__ orbph, zc* __restrict__ A) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nk * NN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / NN;
+        const int e = (int)(idx % NN), m = e / N, n = e % N;
+        zc a = A[idx];
+        if (m == n) {
+            a = mk(0.0, 0.0);
+        } else {
+            a = a * cmul(orbph[kk * N + m], orbph[kk * N + n]);
+        }
+        A[idx] = a;
+    }
+}
+
+// V[k] += i (H A - A H) for one k per block row tile; simple tiled FP64 GEMM.
+__global__ void __launch_bounds__(256) commutator_kernel(int N, const zc* __restrict__ H, int64_t ldH,
+                                                         const zc* __restrict__ A, zc* __restrict__ V,
+                                                         int64_t ldV) {
+    const int64_t kk = blockIdx.z;
+    const zc* Hk = H + kk * ldH;
+    const zc* Ak = A + kk * (int64_t)N * N;
+    zc* Vk = V + kk * ldV;
+    __shared__ zc sH[16][17], sA[16][17], sA2[16][17], sH2[16][17];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
+    zc acc = mk(0.0, 0.0);
+    for (int t0 = 0; t0 < N; t0 += 16) {
+        // (H A)[row][col] = sum_l H[row][l] A[l][col];  (A H)[row][col] = sum_l A[row][l] H[l][col]
+        sH[ty][tx] = (row < N && t0 + tx < N) ? Hk[(int64_t)row * N + t0 + tx] : mk(0.0, 0.0);
+        sA2[ty][tx] = (row < N && t0 + tx < N) ? Ak[(int64_t)row * N + t0 + tx] : mk(0.0, 0.0);
+        sA[ty][tx] = (t0 + ty < N && col < N) ? Ak[(int64_t)(t0 + ty) * N + col] : mk(0.0, 0.0);
+        sH2[ty][tx] = (t0 + ty < N && col < N) ? Hk[(int64_t)(t0 + ty) * N + col] : mk(0.0, 0.0);
+        __syncthreads();
+#pragma unroll
+        for (int l = 0; l < 16; ++l) {
+            fma_cx(acc, sH[ty][l], sA[l][tx]);
+            const zc t = sA2[ty][l] * sH2[l][tx];
+            acc.re -= t.re;
+            acc.im -= t.im;
+        }
+        __syncthreads();
+    }
+    if (row < N && col < N) {
+        zc v = Vk[(int64_t)row * N + col];
+        v.re -= acc.im;
+        v.im += acc.re;
+        Vk[(int64_t)row * N + col] = v;
+    }
+}
+
+// combined rmatrix table for projection p: rm_p[r][e] = sum_d w_pd rmatrix[r][d][e]
+__global__ void rmat_combine_kernel(int64_t n_rmat, int dim, int N, const double* __restrict__ w,
+                                    const zc* __restrict__ rm, zc* __restrict__ out) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n_rmat * NN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / NN, e = idx % NN;
+        zc s = mk(0.0, 0.0);
+        for (int d = 0; d < dim; ++d) {
+            const zc a = rm[(r * dim + d) * NN + e];
+            s.re += w[d] * a.re;
+            s.im += w[d] * a.im;
+        }
+        out[idx] = s;
+    }
+}
+
+}  // namespace
+
+int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge, int nproj,
+                   const double* dirs_d, zc* H, zc* V, int64_t ldH, int64_t ldV) {
+    if (nk <= 0) return TBG_OK;
+    const int N = (int)m.nsta, nR = (int)m.nR;
+    zc *ph = nullptr, *orbph = nullptr;
+    double *coef = nullptr, *taup = nullptr;
+    TBG_CUDA(cudaMallocAsync(&ph, sizeof(zc) * nk * nR, st));
+    TBG_CUDA(cudaMallocAsync(&orbph, sizeof(zc) * nk * N, st));
+    const int npc = std::max(nproj, 1);
+    TBG_CUDA(cudaMallocAsync(&coef, sizeof(double) * npc * nR, st));
+    TBG_CUDA(cudaMallocAsync(&taup, sizeof(double) * npc * N, st));
+    int rc = TBG_OK;
+    {
+        const int64_t total = nk * (int64_t)(nR + N);
+        const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 65535 * 8);
+        phases_kernel<<<blocks, 256, 0, st>>>(nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph, orbph);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_error(e, "phases_kernel");
+    }
+    if (rc == TBG_OK && nproj > 0) {
+        const int total = nproj * (nR + N);
+        proj_coef_kernel<<<(total + 255) / 256, 256, 0, st>>>(nproj, m.dim, dirs_d, nR, m.Rcart_d, N,
+                                                              m.taucart_d, coef, taup);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_error(e, "proj_coef_kernel");
+    }
+    // H together with up to 3 projections per pass
+    for (int p0 = 0; rc == TBG_OK && (p0 < nproj || (p0 == 0 && nproj == 0)); p0 += 3) {
+        const int np = std::min(3, std::max(0, nproj - p0));
+        zc* Hout = (p0 == 0) ? H : nullptr;
+        if (!Hout && np == 0) break;
+        rc = dispatch_gemm(st, np, nk, nR, nR, N, ph, m.ham, coef + (int64_t)p0 * nR, orbph,
+                           taup + (int64_t)p0 * N, gauge, Hout, ldH, V ? V + (int64_t)p0 * N * N : nullptr, ldV);
+        if (nproj == 0) break;
+    }
+    cudaFreeAsync(ph, st);
+    cudaFreeAsync(orbph, st);
+    cudaFreeAsync(coef, st);
+    cudaFreeAsync(taup, st);
+    return rc;
+}
+
+int rmatrix_term(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge, int nproj,
+                 const double* dirs_d, const zc* H, zc* V, zc* /*scratch*/) {
+    if (m.n_rmat <= 0 || nk <= 0 || nproj <= 0) return TBG_OK;
+    const int N = (int)m.nsta, nR = (int)m.nR;
+    const int64_t NN = (int64_t)N * N;
+    zc *ph = nullptr, *orbph = nullptr, *tab = nullptr, *A = nullptr;
+    TBG_CUDA(cudaMallocAsync(&ph, sizeof(zc) * nk * nR, st));
+    TBG_CUDA(cudaMallocAsync(&orbph, sizeof(zc) * nk * N, st));
+    TBG_CUDA(cudaMallocAsync(&tab, sizeof(zc) * m.n_rmat * NN, st));
+    TBG_CUDA(cudaMallocAsync(&A, sizeof(zc) * nk * NN, st));
+    int rc = TBG_OK;
+    {
+        const int64_t total = nk * (int64_t)(nR + N);
+        const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 65535 * 8);
+        phases_kernel<<<blocks, 256, 0, st>>>(nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph, orbph);
+        count_launch();
+    }
+    std::vector<double> dirs_h((size_t)nproj * m.dim);
+    if (cudaMemcpyAsync(dirs_h.data(), dirs_d, sizeof(double) * dirs_h.size(), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        rc = cuda_error(cudaGetLastError(), "rmatrix_term: copy directions");
+    double* w_d = nullptr;
+    if (rc == TBG_OK) {
+        TBG_CUDA(cudaMallocAsync(&w_d, sizeof(double) * m.dim, st));
+    }
+    for (int p = 0; rc == TBG_OK && p < nproj; ++p) {
+        TBG_CUDA(cudaMemcpyAsync(w_d, dirs_d + (int64_t)p * m.dim, sizeof(double) * m.dim,
+                                 cudaMemcpyDeviceToDevice, st));
+        const int64_t tot = m.n_rmat * NN;
+        rmat_combine_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535 * 8), 256, 0, st>>>(
+            m.n_rmat, m.dim, N, w_d, m.rmatrix, tab);
+        count_launch();
+        // A = sum_{r < n_rmat} u(k,r) rm_p[r]   (H-only contraction, lattice gauge)
+        rc = dispatch_gemm(st, 0, nk, (int)m.n_rmat, nR, N, ph, tab, nullptr, orbph, nullptr,
+                           TBG_GAUGE_LATTICE, A, NN, nullptr, 0);
+        if (rc != TBG_OK) break;
+        if (gauge == TBG_GAUGE_ATOM) {
+            const int64_t t2 = nk * NN;
+            rmat_gauge_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+                nk, N, orbph, A);
+            count_launch();
+        }
+        dim3 grid((N + 15) / 16, (N + 15) / 16, (unsigned)nk);
+        commutator_kernel<<<grid, 256, 0, st>>>(N, H, NN, A, V + (int64_t)p * NN, (int64_t)nproj * NN);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_error(e, "rmatrix_term kernels");
+    }
+    if (w_d) cudaFreeAsync(w_d, st);
+    cudaFreeAsync(ph, st);
+    cudaFreeAsync(orbph, st);
+    cudaFreeAsync(tab, st);
+    cudaFreeAsync(A, st);
+    return rc;
+}
+
+}  // namespace tbg

@@ -1,0 +1,159 @@
+// Internal declarations shared by the tbgpu CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tbgpu.h"
+
+namespace tbg {
+
+// ----------------------------------------------------------------- complex --
+template <typename T>
+struct cx {
+    T re, im;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> mk(T r, T i) {
+    cx<T> z;
+    z.re = r;
+    z.im = i;
+    return z;
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return mk(a.re + b.re, a.im + b.im); }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return mk(a.re - b.re, a.im - b.im); }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b) {
+    return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(T s, cx<T> a) { return mk(s * a.re, s * a.im); }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> conj(cx<T> a) { return mk(a.re, -a.im); }
+template <typename T>
+__host__ __device__ __forceinline__ T abs2(cx<T> a) { return a.re * a.re + a.im * a.im; }
+// a * conj(b)
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> mulc(cx<T> a, cx<T> b) {
+    return mk(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
+}
+// conj(a) * b
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return mk(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re);
+}
+// acc += a * b
+template <typename T>
+__host__ __device__ __forceinline__ void fma_cx(cx<T>& acc, cx<T> a, cx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re);
+    acc.re = fma(-a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im);
+    acc.im = fma(a.im, b.re, acc.im);
+}
+// acc += conj(a) * b
+template <typename T>
+__host__ __device__ __forceinline__ void fma_cjx(cx<T>& acc, cx<T> a, cx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re);
+    acc.re = fma(a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im);
+    acc.im = fma(-a.im, b.re, acc.im);
+}
+
+typedef cx<double> zc;
+typedef cx<float> cc;
+
+// -------------------------------------------------------------- model data --
+struct ModelDev {
+    int dim = 0, spin = 0;
+    int64_t norb = 0, nsta = 0, nR = 0;
+    std::vector<int64_t> hamR;   // host copy (nR, dim)
+    std::vector<double> orb;     // host (norb, dim)
+    std::vector<double> lat;     // host (dim, dim)
+    zc* ham = nullptr;           // device (nR, nsta, nsta)
+    int* hamR_d = nullptr;       // device (nR, 3), zero padded
+    double* Rcart_d = nullptr;   // device (nR, 3) Cartesian R = hamR . lat
+    double* tau_d = nullptr;     // device (nsta, 3) fractional, spin-duplicated
+    double* taucart_d = nullptr; // device (nsta, 3) Cartesian
+    int64_t n_rmat = 0;
+    zc* rmatrix = nullptr;       // device (n_rmat, dim, nsta, nsta)
+    // separable-mesh table: dense box copy of ham (built lazily)
+    int box_lo[3] = {0, 0, 0}, box_len[3] = {1, 1, 1};
+    zc* box = nullptr;           // device (L0, L1, L2, nsta, nsta)
+    bool box_ready = false;
+    int device = 0;
+};
+
+// ------------------------------------------------------------------ errors --
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* where);
+void count_launch(int n = 1);
+
+#define TBG_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return cuda_error(_e, #call); \
+    } while (0)
+
+#define TBG_LAUNCHED(where)                                         \
+    do {                                                            \
+        count_launch();                                             \
+        cudaError_t _e = cudaGetLastError();                        \
+        if (_e != cudaSuccess) return cuda_error(_e, where);        \
+    } while (0)
+
+// ---------------------------------------------------------- kernel drivers --
+// Fourier sum, direct form: for nk k-points (device k, (nk, dim)), outputs
+// H (nk, N, N) (may be null) and V (nk, nproj, N, N) (may be null when
+// nproj == 0); dirs (nproj, dim) device (Cartesian weights).
+int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge,
+                   int nproj, const double* dirs_d, zc* H, zc* V, int64_t ldH, int64_t ldV);
+
+// Position-matrix commutator term added to V (HasRMatrix models).
+int rmatrix_term(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge,
+                 int nproj, const double* dirs_d, const zc* H, zc* V, zc* scratch);
+
+// Separable transform on a uniform mesh: k-points with flat indices
+// [k0, k0 + nk) of the mesh kmesh[dim].
+int fourier_mesh(ModelDev& m, cudaStream_t st, const int64_t* kmesh, int64_t k0, int64_t nk,
+                 int gauge, int nproj, const double* dirs_d, zc* H, zc* V, zc* scratch,
+                 size_t scratch_bytes);
+size_t fourier_mesh_scratch_bytes(const ModelDev& m, const int64_t* kmesh, int64_t nk_chunk);
+bool fourier_mesh_supported(const ModelDev& m);
+
+// Batched Hermitian eigensolver: A (batch, N, N) FP64 input (destroyed),
+// E (batch, N) ascending, U (batch, N, N) eigenvectors in columns (may be
+// null).  precision: 0 = FP64, 1 = FP32 solve (U32 out, FP32 values) used by
+// the mixed path.
+size_t eig_workspace_bytes(int N, int64_t batch, int precision);
+int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
+                size_t work_bytes, int* status_d);
+
+// Spin-current dressing J = 1/2 {S, V} (in place through scratch).
+int spin_dress(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, zc* V, int64_t ldV,
+               zc* scratch);
+
+// Rotation into the eigenbasis + band-resolved Berry curvature:
+// Omega (batch, N) from U (batch, N, N), Vx/Vy (batch strided), E.
+int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* Vx, const zc* Vy,
+                 int64_t ldV, const double* E, double eta, double* Omega, zc* scratch);
+
+// Occupation-weighted sums: per k and per mu -> S (batch, nmu).
+int occupation_sums(cudaStream_t st, int N, int64_t batch, const double* Omega, const double* E,
+                    int nmu, const double* mu_d, double width, double* S);
+
+// Deterministic compensated column sums of S (nk, nmu) -> out (nmu), added
+// to a running (sum, compensation) pair held in acc (2*nmu).
+int kahan_column_sums(cudaStream_t st, int64_t nk, int nmu, const double* S, double* acc);
+
+// ------------------------------------------------------------- mixed path --
+int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U,
+                     void* work, size_t work_bytes, int* status_d, int64_t* clusters_d);
+size_t mixed_workspace_bytes(int N, int64_t batch);
+
+}  // namespace tbg
