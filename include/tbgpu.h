@@ -162,11 +162,41 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh,
                           double T, double eta, int spin, int precision,
                           double* sigma_out, tbg_report* report);
 
+/* Unnormalised Direct-integration sums over the k-points of the uniform mesh
+ * kmesh[dim] with flat indices [k_begin, k_begin + k_count) in gen_kmesh order:
+ *   sums_out[j] = sum_k sum_n Omega_n f(E_n, mu_j).
+ * The conductivity is the sum over disjoint ranges covering the mesh, divided
+ * by nk and det(lat).  This splits one mesh across calls or devices; the
+ * reference computes the same sum inside hall_conductivity
+ * (src/response/linear/mod.rs:204-223) over the whole mesh at once. */
+int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begin,
+                        int64_t k_count, const double* dirs2, int64_t nmu,
+                        const double* mu, double T, double eta, int spin,
+                        int precision, double* sums_out, tbg_report* report);
+
 /* ------------------------------------------------------------- utility --- */
+
+/* Measured FMA throughput of this GPU's FP64 and FP32 pipes (TFLOP/s), from a
+ * short register-resident FMA loop.  A measurement aid for roofline
+ * denominators; no reference counterpart. */
+int tbg_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
 
 /* Copy the calling thread's last error message into buf (always NUL-terminated).
  * Returns the status of that error. */
 int tbg_last_error(char* buf, size_t len);
+
+/* Select the CUDA device used by subsequent calls from the calling thread
+ * (models remember the device they were created on). */
+int tbg_set_device(int device);
+
+/* Per-kernel device timing (measurement aid; no reference counterpart).
+ * While enabled, every kernel family the library launches is bracketed by
+ * CUDA events on the stream it is launched on; durations accumulate per
+ * family.  tbg_kernel_timing_read copies up to max_entries records
+ * (names: max_entries x 64 chars, NUL-terminated) and returns how many. */
+int tbg_kernel_timing_enable(int enable);
+int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms,
+                           int max_entries, int reset);
 
 /* Library version string, e.g. "tbgpu 0.1.0 sm_103a". */
 const char* tbg_version(void);

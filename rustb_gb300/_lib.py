@@ -68,6 +68,15 @@ SIGNATURES = [
     ("tbg_hall_conductivity", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p, ctypes.c_int64,
                                              _c_double_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_int, _c_double_p, ctypes.POINTER(TbgReport)]),
+    ("tbg_hall_sums_range", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, ctypes.c_int64, ctypes.c_int64,
+                                           _c_double_p, ctypes.c_int64, _c_double_p, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, ctypes.c_int, _c_double_p,
+                                           ctypes.POINTER(TbgReport)]),
+    ("tbg_measure_fma_peaks", ctypes.c_int, [_c_double_p, _c_double_p]),
+    ("tbg_set_device", ctypes.c_int, [ctypes.c_int]),
+    ("tbg_kernel_timing_enable", ctypes.c_int, [ctypes.c_int]),
+    ("tbg_kernel_timing_read", ctypes.c_int, [ctypes.c_char_p, _c_int64_p, _c_double_p, ctypes.c_int,
+                                              ctypes.c_int]),
     ("tbg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     ("tbg_version", ctypes.c_char_p, []),
     ("tbg_kernel_launch_count", ctypes.c_int64, [ctypes.c_int]),
@@ -132,3 +141,20 @@ def as_c128_view(a) -> np.ndarray:
     """complex128 array as a contiguous float64 view (re, im interleaved)."""
     a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
     return a.view(np.float64)
+
+
+def kernel_timing(reset: bool = True, lib=None) -> dict:
+    """{kernel family: (launches, total_ms)} accumulated while timing is enabled."""
+    lib = lib or load()
+    n = 64
+    names = ctypes.create_string_buffer(64 * n)
+    launches = np.zeros(n, dtype=np.int64)
+    ms = np.zeros(n, dtype=np.float64)
+    cnt = lib.tbg_kernel_timing_read(names, launches.ctypes.data_as(_c_int64_p), ms.ctypes.data_as(_c_double_p),
+                                     n, int(reset))
+    out = {}
+    raw = names.raw
+    for i in range(cnt):
+        name = raw[64 * i:64 * (i + 1)].split(b"\0", 1)[0].decode()
+        out[name] = (int(launches[i]), float(ms[i]))
+    return out

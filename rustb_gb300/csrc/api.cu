@@ -90,12 +90,14 @@ struct Ctx {
     int sync(const char* where) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess && rc == TBG_OK) rc = cuda_error(e, where);
+        timing_flush();
         return rc;
     }
     ~Ctx() {
         if (st) {
             for (void* p : bufs) cudaFreeAsync(p, st);
             cudaStreamSynchronize(st);
+            timing_flush();
             cudaStreamDestroy(st);
         }
     }
@@ -598,9 +600,9 @@ int tbg_occupied_berry_curvature(const tbg_model* m, int64_t nk, const double* k
     return berry_common(m, nk, k, dirs2, spin, eta, precision, nullptr, nullptr, 1, &mu, T, out);
 }
 
-int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double* dirs2, int64_t nmu,
-                          const double* mu, double T, double eta, int spin, int precision, double* sigma_out,
-                          tbg_report* report) {
+static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, int64_t k_count, bool whole,
+                     const double* dirs2, int64_t nmu, const double* mu, double T, double eta, int spin,
+                     int precision, double* out, tbg_report* report) {
     int rc = check_model(m);
     if (rc) return rc;
     const ModelDev& M = m->d;
@@ -610,6 +612,12 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     for (int d = 0; d < M.dim; ++d) {
         if (kmesh[d] <= 0) return set_error(TBG_E_INVALID_KMESH, "Invalid k-point mesh dimensions");
         nk *= kmesh[d];
+    }
+    if (whole) {
+        k_begin = 0;
+        k_count = nk;
+    } else if (k_begin < 0 || k_count < 0 || k_begin + k_count > nk) {
+        return set_error(TBG_E_INVALID_ARGUMENT, "k-range outside the mesh");
     }
     if ((rc = check_dirs(dirs2, 2, M.dim, 2))) return rc;
     if (nmu < 1 || !mu)
@@ -623,9 +631,9 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     if ((rc = check_spin(m, spin))) return rc;
     if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
         return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
-    if (!sigma_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    if (!out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
     const double det = lattice_det(M.lat, M.dim);
-    if (det == 0.0 || !std::isfinite(det))
+    if (whole && (det == 0.0 || !std::isfinite(det)))
         return set_error(TBG_E_LINALG, "Linear algebra operation failed: singular lattice");
     const int N = (int)M.nsta;
     const int64_t NN = (int64_t)N * N;
@@ -640,7 +648,7 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
-    J.chunk = choose_chunk(nk, sizeof(zc) * NN * 5 + 64 * N + 8 * nmu);
+    J.chunk = choose_chunk(std::max<int64_t>(k_count, 1), sizeof(zc) * NN * 5 + 64 * N + 8 * nmu);
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = ctx.alloc<double>(nmu);
@@ -655,9 +663,9 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
     const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
-    for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
-        const int64_t nkc = std::min(J.chunk, nk - c0);
-        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, M.dim, n0, n1, n2, J.k_d);
+    for (int64_t c0 = 0; c0 < k_count; c0 += J.chunk) {
+        const int64_t nkc = std::min(J.chunk, k_count - c0);
+        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(k_begin + c0, nkc, M.dim, n0, n1, n2, J.k_d);
         TBG_LAUNCHED("kmesh_kernel");
         if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
         if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
@@ -670,11 +678,14 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     cudaEventRecord(ev1, ctx.st);
     if (ctx.sync("tbg_hall_conductivity")) return ctx.rc;
     if ((rc = check_status(J.status_d, ctx.st))) return rc;
-    for (int64_t j = 0; j < nmu; ++j) sigma_out[j] = (acc_h[2 * j] - acc_h[2 * j + 1]) / (double)nk / det;
+    for (int64_t j = 0; j < nmu; ++j) {
+        const double s = acc_h[2 * j] - acc_h[2 * j + 1];
+        out[j] = whole ? s / (double)nk / det : s;
+    }
     if (report) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev0, ev1);
-        report->nk = nk;
+        report->nk = k_count;
         report->nsta = N;
         report->precision = precision;
         report->fourier_mode = 0;
@@ -686,6 +697,19 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     return TBG_OK;
+}
+
+int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh, const double* dirs2, int64_t nmu,
+                          const double* mu, double T, double eta, int spin, int precision, double* sigma_out,
+                          tbg_report* report) {
+    return hall_impl(m, kmesh, 0, 0, true, dirs2, nmu, mu, T, eta, spin, precision, sigma_out, report);
+}
+
+int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, int64_t k_count,
+                        const double* dirs2, int64_t nmu, const double* mu, double T, double eta, int spin,
+                        int precision, double* sums_out, tbg_report* report) {
+    return hall_impl(m, kmesh, k_begin, k_count, false, dirs2, nmu, mu, T, eta, spin, precision, sums_out,
+                     report);
 }
 
 }  // extern "C"

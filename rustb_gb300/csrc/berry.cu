@@ -209,6 +209,7 @@ inline unsigned grid_for(int64_t total, int threads) {
 
 int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* A, int64_t sA, const zc* B,
                   int64_t sB, zc* C, int64_t sC) {
+    KTimer kt(st, "zgemm_batched_kernel");
     for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
         const int64_t nb = std::min<int64_t>(65535, batch - b0);
         dim3 grid((N + 63) / 64, (N + 63) / 64, (unsigned)nb);
@@ -223,6 +224,7 @@ int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* 
 
 int spin_dress(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, zc* V, int64_t ldV, zc* scratch) {
     const int64_t NN = (int64_t)N * N;
+    KTimer kt(st, "spin_dress_kernel");
     spin_dress_kernel<<<grid_for(batch * NN, 256), 256, 0, st>>>(N, (int)norb, batch, spin, V, ldV, scratch);
     TBG_LAUNCHED("spin_dress_kernel");
     // copy J back into the V_0 slots
@@ -246,6 +248,7 @@ int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* V
     if (rc) return rc;
     rc = zgemm_batched(st, N, batch, true, U, NN, scratch, NN, Vym, ldV);
     if (rc) return rc;
+    KTimer kt(st, "berry_kernel");
     berry_kernel<<<grid_for(batch * N * 32, 256), 256, 0, st>>>(N, batch, Vx, Vy, ldV, E, eta * eta, Omega);
     TBG_LAUNCHED("berry_kernel");
     return TBG_OK;
@@ -253,6 +256,7 @@ int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* V
 
 int berry_from_bands(cudaStream_t st, int N, int64_t batch, const zc* Bx, const zc* By, int64_t ldB,
                      const double* E, double eta, double* Omega) {
+    KTimer kt(st, "berry_kernel");
     berry_kernel<<<grid_for(batch * N * 32, 256), 256, 0, st>>>(N, batch, Bx, By, ldB, E, eta * eta, Omega);
     TBG_LAUNCHED("berry_kernel");
     return TBG_OK;
@@ -260,12 +264,14 @@ int berry_from_bands(cudaStream_t st, int N, int64_t batch, const zc* Bx, const 
 
 int occupation_sums(cudaStream_t st, int N, int64_t batch, const double* Omega, const double* E, int nmu,
                     const double* mu_d, double width, double* S) {
+    KTimer kt(st, "occupation_kernel");
     occupation_kernel<<<grid_for(batch * nmu, 256), 256, 0, st>>>(N, batch, Omega, E, nmu, mu_d, width, S);
     TBG_LAUNCHED("occupation_kernel");
     return TBG_OK;
 }
 
 int kahan_column_sums(cudaStream_t st, int64_t nk, int nmu, const double* S, double* acc) {
+    KTimer kt(st, "kahan_kernel");
     kahan_kernel<<<nmu, 256, 0, st>>>(nk, nmu, S, acc);
     TBG_LAUNCHED("kahan_kernel");
     return TBG_OK;

@@ -326,6 +326,14 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
             sh.e[N - 1] = 0;
         }
         __syncthreads();
+        // deflation: off-diagonals below eps (|d_i| + |d_i+1|) are set to zero,
+        // as QR-type solvers do, so decoupled 1x1 blocks give d_i exactly
+        for (int i = tid; i < N; i += nthr) {
+            T ei = sh.e[i];
+            if (i < N - 1 && fabs(ei) <= Lim<T>::eps() * (fabs(sh.d[i]) + fabs(sh.d[i + 1]))) ei = 0;
+            sh.e[i] = ei;
+        }
+        __syncthreads();
         for (int i = tid; i < N; i += nthr) sh.e2[i] = sh.e[i] * sh.e[i];
         __syncthreads();
 
@@ -384,7 +392,16 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
                 else
                     c = mid;
             }
-            sh.lam[i] = T(0.5) * (a + c);
+            T lam = T(0.5) * (a + c);
+            // an isolated diagonal entry inside the final bracket is the exact eigenvalue
+            for (int j = 0; j < N; ++j) {
+                const bool iso = (j == 0 || sh.e[j - 1] == T(0)) && (j == N - 1 || sh.e[j] == T(0));
+                if (iso && sh.d[j] >= a && sh.d[j] <= c) {
+                    lam = sh.d[j];
+                    break;
+                }
+            }
+            sh.lam[i] = lam;
         }
         __syncthreads();
         if (Eout) {
@@ -520,6 +537,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     }
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
+    KTimer kt(st, name);
     kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d);
     TBG_LAUNCHED(name);
     return TBG_OK;

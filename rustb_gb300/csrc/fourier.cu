@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "tbgpu_internal.cuh"
@@ -192,6 +193,7 @@ int launch_gemm(cudaStream_t st, int64_t nk, int nR, int ldph, int N, const zc* 
                 const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH,
                 zc* V, int64_t ldV) {
     const int64_t NN = (int64_t)N * N;
+    KTimer kt(st, "fourier_gemm_kernel");
     for (int64_t kb = 0; kb < nk; kb += (int64_t)TK * 65535) {
         const int64_t nkb = std::min<int64_t>(nk - kb, (int64_t)TK * 65535);
         dim3 grid((unsigned)((NN + TE - 1) / TE), (unsigned)((nkb + TK - 1) / TK));
@@ -301,6 +303,7 @@ int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double*
     TBG_CUDA(cudaMallocAsync(&taup, sizeof(double) * npc * N, st));
     int rc = TBG_OK;
     {
+        KTimer kt(st, "phases_kernel");
         const int64_t total = nk * (int64_t)(nR + N);
         const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 65535 * 8);
         phases_kernel<<<blocks, 256, 0, st>>>(nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph, orbph);
@@ -335,6 +338,7 @@ int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double*
 int rmatrix_term(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge, int nproj,
                  const double* dirs_d, const zc* H, zc* V, zc* /*scratch*/) {
     if (m.n_rmat <= 0 || nk <= 0 || nproj <= 0) return TBG_OK;
+    KTimer kt(st, "rmatrix_term");
     const int N = (int)m.nsta, nR = (int)m.nR;
     const int64_t NN = (int64_t)N * N;
     zc *ph = nullptr, *orbph = nullptr, *tab = nullptr, *A = nullptr;

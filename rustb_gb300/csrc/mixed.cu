@@ -29,7 +29,7 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 
 namespace {
 
-constexpr int kMaxCluster = 16;
+constexpr int kMaxCluster = 8;
 
 __global__ void widen_kernel(int64_t n, const cc* __restrict__ a, zc* __restrict__ b) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -312,8 +312,11 @@ int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double*
     if ((rc = zgemm_batched(st, N, batch, false, H, NN, U, NN, HX, NN))) return rc;
     if ((rc = zgemm_batched(st, N, batch, true, U, NN, HX, NN, S, NN))) return rc;
     const size_t smem = sizeof(double) * N + sizeof(int) * N;
+    {
+    KTimer kt(st, "oa_kernel");
     oa_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, R, S, E, clusters_d);
     TBG_LAUNCHED("oa_kernel");
+    }
     // X <- X + X F   (HX reused as the product buffer)
     if ((rc = zgemm_batched(st, N, batch, false, U, NN, R, NN, HX, NN))) return rc;
     add_kernel<<<blocks(batch * NN), 256, 0, st>>>(batch * NN, U, HX);

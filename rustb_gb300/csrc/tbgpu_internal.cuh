@@ -94,6 +94,18 @@ int set_error(int code, const std::string& msg);
 int cuda_error(cudaError_t e, const char* where);
 void count_launch(int n = 1);
 
+// Scoped per-kernel timer: records CUDA events on `st` around the kernels
+// launched in its scope when timing is enabled (tbg_kernel_timing_enable).
+bool timing_enabled();
+struct KTimer {
+    cudaStream_t st;
+    const char* name;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KTimer(cudaStream_t s, const char* n);
+    ~KTimer();
+};
+void timing_flush();  // resolve recorded event pairs (after a stream sync)
+
 #define TBG_CUDA(call)                                   \
     do {                                                 \
         cudaError_t _e = (call);                         \
