@@ -148,43 +148,24 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
     return 24.0 * nR * N * N + 46.0 * N ** 3
 
 
-def kernel_roofline(timing: dict, N: int, nR: int, batch_total: int, peaks: dict) -> tuple[str, dict]:
-    """Roofline entry for the kernel family with the largest device time."""
+def kernel_roofline(timing: dict, peaks: dict) -> dict | None:
+    """Roofline entry for the kernel family with the largest device time:
+    achieved = its algorithmic flops / its device time (CUDA events around
+    every launch, on the launching stream)."""
     if not timing:
-        return None, None
-    name, (launches, ms) = max(timing.items(), key=lambda kv: kv[1][1])
-    avg_s = ms / 1e3 / max(launches, 1)
-    per_launch_k = batch_total / max(launches, 1)
-    out = {"kernel": name, "launches": launches, "avg_ms": ms / max(launches, 1)}
-    if name.startswith("zgemm"):
-        # 8 N^3 flops per complex N x N GEMM; launches are per batch of k-points
-        flops = 8.0 * N ** 3 * (batch_total * 4 / max(launches, 1))
-        out.update(bound="fp64", unit="TFLOP/s", achieved=flops / avg_s / 1e12, peak=peaks["fp64_tflops"],
-                   peak_source="tbg_measure_fma_peaks (FP64 FMA loop on this GPU)")
-    elif name.startswith("fourier_gemm"):
-        flops = 24.0 * nR * N * N * per_launch_k
-        out.update(bound="fp64", unit="TFLOP/s", achieved=flops / avg_s / 1e12, peak=peaks["fp64_tflops"],
-                   peak_source="tbg_measure_fma_peaks (FP64 FMA loop on this GPU)")
-    elif name.startswith("heev_kernel<float"):
-        flops = 14.0 * N ** 3 * per_launch_k
-        out.update(bound="fp32", unit="TFLOP/s", achieved=flops / avg_s / 1e12, peak=peaks["fp32_tflops"],
-                   peak_source="tbg_measure_fma_peaks (FP32 FMA loop on this GPU)")
-    elif name.startswith("heev_kernel"):
-        flops = 14.0 * N ** 3 * per_launch_k
-        out.update(bound="fp64", unit="TFLOP/s", achieved=flops / avg_s / 1e12, peak=peaks["fp64_tflops"],
-                   peak_source="tbg_measure_fma_peaks (FP64 FMA loop on this GPU)")
+        return None
+    name, (launches, ms, work) = max(timing.items(), key=lambda kv: kv[1][1])
+    if name.startswith("heev_kernel<float") or name.startswith("fp32"):
+        bound, peak, src = "fp32", peaks["fp32_tflops"], "FP32 FMA loop on this GPU (tbg_measure_fma_peaks)"
     elif name.startswith("ozaki"):
-        flops = out_flops = 8.0 * N ** 3 * per_launch_k
-        out.update(bound="tensor", unit="TFLOP/s", achieved=out_flops / avg_s / 1e12, peak=peaks.get("bf16_tflops"),
-                   peak_source="MEASURED_PEAKS.json bf16_tflops (burst)")
+        bound, peak, src = "tensor", peaks.get("bf16_tflops"), "MEASURED_PEAKS.json bf16_tflops (burst)"
     else:
-        out.update(bound="unknown", unit="TFLOP/s", achieved=None, peak=None, peak_source=None)
-    if out.get("achieved") is not None and out.get("peak"):
-        out["frac"] = out["achieved"] / out["peak"]
-    else:
-        out["frac"] = None
-    out["traffic"] = None
-    return name, out
+        bound, peak, src = "fp64", peaks["fp64_tflops"], "FP64 FMA loop on this GPU (tbg_measure_fma_peaks)"
+    achieved = work / (ms / 1e3) / 1e12 if ms > 0 and work > 0 else None
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+            "kernel": name, "launches": launches, "avg_launch_ms": ms / max(launches, 1),
+            "peak_source": src}
 
 
 def measured_peaks(lib) -> dict:
@@ -343,13 +324,7 @@ def main():
         fp64_val = fs / t_fp64
         acc = {"ahc_partial_rel_err_mixed_vs_fp64": float(abs(mixed_sum[0] - plain_sum[0]) / abs(plain_sum[0])),
                "sample": f"flat k indices [0, {fs}) of the 64^3 mesh"}
-        name, roof = kernel_roofline(timing, N, nR, done, peaks)
-        roof_line = None
-        if roof:
-            roof_line = {"bound": roof["bound"], "achieved": roof["achieved"], "peak": roof["peak"],
-                         "unit": roof["unit"], "frac": roof["frac"], "traffic": roof["traffic"],
-                         "kernel": roof["kernel"], "peak_source": roof["peak_source"],
-                         "avg_launch_ms": roof["avg_ms"]}
+        roof_line = kernel_roofline(timing, peaks)
         cpu = None
         if not args.no_cpu_baseline:
             from oracle import build_port
@@ -378,8 +353,8 @@ def main():
                            "mixed_speedup": value / fp64_val},
             "accuracy": acc,
             "roofline": roof_line,
-            "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in sorted(
-                timing.items(), key=lambda kv: -kv[1][1])},
+            "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1], "tflops": (v[2] / v[1] / 1e9 if v[1] else None)}
+                                for k, v in sorted(timing.items(), key=lambda kv: -kv[1][1])},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "k-pts/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(sums.nbytes), "steps": e2e_steps,

@@ -192,11 +192,12 @@ int tbg_set_device(int device);
 /* Per-kernel device timing (measurement aid; no reference counterpart).
  * While enabled, every kernel family the library launches is bracketed by
  * CUDA events on the stream it is launched on; durations accumulate per
- * family.  tbg_kernel_timing_read copies up to max_entries records
- * (names: max_entries x 64 chars, NUL-terminated) and returns how many. */
+ * family together with the algorithmic flops of those launches.
+ * tbg_kernel_timing_read copies up to max_entries records (names:
+ * max_entries x 64 chars, NUL-terminated) and returns how many. */
 int tbg_kernel_timing_enable(int enable);
 int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms,
-                           int max_entries, int reset);
+                           double* total_flops, int max_entries, int reset);
 
 /* Library version string, e.g. "tbgpu 0.1.0 sm_103a". */
 const char* tbg_version(void);

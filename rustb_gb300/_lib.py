@@ -75,8 +75,8 @@ SIGNATURES = [
     ("tbg_measure_fma_peaks", ctypes.c_int, [_c_double_p, _c_double_p]),
     ("tbg_set_device", ctypes.c_int, [ctypes.c_int]),
     ("tbg_kernel_timing_enable", ctypes.c_int, [ctypes.c_int]),
-    ("tbg_kernel_timing_read", ctypes.c_int, [ctypes.c_char_p, _c_int64_p, _c_double_p, ctypes.c_int,
-                                              ctypes.c_int]),
+    ("tbg_kernel_timing_read", ctypes.c_int, [ctypes.c_char_p, _c_int64_p, _c_double_p, _c_double_p,
+                                              ctypes.c_int, ctypes.c_int]),
     ("tbg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     ("tbg_version", ctypes.c_char_p, []),
     ("tbg_kernel_launch_count", ctypes.c_int64, [ctypes.c_int]),
@@ -144,17 +144,18 @@ def as_c128_view(a) -> np.ndarray:
 
 
 def kernel_timing(reset: bool = True, lib=None) -> dict:
-    """{kernel family: (launches, total_ms)} accumulated while timing is enabled."""
+    """{kernel family: (launches, total_ms, total_flops)} accumulated while timing is enabled."""
     lib = lib or load()
     n = 64
     names = ctypes.create_string_buffer(64 * n)
     launches = np.zeros(n, dtype=np.int64)
     ms = np.zeros(n, dtype=np.float64)
+    work = np.zeros(n, dtype=np.float64)
     cnt = lib.tbg_kernel_timing_read(names, launches.ctypes.data_as(_c_int64_p), ms.ctypes.data_as(_c_double_p),
-                                     n, int(reset))
+                                     work.ctypes.data_as(_c_double_p), n, int(reset))
     out = {}
     raw = names.raw
     for i in range(cnt):
         name = raw[64 * i:64 * (i + 1)].split(b"\0", 1)[0].decode()
-        out[name] = (int(launches[i]), float(ms[i]))
+        out[name] = (int(launches[i]), float(ms[i]), float(work[i]))
     return out

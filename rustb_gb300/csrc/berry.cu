@@ -209,7 +209,7 @@ inline unsigned grid_for(int64_t total, int threads) {
 
 int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* A, int64_t sA, const zc* B,
                   int64_t sB, zc* C, int64_t sC) {
-    KTimer kt(st, "zgemm_batched_kernel");
+    KTimer kt(st, "zgemm_batched_kernel", 8.0 * (double)N * N * N * batch);
     for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
         const int64_t nb = std::min<int64_t>(65535, batch - b0);
         dim3 grid((N + 63) / 64, (N + 63) / 64, (unsigned)nb);

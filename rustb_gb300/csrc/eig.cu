@@ -537,7 +537,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     }
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
-    KTimer kt(st, name);
+    KTimer kt(st, name, 14.0 * (double)N * N * N * batch);
     kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d);
     TBG_LAUNCHED(name);
     return TBG_OK;

@@ -193,7 +193,7 @@ int launch_gemm(cudaStream_t st, int64_t nk, int nR, int ldph, int N, const zc* 
                 const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH,
                 zc* V, int64_t ldV) {
     const int64_t NN = (int64_t)N * N;
-    KTimer kt(st, "fourier_gemm_kernel");
+    KTimer kt(st, "fourier_gemm_kernel", 8.0 * nR * (double)NN * nk * ((H ? 1 : 0) + NP));
     for (int64_t kb = 0; kb < nk; kb += (int64_t)TK * 65535) {
         const int64_t nkb = std::min<int64_t>(nk - kb, (int64_t)TK * 65535);
         dim3 grid((unsigned)((NN + TE - 1) / TE), (unsigned)((nkb + TK - 1) / TK));

@@ -100,8 +100,9 @@ bool timing_enabled();
 struct KTimer {
     cudaStream_t st;
     const char* name;
+    double work;  // algorithmic flops of the launches in scope
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    KTimer(cudaStream_t s, const char* n);
+    KTimer(cudaStream_t s, const char* n, double work_flops = 0.0);
     ~KTimer();
 };
 void timing_flush();  // resolve recorded event pairs (after a stream sync)

@@ -19,10 +19,12 @@ std::mutex g_mu;
 struct Acc {
     int64_t launches = 0;
     double ms = 0.0;
+    double work = 0.0;
 };
 std::map<std::string, Acc> g_table;
 struct Pending {
     std::string name;
+    double work;
     cudaEvent_t e0, e1;
 };
 thread_local std::vector<Pending> t_pending;
@@ -31,7 +33,7 @@ thread_local std::vector<Pending> t_pending;
 
 bool timing_enabled() { return g_enabled.load(std::memory_order_relaxed); }
 
-KTimer::KTimer(cudaStream_t s, const char* n) : st(s), name(n) {
+KTimer::KTimer(cudaStream_t s, const char* n, double work_flops) : st(s), name(n), work(work_flops) {
     if (!timing_enabled()) return;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
         e0 = e1 = nullptr;
@@ -43,7 +45,7 @@ KTimer::KTimer(cudaStream_t s, const char* n) : st(s), name(n) {
 KTimer::~KTimer() {
     if (!e0) return;
     cudaEventRecord(e1, st);
-    t_pending.push_back({name, e0, e1});
+    t_pending.push_back({name, work, e0, e1});
 }
 
 void timing_flush() {
@@ -55,6 +57,7 @@ void timing_flush() {
             Acc& a = g_table[p.name];
             a.launches += 1;
             a.ms += ms;
+            a.work += p.work;
         }
         cudaEventDestroy(p.e0);
         cudaEventDestroy(p.e1);
@@ -69,7 +72,8 @@ extern "C" int tbg_kernel_timing_enable(int enable) {
     return TBG_OK;
 }
 
-extern "C" int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms, int max_entries, int reset) {
+extern "C" int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms, double* total_work,
+                                      int max_entries, int reset) {
     tbg::timing_flush();
     std::lock_guard<std::mutex> lk(tbg::g_mu);
     int i = 0;
@@ -81,6 +85,7 @@ extern "C" int tbg_kernel_timing_read(char* names, int64_t* launches, double* to
         }
         if (launches) launches[i] = kv.second.launches;
         if (total_ms) total_ms[i] = kv.second.ms;
+        if (total_work) total_work[i] = kv.second.work;
         ++i;
     }
     if (reset) tbg::g_table.clear();
