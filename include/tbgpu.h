@@ -174,6 +174,32 @@ int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begi
                         const double* mu, double T, double eta, int spin,
                         int precision, double* sums_out, tbg_report* report);
 
+/* ------------------------------------------------ no-allocation variant --- */
+
+/* Size of the fixed device scratch array used by tbg_eigvalsh_noalloc. */
+#define TBG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* Band energies (ascending, FP64) of nk device-resident Hermitian matrices,
+ * without allocating any device memory.  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc -- code that hands all device
+ * memory to its own allocator or pool, or a latency-critical loop in which
+ * cudaMalloc/cudaFree would synchronise the device.
+ *
+ * H_d (nk, n, n) complex FP64 and E_d (nk, n) FP64 are DEVICE pointers owned
+ * by the caller; H_d is not modified.  The solver works on a copy of H_d in a
+ * fixed static device array of TBG_NOALLOC_SCRATCH_BYTES that every GPU that
+ * loads this library holds until the process exits; a call needs
+ * nk * n * n * 16 bytes of it and is rejected with TBG_E_UNSUPPORTED beyond
+ * that.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream) and
+ * the call returns without waiting.  All calls share the one array: calls
+ * whose work overlaps on the GPU (different streams, no ordering between them)
+ * race on it; calls on one stream are ordered and safe.  Each call overwrites
+ * the part of the array it uses, so nothing in it has to start at zero. */
+int tbg_eigvalsh_noalloc(int64_t n, int64_t nk, const double* H_d, double* E_d,
+                         void* stream);
+
 /* ------------------------------------------------------------- utility --- */
 
 /* Measured FMA throughput of this GPU's FP64 and FP32 pipes (TFLOP/s), from a

@@ -77,6 +77,8 @@ SIGNATURES = [
     ("tbg_kernel_timing_enable", ctypes.c_int, [ctypes.c_int]),
     ("tbg_kernel_timing_read", ctypes.c_int, [ctypes.c_char_p, _c_int64_p, _c_double_p, _c_double_p,
                                               ctypes.c_int, ctypes.c_int]),
+    ("tbg_eigvalsh_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
     ("tbg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     ("tbg_version", ctypes.c_char_p, []),
     ("tbg_kernel_launch_count", ctypes.c_int64, [ctypes.c_int]),

@@ -560,6 +560,27 @@ int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, 
                                               "heev_kernel<double>");
 }
 
+// Eigenvalues only, FP64, of `batch` matrices held in caller-provided device
+// memory `A` (destroyed).  Launches the solver directly: no allocation, no
+// events, nothing but the kernel on `st`.
+int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double* E) {
+    if (batch <= 0) return TBG_OK;
+    const size_t smem = eig_smem_bytes<double>(N, false, 16, 16);
+    auto kern = heev_kernel<double, false, 16, 16>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
+    int dev = 0, nsm = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = (N <= 32) ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
+    if (e != cudaSuccess || perSM < 1) perSM = 1;
+    const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, E, nullptr, nullptr, nullptr);
+    TBG_LAUNCHED("heev_kernel<double> (static scratch)");
+    return TBG_OK;
+}
+
 // FP32 driver (mixed path): H preserved, U complex<float>.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
                     size_t work_bytes, int* status_d) {
