@@ -255,7 +255,7 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
     J.work = nullptr;
     J.work_bytes = 0;
     if (J.precision == TBG_PREC_MIXED) {
-        J.work_bytes = std::max(mixed_workspace_bytes(N, c), eig_workspace_bytes(N, c, 1));
+        J.work_bytes = mixed_berry_workspace_bytes(N, c);
         J.work = J.work_bytes ? ctx.alloc<unsigned char>(J.work_bytes) : nullptr;
     }
     if (ctx.rc == TBG_OK) {
@@ -279,11 +279,10 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
         rc = spin_dress(ctx.st, N, m.norb, nkc, J.spin, J.V, 2 * NN, J.scratch);
         if (rc) return rc;
     }
-    if (J.precision == TBG_PREC_MIXED) {
-        rc = mixed_eig_refine(ctx.st, N, nkc, J.H, J.E, J.U, J.work, J.work_bytes, J.status_d, clusters_d);
-    } else {
-        rc = eig_batched(ctx.st, N, nkc, J.H, J.E, J.U, nullptr, 0, J.status_d);
-    }
+    if (J.precision == TBG_PREC_MIXED)
+        return mixed_berry(ctx.st, N, nkc, J.H, J.V, J.V + NN, 2 * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
+                           J.status_d, clusters_d);
+    rc = eig_batched(ctx.st, N, nkc, J.H, J.E, J.U, nullptr, 0, J.status_d);
     if (rc) return rc;
     return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch);
 }
@@ -557,7 +556,7 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
-    J.chunk = choose_chunk(nk, sizeof(zc) * NN * 5 + 64 * N);
+    J.chunk = choose_chunk(nk, sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 12 : 5) + 64 * N);
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = (nmu > 0) ? ctx.alloc<double>(nmu) : nullptr;
@@ -648,7 +647,8 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
-    J.chunk = choose_chunk(std::max<int64_t>(k_count, 1), sizeof(zc) * NN * 5 + 64 * N + 8 * nmu);
+    J.chunk = choose_chunk(std::max<int64_t>(k_count, 1),
+                           sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 12 : 5) + 64 * N + 8 * nmu);
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = ctx.alloc<double>(nmu);

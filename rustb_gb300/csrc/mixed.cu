@@ -327,3 +327,195 @@ int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double*
 }
 
 }  // namespace tbg
+
+// ===========================================================================
+// Mixed path on the tensor cores: FP32 eigensolve, Ogita-Aishima refinement
+// and the velocity rotation with the exact-slice BF16 GEMM.
+// ===========================================================================
+namespace tbg {
+
+int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
+                int64_t sC, int* EA, int* EB);
+size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
+
+namespace {
+
+enum { F64 = 0, F32 = 1, PAIR = 2 };
+
+// pair -> FP64 complex, optionally as I - X (for R = I - X^H X)
+__global__ void pairs_to_z_kernel(int N, int64_t batch, const float4* __restrict__ in, zc* __restrict__ out,
+                                  int eye_minus) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < batch * NN;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = in[i];
+        double re = (double)v.x + (double)v.y, im = (double)v.z + (double)v.w;
+        if (eye_minus) {
+            const int e = (int)(i % NN);
+            re = ((e / N == e % N) ? 1.0 : 0.0) - re;
+            im = -im;
+        }
+        out[i] = mk(re, im);
+    }
+}
+
+// X' = X + X F as a float pair: hi = X (exact FP32 eigenvectors), lo = X F.
+__global__ void xprime_kernel(int64_t n, const cc* __restrict__ X, const float4* __restrict__ XF,
+                              float4* __restrict__ Xp) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const cc x = X[i];
+        const float4 f = XF[i];
+        Xp[i] = make_float4(x.re, f.x + f.y, x.im, f.z + f.w);
+    }
+}
+
+// Omega_n = sum_{m != n} -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2) from
+// float-pair band-basis velocities; one warp per row n.
+__global__ void berry_pairs_kernel(int N, int64_t batch, const float4* __restrict__ Bx, const float4* __restrict__ By,
+                                   const double* __restrict__ E, double eta2, double* __restrict__ Omega) {
+    const int lane = threadIdx.x & 31;
+    const int64_t NN = (int64_t)N * N;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = gw; w < batch * N; w += nw) {
+        const int64_t b = w / N;
+        const int n = (int)(w % N);
+        const float4* bx = Bx + b * NN + (int64_t)n * N;
+        const float4* by = By + b * NN;
+        const double* Eb = E + b * N;
+        const double en = Eb[n];
+        double s = 0.0;
+        for (int m = lane; m < N; m += 32) {
+            if (m == n) continue;
+            const float4 x = bx[m];
+            const float4 y = by[(int64_t)m * N + n];
+            const double xr = (double)x.x + (double)x.y, xi = (double)x.z + (double)x.w;
+            const double yr = (double)y.x + (double)y.y, yi = (double)y.z + (double)y.w;
+            const double im = xr * yi + xi * yr;
+            const double de = en - Eb[m];
+            s += -2.0 * im / (de * de + eta2);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) Omega[b * N + n] = s;
+    }
+}
+
+// Keep E ascending (with Omega) after refinement; a no-op when already sorted.
+__global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, double* __restrict__ Om) {
+    extern __shared__ double sm3[];
+    double* e = sm3;
+    double* o = sm3 + N;
+    __shared__ int s_sorted;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        if (threadIdx.x == 0) s_sorted = 1;
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            e[i] = E[b * N + i];
+            o[i] = Om[b * N + i];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < N - 1; i += blockDim.x)
+            if (e[i + 1] < e[i]) s_sorted = 0;
+        __syncthreads();
+        if (!s_sorted) {
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                int rank = 0;
+                for (int j = 0; j < N; ++j) rank += (e[j] < e[i]) || (e[j] == e[i] && j < i);
+                E[b * N + rank] = e[i];
+                Om[b * N + rank] = o[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+inline unsigned nblk(int64_t total) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152LL * 64));
+}
+
+}  // namespace
+
+size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
+    const size_t NN = (size_t)N * N;
+    // X (cc) + 5 pair buffers + R, S (zc) + exponents + FP32 solver workspace
+    return (size_t)batch * NN * (sizeof(cc) + 5 * sizeof(float4) + 2 * sizeof(zc)) +
+           ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) + 4096;
+}
+
+// H (FP64, preserved), Vx/Vy (FP64, stride ldV) -> E (refined, ascending), Omega.
+int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx, const zc* Vy, int64_t ldV,
+                double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
+                int64_t* clusters_d) {
+    if (batch <= 0) return TBG_OK;
+    const int64_t NN = (int64_t)N * N;
+    if (work_bytes < mixed_berry_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
+    unsigned char* p = static_cast<unsigned char*>(work);
+    auto take = [&](size_t bytes) {
+        void* q = p;
+        p += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    cc* X = static_cast<cc*>(take(sizeof(cc) * batch * NN));
+    float4* bA = static_cast<float4*>(take(sizeof(float4) * batch * NN));
+    float4* bB = static_cast<float4*>(take(sizeof(float4) * batch * NN));
+    float4* bC = static_cast<float4*>(take(sizeof(float4) * batch * NN));
+    float4* bD = static_cast<float4*>(take(sizeof(float4) * batch * NN));
+    float4* bE = static_cast<float4*>(take(sizeof(float4) * batch * NN));
+    zc* Rz = static_cast<zc*>(take(sizeof(zc) * batch * NN));
+    zc* Sz = static_cast<zc*>(take(sizeof(zc) * batch * NN));
+    int* EA = static_cast<int*>(take(ozaki_exp_bytes(batch, N, N)));
+    int* EB = EA + batch * N;
+    const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
+    void* eigw = take(eigw_bytes);
+    int rc;
+    // 1. FP32 eigenpairs
+    if ((rc = eig_batched_f32(st, N, batch, const_cast<zc*>(H), E, X, eigw, eigw_bytes, status_d))) return rc;
+    // 2. R = I - X^H X, S = X^H (H X)   (FP64-class, tensor cores)
+    if ((rc = ozaki_zgemm(st, true, true, F32, F32, batch, N, N, N, X, N, NN, X, N, NN, bA, N, NN, EA, EB))) return rc;
+    if ((rc = ozaki_zgemm(st, true, false, F64, F32, batch, N, N, N, H, N, NN, X, N, NN, bB, N, NN, EA, EB))) return rc;
+    if ((rc = ozaki_zgemm(st, true, true, F32, PAIR, batch, N, N, N, X, N, NN, bB, N, NN, bC, N, NN, EA, EB))) return rc;
+    {
+        KTimer kt(st, "pairs_to_z_kernel");
+        pairs_to_z_kernel<<<nblk(batch * NN), 256, 0, st>>>(N, batch, bA, Rz, 1);
+        pairs_to_z_kernel<<<nblk(batch * NN), 256, 0, st>>>(N, batch, bC, Sz, 0);
+        count_launch(2);
+    }
+    // 3. Ogita-Aishima update F (into Rz) and refined eigenvalues
+    {
+        KTimer kt(st, "oa_kernel");
+        const size_t smem = sizeof(double) * N + sizeof(int) * N;
+        oa_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, Rz, Sz, E, clusters_d);
+        TBG_LAUNCHED("oa_kernel");
+    }
+    // 4. X' = X + X F  (float pair: hi = X, lo = X F)
+    if ((rc = ozaki_zgemm(st, false, false, F32, F64, batch, N, N, N, X, N, NN, Rz, N, NN, bE, N, NN, EA, EB)))
+        return rc;
+    {
+        KTimer kt(st, "xprime_kernel");
+        xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, X, bE, bA);
+        TBG_LAUNCHED("xprime_kernel");
+    }
+    // 5. band-basis velocities B = X'^H V X'
+    if ((rc = ozaki_zgemm(st, true, false, F64, PAIR, batch, N, N, N, Vx, N, ldV, bA, N, NN, bB, N, NN, EA, EB)))
+        return rc;
+    if ((rc = ozaki_zgemm(st, true, false, F64, PAIR, batch, N, N, N, Vy, N, ldV, bA, N, NN, bC, N, NN, EA, EB)))
+        return rc;
+    if ((rc = ozaki_zgemm(st, true, true, PAIR, PAIR, batch, N, N, N, bA, N, NN, bB, N, NN, bD, N, NN, EA, EB)))
+        return rc;
+    if ((rc = ozaki_zgemm(st, true, true, PAIR, PAIR, batch, N, N, N, bA, N, NN, bC, N, NN, bE, N, NN, EA, EB)))
+        return rc;
+    // 6. Omega
+    {
+        KTimer kt(st, "berry_kernel");
+        berry_pairs_kernel<<<nblk(batch * N * 32), 256, 0, st>>>(N, batch, bD, bE, E, eta * eta, Om);
+        TBG_LAUNCHED("berry_pairs_kernel");
+    }
+    sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 2 * sizeof(double) * N, st>>>(N, batch, E,
+                                                                                                      Om);
+    TBG_LAUNCHED("sort_e_om_kernel");
+    return TBG_OK;
+}
+
+}  // namespace tbg

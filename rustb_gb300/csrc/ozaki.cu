@@ -1,0 +1,429 @@
+// Batched complex GEMM with FP64-class accuracy on the BF16 tensor cores.
+//
+//   C[b] (M x Nc) = op(A[b]) (M x K) . B[b] (K x Nc),   op = identity or ^H
+//
+// Exact-slice scheme (after Ozaki, Ogita, Oishi & Rump, "Error-free
+// transformations of matrix multiplication", 2012, restated for BF16):
+//   * every row i of op(A) is scaled by 2^-EA_i and every column j of B by
+//     2^-EB_j (powers of two, |x| < 2^E), so entries lie in (-1, 1);
+//   * each scaled entry is written with 42 fractional bits and cut into S
+//     signed digits of 7 bits by rounding: x = 2^-7 sum_s q_s 2^-7s with
+//     |q_0| <= 128 and |q_s| <= 64 (s >= 1); the slice q_s 2^-7s is exact in BF16;
+//   * slice products are summed by BF16 MMA with FP32 accumulation.  Pairs with
+//     s + t = 0, 1 and 2 each go to their own accumulator, whose partial sums
+//     stay below 2^24 units for K <= 256, so they are exact; the pairs with
+//     s + t in [3, LMAX] share a fourth accumulator (relative weight <= 2^-21);
+//   * the accumulators are combined into an unevaluated float pair (hi, lo) by
+//     error-free TwoSums and scaled by 2^(EA_i + EB_j - 14).
+// Complex operands use the real embedding
+//   [Re C | Im C] = [Re A | Im A] . [[Re B, Im B], [-Im B, Re B]].
+// The slicing works on the integer bits of the inputs (no FP64 arithmetic).
+//
+// Operand formats: complex double, complex float, or complex float pair
+// {re_hi, re_lo, im_hi, im_lo}.  The output is always a complex float pair.
+//
+// This version issues mma.sync.m16n8k16 (BF16 -> FP32) from ldmatrix-loaded
+// fragments.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "tbgpu_internal.cuh"
+
+namespace tbg {
+
+namespace {
+
+constexpr int OZ_TM = 64;      // output rows per CTA
+constexpr int OZ_TN = 64;      // complex output columns per CTA (128 real)
+constexpr int OZ_TK = 16;      // complex k per stage (32 real)
+constexpr int OZ_PAD = 40;     // bf16 per smem row (32 + 8 pad, 80 bytes)
+constexpr int OZ_ZERO_EXP = -100000;
+
+__device__ __forceinline__ int exp_of_max(float m) {
+    if (!(m > 0.f)) return OZ_ZERO_EXP;
+    return ilogbf(m) + 1;  // m < 2^E
+}
+
+// Signed fixed-point value trunc(x * 2^(42 - E)) of a double, |x| < 2^E.
+__device__ __forceinline__ long long fixed_f64(double x, int E) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0) return 0;
+    const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 10 + E - (ex - 1023);  // >= 11 when |x| < 2^E
+    const long long F = (sh >= 64) ? 0 : (long long)(M >> sh);
+    return (b >> 63) ? -F : F;
+}
+
+// Same for a float: |x| < 2^E.
+__device__ __forceinline__ long long fixed_f32(float x, int E) {
+    const unsigned b = __float_as_uint(x);
+    const int ex = (int)((b >> 23) & 0xff);
+    if (ex == 0) return 0;
+    const unsigned long long M = (unsigned long long)((b & 0x7FFFFFu) | 0x800000u);
+    const int sh = (ex - 127) - 23 + 42 - E;  // F = M * 2^sh
+    long long F;
+    if (sh >= 0)
+        F = (sh >= 40) ? 0 : (long long)(M << sh);  // sh <= 18 when |x| < 2^E
+    else
+        F = (-sh >= 64) ? 0 : (long long)(M >> (-sh));
+    return (b >> 31) ? -F : F;
+}
+
+// Signed 7-bit digits of F (42 fractional bits) by rounding, pre-scaled:
+// slice s = q_s 2^-7s with |q_0| <= 128, |q_s| <= 64 for s >= 1.
+template <int S>
+__device__ __forceinline__ void slices_of(long long F, __nv_bfloat16* out, int stride) {
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int sh = 35 - 7 * s;
+        long long q;
+        if (s == S - 1 && sh == 0) {
+            q = F;
+        } else {
+            q = (F + (1ll << (sh - 1))) >> sh;  // round half up (arithmetic shift)
+            F -= q << sh;
+        }
+        const float v = (float)(int)q * __int_as_float((127 - 7 * s) << 23);  // q * 2^-7s, exact
+        out[s * stride] = __float2bfloat16_rn(v);
+    }
+}
+
+enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2 };
+
+template <int FMT>
+__device__ __forceinline__ void load_fixed(const void* base, int64_t idx, int E, long long& re, long long& im) {
+    if (E == OZ_ZERO_EXP) {
+        re = im = 0;
+        return;
+    }
+    if (FMT == FMT_F64) {
+        const double2 v = reinterpret_cast<const double2*>(base)[idx];
+        re = fixed_f64(v.x, E);
+        im = fixed_f64(v.y, E);
+    } else if (FMT == FMT_F32) {
+        const float2 v = reinterpret_cast<const float2*>(base)[idx];
+        re = fixed_f32(v.x, E);
+        im = fixed_f32(v.y, E);
+    } else {
+        const float4 v = reinterpret_cast<const float4*>(base)[idx];
+        re = fixed_f32(v.x, E) + fixed_f32(v.y, E);
+        im = fixed_f32(v.z, E) + fixed_f32(v.w, E);
+    }
+}
+
+template <int FMT>
+__device__ __forceinline__ float mag_of(const void* base, int64_t idx) {
+    if (FMT == FMT_F64) {
+        const double2 v = reinterpret_cast<const double2*>(base)[idx];
+        return (float)fmax(fabs(v.x), fabs(v.y)) * 1.0000002f;
+    } else if (FMT == FMT_F32) {
+        const float2 v = reinterpret_cast<const float2*>(base)[idx];
+        return fmaxf(fabsf(v.x), fabsf(v.y));
+    } else {
+        const float4 v = reinterpret_cast<const float4*>(base)[idx];
+        return fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w));
+    }
+}
+
+// Exponents: EA[b][i] for rows of op(A) (conj: columns of A), EB[b][j] for
+// columns of B.  One warp per (b, line).
+template <int FMTA, int FMTB, bool CONJ_A>
+__global__ void oz_exp_kernel(int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
+                              const void* B, int64_t ldb, int64_t sB, int* EA, int* EB) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t per = (int64_t)M + Nc;
+    for (int64_t w = gw; w < batch * per; w += nw) {
+        const int64_t b = w / per;
+        const int line = (int)(w % per);
+        float m = 0.f;
+        if (line < M) {
+            for (int k = lane; k < K; k += 32) {
+                const int64_t idx = CONJ_A ? (b * sA + (int64_t)k * lda + line) : (b * sA + (int64_t)line * lda + k);
+                m = fmaxf(m, mag_of<FMTA>(A, idx));
+            }
+        } else {
+            const int j = line - M;
+            for (int k = lane; k < K; k += 32) m = fmaxf(m, mag_of<FMTB>(B, b * sB + (int64_t)k * ldb + j));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) {
+            if (line < M)
+                EA[b * M + line] = exp_of_max(m);
+            else
+                EB[b * Nc + (line - M)] = exp_of_max(m);
+        }
+    }
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned addr, unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, const unsigned* a, unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// smem: sA[SA][OZ_TM][OZ_PAD], sB[SB][2*OZ_TN][OZ_PAD] (bf16)
+template <int SA, int SB, int LMAX, bool CONJ_A, int FMTA, int FMTB>
+__global__ void __launch_bounds__(256, 1) oz_gemm_kernel(int M, int Nc, int K, const void* __restrict__ A,
+                                                         int64_t lda, int64_t sA_, const void* __restrict__ B,
+                                                         int64_t ldb, int64_t sB_, const int* __restrict__ EA,
+                                                         const int* __restrict__ EB, float4* __restrict__ C,
+                                                         int64_t ldc, int64_t sC) {
+    extern __shared__ __align__(16) unsigned char oz_smem[];
+    __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(oz_smem);
+    __nv_bfloat16* sB = sA + SA * OZ_TM * OZ_PAD;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int warp_m = warp & 1, warp_n = warp >> 1;
+    const int64_t b = blockIdx.z;
+    const int row0 = blockIdx.y * OZ_TM, col0 = blockIdx.x * OZ_TN;
+
+    float acc[4][2][4][4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[l][i][j][c] = 0.f;
+
+    for (int k0 = 0; k0 < K; k0 += OZ_TK) {
+        // ---- stage A: 64 rows x 16 complex k -> sA[s][row][k (re) | 16 + k (im)]
+#pragma unroll
+        for (int rep = 0; rep < 4; ++rep) {
+            const int e = tid + 256 * rep;
+            int r, kk;
+            if (CONJ_A) {
+                r = e & 63;
+                kk = e >> 6;
+            } else {
+                kk = e & 15;
+                r = e >> 4;
+            }
+            const int gi = row0 + r, gk = k0 + kk;
+            long long fre = 0, fim = 0;
+            if (gi < M && gk < K) {
+                const int E = EA[b * M + gi];
+                const int64_t idx = CONJ_A ? (b * sA_ + (int64_t)gk * lda + gi) : (b * sA_ + (int64_t)gi * lda + gk);
+                load_fixed<FMTA>(A, idx, E, fre, fim);
+                if (CONJ_A) fim = -fim;
+            }
+            __nv_bfloat16* dst = sA + r * OZ_PAD;
+            slices_of<SA>(fre, dst + kk, OZ_TM * OZ_PAD);
+            slices_of<SA>(fim, dst + 16 + kk, OZ_TM * OZ_PAD);
+        }
+        // ---- stage B: 16 complex k x 64 complex columns
+#pragma unroll
+        for (int rep = 0; rep < 4; ++rep) {
+            const int e = tid + 256 * rep;
+            const int j = e & 63, kk = e >> 6;
+            const int gj = col0 + j, gk = k0 + kk;
+            long long fre = 0, fim = 0;
+            if (gj < Nc && gk < K) {
+                const int E = EB[b * Nc + gj];
+                load_fixed<FMTB>(B, b * sB_ + (int64_t)gk * ldb + gj, E, fre, fim);
+            }
+            // real output column j:    rows k -> Re B, rows 16+k -> -Im B
+            // imag output column 64+j: rows k -> Im B, rows 16+k ->  Re B
+            __nv_bfloat16* d0 = sB + j * OZ_PAD;
+            __nv_bfloat16* d1 = sB + (OZ_TN + j) * OZ_PAD;
+            slices_of<SB>(fre, d0 + kk, 2 * OZ_TN * OZ_PAD);
+            slices_of<SB>(-fim, d0 + 16 + kk, 2 * OZ_TN * OZ_PAD);
+            slices_of<SB>(fim, d1 + kk, 2 * OZ_TN * OZ_PAD);
+            slices_of<SB>(fre, d1 + 16 + kk, 2 * OZ_TN * OZ_PAD);
+        }
+        __syncthreads();
+        // ---- tensor-core products over the 32 real k of this stage
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+            unsigned af[SA][2][4];
+#pragma unroll
+            for (int s = 0; s < SA; ++s)
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    const __nv_bfloat16* p = sA + s * OZ_TM * OZ_PAD +
+                                             (warp_m * 32 + mt * 16 + (lane & 15)) * OZ_PAD + ks * 16 + (lane >> 4) * 8;
+                    ldsm_x4((unsigned)__cvta_generic_to_shared(p), af[s][mt][0], af[s][mt][1], af[s][mt][2],
+                            af[s][mt][3]);
+                }
+#pragma unroll
+            for (int t = 0; t < SB; ++t) {
+                unsigned bf[4][2];
+#pragma unroll
+                for (int np = 0; np < 2; ++np) {
+                    // lanes 0-7: n 0-7 k 0; 8-15: n 0-7 k 8; 16-23: n 8-15 k 0; 24-31: n 8-15 k 8
+                    const int nrow = warp_n * 32 + np * 16 + (lane & 7) + ((lane >> 4) << 3);
+                    const int kof = ks * 16 + ((lane >> 3) & 1) * 8;
+                    const __nv_bfloat16* p = sB + t * 2 * OZ_TN * OZ_PAD + nrow * OZ_PAD + kof;
+                    ldsm_x4((unsigned)__cvta_generic_to_shared(p), bf[2 * np][0], bf[2 * np][1], bf[2 * np + 1][0],
+                            bf[2 * np + 1][1]);
+                }
+#pragma unroll
+                for (int s = 0; s < SA; ++s) {
+                    if (s + t > LMAX) continue;
+                    const int lv = (s + t) < 3 ? (s + t) : 3;
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                        for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[lv][mt][nt], af[s][mt], bf[nt][0], bf[nt][1]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- epilogue: exact TwoSum of the exact levels, scaled float pair out
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int r = row0 + warp_m * 32 + mt * 16 + (lane >> 2) + ((c >> 1) << 3);
+                const int cn = warp_n * 32 + nt * 8 + (lane & 3) * 2 + (c & 1);
+                const bool im = cn >= OZ_TN;
+                const int j = col0 + (im ? cn - OZ_TN : cn);
+                if (r >= M || j >= Nc) continue;
+                const float a0 = acc[0][mt][nt][c], a1 = acc[1][mt][nt][c];
+                const float a2 = acc[2][mt][nt][c], a3 = acc[3][mt][nt][c];
+                // exact levels a0 + a1 + a2 -> (hi, e1 + e2), inexact level a3 into lo
+                const float s1 = a0 + a1;
+                const float t1 = s1 - a0;
+                const float e1 = (a0 - (s1 - t1)) + (a1 - t1);
+                const float hi = s1 + a2;
+                const float t2 = hi - s1;
+                const float e2 = (s1 - (hi - t2)) + (a2 - t2);
+                const float lo = (e1 + e2) + a3;
+                const int ea = EA[b * M + r], eb = EB[b * Nc + j];
+                float2 out = make_float2(0.f, 0.f);
+                if (ea != OZ_ZERO_EXP && eb != OZ_ZERO_EXP) {
+                    int n = ea + eb - 14;
+                    n = max(-126, min(127, n));
+                    const float sc = __int_as_float((127 + n) << 23);
+                    out = make_float2(hi * sc, lo * sc);
+                }
+                float* dst = reinterpret_cast<float*>(C + b * sC + (int64_t)r * ldc + j) + (im ? 2 : 0);
+                *reinterpret_cast<float2*>(dst) = out;
+            }
+}
+
+template <int SA, int SB, int LMAX, bool CONJ_A, int FMTA, int FMTB>
+int launch_oz(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
+              const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB) {
+    {
+        const int64_t lines = batch * (M + Nc);
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((lines * 32 + 255) / 256, 152 * 64));
+        oz_exp_kernel<FMTA, FMTB, CONJ_A><<<blocks, 256, 0, st>>>(batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
+        TBG_LAUNCHED("oz_exp_kernel");
+    }
+    const size_t smem = sizeof(__nv_bfloat16) * OZ_PAD * (SA * OZ_TM + SB * 2 * OZ_TN);
+    auto kern = oz_gemm_kernel<SA, SB, LMAX, CONJ_A, FMTA, FMTB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_gemm)");
+    int pairs = 0;
+    for (int s = 0; s < SA; ++s)
+        for (int t = 0; t < SB; ++t) pairs += (s + t <= LMAX);
+    // algorithmic flops of the complex product, counted once (8 M Nc K); the
+    // tensor pipe executes `pairs` times that
+    KTimer kt(st, pairs >= 10 ? "ozaki_gemm_kernel<high>" : "ozaki_gemm_kernel<low>",
+              8.0 * (double)M * Nc * K * batch);
+    for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
+        const int64_t nb = std::min<int64_t>(65535, batch - b0);
+        dim3 grid((Nc + OZ_TN - 1) / OZ_TN, (M + OZ_TM - 1) / OZ_TM, (unsigned)nb);
+        const size_t ea = FMTA == FMT_F64 ? 16 : (FMTA == FMT_F32 ? 8 : 16);
+        const size_t eb = FMTB == FMT_F64 ? 16 : (FMTB == FMT_F32 ? 8 : 16);
+        kern<<<grid, 256, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
+                                      static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M, EB + b0 * Nc,
+                                      C + b0 * sC, ldc, sC);
+        TBG_LAUNCHED("ozaki_gemm_kernel");
+    }
+    return TBG_OK;
+}
+
+}  // namespace
+
+size_t ozaki_exp_bytes(int64_t batch, int M, int Nc) { return sizeof(int) * (size_t)batch * (M + Nc) + 256; }
+
+// Precision classes used by the mixed path:
+//   HIGH: 6 x 6 slices, levels s + t <= 5  (about 2^-43 of the product scale)
+//   LOW : 3 x 3 slices, levels s + t <= 2  (about 2^-22; corrections that are
+//         themselves ~1e-7 of the result)
+int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
+                int64_t sC, int* EA, int* EB) {
+    if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm: K > 256");
+#define OZ_CASE(H, CJ, FA, FB)                                                                                   \
+    if (high == H && conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                 \
+        return H ? launch_oz<6, 6, 5, CJ, FA, FB>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB) \
+                 : launch_oz<3, 3, 2, CJ, FA, FB>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB);
+    // combinations used by the mixed path and by the unit test
+    OZ_CASE(true, false, FMT_F64, FMT_F64)
+    OZ_CASE(true, true, FMT_F64, FMT_F64)
+    OZ_CASE(true, true, FMT_F32, FMT_F32)   // X^H X
+    OZ_CASE(true, false, FMT_F64, FMT_F32)  // H X
+    OZ_CASE(true, true, FMT_F32, FMT_PAIR)  // X^H (H X)
+    OZ_CASE(true, false, FMT_F64, FMT_PAIR) // V X'
+    OZ_CASE(true, true, FMT_PAIR, FMT_PAIR) // X'^H (V X')
+    OZ_CASE(false, false, FMT_F32, FMT_F64) // X F
+    OZ_CASE(false, false, FMT_F64, FMT_F64)
+#undef OZ_CASE
+    return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm: operand format combination not instantiated");
+}
+
+}  // namespace tbg
+
+// Internal test hook (not part of the public header): C = op(A) B for host
+// complex-double inputs, result as complex double (hi + lo).
+extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int M, int Nc, int K, const double* A,
+                                        const double* B, double* C) {
+    using namespace tbg;
+    const int64_t ar = conj_a ? K : M, ac = conj_a ? M : K;
+    const size_t abytes = sizeof(double) * 2 * ar * ac * batch, bbytes = sizeof(double) * 2 * (size_t)K * Nc * batch;
+    const size_t cbytes = sizeof(float4) * (size_t)M * Nc * batch;
+    void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dE = nullptr;
+    cudaStream_t st = nullptr;
+    cudaStreamCreate(&st);
+    int rc = TBG_OK;
+    if (cudaMalloc(&dA, abytes) || cudaMalloc(&dB, bbytes) || cudaMalloc(&dC, cbytes) ||
+        cudaMalloc(&dE, ozaki_exp_bytes(batch, M, Nc)))
+        rc = set_error(TBG_E_OOM, "ozaki test alloc");
+    if (!rc) {
+        cudaMemcpy(dA, A, abytes, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, B, bbytes, cudaMemcpyHostToDevice);
+        int* EA = static_cast<int*>(dE);
+        rc = ozaki_zgemm(st, high != 0, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
+                         static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (!rc && e != cudaSuccess) rc = cuda_error(e, "ozaki test");
+        if (!rc) {
+            std::vector<float4> h((size_t)M * Nc * batch);
+            cudaMemcpy(h.data(), dC, cbytes, cudaMemcpyDeviceToHost);
+            for (size_t i = 0; i < h.size(); ++i) {
+                C[2 * i] = (double)h[i].x + (double)h[i].y;
+                C[2 * i + 1] = (double)h[i].z + (double)h[i].w;
+            }
+        }
+    }
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(dE);
+    cudaStreamDestroy(st);
+    return rc;
+}

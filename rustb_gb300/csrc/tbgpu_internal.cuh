@@ -168,5 +168,13 @@ int kahan_column_sums(cudaStream_t st, int64_t nk, int nmu, const double* S, dou
 int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U,
                      void* work, size_t work_bytes, int* status_d, int64_t* clusters_d);
 size_t mixed_workspace_bytes(int N, int64_t batch);
+int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
+                    size_t work_bytes, int* status_d);
+// Mixed path end to end: FP32 eigensolve, refinement and rotation on the
+// tensor cores -> refined E (ascending) and Omega.
+size_t mixed_berry_workspace_bytes(int N, int64_t batch);
+int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx, const zc* Vy, int64_t ldV,
+                double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
+                int64_t* clusters_d);
 
 }  // namespace tbg

@@ -1,0 +1,69 @@
+"""Exact-slice BF16 tensor-core complex GEMM against numpy FP64 (GPU).
+
+The HIGH class must reach 1e-12 of the natural product scale
+(max|row of op(A)| * max|column of B| * K); the LOW class 1e-5."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from rustb_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+def ozaki(lib, A, B, conj_a, high):
+    batch = A.shape[0]
+    if conj_a:
+        K, M = A.shape[1], A.shape[2]
+    else:
+        M, K = A.shape[1], A.shape[2]
+    Nc = B.shape[2]
+    C = np.zeros((batch, M, Nc), dtype=np.complex128)
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn = lib.tbg_internal_ozaki_zgemm
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+    A = np.ascontiguousarray(A)
+    B = np.ascontiguousarray(B)
+    st = fn(int(high), int(conj_a), batch, M, Nc, K, A.view(np.float64).ctypes.data_as(dp),
+            B.view(np.float64).ctypes.data_as(dp), C.view(np.float64).ctypes.data_as(dp))
+    _lib.check(st, lib)
+    return C
+
+
+@pytest.mark.parametrize("conj_a", [False, True])
+@pytest.mark.parametrize("M,Nc,K", [(128, 128, 128), (70, 40, 100), (256, 64, 256), (1, 3, 2)])
+def test_ozaki_high_precision(conj_a, M, Nc, K):
+    lib = _lib.load()
+    rng = np.random.default_rng(M + Nc + K)
+    batch = 3
+    shapeA = (batch, K, M) if conj_a else (batch, M, K)
+    A = rng.standard_normal(shapeA) + 1j * rng.standard_normal(shapeA)
+    B = rng.standard_normal((batch, K, Nc)) + 1j * rng.standard_normal((batch, K, Nc))
+    # rows/columns of very different magnitude
+    if conj_a:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, 1, M))
+    else:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, M, 1))
+    B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
+    opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
+    ref = opA @ B
+    C = ozaki(lib, A, B, conj_a, True)
+    scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
+    err = np.abs(C - ref) / scale
+    assert err.max() < 1e-12, err.max()
+
+
+def test_ozaki_low_precision_and_zeros():
+    lib = _lib.load()
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((2, 64, 64)) + 1j * rng.standard_normal((2, 64, 64))
+    B = rng.standard_normal((2, 64, 64)) + 1j * rng.standard_normal((2, 64, 64))
+    A[0, 5, :] = 0.0  # an all-zero row
+    ref = A @ B
+    C = ozaki(lib, A, B, False, False)
+    scale = np.abs(A).max() * np.abs(B).max() * 64
+    assert np.abs(C - ref).max() / scale < 1e-5
+    assert np.all(C[0, 5, :] == 0.0)
