@@ -223,7 +223,7 @@ double lattice_det(const std::vector<double>& lat, int dim) {
 
 // Shared per-chunk response pipeline: (k on device) -> Omega, E.
 struct BerryJob {
-    const ModelDev* m;
+    ModelDev* m;
     int spin;
     double eta;
     int precision;
@@ -236,6 +236,8 @@ struct BerryJob {
     int* status_d;
     void* work;
     size_t work_bytes;
+    void* fwork;
+    size_t fwork_bytes;
     cc* U32;
 };
 
@@ -254,9 +256,13 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
     J.U32 = nullptr;
     J.work = nullptr;
     J.work_bytes = 0;
+    J.fwork = nullptr;
+    J.fwork_bytes = 0;
     if (J.precision == TBG_PREC_MIXED) {
         J.work_bytes = mixed_berry_workspace_bytes(N, c);
         J.work = J.work_bytes ? ctx.alloc<unsigned char>(J.work_bytes) : nullptr;
+        J.fwork_bytes = fourier_mixed_scratch_bytes(*J.m, c);
+        J.fwork = ctx.alloc<unsigned char>(J.fwork_bytes);
     }
     if (ctx.rc == TBG_OK) {
         cudaError_t e = cudaMemsetAsync(J.status_d, 0, sizeof(int), ctx.st);
@@ -266,10 +272,12 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
 }
 
 int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
-    const ModelDev& m = *J.m;
+    ModelDev& m = *J.m;
     const int N = (int)m.nsta;
     const int64_t NN = (int64_t)N * N;
-    int rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
+    int rc = (J.precision == TBG_PREC_MIXED)
+                 ? fourier_mixed(m, ctx.st, nkc, J.k_d, J.dirs_d, J.H, J.V, J.fwork, J.fwork_bytes)
+                 : fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
     if (rc) return rc;
     if (m.n_rmat > 0) {
         rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
@@ -417,6 +425,8 @@ int tbg_model_destroy(tbg_model* m) {
     cudaFree(M.taucart_d);
     cudaFree(M.rmatrix);
     cudaFree(M.box);
+    cudaFree(M.hop_slices);
+    cudaFree(M.hop_EB);
     M.ham = nullptr;
     delete m;
     return TBG_OK;
@@ -552,11 +562,12 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     const int64_t NN = (int64_t)N * N;
     Ctx ctx;
     BerryJob J;
-    J.m = &M;
+    J.m = const_cast<ModelDev*>(&M);
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
-    J.chunk = choose_chunk(nk, sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 12 : 5) + 64 * N);
+    J.chunk = choose_chunk(nk, sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 15 : 5) + 64 * N +
+                                   (precision == TBG_PREC_MIXED ? 48 * (int64_t)M.nR : 0));
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = (nmu > 0) ? ctx.alloc<double>(nmu) : nullptr;
@@ -643,12 +654,13 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     cudaEventCreate(&ev1);
     cudaEventRecord(ev0, ctx.st);
     BerryJob J;
-    J.m = &M;
+    J.m = const_cast<ModelDev*>(&M);
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
     J.chunk = choose_chunk(std::max<int64_t>(k_count, 1),
-                           sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 12 : 5) + 64 * N + 8 * nmu);
+                           sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 15 : 5) + 64 * N + 8 * nmu +
+                               (precision == TBG_PREC_MIXED ? 48 * (int64_t)M.nR : 0));
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = ctx.alloc<double>(nmu);

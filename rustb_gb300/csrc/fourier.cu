@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "tbgpu_internal.cuh"
 
@@ -288,7 +289,135 @@ __global__ void rmat_combine_kernel(int64_t n_rmat, int dim, int N, const double
     }
 }
 
+// ph3 rows: [0, nk) = u(k,R); [nk, 2nk) = i c_0(R) u; [2nk, 3nk) = i c_1(R) u.
+__global__ void phases3_kernel(int64_t nk, int dim, const double* __restrict__ k, int nR,
+                               const int* __restrict__ hamR, const double* __restrict__ coef,
+                               zc* __restrict__ ph3) {
+    const int64_t total = nk * (int64_t)nR;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / nR;
+        const int j = (int)(idx % nR);
+        const double* kv = k + kk * dim;
+        const int* r = hamR + 3 * j;
+        double s = (double)r[0] * kv[0];
+        if (dim > 1) s += (double)r[1] * kv[1];
+        if (dim > 2) s += (double)r[2] * kv[2];
+        double sn, cs;
+        sincos(kTwoPi * s, &sn, &cs);
+        ph3[idx] = mk(cs, sn);
+        const double c0 = coef[j], c1 = coef[nR + j];
+        ph3[total + idx] = mk(-c0 * sn, c0 * cs);      // i c0 u
+        ph3[2 * total + idx] = mk(-c1 * sn, c1 * cs);  // i c1 u
+    }
+}
+
+// Atom gauge and tau term from the lattice-gauge float-pair sums:
+//   H = conj(phi_m) H_l phi_n,  V_p = (V_l,p + i (tau_p,n - tau_p,m) H_l) conj(phi_m) phi_n
+__global__ void gauge_pairs_kernel(int64_t nk, int N, const float4* __restrict__ C, const zc* __restrict__ orbph,
+                                   const double* __restrict__ taup, zc* __restrict__ H, zc* __restrict__ V) {
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nk * NN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / NN;
+        const int e = (int)(idx % NN), mrow = e / N, ncol = e % N;
+        const float4 h4 = C[idx];
+        const zc hl = mk((double)h4.x + (double)h4.y, (double)h4.z + (double)h4.w);
+        const zc g = cmul(orbph[kk * N + mrow], orbph[kk * N + ncol]);
+        H[idx] = hl * g;
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float4 v4 = C[(1 + p) * nk * NN + idx];
+            zc v = mk((double)v4.x + (double)v4.y, (double)v4.z + (double)v4.w);
+            const double diff = taup[p * N + ncol] - taup[p * N + mrow];
+            v.re -= diff * hl.im;
+            v.im += diff * hl.re;
+            V[kk * 2 * NN + p * NN + e] = v * g;
+        }
+    }
+}
+
+std::mutex g_hop_mu;
+
 }  // namespace
+
+int ozaki_fourier_max_k();
+size_t ozaki_hop_slices_bytes(int K, int64_t Nc);
+int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs);
+int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
+                  const void* Bs, float4* C);
+
+size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
+    const size_t N = (size_t)m.nsta, NN = N * N, nR = (size_t)m.nR;
+    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) + 3 * NN * sizeof(float4)) +
+           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 8 * 256;
+}
+
+int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H, zc* V,
+                  void* scratch, size_t scratch_bytes) {
+    if (nk <= 0) return TBG_OK;
+    const int N = (int)m.nsta, nR = (int)m.nR;
+    const int64_t NN = (int64_t)N * N;
+    if (nR > ozaki_fourier_max_k() || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
+        return fourier_direct(m, st, nk, k_d, TBG_GAUGE_ATOM, 2, dirs_d, H, V, NN, 2 * NN);
+    {
+        std::lock_guard<std::mutex> lk(g_hop_mu);
+        if (!m.hop_slices) {
+            void* bs = nullptr;
+            int* eb = nullptr;
+            TBG_CUDA(cudaMalloc(&bs, ozaki_hop_slices_bytes(nR, NN)));
+            if (cudaMalloc(&eb, sizeof(int) * NN) != cudaSuccess) {
+                cudaFree(bs);
+                return set_error(TBG_E_OOM, "hop table digit planes");
+            }
+            int rc = ozaki_build_hop_slices(st, nR, NN, m.ham, eb, bs);
+            cudaError_t e = cudaStreamSynchronize(st);
+            if (rc || e != cudaSuccess) {
+                cudaFree(bs);
+                cudaFree(eb);
+                return rc ? rc : cuda_error(e, "hop table digit planes");
+            }
+            m.hop_slices = bs;
+            m.hop_EB = eb;
+        }
+    }
+    unsigned char* p = static_cast<unsigned char*>(scratch);
+    auto take = [&](size_t bytes) {
+        void* q = p;
+        p += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    zc* ph3 = static_cast<zc*>(take(sizeof(zc) * 3 * nk * nR));
+    zc* orbph = static_cast<zc*>(take(sizeof(zc) * nk * N));
+    double* coef = static_cast<double*>(take(sizeof(double) * 2 * nR));
+    double* taup = static_cast<double*>(take(sizeof(double) * 2 * N));
+    int* EA = static_cast<int*>(take(sizeof(int) * 3 * nk));
+    float4* C = static_cast<float4*>(take(sizeof(float4) * 3 * nk * NN));
+    {
+        KTimer kt(st, "phases_kernel");
+        const int total = 2 * (nR + N);
+        proj_coef_kernel<<<(total + 255) / 256, 256, 0, st>>>(2, m.dim, dirs_d, nR, m.Rcart_d, N, m.taucart_d, coef,
+                                                              taup);
+        const int64_t t1 = nk * (int64_t)(nR + N);
+        phases_kernel<<<(unsigned)std::min<int64_t>((t1 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+            nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph3, orbph);  // ph3[0 .. nk*nR) reused below
+        const int64_t t2 = nk * (int64_t)nR;
+        phases3_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+            nk, m.dim, k_d, nR, m.hamR_d, coef, ph3);
+        count_launch(3);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_error(e, "phases");
+    }
+    int rc = ozaki_fourier(st, 3 * nk, NN, nR, ph3, EA, m.hop_EB, m.hop_slices, C);
+    if (rc) return rc;
+    {
+        KTimer kt(st, "gauge_pairs_kernel");
+        gauge_pairs_kernel<<<(unsigned)std::min<int64_t>((nk * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
+            nk, N, C, orbph, taup, H, V);
+        TBG_LAUNCHED("gauge_pairs_kernel");
+    }
+    return TBG_OK;
+}
 
 int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, int gauge, int nproj,
                    const double* dirs_d, zc* H, zc* V, int64_t ldH, int64_t ldV) {

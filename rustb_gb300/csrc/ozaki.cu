@@ -94,7 +94,7 @@ __device__ __forceinline__ void slices_of(long long F, __nv_bfloat16* out, int s
     }
 }
 
-enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2 };
+enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2, FMT_PRESLICED = 3 };
 
 template <int FMT>
 __device__ __forceinline__ void load_fixed(const void* base, int64_t idx, int E, long long& re, long long& im) {
@@ -110,10 +110,12 @@ __device__ __forceinline__ void load_fixed(const void* base, int64_t idx, int E,
         const float2 v = reinterpret_cast<const float2*>(base)[idx];
         re = fixed_f32(v.x, E);
         im = fixed_f32(v.y, E);
-    } else {
+    } else if (FMT == FMT_PAIR) {
         const float4 v = reinterpret_cast<const float4*>(base)[idx];
         re = fixed_f32(v.x, E) + fixed_f32(v.y, E);
         im = fixed_f32(v.z, E) + fixed_f32(v.w, E);
+    } else {
+        re = im = 0;
     }
 }
 
@@ -125,10 +127,11 @@ __device__ __forceinline__ float mag_of(const void* base, int64_t idx) {
     } else if (FMT == FMT_F32) {
         const float2 v = reinterpret_cast<const float2*>(base)[idx];
         return fmaxf(fabsf(v.x), fabsf(v.y));
-    } else {
+    } else if (FMT == FMT_PAIR) {
         const float4 v = reinterpret_cast<const float4*>(base)[idx];
         return fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w));
     }
+    return 0.f;
 }
 
 // Exponents: EA[b][i] for rows of op(A) (conj: columns of A), EB[b][j] for
@@ -229,6 +232,29 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(int M, int Nc, int K, c
             slices_of<SA>(fim, dst + 16 + kk, OZ_TM * OZ_PAD);
         }
         // ---- stage B: 16 complex k x 64 complex columns
+        if (FMTB == FMT_PRESLICED) {
+            // B points at digit planes laid out [col tile][k chunk][slice][re|im][16 k][64 cols]
+            const int kc = k0 / OZ_TK;
+            const int nkc = (K + OZ_TK - 1) / OZ_TK;
+            const __nv_bfloat16* src = static_cast<const __nv_bfloat16*>(B) +
+                                       ((int64_t)blockIdx.x * nkc + kc) * (int64_t)SB * 2 * OZ_TK * OZ_TN;
+#pragma unroll
+            for (int rep = 0; rep < 4; ++rep) {
+                const int e = tid + 256 * rep;
+                const int j = e & 63, kk = e >> 6;
+#pragma unroll
+                for (int t = 0; t < SB; ++t) {
+                    const __nv_bfloat16 re = src[((t * 2 + 0) * OZ_TK + kk) * OZ_TN + j];
+                    const __nv_bfloat16 im = src[((t * 2 + 1) * OZ_TK + kk) * OZ_TN + j];
+                    __nv_bfloat16* d0 = sB + t * 2 * OZ_TN * OZ_PAD + j * OZ_PAD;
+                    __nv_bfloat16* d1 = sB + t * 2 * OZ_TN * OZ_PAD + (OZ_TN + j) * OZ_PAD;
+                    d0[kk] = re;
+                    d0[16 + kk] = __hneg(im);
+                    d1[kk] = im;
+                    d1[16 + kk] = re;
+                }
+            }
+        } else
 #pragma unroll
         for (int rep = 0; rep < 4; ++rep) {
             const int e = tid + 256 * rep;
@@ -359,6 +385,104 @@ int launch_oz(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* 
 }  // namespace
 
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc) { return sizeof(int) * (size_t)batch * (M + Nc) + 256; }
+
+namespace {
+
+// Column exponents of the hop table: EB[e] over R (one warp per column e).
+__global__ void hop_exp_kernel(int K, int64_t Nc, const zc* __restrict__ ham, int* __restrict__ EB) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = gw; e < Nc; e += nw) {
+        float m = 0.f;
+        for (int r = lane; r < K; r += 32) m = fmaxf(m, mag_of<FMT_F64>(ham, (int64_t)r * Nc + e));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) EB[e] = exp_of_max(m);
+    }
+}
+
+// Digit planes of the hop table: [col tile][k chunk][slice][re|im][16 k][64 cols].
+template <int S>
+__global__ void hop_slice_kernel(int K, int64_t Nc, const zc* __restrict__ ham, const int* __restrict__ EB,
+                                 __nv_bfloat16* __restrict__ Bs) {
+    const int nkc = (K + OZ_TK - 1) / OZ_TK;
+    const int64_t nct = (Nc + OZ_TN - 1) / OZ_TN;
+    const int64_t total = nct * nkc * OZ_TK * OZ_TN;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(idx % OZ_TN);
+        const int kk = (int)((idx / OZ_TN) % OZ_TK);
+        const int64_t blk = idx / (OZ_TN * OZ_TK);  // = ct * nkc + kc
+        const int kc = (int)(blk % nkc);
+        const int64_t ct = blk / nkc;
+        const int64_t e = ct * OZ_TN + j;
+        const int r = kc * OZ_TK + kk;
+        long long fre = 0, fim = 0;
+        if (e < Nc && r < K) load_fixed<FMT_F64>(ham, (int64_t)r * Nc + e, EB[e], fre, fim);
+        __nv_bfloat16* dst = Bs + blk * (int64_t)S * 2 * OZ_TK * OZ_TN + kk * OZ_TN + j;
+        slices_of<S>(fre, dst, 2 * OZ_TK * OZ_TN);
+        slices_of<S>(fim, dst + OZ_TK * OZ_TN, 2 * OZ_TK * OZ_TN);
+    }
+}
+
+// Row exponents of a plain complex-double A (M x K): one warp per row.
+__global__ void row_exp_kernel(int64_t M, int K, const zc* __restrict__ A, int64_t lda, int* __restrict__ EA) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = gw; r < M; r += nw) {
+        float m = 0.f;
+        for (int k = lane; k < K; k += 32) m = fmaxf(m, mag_of<FMT_F64>(A, r * lda + k));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) EA[r] = exp_of_max(m);
+    }
+}
+
+}  // namespace
+
+// Largest contraction length for which levels 0-2 stay exact.
+int ozaki_fourier_max_k() { return 408; }
+
+size_t ozaki_hop_slices_bytes(int K, int64_t Nc) {
+    const int64_t nkc = (K + OZ_TK - 1) / OZ_TK, nct = (Nc + OZ_TN - 1) / OZ_TN;
+    return sizeof(__nv_bfloat16) * (size_t)nct * nkc * 6 * 2 * OZ_TK * OZ_TN;
+}
+
+// Build the digit planes of the hop table (K = nR rows of Nc = N^2 elements).
+int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs) {
+    KTimer kt(st, "hop_slice_kernel");
+    hop_exp_kernel<<<(unsigned)std::min<int64_t>((Nc * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(K, Nc, ham, EB);
+    TBG_LAUNCHED("hop_exp_kernel");
+    const int64_t total = ((Nc + OZ_TN - 1) / OZ_TN) * ((K + OZ_TK - 1) / OZ_TK) * OZ_TK * OZ_TN;
+    hop_slice_kernel<6><<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
+        K, Nc, ham, EB, static_cast<__nv_bfloat16*>(Bs));
+    TBG_LAUNCHED("hop_slice_kernel");
+    return TBG_OK;
+}
+
+// C (M x Nc, float pairs) = A (M x K, complex double) . hop (digit planes).
+int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
+                  const void* Bs, float4* C) {
+    if (K > ozaki_fourier_max_k()) return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier: nR > 408");
+    row_exp_kernel<<<(unsigned)std::min<int64_t>((M * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(M, K, A, K, EA);
+    TBG_LAUNCHED("row_exp_kernel");
+    constexpr int SA = 6, SB = 6, LMAX = 5;
+    const size_t smem = sizeof(__nv_bfloat16) * OZ_PAD * (SA * OZ_TM + SB * 2 * OZ_TN);
+    auto kern = oz_gemm_kernel<SA, SB, LMAX, false, FMT_F64, FMT_PRESLICED>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_fourier)");
+    KTimer kt(st, "ozaki_fourier_kernel", 8.0 * (double)M * Nc * K);
+    for (int64_t m0 = 0; m0 < M; m0 += (int64_t)OZ_TM * 65535) {
+        const int64_t mb = std::min<int64_t>(M - m0, (int64_t)OZ_TM * 65535);
+        dim3 grid((unsigned)((Nc + OZ_TN - 1) / OZ_TN), (unsigned)((mb + OZ_TM - 1) / OZ_TM), 1);
+        kern<<<grid, 256, smem, st>>>((int)mb, (int)Nc, K, A + m0 * K, K, 0, Bs, Nc, 0, EA + m0, EB, C + m0 * Nc, Nc,
+                                      0);
+        TBG_LAUNCHED("ozaki_fourier_kernel");
+    }
+    return TBG_OK;
+}
 
 // Precision classes used by the mixed path:
 //   HIGH: 6 x 6 slices, levels s + t <= 5  (about 2^-43 of the product scale)

@@ -87,6 +87,9 @@ struct ModelDev {
     zc* box = nullptr;           // device (L0, L1, L2, nsta, nsta)
     bool box_ready = false;
     int device = 0;
+    // digit planes of the hop table for the tensor-core Fourier sum (built lazily)
+    void* hop_slices = nullptr;
+    int* hop_EB = nullptr;
 };
 
 // ------------------------------------------------------------------ errors --
@@ -138,6 +141,14 @@ int fourier_mesh(ModelDev& m, cudaStream_t st, const int64_t* kmesh, int64_t k0,
                  size_t scratch_bytes);
 size_t fourier_mesh_scratch_bytes(const ModelDev& m, const int64_t* kmesh, int64_t nk_chunk);
 bool fourier_mesh_supported(const ModelDev& m);
+
+// Fourier sum for H and two projected velocities on the tensor cores
+// (exact-slice BF16 contraction), Atom gauge, FP64 outputs H (nk, N, N) and
+// V (nk, 2, N, N).  Falls back to fourier_direct when nR exceeds the exact
+// contraction length.
+size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk);
+int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H,
+                  zc* V, void* scratch, size_t scratch_bytes);
 
 // Batched Hermitian eigensolver: A (batch, N, N) FP64 input (destroyed),
 // E (batch, N) ascending, U (batch, N, N) eigenvectors in columns (may be
