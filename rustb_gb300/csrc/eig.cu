@@ -185,7 +185,7 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     b += sizeof(cx<T>) * 3 * (size_t)N;
     b += sizeof(T) * 64;
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-    size_t s2 = sizeof(cx<T>) * (size_t)N * PB;
+    size_t s2 = sizeof(cx<T>) * (size_t)(N + 1) * PB;
     b += std::max(s1, s2);
     b += 16;
     return b;
@@ -194,7 +194,7 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
 template <typename T, bool A_SMEM, int G, int PB>
-__global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
+__global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    double* __restrict__ Eout, cx<T>* __restrict__ Uout,
                                                    cx<T>* __restrict__ Awork, int* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
         p += sizeof(T) * 64;
         sh.scratch = reinterpret_cast<T*>(p);
         size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-        size_t s2 = sizeof(cx<T>) * (size_t)N * PB;
+        size_t s2 = sizeof(cx<T>) * (size_t)(N + 1) * PB;
         p += std::max(s1, s2);
         sh.flags = reinterpret_cast<int*>(p);
     }
@@ -255,12 +255,12 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
         for (int j = 0; j < N - 1; ++j) {
             const int m = N - 1 - j;
             cx<T>* rowj = A + (size_t)j * N + (j + 1);  // row j, columns j+1.. = conj(column j)
-            T part = 0, dummy = 0;
-            for (int i = 1 + tid; i < m; i += nthr) part += abs2(rowj[i]);
-            block_sum2(part, dummy, sh.red);
-            if (tid == 0) {
+            // reflector by warp 0: H_j^H [alpha; x] = [beta; 0]
+            if (warp == 0) {
+                T part = 0;
+                for (int i = 1 + lane; i < m; i += 32) part += abs2(rowj[i]);
+                const T xnorm2 = warp_sum(part);
                 const cx<T> alpha = conj(rowj[0]);
-                const T xnorm2 = part;
                 cx<T> tau, scal;
                 T beta;
                 if (xnorm2 == T(0) && alpha.im == T(0)) {
@@ -275,48 +275,52 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
                     const T dd = den.re * den.re + den.im * den.im;
                     scal = mk<T>(den.re / dd, -den.im / dd);
                 }
-                sh.tau[j] = tau;
-                sh.w[0] = scal;  // broadcast slot, read before w is overwritten
-                sh.e[j] = beta;
-                sh.d[j] = A[(size_t)j * N + j].re;
+                for (int i = lane; i < m; i += 32) {
+                    const cx<T> vi = (i == 0) ? mk<T>(1, 0) : conj(rowj[i]) * scal;
+                    sh.v[i] = vi;
+                    rowj[i] = vi;  // keep v_j in row j for the back-transformation
+                }
+                if (lane == 0) {
+                    sh.tau[j] = tau;
+                    sh.e[j] = beta;
+                    sh.d[j] = A[(size_t)j * N + j].re;
+                }
             }
             __syncthreads();
             const cx<T> tau = sh.tau[j];
-            const cx<T> scal = sh.w[0];
-            __syncthreads();
-            for (int i = tid; i < m; i += nthr) {
-                cx<T> vi = (i == 0) ? mk<T>(1, 0) : conj(rowj[i]) * scal;
-                sh.v[i] = vi;
-                rowj[i] = vi;  // keep v_j in row j for the back-transformation
-            }
-            __syncthreads();
             if (tau.re == T(0) && tau.im == T(0)) continue;
-            // w = tau * A22 v  (warp per row)
+            // w = tau * A22 v (warp per row); per-warp partial of w^H v
+            cx<T> dpart = mk<T>(0, 0);
             for (int i = warp; i < m; i += nwarps) {
                 const cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
                 cx<T> acc = mk<T>(0, 0);
                 for (int l = lane; l < m; l += 32) fma_cx(acc, row[l], sh.v[l]);
                 acc.re = warp_sum(acc.re);
                 acc.im = warp_sum(acc.im);
-                if (lane == 0) sh.w[i] = tau * acc;
+                const cx<T> wi = tau * acc;
+                if (lane == 0) sh.w[i] = wi;
+                fma_cjx(dpart, wi, sh.v[i]);
+            }
+            if (lane == 0) {
+                sh.red[warp] = dpart.re;
+                sh.red[32 + warp] = dpart.im;
             }
             __syncthreads();
-            // alpha2 = -1/2 tau (w^H v); w += alpha2 v
             cx<T> dp = mk<T>(0, 0);
-            for (int i = tid; i < m; i += nthr) fma_cjx(dp, sh.w[i], sh.v[i]);
-            block_sum2(dp.re, dp.im, sh.red);
+            for (int w2 = 0; w2 < nwarps; ++w2) {
+                dp.re += sh.red[w2];
+                dp.im += sh.red[32 + w2];
+            }
+            // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H
             const cx<T> alpha2 = T(-0.5) * (tau * dp);
-            for (int i = tid; i < m; i += nthr) sh.w[i] = sh.w[i] + alpha2 * sh.v[i];
-            __syncthreads();
-            // A22 -= v w^H + w v^H
             for (int i = warp; i < m; i += nwarps) {
                 cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
-                const cx<T> vi = sh.v[i], wi = sh.w[i];
+                const cx<T> vi = sh.v[i];
+                const cx<T> wi = sh.w[i] + alpha2 * vi;
                 for (int l = lane; l < m; l += 32) {
-                    cx<T> a = row[l];
-                    const cx<T> vl = sh.v[l], wl = sh.w[l];
-                    a = a - mulc(vi, wl) - mulc(wi, vl);
-                    row[l] = a;
+                    const cx<T> vl = sh.v[l];
+                    const cx<T> wl = sh.w[l] + alpha2 * vl;
+                    row[l] = row[l] - mulc(vi, wl) - mulc(wi, vl);
                 }
             }
             __syncthreads();
@@ -439,7 +443,7 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
                             const unsigned h = hash32((unsigned)(r * 7919 + jj * 104729 + 12345));
                             x[(size_t)r * G] = T(1) + T(0.5) * ((T)(h & 0xffff) / T(65535) - T(0.5));
                         }
-                        for (int iter = 0; iter < 3; ++iter) {
+                        for (int iter = 0; iter < (sizeof(T) == sizeof(float) ? 2 : 3); ++iter) {
                             tri_solve<T>(N, sh.d, sh.e, shift, pert, x, u0, u1, u2, G);
                             // Gram-Schmidt against earlier cluster members (stored in U, real parts)
                             for (int pp = i; pp < jj; ++pp) {
@@ -472,13 +476,14 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
         __syncthreads();
 
         // ----------------------------------------------- back-transform --
-        // Panel P holds PB columns of U, column-major (P[c*N + r]).
+        // Panel P holds PB columns of U, column-major with stride N + 1.
         cx<T>* P = reinterpret_cast<cx<T>*>(sh.scratch);
+        const int PS = N + 1;
         for (int c0 = 0; c0 < N; c0 += PB) {
             const int pw = min(PB, N - c0);
             for (int idx = tid; idx < N * pw; idx += nthr) {
                 const int r = idx / pw, c = idx % pw;
-                P[(size_t)c * N + r] = U[(size_t)r * N + c0 + c];
+                P[(size_t)c * PS + r] = U[(size_t)r * N + c0 + c];
             }
             __syncthreads();
             for (int j = N - 2; j >= 0; --j) {
@@ -486,26 +491,21 @@ __global__ void __launch_bounds__(256) heev_kernel(int N, int64_t batch, zc* __r
                 if (tau.re == T(0) && tau.im == T(0)) continue;
                 const int m = N - 1 - j;
                 const cx<T>* vj = A + (size_t)j * N + (j + 1);
-                // s_c = tau * sum_i conj(v_i) P[c][j+1+i]: one warp per column
+                // one warp per column: s_c = tau sum_i conj(v_i) P[c][j+1+i], then the update
                 for (int c = warp; c < pw; c += nwarps) {
-                    const cx<T>* pc = P + (size_t)c * N + (j + 1);
+                    cx<T>* pc = P + (size_t)c * PS + (j + 1);
                     cx<T> acc = mk<T>(0, 0);
                     for (int i = lane; i < m; i += 32) fma_cjx(acc, vj[i], pc[i]);
                     acc.re = warp_sum(acc.re);
                     acc.im = warp_sum(acc.im);
-                    if (lane == 0) sh.w[c] = tau * acc;
-                }
-                __syncthreads();
-                for (int c = warp; c < pw; c += nwarps) {
-                    cx<T>* pc = P + (size_t)c * N + (j + 1);
-                    const cx<T> sc = sh.w[c];
+                    const cx<T> sc = tau * acc;
                     for (int i = lane; i < m; i += 32) pc[i] = pc[i] - vj[i] * sc;
                 }
                 __syncthreads();
             }
             for (int idx = tid; idx < N * pw; idx += nthr) {
                 const int r = idx / pw, c = idx % pw;
-                U[(size_t)r * N + c0 + c] = P[(size_t)c * N + r];
+                U[(size_t)r * N + c0 + c] = P[(size_t)c * PS + r];
             }
             __syncthreads();
         }
@@ -524,7 +524,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     int dev = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = (N <= 32) ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    const int threads = (N <= 16) ? 32 : (N <= 48 ? 128 : (sizeof(T) == sizeof(float) ? 512 : 256));
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     int64_t grid = (int64_t)nsm * perSM;
@@ -547,8 +547,8 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (precision == 0) return 0;
-    const size_t smem = eig_smem_bytes<float>(N, true, 32, 32);
-    if (smem <= 200 * 1024) return 0;
+    const size_t smem = eig_smem_bytes<float>(N, true, 32, 64);
+    if (smem <= 210 * 1024) return 0;
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
@@ -572,7 +572,7 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     int dev = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = (N <= 32) ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    const int threads = (N <= 16) ? 32 : (N <= 48 ? 128 : 256);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
@@ -585,11 +585,11 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
                     size_t work_bytes, int* status_d) {
     if (batch <= 0) return TBG_OK;
-    const size_t smem = eig_smem_bytes<float>(N, true, 32, 32);
-    if (smem <= 200 * 1024)
-        return launch_heev<float, true, 32, 32>(st, N, batch, H, E, U, work, work_bytes, status_d,
+    const size_t smem = eig_smem_bytes<float>(N, true, 32, 64);
+    if (smem <= 210 * 1024)
+        return launch_heev<float, true, 32, 64>(st, N, batch, H, E, U, work, work_bytes, status_d,
                                                 "heev_kernel<float,smem>");
-    return launch_heev<float, false, 32, 32>(st, N, batch, H, E, U, work, work_bytes, status_d,
+    return launch_heev<float, false, 32, 64>(st, N, batch, H, E, U, work, work_bytes, status_d,
                                              "heev_kernel<float,global>");
 }
 
