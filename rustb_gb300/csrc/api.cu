@@ -577,9 +577,24 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
     if (nmu > 0) TBG_CUDA(cudaMemcpyAsync(mu_d, mu, sizeof(double) * nmu, cudaMemcpyHostToDevice, ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
+    const bool small = N <= kSmallMaxN && M.n_rmat == 0;
     for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
         const int64_t nkc = std::min(J.chunk, nk - c0);
         TBG_CUDA(cudaMemcpyAsync(J.k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
+        if (small) {
+            if ((rc = small_fused(M, ctx.st, nkc, J.k_d, 0, nullptr, dirs_d, spin, eta, occ_out ? nmu : 0, mu_d, width,
+                                  J.Om, J.E, occ_out ? S : nullptr)))
+                return rc;
+            if (Omega_out)
+                TBG_CUDA(cudaMemcpyAsync(Omega_out + c0 * N, J.Om, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost,
+                                         ctx.st));
+            if (E_out)
+                TBG_CUDA(cudaMemcpyAsync(E_out + c0 * N, J.E, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+            if (occ_out)
+                TBG_CUDA(cudaMemcpyAsync(occ_out + c0, S, sizeof(double) * nkc, cudaMemcpyDeviceToHost, ctx.st));
+            if (ctx.sync("berry")) return ctx.rc;
+            continue;
+        }
         if ((rc = run_berry_chunk(ctx, J, nkc, nullptr))) return rc;
         if (Omega_out)
             TBG_CUDA(cudaMemcpyAsync(Omega_out + c0 * N, J.Om, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
@@ -675,12 +690,19 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
     const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
+    const bool small = N <= kSmallMaxN && M.n_rmat == 0;
     for (int64_t c0 = 0; c0 < k_count; c0 += J.chunk) {
         const int64_t nkc = std::min(J.chunk, k_count - c0);
-        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(k_begin + c0, nkc, M.dim, n0, n1, n2, J.k_d);
-        TBG_LAUNCHED("kmesh_kernel");
-        if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
-        if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
+        if (small) {
+            if ((rc = small_fused(M, ctx.st, nkc, nullptr, k_begin + c0, kmesh, dirs_d, spin, eta, (int)nmu, mu_d,
+                                  width, nullptr, nullptr, S)))
+                return rc;
+        } else {
+            kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(k_begin + c0, nkc, M.dim, n0, n1, n2, J.k_d);
+            TBG_LAUNCHED("kmesh_kernel");
+            if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
+            if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
+        }
         if ((rc = kahan_column_sums(ctx.st, nkc, (int)nmu, S, acc))) return rc;
     }
     std::vector<double> acc_h(2 * nmu);

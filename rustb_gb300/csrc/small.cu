@@ -1,0 +1,289 @@
+// Fused path for small models (nsta <= 8): one thread per k-point runs the
+// whole of berry_curvature_at_impl (src/response/traits.rs:160-200) in
+// registers / local memory, FP64:
+//   H, V_0, V_1 by the Fourier sum over R with the Atom gauge and tau term
+//   (src/velocity.rs:538-622), optional spin dressing (traits.rs:170-175),
+//   eigenpairs by cyclic complex Jacobi, U^H V U, Omega_n, and the
+//   occupation sums per chemical potential (linear/mod.rs:204-223).
+// For nsta <= 8 the per-k work is a few thousand flops, so one launch covers
+// tens of thousands of k-points and the batched per-matrix kernels would be
+// dominated by launch and synchronisation overhead.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "tbgpu_internal.cuh"
+
+namespace tbg {
+namespace {
+
+constexpr double kTwoPiS = 6.283185307179586476925286766559;
+
+__device__ __forceinline__ double fermi_s(double e, double mu, double width) {
+    if (width == 0.0) return (e < mu) ? 1.0 : ((e > mu) ? 0.0 : 0.5);
+    const double x = (e - mu) / width;
+    if (x > 50.0) return 0.0;
+    if (x < -50.0) return 1.0;
+    return 1.0 / (1.0 + exp(x));
+}
+
+// Cyclic complex Jacobi on the Hermitian NM x NM (active N) matrix A; W gets
+// the eigenvectors in columns.  Rotation: G = diag(1, e^{-i phi}) [[c,-s],[s,c]]
+// with e^{i phi} = a_pq / |a_pq|, tan 2 theta = 2 |a_pq| / (a_pp - a_qq).
+template <int NM>
+__device__ void jacobi(int N, zc (&A)[NM][NM], zc (&W)[NM][NM]) {
+    for (int i = 0; i < NM; ++i)
+        for (int j = 0; j < NM; ++j) W[i][j] = mk(i == j ? 1.0 : 0.0, 0.0);
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        double off = 0.0, dia = 0.0;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                if (i != j)
+                    off += abs2(A[i][j]);
+                else
+                    dia += abs2(A[i][j]);
+            }
+        if (off <= 1e-32 * dia || off == 0.0) break;
+        for (int p = 0; p < N - 1; ++p)
+            for (int q = p + 1; q < N; ++q) {
+                const zc apq = A[p][q];
+                const double mag = sqrt(abs2(apq));
+                if (mag == 0.0) continue;
+                const double app = A[p][p].re, aqq = A[q][q].re;
+                const zc ph = mk(apq.re / mag, apq.im / mag);
+                const zc emi = conj(ph);
+                const double theta = 0.5 * atan2(2.0 * mag, app - aqq);
+                double sn, cs;
+                sincos(theta, &sn, &cs);
+                for (int k = 0; k < N; ++k) {
+                    const zc akp = A[k][p], akq = emi * A[k][q];
+                    A[k][p] = cs * akp + sn * akq;
+                    A[k][q] = cs * akq - sn * akp;
+                }
+                for (int k = 0; k < N; ++k) {
+                    const zc apk = A[p][k], aqk = ph * A[q][k];
+                    A[p][k] = cs * apk + sn * aqk;
+                    A[q][k] = cs * aqk - sn * apk;
+                }
+                A[p][q] = mk(0.0, 0.0);
+                A[q][p] = mk(0.0, 0.0);
+                A[p][p].im = 0.0;
+                A[q][q].im = 0.0;
+                for (int k = 0; k < N; ++k) {
+                    const zc wkp = W[k][p], wkq = emi * W[k][q];
+                    W[k][p] = cs * wkp + sn * wkq;
+                    W[k][q] = cs * wkq - sn * wkp;
+                }
+            }
+    }
+}
+
+template <int NM>
+__global__ void __launch_bounds__(128) small_fused_kernel(
+    int N, int norb, int dim, int nR, int64_t nk, const double* __restrict__ klist, int64_t k0, int64_t n0,
+    int64_t n1, int64_t n2, const zc* __restrict__ ham, const int* __restrict__ hamR, const double* __restrict__ Rcart,
+    const double* __restrict__ tau, const double* __restrict__ taucart, const double* __restrict__ dirs, int spin,
+    double eta, int nmu, const double* __restrict__ mu, double width, double* __restrict__ Om_out,
+    double* __restrict__ E_out, double* __restrict__ S_out) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nk) return;
+    double kv[3] = {0.0, 0.0, 0.0};
+    if (klist) {
+        for (int d = 0; d < dim; ++d) kv[d] = klist[t * dim + d];
+    } else {
+        const int64_t idx = k0 + t;  // gen_kmesh order (src/kpoints.rs:49-87)
+        if (dim == 1) {
+            kv[0] = (double)idx / (double)n0;
+        } else if (dim == 2) {
+            kv[0] = (double)(idx / n1) / (double)n0;
+            kv[1] = (double)(idx % n1) / (double)n1;
+        } else {
+            kv[0] = (double)(idx / (n1 * n2)) / (double)n0;
+            kv[1] = (double)((idx / n2) % n1) / (double)n1;
+            kv[2] = (double)(idx % n2) / (double)n2;
+        }
+    }
+    zc H[NM][NM], V0[NM][NM], V1[NM][NM];
+    for (int i = 0; i < NM; ++i)
+        for (int j = 0; j < NM; ++j) H[i][j] = V0[i][j] = V1[i][j] = mk(0.0, 0.0);
+    const double* w0 = dirs;
+    const double* w1 = dirs + dim;
+    for (int r = 0; r < nR; ++r) {
+        const int* R = hamR + 3 * r;
+        double s = (double)R[0] * kv[0];
+        if (dim > 1) s += (double)R[1] * kv[1];
+        if (dim > 2) s += (double)R[2] * kv[2];
+        double sn, cs;
+        sincos(kTwoPiS * s, &sn, &cs);
+        const zc u = mk(cs, sn);
+        const double* rc = Rcart + 3 * r;
+        double c0 = w0[0] * rc[0], c1 = w1[0] * rc[0];
+        if (dim > 1) {
+            c0 += w0[1] * rc[1];
+            c1 += w1[1] * rc[1];
+        }
+        if (dim > 2) {
+            c0 += w0[2] * rc[2];
+            c1 += w1[2] * rc[2];
+        }
+        const zc* hr = ham + (int64_t)r * N * N;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                const zc tt = u * hr[i * N + j];
+                H[i][j] = H[i][j] + tt;
+                V0[i][j] = V0[i][j] + mk(-c0 * tt.im, c0 * tt.re);  // i c0 t
+                V1[i][j] = V1[i][j] + mk(-c1 * tt.im, c1 * tt.re);
+            }
+    }
+    // Atom gauge + tau term
+    zc ph[NM];
+    double tp0[NM], tp1[NM];
+    for (int s = 0; s < N; ++s) {
+        const double* ts = tau + 3 * s;
+        double a = ts[0] * kv[0];
+        if (dim > 1) a += ts[1] * kv[1];
+        if (dim > 2) a += ts[2] * kv[2];
+        double sn, cs;
+        sincos(kTwoPiS * a, &sn, &cs);
+        ph[s] = mk(cs, sn);
+        const double* tc = taucart + 3 * s;
+        double p0 = w0[0] * tc[0], p1 = w1[0] * tc[0];
+        if (dim > 1) {
+            p0 += w0[1] * tc[1];
+            p1 += w1[1] * tc[1];
+        }
+        if (dim > 2) {
+            p0 += w0[2] * tc[2];
+            p1 += w1[2] * tc[2];
+        }
+        tp0[s] = p0;
+        tp1[s] = p1;
+    }
+    for (int m = 0; m < N; ++m)
+        for (int n = 0; n < N; ++n) {
+            const zc g = cmul(ph[m], ph[n]);
+            const zc hl = H[m][n];
+            const double d0 = tp0[n] - tp0[m], d1 = tp1[n] - tp1[m];
+            V0[m][n] = (V0[m][n] + mk(-d0 * hl.im, d0 * hl.re)) * g;
+            V1[m][n] = (V1[m][n] + mk(-d1 * hl.im, d1 * hl.re)) * g;
+            H[m][n] = hl * g;
+        }
+    if (spin >= 0) {  // J = 1/2 (S V0 + V0 S), S = sigma (x) I / 2
+        zc J[NM][NM];
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                auto ent = [&](int x, int& px, zc& sx) {
+                    const bool up = x < norb;
+                    if (spin == TBG_SPIN_X) {
+                        px = up ? x + norb : x - norb;
+                        sx = mk(0.5, 0.0);
+                    } else if (spin == TBG_SPIN_Y) {
+                        px = up ? x + norb : x - norb;
+                        sx = up ? mk(0.0, -0.5) : mk(0.0, 0.5);
+                    } else {
+                        px = x;
+                        sx = up ? mk(0.5, 0.0) : mk(-0.5, 0.0);
+                    }
+                };
+                int pi, pj, ppj;
+                zc si, sj;
+                ent(i, pi, si);
+                ent(j, pj, sj);
+                ent(pj, ppj, sj);  // (V S)[i][j] = V[i][pi(j)] S[pi(j)][j]
+                const zc a = si * V0[pi][j];
+                const zc c = V0[i][pj] * sj;
+                J[i][j] = mk(0.5 * (a.re + c.re), 0.5 * (a.im + c.im));
+            }
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) V0[i][j] = J[i][j];
+    }
+    zc W[NM][NM];
+    jacobi<NM>(N, H, W);
+    double E[NM];
+    int ord[NM];
+    for (int i = 0; i < N; ++i) {
+        E[i] = H[i][i].re;
+        ord[i] = i;
+    }
+    for (int i = 1; i < N; ++i) {  // ascending order (insertion sort of the index)
+        const int oi = ord[i];
+        int j = i - 1;
+        while (j >= 0 && E[ord[j]] > E[oi]) {
+            ord[j + 1] = ord[j];
+            --j;
+        }
+        ord[j + 1] = oi;
+    }
+    // band-basis velocities B = W^H V W (H reused as scratch)
+    zc Bx[NM][NM], By[NM][NM];
+    for (int a = 0; a < N; ++a)
+        for (int b = 0; b < N; ++b) {
+            zc sx = mk(0.0, 0.0), sy = mk(0.0, 0.0);
+            for (int i = 0; i < N; ++i) {
+                zc tx = mk(0.0, 0.0), ty = mk(0.0, 0.0);
+                for (int j = 0; j < N; ++j) {
+                    fma_cx(tx, V0[i][j], W[j][b]);
+                    fma_cx(ty, V1[i][j], W[j][b]);
+                }
+                fma_cjx(sx, W[i][a], tx);
+                fma_cjx(sy, W[i][a], ty);
+            }
+            Bx[a][b] = sx;
+            By[a][b] = sy;
+        }
+    const double eta2 = eta * eta;
+    double Om[NM];
+    for (int a = 0; a < N; ++a) {
+        double v = 0.0;
+        for (int b = 0; b < N; ++b) {
+            if (a == b) continue;
+            const double im = Bx[a][b].re * By[b][a].im + Bx[a][b].im * By[b][a].re;
+            const double de = E[a] - E[b];
+            v += -2.0 * im / (de * de + eta2);
+        }
+        Om[a] = v;
+    }
+    for (int i = 0; i < N; ++i) {
+        if (Om_out) Om_out[t * N + i] = Om[ord[i]];
+        if (E_out) E_out[t * N + i] = E[ord[i]];
+    }
+    if (S_out) {
+        for (int j = 0; j < nmu; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < N; ++i) s += Om[ord[i]] * fermi_s(E[ord[i]], mu[j], width);
+            S_out[t * nmu + j] = s;
+        }
+    }
+}
+
+}  // namespace
+
+int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* klist_d, int64_t k0,
+                const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
+                double width, double* Om, double* E, double* S) {
+    if (nk <= 0) return TBG_OK;
+    const int N = (int)m.nsta;
+    const int64_t n0 = kmesh ? kmesh[0] : 1, n1 = (kmesh && m.dim > 1) ? kmesh[1] : 1,
+                  n2 = (kmesh && m.dim > 2) ? kmesh[2] : 1;
+    const unsigned blocks = (unsigned)((nk + 127) / 128);
+    KTimer kt(st, "small_fused_kernel");
+#define SMALL_LAUNCH(NM)                                                                                          \
+    small_fused_kernel<NM><<<blocks, 128, 0, st>>>(N, (int)m.norb, m.dim, (int)m.nR, nk, klist_d, k0, n0, n1, n2, \
+                                                   m.ham, m.hamR_d, m.Rcart_d, m.tau_d, m.taucart_d, dirs_d, spin,  \
+                                                   eta, nmu, mu_d, width, Om, E, S)
+    if (N <= 2)
+        SMALL_LAUNCH(2);
+    else if (N <= 4)
+        SMALL_LAUNCH(4);
+    else if (N <= 8)
+        SMALL_LAUNCH(8);
+    else
+        return set_error(TBG_E_UNSUPPORTED, "small_fused: nsta > 8");
+#undef SMALL_LAUNCH
+    TBG_LAUNCHED("small_fused_kernel");
+    return TBG_OK;
+}
+
+}  // namespace tbg

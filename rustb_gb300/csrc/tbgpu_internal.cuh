@@ -175,6 +175,14 @@ int occupation_sums(cudaStream_t st, int N, int64_t batch, const double* Omega, 
 // to a running (sum, compensation) pair held in acc (2*nmu).
 int kahan_column_sums(cudaStream_t st, int64_t nk, int nmu, const double* S, double* acc);
 
+// Fused one-thread-per-k path for nsta <= 8 (FP64): Omega, E and/or the
+// occupation sums S (nk, nmu).  k from klist_d (nk, dim), or, when klist_d is
+// null, the mesh points [k0, k0 + nk) of kmesh.
+int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* klist_d, int64_t k0,
+                const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
+                double width, double* Om, double* E, double* S);
+constexpr int kSmallMaxN = 8;
+
 // ------------------------------------------------------------- mixed path --
 int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U,
                      void* work, size_t work_bytes, int* status_d, int64_t* clusters_d);

@@ -289,3 +289,29 @@ def test_empty_k_list_is_ok():
     h = M.haldane()
     E = h.solve_band_all_parallel(np.zeros((0, 2)))
     assert E.shape == (0, 2)
+
+
+# ----------------------------------------------------- small-N fused path --
+@pytest.mark.parametrize("norb,spin_model,dim,spin", [(3, False, 2, None), (5, False, 3, None),
+                                                      (4, True, 2, SpinDirection.Z), (4, True, 3, SpinDirection.X),
+                                                      (2, True, 2, SpinDirection.Y), (1, False, 1, None)])
+def test_small_fused_path_matches_oracle(norb, spin_model, dim, spin):
+    m = W.random_model(dim, norb, spin_model, 1, seed=50 + norb + dim)
+    rng = np.random.default_rng(norb)
+    k = rng.uniform(0, 1, (37, dim))
+    dirs = np.eye(dim)[:2] if dim > 1 else np.array([[1.0], [1.0]])
+    p = Parameters(kmesh=(1,) * dim, direction=dirs, mu=[0.0])
+    if spin is not None:
+        p = p.with_spin(spin)
+    Om, E = m.berry_curvature_on(k, p)
+    Omr, Er = O.berry_on(m, k, dirs, -1 if spin is None else int(spin))
+    assert np.max(np.abs(E - Er)) <= 1e-12 * max(1.0, np.max(np.abs(Er)))
+    assert rel(Om, Omr) < 1e-8
+    if dim > 1:
+        mus = np.array([-0.3, 0.0, 0.4])
+        ph = Parameters(kmesh=(5,) * dim, direction=dirs, mu=mus)
+        if spin is not None:
+            ph = ph.with_spin(spin)
+        s = m.hall_conductivity(ph).conductivity
+        ref = O.hall_conductivity(m, (5,) * dim, dirs, mus, 0.0, 1e-3, -1 if spin is None else int(spin))
+        assert np.max(np.abs(s - ref)) <= 1e-8 * max(np.max(np.abs(ref)), 1e-12)
