@@ -57,10 +57,13 @@ enum tbg_gauge { TBG_GAUGE_LATTICE = 0, TBG_GAUGE_ATOM = 1 };
 /* Spin-current polarisation (src/model.rs:470-474); -1 = None (charge current). */
 enum tbg_spin { TBG_SPIN_NONE = -1, TBG_SPIN_X = 0, TBG_SPIN_Y = 1, TBG_SPIN_Z = 2 };
 
-/* Arithmetic of tbg_hall_conductivity / tbg_berry_curvature. */
+/* Arithmetic of tbg_hall_conductivity / tbg_berry_curvature.  MIXED applies
+ * to models with nsta <= 256; larger models run FP64 (tbg_report.precision
+ * says which ran). */
 enum tbg_precision {
     TBG_PREC_FP64 = 0,  /* plain: FP64 end to end (the drop-in) */
-    TBG_PREC_MIXED = 1  /* FP32 eigensolve + FP64 eigenpair refinement */
+    TBG_PREC_MIXED = 1  /* FP32 eigensolve, refinement and rotation on the
+                           tensor cores with FP64-class exact-slice products */
 };
 
 typedef struct tbg_model tbg_model;
@@ -70,7 +73,8 @@ typedef struct tbg_report {
     int64_t nk;              /* k-points processed */
     int64_t nsta;            /* bands per k-point */
     int32_t precision;       /* tbg_precision used */
-    int32_t fourier_mode;    /* 0 = direct phase x hop contraction, 1 = separable mesh transform */
+    int32_t fourier_mode;    /* 0 = FP64 phase x hop contraction, 1 = exact-slice tensor-core
+                                contraction, 2 = fused small-model path (nsta <= 8) */
     int64_t kernel_launches; /* device kernels launched by the call */
     double device_ms;        /* device time of the call (CUDA events) */
     double eig_ms;           /* device time spent in the eigensolver kernels */

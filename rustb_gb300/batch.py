@@ -1,0 +1,185 @@
+"""Batched Hall conductivity over many models of uneven size.
+
+Every model is uploaded once and stays resident.  The k-mesh of each model is
+cut into work items (model, flat k-range); items are bucketed by band count
+and run largest-first by a pool of host threads.  Each thread calls the
+thread-safe C-ABI (``tbg_hall_sums_range``), which runs on its own CUDA stream,
+so items of different models overlap on the device.  Partial sums of each
+model are combined on the host with an exactly rounded sum (``math.fsum``) and
+normalised as ``hall_conductivity`` does (src/response/linear/mod.rs:204-223).
+
+The chunk size (k-points per item) and the number of concurrent items are
+chosen per band-count bucket by :class:`Autotuner`, which times a few
+candidates on the first models of a bucket and caches the winner in a JSON
+file keyed by GPU name, bucket and precision.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import ctypes
+import json
+import math
+import os
+import threading
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .model import Model
+from .params import HallConductivityResult, Parameters, Precision, spin_code
+
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def bucket_of(nsta: int) -> int:
+    """Band-count bucket: the next power of two (>= 8)."""
+    b = 8
+    while b < nsta:
+        b *= 2
+    return b
+
+
+@dataclass
+class Job:
+    model: Model
+    params: Parameters
+
+
+class Autotuner:
+    """Chooses (chunk k-points, concurrent items) per (bucket, precision)."""
+
+    CHUNKS = (256, 1024, 4096, 16384)
+    WORKERS = (1, 2, 4)
+
+    def __init__(self, path: str = DEFAULT_CACHE, gpu: str = "GPU"):
+        self.path = path
+        self.gpu = gpu
+        self.lock = threading.Lock()
+        self.table = {}
+        if os.path.exists(path):
+            try:
+                self.table = json.load(open(path))
+            except (OSError, ValueError):
+                self.table = {}
+
+    def key(self, bucket: int, precision: int) -> str:
+        return f"{self.gpu}|{bucket}|{precision}"
+
+    def get(self, bucket: int, precision: int):
+        return self.table.get(self.key(bucket, precision))
+
+    def tune(self, bucket: int, precision: int, job: Job, lib) -> dict:
+        """Time each candidate on a slice of this job's mesh."""
+        m, p = job.model, job.params
+        nk = int(np.prod(p.kmesh))
+        best = None
+        for chunk in self.CHUNKS:
+            if chunk > max(256, nk):
+                break
+            for workers in self.WORKERS:
+                n_items = max(1, min(workers * 2, nk // chunk))
+                t0 = time.perf_counter()
+                ranges = [(i * chunk % nk, min(chunk, nk - (i * chunk % nk))) for i in range(n_items)]
+                with cf.ThreadPoolExecutor(workers) as ex:
+                    list(ex.map(lambda r: _run_range(lib, m, p, precision, r[0], r[1]), ranges))
+                dt = time.perf_counter() - t0
+                rate = sum(r[1] for r in ranges) / dt
+                if best is None or rate > best["rate"]:
+                    best = {"chunk": chunk, "workers": workers, "rate": rate}
+        with self.lock:
+            self.table[self.key(bucket, precision)] = best
+            try:
+                os.makedirs(os.path.dirname(self.path), exist_ok=True)
+                json.dump(self.table, open(self.path, "w"), indent=1)
+            except OSError:
+                pass
+        return best
+
+
+def _run_range(lib, model: Model, p: Parameters, precision: int, k0: int, cnt: int) -> np.ndarray:
+    km = np.ascontiguousarray(p.kmesh, dtype=np.int64)
+    d = _lib.as_f64(p.direction)
+    mu = _lib.as_f64(p.mu)
+    out = np.empty(len(mu))
+    _lib.check(lib.tbg_hall_sums_range(model.device_handle(), _lib.iptr(km), int(k0), int(cnt), _lib.dptr(d),
+                                       len(mu), _lib.dptr(mu), float(p.T[0]), float(p.eta), spin_code(p.spin),
+                                       int(precision), _lib.dptr(out), None), lib)
+    return out
+
+
+class BatchRunner:
+    def __init__(self, precision=Precision.MIXED, autotune: bool = True, cache_path: str = DEFAULT_CACHE,
+                 max_workers: int = 4):
+        self.lib = _lib.load()
+        self.precision = int(precision)
+        self.autotune = autotune
+        self.tuner = Autotuner(cache_path, gpu=_gpu_name())
+        self.max_workers = max_workers
+        self.stats = {}
+
+    def hall_many(self, jobs: list[Job]) -> list[HallConductivityResult]:
+        for j in jobs:
+            j.params.validate_rank2(j.model.dim)
+            j.model.device_handle()  # upload once, resident
+        buckets = {}
+        for idx, j in enumerate(jobs):
+            buckets.setdefault(bucket_of(j.model.nsta), []).append(idx)
+        plan = {}
+        for b, idxs in buckets.items():
+            cfg = self.tuner.get(b, self.precision)
+            if cfg is None and self.autotune:
+                probe = max(idxs, key=lambda i: np.prod(jobs[i].params.kmesh))
+                cfg = self.tuner.tune(b, self.precision, jobs[probe], self.lib)
+            plan[b] = cfg or {"chunk": 4096, "workers": 2}
+        items = []
+        for b, idxs in buckets.items():
+            chunk = plan[b]["chunk"]
+            for i in idxs:
+                nk = int(np.prod(jobs[i].params.kmesh))
+                for k0 in range(0, nk, chunk):
+                    cost = min(chunk, nk - k0) * _work_per_k(jobs[i].model)
+                    items.append((cost, i, k0, min(chunk, nk - k0)))
+        items.sort(key=lambda it: -it[0])  # largest first
+        partial = [[] for _ in jobs]
+        lock = threading.Lock()
+        workers = max(1, min(self.max_workers, max(p["workers"] for p in plan.values())))
+
+        def run(it):
+            _, i, k0, cnt = it
+            s = _run_range(self.lib, jobs[i].model, jobs[i].params, self.precision, k0, cnt)
+            with lock:
+                partial[i].append(s)
+
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(workers) as ex:
+            list(ex.map(run, items))
+        dt = time.perf_counter() - t0
+        out = []
+        for i, j in enumerate(jobs):
+            arr = np.array(partial[i])
+            nk = int(np.prod(j.params.kmesh))
+            det = float(np.linalg.det(j.model.lat))
+            sig = np.array([math.fsum(arr[:, c]) for c in range(arr.shape[1])]) / nk / det
+            out.append(HallConductivityResult(chemical_potentials=j.params.mu.copy(), conductivity=sig))
+        self.stats = {"seconds": dt, "items": len(items), "workers": workers, "plan": plan,
+                      "k_points": sum(int(np.prod(j.params.kmesh)) for j in jobs)}
+        return out
+
+
+def _work_per_k(m: Model) -> float:
+    N = m.nsta
+    return 24.0 * m.nR * N * N + 46.0 * N ** 3
+
+
+def _gpu_name() -> str:
+    try:
+        import subprocess
+
+        r = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                           capture_output=True, text=True, timeout=10)
+        return r.stdout.strip() or "GPU"
+    except Exception:
+        return "GPU"

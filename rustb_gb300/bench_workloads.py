@@ -1,0 +1,266 @@
+"""Measurements of the other k-mesh workloads (used by ``bench.py --workload``).
+
+* ``haldane``   -- Haldane model, 200 x 200 mesh, sigma_xy at mu = 0 (Chern
+                   number checked); a step is the whole mesh.
+* ``supercell`` -- 1024-orbital 2D supercell, 9 R vectors, 64 x 64 mesh; a step
+                   is one batch of mesh points (FP64: models above 256 bands
+                   run the plain path).
+* ``batched``   -- the first ``--models`` of the 512 seeded uneven models
+                   (norb log-uniform in [4, 256], half 2D / half 3D, their full
+                   meshes); a step is the whole set through BatchRunner.
+* ``serve``     -- resident models, Poisson arrivals of (model, k-list of
+                   1-4096 points, observable) requests at 20-100 % of the
+                   measured peak; p50 / p99 latency per load.
+
+Each prints one JSON line in the bench.py format.  The CPU baseline of each
+(``--impl reference``) is the C port of the reference path on the host cores.
+"""
+
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import _lib, batch, serve, workloads as W
+from .params import Parameters, Precision
+
+METRIC_K = "k-pts/s (H+eig+Berry, norb=128) mixed vs FP64 GPU @AHC err≤1e-6; serve p99"
+
+
+def _line(args, world, metric, value, unit, ms_per_step, dtype, config, extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": unit != "ms",
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+           "data": "synthetic (seeded models, numpy default_rng)", "config": config}
+    out.update(extra)
+    print(json.dumps(out), flush=True)
+
+
+def _cpu_port(model, dirs, mu, kmesh, k0, nk, threads=None):
+    from oracle import build_port
+
+    build_port.load()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    build_port.hall_sums(model, dirs, mu, 0.0, 1e-3, -1, kmesh=kmesh, k0=k0, nk=nk, threads=threads)
+    return nk / (time.perf_counter() - t0), threads
+
+
+def run(args, rank, world, local):
+    if rank != 0 and args.impl == "reference":
+        return 0
+    fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench}[args.workload]
+    return fn(args, rank, world, local)
+
+
+# ----------------------------------------------------------------- haldane --
+def haldane(args, rank, world, local):
+    model = W.haldane_200()
+    mesh = (200, 200)
+    nk = 40000
+    dirs = np.eye(2)
+    cfg = {"workload": "Haldane model (lattice [sqrt3,-1],[sqrt3,1]; t1=-1, t2=0.15i, M=0.2), 200x200 mesh, "
+                       "sigma_xy at mu=0, T=0, eta=1e-3", "k_mesh": list(mesh)}
+    if args.impl == "reference":
+        val, thr = _cpu_port(model, dirs, [0.0], mesh, 0, nk)
+        _line(args, world, METRIC_K, val, "k-pts/s", nk / val * 1e3, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "k-pts/s", "cores": thr, "kind": "port",
+                                                     "sample": "the whole 200x200 mesh"},
+               "e2e": {"value": val, "unit": "k-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    p = Parameters.rank2(mesh, [1.0, 0.0], [0.0, 1.0], [0.0])
+    rep = {}
+    for _ in range(args.warmup):
+        model.hall_conductivity(p)
+    t_dev = 0.0
+    l0 = lib.tbg_kernel_launch_count(0)
+    for _ in range(args.steps):
+        s = model.hall_conductivity(p, report=rep).conductivity[0]
+        t_dev += rep["device_ms"] / 1e3
+    launches = lib.tbg_kernel_launch_count(0) - l0
+    val = args.steps * nk * world / t_dev
+    # e2e: model upload + the whole mesh + sigma readback per step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m2 = W.haldane_200()
+        m2.hall_conductivity(p)
+        m2._invalidate()
+    e2e = args.steps * nk / (time.perf_counter() - t0)
+    cpu, thr = _cpu_port(model, dirs, [0.0], mesh, 0, nk)
+    _line(args, world, METRIC_K, val, "k-pts/s", t_dev / args.steps * 1e3, "f64", cfg,
+          {"chern": 2 * math.pi * s, "gpu_launches": int(launches),
+           "cpu_baseline": {"value": cpu, "unit": "k-pts/s", "cores": thr, "kind": "port",
+                            "sample": "the whole 200x200 mesh"},
+           "e2e": {"value": e2e, "unit": "k-pts/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
+                   "d2h_bytes_per_step": 8}})
+    return 0
+
+
+# --------------------------------------------------------------- supercell --
+def supercell(args, rank, world, local):
+    model = W.supercell_2d()
+    mesh = (64, 64)
+    B = args.batch if args.batch != 8192 else 152
+    dirs = np.eye(2)
+    cfg = {"workload": "2D supercell, 1024 orbitals, R in {-1,0,1}^2, t=exp(-d/0.8) N(0,1) complex, onsite "
+                       "U(-0.5,0.5), 64x64 mesh, sigma_xy at mu=0", "k_mesh": list(mesh), "batch_kpts": B}
+    if args.impl == "reference":
+        n = max(1, (os.cpu_count() or 1))
+        val, thr = _cpu_port(model, dirs, [0.0], mesh, 0, n)
+        _line(args, world, METRIC_K, val, "k-pts/s", n / val * 1e3, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "k-pts/s", "cores": thr, "kind": "port",
+                                                     "sample": f"{n} k-points of the 64x64 mesh"},
+               "e2e": {"value": val, "unit": "k-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    h = model.device_handle()
+    import ctypes
+
+    km = np.ascontiguousarray(mesh, dtype=np.int64)
+    mu = np.array([0.0])
+    out = np.zeros(1)
+    rep = _lib.TbgReport()
+
+    def step(s):
+        k0 = (s * B) % 4096
+        _lib.check(lib.tbg_hall_sums_range(h, _lib.iptr(km), k0, min(B, 4096 - k0), _lib.dptr(dirs), 1,
+                                           _lib.dptr(mu), 0.0, 1e-3, -1, int(Precision.MIXED), _lib.dptr(out),
+                                           ctypes.byref(rep)), lib)
+        return rep.device_ms / 1e3
+
+    for w in range(args.warmup):
+        step(w)
+    lib.tbg_kernel_timing_enable(1)
+    _lib.kernel_timing(reset=True)
+    t = sum(step(args.warmup + s) for s in range(args.steps))
+    lib.tbg_kernel_timing_enable(0)
+    timing = _lib.kernel_timing(reset=True)
+    val = args.steps * B * world / t
+    _line(args, world, METRIC_K, val, "k-pts/s", t / args.steps * 1e3, "f64 (mixed path is limited to 256 bands)", cfg,
+          {"precision_ran": int(rep.precision),
+           "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in timing.items()},
+           "flops_per_k": 24.0 * model.nR * 1024 ** 2 + 46.0 * 1024 ** 3})
+    return 0
+
+
+# ----------------------------------------------------------------- batched --
+def _batched_jobs(n_models):
+    specs = W.batched_uneven_specs(512)[:n_models]
+    jobs = []
+    for dim, norb, mesh, seed in specs:
+        m = W.random_model(dim, norb, False, 3, seed=seed)
+        dirs = np.eye(dim)[:2]
+        jobs.append(batch.Job(m, Parameters(kmesh=mesh, direction=dirs, mu=[0.0])))
+    return jobs
+
+
+def batched(args, rank, world, local):
+    # 512 specs alternate 2D/3D by halves: take the subset from both halves
+    n = args.models
+    specs_all = W.batched_uneven_specs(512)
+    idx = list(range(n // 2)) + list(range(256, 256 + n - n // 2))
+    jobs = []
+    for i in idx:
+        dim, norb, mesh, seed = specs_all[i]
+        m = W.random_model(dim, norb, False, 3, seed=seed)
+        jobs.append(batch.Job(m, Parameters(kmesh=mesh, direction=np.eye(dim)[:2], mu=[0.0])))
+    nk = sum(int(np.prod(j.params.kmesh)) for j in jobs)
+    flops = sum(int(np.prod(j.params.kmesh)) * batch._work_per_k(j.model) for j in jobs)
+    cfg = {"workload": f"batched uneven: {len(jobs)} of the 512 seeded models (norb log-uniform [4,256], half 2D "
+                       "R|<=3 (49 R), half 3D (343 R), meshes 32^2-128^2 / 16^3-48^3), sigma_xy mu=0",
+           "models": len(jobs), "k_points": nk}
+    if args.impl == "reference":
+        j = max(jobs, key=lambda j: j.model.nsta)
+        sample = 64
+        val, thr = _cpu_port(j.model, j.params.direction, [0.0], j.params.kmesh, 0, sample)
+        val_flops = val * batch._work_per_k(j.model)
+        _line(args, world, "algorithmic GFLOP/s (batched uneven models)", val_flops / 1e9, "GFLOP/s", 0.0, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val_flops / 1e9, "unit": "GFLOP/s", "cores": thr,
+                                                     "kind": "port", "sample": f"{sample} k of the largest model"},
+               "e2e": {"value": val_flops / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    runner = batch.BatchRunner(Precision.MIXED, autotune=True)
+    runner.hall_many(jobs)  # warm-up + autotune
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        runner.hall_many(jobs)
+    dt = (time.perf_counter() - t0) / args.steps
+    _line(args, world, "algorithmic GFLOP/s (batched uneven models)", flops / dt / 1e9, "GFLOP/s", dt * 1e3,
+          "f32 eigensolve + exact-slice tensor products", cfg,
+          {"k_pts_per_s": nk / dt, "plan": runner.stats["plan"], "items": runner.stats["items"],
+           "workers": runner.stats["workers"]})
+    return 0
+
+
+# ------------------------------------------------------------------- serve --
+def serve_bench(args, rank, world, local):
+    rng = np.random.default_rng(20260105)
+    models = {}
+    for i in range(16):
+        dim = 2 if i % 2 == 0 else 3
+        norb = int(round(math.exp(rng.uniform(math.log(4), math.log(256)))))
+        models[i] = W.random_model(dim, norb, False, 3, seed=500 + i)
+    cfg = {"workload": "serving: 16 resident seeded models (norb log-uniform [4,256]), requests of 1-4096 random "
+                       "k-points, observable uniform in {bands, berry, sigma_xy}, Poisson arrivals",
+           "models": len(models)}
+    if args.impl == "reference":
+        _line(args, world, "p99 latency (serving, 80% load)", None, "ms", 0.0, "f64", cfg,
+              {"impl": "reference", "unavailable": "the reference has no serving loop; see the k-pts/s arms"})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+
+    def make_req():
+        mid = int(rng.integers(0, len(models)))
+        nk = int(rng.integers(1, 4097))
+        obs = serve.OBSERVABLES[int(rng.integers(0, 3))]
+        return serve.Request(mid, rng.uniform(0, 1, (nk, models[mid].dim)), obs)
+
+    for _ in range(6):  # warm-up of every code path
+        r = make_req()
+        serve.execute(models[r.model_id], r)
+    # peak: a saturating burst
+    srv = serve.Server(models, hbm_budget_bytes=96 << 30, max_inflight=8)
+    burst = [make_req() for _ in range(64)]
+    t0 = time.perf_counter()
+    futs = [srv.submit(r) for r in burst]
+    for f in futs:
+        f.result()
+    t_burst = time.perf_counter() - t0
+    srv.close()
+    peak_req = len(burst) / t_burst
+    peak_k = sum(len(r.k) for r in burst) / t_burst
+    loads = {}
+    for frac in (0.2, 0.4, 0.6, 0.8, 1.0):
+        srv = serve.Server(models, hbm_budget_bytes=96 << 30, max_inflight=8)
+        rate = frac * peak_req
+        t_end = time.perf_counter() + args.serve_seconds
+        futs = []
+        kpts = 0
+        t_start = time.perf_counter()
+        while time.perf_counter() < t_end:
+            r = make_req()
+            kpts += len(r.k)
+            futs.append(srv.submit(r))
+            time.sleep(rng.exponential(1.0 / rate))
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t_start
+        srv.close()
+        lat = srv.latencies() * 1e3
+        loads[f"{int(frac * 100)}%"] = {"requests": len(futs), "p50_ms": float(np.percentile(lat, 50)),
+                                        "p99_ms": float(np.percentile(lat, 99)), "k_pts_per_s": kpts / wall}
+    p99_80 = loads["80%"]["p99_ms"]
+    _line(args, world, "p99 latency (serving, 80% load)", p99_80, "ms", p99_80, "f32 eigensolve + exact-slice tensor products",
+          cfg, {"loads": loads, "peak_requests_per_s": peak_req, "peak_k_pts_per_s": peak_k})
+    return 0

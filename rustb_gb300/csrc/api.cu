@@ -221,6 +221,13 @@ double lattice_det(const std::vector<double>& lat, int dim) {
            lat[2] * (lat[3] * lat[7] - lat[4] * lat[6]);
 }
 
+// The mixed path's exact-slice tensor-core GEMM contracts over the band index
+// with K <= 256; larger models run the FP64 path (reported in tbg_report).
+int effective_precision(const ModelDev& M, int precision) {
+    if (precision == TBG_PREC_MIXED && M.nsta > 256) return TBG_PREC_FP64;
+    return precision;
+}
+
 // Shared per-chunk response pipeline: (k on device) -> Omega, E.
 struct BerryJob {
     ModelDev* m;
@@ -558,6 +565,7 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
         return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
     if (nk == 0) return TBG_OK;
+    precision = effective_precision(M, precision);
     const int N = (int)M.nsta;
     const int64_t NN = (int64_t)N * N;
     Ctx ctx;
@@ -657,6 +665,7 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
         return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
     if (!out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    precision = effective_precision(M, precision);
     const double det = lattice_det(M.lat, M.dim);
     if (whole && (det == 0.0 || !std::isfinite(det)))
         return set_error(TBG_E_LINALG, "Linear algebra operation failed: singular lattice");
@@ -722,7 +731,7 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
         report->nk = k_count;
         report->nsta = N;
         report->precision = precision;
-        report->fourier_mode = 0;
+        report->fourier_mode = small ? 2 : (precision == TBG_PREC_MIXED ? 1 : 0);
         report->kernel_launches = g_launches - launches0;
         report->device_ms = ms;
         report->eig_ms = 0.0;

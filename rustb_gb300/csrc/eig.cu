@@ -193,10 +193,11 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
-template <typename T, bool A_SMEM, int G, int PB>
+template <typename T, bool A_SMEM>
 __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    double* __restrict__ Eout, cx<T>* __restrict__ Uout,
-                                                   cx<T>* __restrict__ Awork, int* __restrict__ status) {
+                                                   cx<T>* __restrict__ Awork, int* __restrict__ status, int G,
+                                                   int PB) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     EigShared<T> sh;
     {
@@ -514,11 +515,22 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
     }
 }
 
-template <typename T, bool A_SMEM, int G, int PB>
+// Inverse-iteration group G and back-transform panel PB sized to the shared
+// memory left after the matrix (when resident) and the per-matrix vectors.
+template <typename T>
+inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB) {
+    const size_t budget = 200 * 1024;
+    const size_t fixed = eig_smem_bytes<T>(N, a_smem, 0, 0);
+    const size_t left = budget > fixed ? budget - fixed : 0;
+    G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
+    PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 1))));
+}
+
+template <typename T, bool A_SMEM>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
-                size_t work_bytes, int* status_d, const char* name) {
+                size_t work_bytes, int* status_d, const char* name, int G, int PB) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
-    auto kern = heev_kernel<T, A_SMEM, G, PB>;
+    auto kern = heev_kernel<T, A_SMEM>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
     int dev = 0, nsm = 0, perSM = 0;
@@ -538,17 +550,23 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
     KTimer kt(st, name, 14.0 * (double)N * N * N * batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d, G, PB);
     TBG_LAUNCHED(name);
     return TBG_OK;
+}
+
+// FP32 solver: matrix in shared memory when it fits.
+inline bool f32_in_smem(int N) {
+    int G, PB;
+    choose_g_pb<float>(N, true, 32, 64, G, PB);
+    return eig_smem_bytes<float>(N, true, G, PB) <= 200 * 1024 && G >= 8 && PB >= 16;
 }
 
 }  // namespace
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (precision == 0) return 0;
-    const size_t smem = eig_smem_bytes<float>(N, true, 32, 64);
-    if (smem <= 210 * 1024) return 0;
+    if (f32_in_smem(N)) return 0;
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
@@ -556,8 +574,10 @@ size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
 int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
                 size_t work_bytes, int* status_d) {
     if (batch <= 0) return TBG_OK;
-    return launch_heev<double, false, 16, 16>(st, N, batch, A, E, U, work, work_bytes, status_d,
-                                              "heev_kernel<double>");
+    int G, PB;
+    choose_g_pb<double>(N, false, 16, 16, G, PB);
+    return launch_heev<double, false>(st, N, batch, A, E, U, work, work_bytes, status_d, "heev_kernel<double>", G,
+                                      PB);
 }
 
 // Eigenvalues only, FP64, of `batch` matrices held in caller-provided device
@@ -565,8 +585,10 @@ int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, 
 // events, nothing but the kernel on `st`.
 int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double* E) {
     if (batch <= 0) return TBG_OK;
-    const size_t smem = eig_smem_bytes<double>(N, false, 16, 16);
-    auto kern = heev_kernel<double, false, 16, 16>;
+    int G, PB;
+    choose_g_pb<double>(N, false, 16, 16, G, PB);
+    const size_t smem = eig_smem_bytes<double>(N, false, G, PB);
+    auto kern = heev_kernel<double, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
     int dev = 0, nsm = 0, perSM = 0;
@@ -576,7 +598,7 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, E, nullptr, nullptr, nullptr);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, E, nullptr, nullptr, nullptr, G, PB);
     TBG_LAUNCHED("heev_kernel<double> (static scratch)");
     return TBG_OK;
 }
@@ -585,12 +607,15 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
                     size_t work_bytes, int* status_d) {
     if (batch <= 0) return TBG_OK;
-    const size_t smem = eig_smem_bytes<float>(N, true, 32, 64);
-    if (smem <= 210 * 1024)
-        return launch_heev<float, true, 32, 64>(st, N, batch, H, E, U, work, work_bytes, status_d,
-                                                "heev_kernel<float,smem>");
-    return launch_heev<float, false, 32, 64>(st, N, batch, H, E, U, work, work_bytes, status_d,
-                                             "heev_kernel<float,global>");
+    int G, PB;
+    if (f32_in_smem(N)) {
+        choose_g_pb<float>(N, true, 32, 64, G, PB);
+        return launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
+                                        G, PB);
+    }
+    choose_g_pb<float>(N, false, 32, 64, G, PB);
+    return launch_heev<float, false>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,global>",
+                                     G, PB);
 }
 
 }  // namespace tbg

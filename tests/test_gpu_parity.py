@@ -315,3 +315,24 @@ def test_small_fused_path_matches_oracle(norb, spin_model, dim, spin):
         s = m.hall_conductivity(ph).conductivity
         ref = O.hall_conductivity(m, (5,) * dim, dirs, mus, 0.0, 1e-3, -1 if spin is None else int(spin))
         assert np.max(np.abs(s - ref)) <= 1e-8 * max(np.max(np.abs(ref)), 1e-12)
+
+
+# ------------------------------------------------------------ large models --
+@pytest.mark.parametrize("norb,spin", [(256, False), (160, True), (512, False)])
+def test_large_models_eigenvalues_and_berry(norb, spin):
+    m = W.random_model(2, norb, spin, 1, seed=norb)
+    k = np.random.default_rng(2).uniform(0, 1, (2, 2))
+    E = m.solve_band_all_parallel(k)
+    Hs = O.gen_ham_batch(m, k, 1)
+    for i in range(len(k)):
+        nrm = np.linalg.norm(Hs[i], 2)
+        assert np.max(np.abs(E[i] - O.eigvalsh(Hs[i]))) <= 1e-10 * nrm
+    if m.nsta <= 320:
+        p = Parameters.rank2((1, 1), [1.0, 0.0], [0.0, 1.0], [0.0])
+        Om, E2 = m.berry_curvature_on(k[:1], p)
+        Omr, Er = O.berry_on(m, k[:1], np.eye(2))
+        assert rel(Om, Omr) < 1e-8
+        Omm, Em = m.berry_curvature_on(k[:1], p, Precision.MIXED)
+        assert np.max(np.abs(Em - Er)) <= 1e-9 * np.linalg.norm(Hs[0], 2)
+        occ = Er[0] < 0
+        assert abs((Omm[0] * occ).sum() - (Omr[0] * occ).sum()) <= 1e-6 * np.abs(Omr[0]).sum()
