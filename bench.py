@@ -263,9 +263,10 @@ def main():
     sums = np.zeros(1)
     rep = _lib.TbgReport()
 
+    from rustb_gb300 import shard
+
     def step(s, precision=prec, batch=B):
-        k0 = ((s * world + rank) * batch) % NK
-        cnt = min(batch, NK - k0)
+        k0, cnt = shard.step_range(NK, batch, world, rank, s)
         _lib.check(lib.tbg_hall_sums_range(handle, _lib.iptr(km), k0, cnt, _lib.dptr(DIRS), 1, _lib.dptr(MU), 0.0,
                                            ETA, -1, int(precision), _lib.dptr(sums), ctypes.byref(rep)), lib)
         return cnt
