@@ -158,7 +158,11 @@ def kernel_roofline(timing: dict, peaks: dict) -> dict | None:
     if name.startswith("heev_kernel<float") or name.startswith("fp32"):
         bound, peak, src = "fp32", peaks["fp32_tflops"], "FP32 FMA loop on this GPU (tbg_measure_fma_peaks)"
     elif name.startswith("ozaki"):
-        bound, peak, src = "tensor", peaks.get("bf16_tflops"), "MEASURED_PEAKS.json bf16_tflops (burst)"
+        # FP64-class products from 21 BF16 digit products (6 for the low class):
+        # the attainable algorithmic rate is the BF16 peak divided by the pair count
+        pairs = 6 if "low" in name else 21
+        bound, peak = "tensor", (peaks.get("bf16_tflops") or 0.0) / pairs
+        src = f"MEASURED_PEAKS.json bf16_tflops (burst) / {pairs} slice products"
     else:
         bound, peak, src = "fp64", peaks["fp64_tflops"], "FP64 FMA loop on this GPU (tbg_measure_fma_peaks)"
     achieved = work / (ms / 1e3) / 1e12 if ms > 0 and work > 0 else None

@@ -211,6 +211,7 @@ int check_status(int* status_d, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "status readback");
     if (h & 1) return set_error(TBG_E_NOCONV, "eigensolver input contains NaN or Inf");
+    if (h & 2) return set_error(TBG_E_TIMEOUT, "a bounded device wait ran out in a tensor-core kernel");
     return TBG_OK;
 }
 

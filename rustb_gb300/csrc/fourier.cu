@@ -345,12 +345,12 @@ int ozaki_fourier_max_k();
 size_t ozaki_hop_slices_bytes(int K, int64_t Nc);
 int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs);
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
-                  const void* Bs, float4* C);
+                  const void* Bs, float4* C, int* err);
 
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
     const size_t N = (size_t)m.nsta, NN = N * N, nR = (size_t)m.nR;
     return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) + 3 * NN * sizeof(float4)) +
-           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 8 * 256;
+           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 9 * 256;
 }
 
 int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H, zc* V,
@@ -393,6 +393,7 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
     double* taup = static_cast<double*>(take(sizeof(double) * 2 * N));
     int* EA = static_cast<int*>(take(sizeof(int) * 3 * nk));
     float4* C = static_cast<float4*>(take(sizeof(float4) * 3 * nk * NN));
+    int* err = static_cast<int*>(take(sizeof(int)));
     {
         KTimer kt(st, "phases_kernel");
         const int total = 2 * (nR + N);
@@ -408,7 +409,9 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_error(e, "phases");
     }
-    int rc = ozaki_fourier(st, 3 * nk, NN, nR, ph3, EA, m.hop_EB, m.hop_slices, C);
+    int rc = cudaMemsetAsync(err, 0, sizeof(int), st) == cudaSuccess ? TBG_OK : set_error(TBG_E_CUDA, "memset");
+    if (rc) return rc;
+    rc = ozaki_fourier(st, 3 * nk, NN, nR, ph3, EA, m.hop_EB, m.hop_slices, C, err);
     if (rc) return rc;
     {
         KTimer kt(st, "gauge_pairs_kernel");

@@ -337,6 +337,10 @@ namespace tbg {
 int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                 const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
                 int64_t sC, int* EA, int* EB);
+int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+bool ozaki_use_tc();
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
 
 namespace {
@@ -469,13 +473,20 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx
     int* EB = EA + batch * N;
     const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
     void* eigw = take(eigw_bytes);
+    // FP64-class products: tcgen05 form unless the mma.sync form is selected
+    auto hp = [&](bool conj_a, int fa, int fb, const void* A, int64_t sA, const void* B, int64_t sB,
+                  float4* C) -> int {
+        if (ozaki_use_tc())
+            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, sA, B, N, sB, C, N, NN, EA, EB, status_d);
+        return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, sA, B, N, sB, C, N, NN, EA, EB);
+    };
     int rc;
     // 1. FP32 eigenpairs
     if ((rc = eig_batched_f32(st, N, batch, const_cast<zc*>(H), E, X, eigw, eigw_bytes, status_d))) return rc;
     // 2. R = I - X^H X, S = X^H (H X)   (FP64-class, tensor cores)
-    if ((rc = ozaki_zgemm(st, true, true, F32, F32, batch, N, N, N, X, N, NN, X, N, NN, bA, N, NN, EA, EB))) return rc;
-    if ((rc = ozaki_zgemm(st, true, false, F64, F32, batch, N, N, N, H, N, NN, X, N, NN, bB, N, NN, EA, EB))) return rc;
-    if ((rc = ozaki_zgemm(st, true, true, F32, PAIR, batch, N, N, N, X, N, NN, bB, N, NN, bC, N, NN, EA, EB))) return rc;
+    if ((rc = hp(true, F32, F32, X, NN, X, NN, bA))) return rc;
+    if ((rc = hp(false, F64, F32, H, NN, X, NN, bB))) return rc;
+    if ((rc = hp(true, F32, PAIR, X, NN, bB, NN, bC))) return rc;
     {
         KTimer kt(st, "pairs_to_z_kernel");
         pairs_to_z_kernel<<<nblk(batch * NN), 256, 0, st>>>(N, batch, bA, Rz, 1);
@@ -498,14 +509,10 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx
         TBG_LAUNCHED("xprime_kernel");
     }
     // 5. band-basis velocities B = X'^H V X'
-    if ((rc = ozaki_zgemm(st, true, false, F64, PAIR, batch, N, N, N, Vx, N, ldV, bA, N, NN, bB, N, NN, EA, EB)))
-        return rc;
-    if ((rc = ozaki_zgemm(st, true, false, F64, PAIR, batch, N, N, N, Vy, N, ldV, bA, N, NN, bC, N, NN, EA, EB)))
-        return rc;
-    if ((rc = ozaki_zgemm(st, true, true, PAIR, PAIR, batch, N, N, N, bA, N, NN, bB, N, NN, bD, N, NN, EA, EB)))
-        return rc;
-    if ((rc = ozaki_zgemm(st, true, true, PAIR, PAIR, batch, N, N, N, bA, N, NN, bC, N, NN, bE, N, NN, EA, EB)))
-        return rc;
+    if ((rc = hp(false, F64, PAIR, Vx, ldV, bA, NN, bB))) return rc;
+    if ((rc = hp(false, F64, PAIR, Vy, ldV, bA, NN, bC))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, NN, bB, NN, bD))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, NN, bC, NN, bE))) return rc;
     // 6. Omega
     {
         KTimer kt(st, "berry_kernel");

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 #include "tbgpu_internal.cuh"
@@ -386,6 +387,46 @@ int launch_oz(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* 
 
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc) { return sizeof(int) * (size_t)batch * (M + Nc) + 256; }
 
+// Row / column exponents for any operand format combination (shared by the
+// mma.sync and tcgen05 forms).
+int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                     const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, int* EA, int* EB) {
+    const int64_t lines = batch * (M + Nc);
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((lines * 32 + 255) / 256, 152 * 64));
+#define EXP_CASE(CJ, FA, FB)                                                                              \
+    if (conj_a == CJ && fmt_a == FA && fmt_b == FB) {                                                     \
+        oz_exp_kernel<FA, FB, CJ><<<blocks, 256, 0, st>>>(batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB); \
+        TBG_LAUNCHED("oz_exp_kernel");                                                                    \
+        return TBG_OK;                                                                                    \
+    }
+    EXP_CASE(false, FMT_F64, FMT_F64)
+    EXP_CASE(true, FMT_F64, FMT_F64)
+    EXP_CASE(true, FMT_F32, FMT_F32)
+    EXP_CASE(false, FMT_F64, FMT_F32)
+    EXP_CASE(true, FMT_F32, FMT_PAIR)
+    EXP_CASE(false, FMT_F64, FMT_PAIR)
+    EXP_CASE(true, FMT_PAIR, FMT_PAIR)
+    EXP_CASE(false, FMT_F32, FMT_F64)
+#undef EXP_CASE
+    return set_error(TBG_E_UNSUPPORTED, "ozaki_exp_launch: format combination");
+}
+
+int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
+                     const void* Bs, float4* C, int* err);
+
+// tcgen05 kernels are used unless TBG_OZAKI_MMA_SYNC=1 (the mma.sync form).
+bool ozaki_use_tc() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("TBG_OZAKI_MMA_SYNC");
+        v = (e && e[0] == '1') ? 0 : 1;
+    }
+    return v == 1;
+}
+
 namespace {
 
 // Column exponents of the hop table: EB[e] over R (one warp per column e).
@@ -464,10 +505,11 @@ int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, in
 
 // C (M x Nc, float pairs) = A (M x K, complex double) . hop (digit planes).
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
-                  const void* Bs, float4* C) {
+                  const void* Bs, float4* C, int* err) {
     if (K > ozaki_fourier_max_k()) return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier: nR > 408");
     row_exp_kernel<<<(unsigned)std::min<int64_t>((M * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(M, K, A, K, EA);
     TBG_LAUNCHED("row_exp_kernel");
+    if (ozaki_use_tc() && err) return ozaki_fourier_tc(st, M, Nc, K, A, EA, EB, Bs, C, err);
     constexpr int SA = 6, SB = 6, LMAX = 5;
     const size_t smem = sizeof(__nv_bfloat16) * OZ_PAD * (SA * OZ_TM + SB * 2 * OZ_TN);
     auto kern = oz_gemm_kernel<SA, SB, LMAX, false, FMT_F64, FMT_PRESLICED>;
@@ -515,7 +557,7 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
 // Internal test hook (not part of the public header): C = op(A) B for host
 // complex-double inputs, result as complex double (hi + lo).
 extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int M, int Nc, int K, const double* A,
-                                        const double* B, double* C) {
+                                        const double* B, double* C, int use_tc) {
     using namespace tbg;
     const int64_t ar = conj_a ? K : M, ac = conj_a ? M : K;
     const size_t abytes = sizeof(double) * 2 * ar * ac * batch, bbytes = sizeof(double) * 2 * (size_t)K * Nc * batch;
@@ -531,8 +573,20 @@ extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int
         cudaMemcpy(dA, A, abytes, cudaMemcpyHostToDevice);
         cudaMemcpy(dB, B, bbytes, cudaMemcpyHostToDevice);
         int* EA = static_cast<int*>(dE);
-        rc = ozaki_zgemm(st, high != 0, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
-                         static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M);
+        int* derr = nullptr;
+        cudaMalloc(&derr, sizeof(int));
+        cudaMemset(derr, 0, sizeof(int));
+        if (use_tc && high)
+            rc = ozaki_zgemm_tc(st, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
+                                static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr);
+        else
+            rc = ozaki_zgemm(st, high != 0, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc,
+                             (int64_t)K * Nc, static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M);
+        int herr = 0;
+        cudaStreamSynchronize(st);
+        cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+        cudaFree(derr);
+        if (!rc && (herr & 2)) rc = set_error(TBG_E_TIMEOUT, "ozaki tcgen05 kernel: a bounded wait ran out");
         cudaError_t e = cudaStreamSynchronize(st);
         if (!rc && e != cudaSuccess) rc = cuda_error(e, "ozaki test");
         if (!rc) {

@@ -13,7 +13,7 @@ from rustb_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 
-def ozaki(lib, A, B, conj_a, high):
+def ozaki(lib, A, B, conj_a, high, use_tc=0):
     batch = A.shape[0]
     if conj_a:
         K, M = A.shape[1], A.shape[2]
@@ -24,18 +24,20 @@ def ozaki(lib, A, B, conj_a, high):
     dp = ctypes.POINTER(ctypes.c_double)
     fn = lib.tbg_internal_ozaki_zgemm
     fn.restype = ctypes.c_int
-    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
+                   ctypes.c_int]
     A = np.ascontiguousarray(A)
     B = np.ascontiguousarray(B)
     st = fn(int(high), int(conj_a), batch, M, Nc, K, A.view(np.float64).ctypes.data_as(dp),
-            B.view(np.float64).ctypes.data_as(dp), C.view(np.float64).ctypes.data_as(dp))
+            B.view(np.float64).ctypes.data_as(dp), C.view(np.float64).ctypes.data_as(dp), int(use_tc))
     _lib.check(st, lib)
     return C
 
 
+@pytest.mark.parametrize("use_tc", [0, 1], ids=["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("conj_a", [False, True])
-@pytest.mark.parametrize("M,Nc,K", [(128, 128, 128), (70, 40, 100), (256, 64, 256), (1, 3, 2)])
-def test_ozaki_high_precision(conj_a, M, Nc, K):
+@pytest.mark.parametrize("M,Nc,K", [(128, 128, 128), (70, 40, 100), (256, 64, 256), (1, 3, 2), (200, 130, 48)])
+def test_ozaki_high_precision(conj_a, M, Nc, K, use_tc):
     lib = _lib.load()
     rng = np.random.default_rng(M + Nc + K)
     batch = 3
@@ -50,7 +52,7 @@ def test_ozaki_high_precision(conj_a, M, Nc, K):
     B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
     opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
     ref = opA @ B
-    C = ozaki(lib, A, B, conj_a, True)
+    C = ozaki(lib, A, B, conj_a, True, use_tc)
     scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
     err = np.abs(C - ref) / scale
     assert err.max() < 1e-12, err.max()
