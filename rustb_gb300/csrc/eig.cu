@@ -125,7 +125,7 @@ __device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ 
         if (fabs(cd) >= fabs(b)) {
             T piv = cd;
             if (fabs(piv) < pert) piv = (piv < 0) ? -pert : pert;
-            const T mlt = b / piv;
+            const T mlt = Lim<T>::div(b, piv);
             u0[i * G] = piv;
             u1[i * G] = cs;
             u2[i * G] = 0;
@@ -134,7 +134,7 @@ __device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ 
             cs = b1;
             cr = xn - mlt * cr;
         } else {
-            const T mlt = cd / b;
+            const T mlt = Lim<T>::div(cd, b);
             u0[i * G] = b;
             u1[i * G] = a1;
             u2[i * G] = b1;
@@ -155,7 +155,7 @@ __device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ 
         T r = x[i * G];
         if (i + 1 < N) r -= u1[i * G] * y1;
         if (i + 2 < N) r -= u2[i * G] * y2;
-        const T yi = r / u0[i * G];
+        const T yi = Lim<T>::div(r, u0[i * G]);
         x[i * G] = yi;
         y2 = y1;
         y1 = yi;
@@ -180,12 +180,12 @@ struct EigShared {
 template <typename T>
 __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB) {
     size_t b = 0;
-    if (a_smem) b += sizeof(cx<T>) * (size_t)N * N;
+    if (a_smem) b += sizeof(cx<T>) * (size_t)N * (N + 4);  // rows padded to N + 4 (bank spread)
     b += sizeof(T) * 4 * (size_t)N;
     b += sizeof(cx<T>) * 3 * (size_t)N;
     b += sizeof(T) * 64;
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-    size_t s2 = sizeof(cx<T>) * (size_t)(N + 1) * PB;
+    size_t s2 = sizeof(cx<T>) * (size_t)(N + 4) * PB;
     b += std::max(s1, s2);
     b += 16;
     return b;
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         unsigned char* p = smem_raw;
         if (A_SMEM) {
             sh.A = reinterpret_cast<cx<T>*>(p);
-            p += sizeof(cx<T>) * (size_t)N * N;
+            p += sizeof(cx<T>) * (size_t)N * (N + 4);
         }
         sh.tau = reinterpret_cast<cx<T>*>(p);
         p += sizeof(cx<T>) * N;
@@ -224,13 +224,14 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         p += sizeof(T) * 64;
         sh.scratch = reinterpret_cast<T*>(p);
         size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-        size_t s2 = sizeof(cx<T>) * (size_t)(N + 1) * PB;
+        size_t s2 = sizeof(cx<T>) * (size_t)(N + 4) * PB;
         p += std::max(s1, s2);
         sh.flags = reinterpret_cast<int*>(p);
     }
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
     const size_t NN = (size_t)N * N;
+    const int LDA = A_SMEM ? N + 4 : N;  // row stride of the working matrix
 
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         cx<T>* A;
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             const zc* src = Hin + b * NN;
             for (size_t idx = tid; idx < NN; idx += nthr) {
                 zc h = src[idx];
-                A[idx] = mk<T>((T)h.re, (T)h.im);
+                A[(idx / N) * LDA + idx % N] = mk<T>((T)h.re, (T)h.im);
             }
         }
         if (tid == 0) sh.flags[0] = 0;
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         // ------------------------------------------------- tridiagonalise --
         for (int j = 0; j < N - 1; ++j) {
             const int m = N - 1 - j;
-            cx<T>* rowj = A + (size_t)j * N + (j + 1);  // row j, columns j+1.. = conj(column j)
+            cx<T>* rowj = A + (size_t)j * LDA + (j + 1);  // row j, columns j+1.. = conj(column j)
             // reflector by warp 0: H_j^H [alpha; x] = [beta; 0]
             if (warp == 0) {
                 T part = 0;
@@ -284,23 +285,33 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                 if (lane == 0) {
                     sh.tau[j] = tau;
                     sh.e[j] = beta;
-                    sh.d[j] = A[(size_t)j * N + j].re;
+                    sh.d[j] = A[(size_t)j * LDA + j].re;
                 }
             }
             __syncthreads();
             const cx<T> tau = sh.tau[j];
             if (tau.re == T(0) && tau.im == T(0)) continue;
-            // w = tau * A22 v (warp per row); per-warp partial of w^H v
+            // w = tau * A22 v: four threads per row, two-level butterfly; partial of w^H v
             cx<T> dpart = mk<T>(0, 0);
-            for (int i = warp; i < m; i += nwarps) {
-                const cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
-                cx<T> acc = mk<T>(0, 0);
-                for (int l = lane; l < m; l += 32) fma_cx(acc, row[l], sh.v[l]);
-                acc.re = warp_sum(acc.re);
-                acc.im = warp_sum(acc.im);
-                const cx<T> wi = tau * acc;
-                if (lane == 0) sh.w[i] = wi;
-                fma_cjx(dpart, wi, sh.v[i]);
+            {
+                const int q = tid & 3;
+                const unsigned gm = 0xFu << (lane & 28);
+                for (int i = tid >> 2; i < m; i += nthr >> 2) {
+                    const cx<T>* row = A + (size_t)(j + 1 + i) * LDA + (j + 1);
+                    cx<T> acc = mk<T>(0, 0);
+                    for (int l = q; l < m; l += 4) fma_cx(acc, row[l], sh.v[l]);
+                    acc.re += __shfl_xor_sync(gm, acc.re, 1);
+                    acc.im += __shfl_xor_sync(gm, acc.im, 1);
+                    acc.re += __shfl_xor_sync(gm, acc.re, 2);
+                    acc.im += __shfl_xor_sync(gm, acc.im, 2);
+                    if (q == 0) {
+                        const cx<T> wi = tau * acc;
+                        sh.w[i] = wi;
+                        fma_cjx(dpart, wi, sh.v[i]);
+                    }
+                }
+                dpart.re = warp_sum(dpart.re);
+                dpart.im = warp_sum(dpart.im);
             }
             if (lane == 0) {
                 sh.red[warp] = dpart.re;
@@ -315,7 +326,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H
             const cx<T> alpha2 = T(-0.5) * (tau * dp);
             for (int i = warp; i < m; i += nwarps) {
-                cx<T>* row = A + (size_t)(j + 1 + i) * N + (j + 1);
+                cx<T>* row = A + (size_t)(j + 1 + i) * LDA + (j + 1);
                 const cx<T> vi = sh.v[i];
                 const cx<T> wi = sh.w[i] + alpha2 * vi;
                 for (int l = lane; l < m; l += 32) {
@@ -327,7 +338,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             __syncthreads();
         }
         if (tid == 0) {
-            sh.d[N - 1] = A[(size_t)(N - 1) * N + (N - 1)].re;
+            sh.d[N - 1] = A[(size_t)(N - 1) * LDA + (N - 1)].re;
             sh.e[N - 1] = 0;
         }
         __syncthreads();
@@ -477,9 +488,11 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         __syncthreads();
 
         // ----------------------------------------------- back-transform --
-        // Panel P holds PB columns of U, column-major with stride N + 1.
+        // Panel P holds PB columns of U, column-major with stride N + 4.  Column
+        // c belongs to the 8 threads 8c .. 8c+7 (rows interleaved), which apply
+        // every reflector to it without block barriers.
         cx<T>* P = reinterpret_cast<cx<T>*>(sh.scratch);
-        const int PS = N + 1;
+        const int PS = N + 4;
         for (int c0 = 0; c0 < N; c0 += PB) {
             const int pw = min(PB, N - c0);
             for (int idx = tid; idx < N * pw; idx += nthr) {
@@ -487,23 +500,29 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                 P[(size_t)c * PS + r] = U[(size_t)r * N + c0 + c];
             }
             __syncthreads();
-            for (int j = N - 2; j >= 0; --j) {
-                const cx<T> tau = sh.tau[j];
-                if (tau.re == T(0) && tau.im == T(0)) continue;
-                const int m = N - 1 - j;
-                const cx<T>* vj = A + (size_t)j * N + (j + 1);
-                // one warp per column: s_c = tau sum_i conj(v_i) P[c][j+1+i], then the update
-                for (int c = warp; c < pw; c += nwarps) {
-                    cx<T>* pc = P + (size_t)c * PS + (j + 1);
+            const int ngroups = nthr >> 3;
+            const int q8 = tid & 7;
+            const unsigned gm = 0xFFu << (lane & 24);
+            for (int c = tid >> 3; c < pw; c += ngroups) {
+                cx<T>* pc = P + (size_t)c * PS;
+                for (int j = N - 2; j >= 0; --j) {
+                    const cx<T> tau = sh.tau[j];
+                    if (tau.re == T(0) && tau.im == T(0)) continue;
+                    const int m = N - 1 - j;
+                    const cx<T>* vj = A + (size_t)j * LDA + (j + 1);
                     cx<T> acc = mk<T>(0, 0);
-                    for (int i = lane; i < m; i += 32) fma_cjx(acc, vj[i], pc[i]);
-                    acc.re = warp_sum(acc.re);
-                    acc.im = warp_sum(acc.im);
+                    for (int i = q8; i < m; i += 8) fma_cjx(acc, vj[i], pc[j + 1 + i]);
+#pragma unroll
+                    for (int o = 1; o < 8; o <<= 1) {
+                        acc.re += __shfl_xor_sync(gm, acc.re, o);
+                        acc.im += __shfl_xor_sync(gm, acc.im, o);
+                    }
                     const cx<T> sc = tau * acc;
-                    for (int i = lane; i < m; i += 32) pc[i] = pc[i] - vj[i] * sc;
+                    for (int i = q8; i < m; i += 8) pc[j + 1 + i] = pc[j + 1 + i] - vj[i] * sc;
+                    __syncwarp(gm);
                 }
-                __syncthreads();
             }
+            __syncthreads();
             for (int idx = tid; idx < N * pw; idx += nthr) {
                 const int r = idx / pw, c = idx % pw;
                 U[(size_t)r * N + c0 + c] = P[(size_t)c * PS + r];
@@ -519,7 +538,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
 // memory left after the matrix (when resident) and the per-matrix vectors.
 template <typename T>
 inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB) {
-    const size_t budget = 200 * 1024;
+    const size_t budget = 220 * 1024;
     const size_t fixed = eig_smem_bytes<T>(N, a_smem, 0, 0);
     const size_t left = budget > fixed ? budget - fixed : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
@@ -559,7 +578,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
 inline bool f32_in_smem(int N) {
     int G, PB;
     choose_g_pb<float>(N, true, 32, 64, G, PB);
-    return eig_smem_bytes<float>(N, true, G, PB) <= 200 * 1024 && G >= 8 && PB >= 16;
+    return eig_smem_bytes<float>(N, true, G, PB) <= 220 * 1024 && G >= 8 && PB >= 16;
 }
 
 }  // namespace
