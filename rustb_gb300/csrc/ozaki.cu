@@ -486,7 +486,13 @@ __global__ void row_exp_kernel(int64_t M, int K, const zc* __restrict__ A, int64
 // Largest contraction length for which levels 0-2 stay exact.
 int ozaki_fourier_max_k() { return 408; }
 
+size_t ozaki_hop_image_bytes(int K, int64_t Nc);
+int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img);
+
+// Bytes of the hop table's digit planes in the layout of the selected kernel
+// (tcgen05 stage images, or the mma.sync slice layout).
 size_t ozaki_hop_slices_bytes(int K, int64_t Nc) {
+    if (ozaki_use_tc()) return ozaki_hop_image_bytes(K, Nc);
     const int64_t nkc = (K + OZ_TK - 1) / OZ_TK, nct = (Nc + OZ_TN - 1) / OZ_TN;
     return sizeof(__nv_bfloat16) * (size_t)nct * nkc * 6 * 2 * OZ_TK * OZ_TN;
 }
@@ -496,6 +502,7 @@ int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, in
     KTimer kt(st, "hop_slice_kernel");
     hop_exp_kernel<<<(unsigned)std::min<int64_t>((Nc * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(K, Nc, ham, EB);
     TBG_LAUNCHED("hop_exp_kernel");
+    if (ozaki_use_tc()) return ozaki_hop_image_launch(st, K, Nc, ham, EB, Bs);
     const int64_t total = ((Nc + OZ_TN - 1) / OZ_TN) * ((K + OZ_TK - 1) / OZ_TK) * OZ_TK * OZ_TN;
     hop_slice_kernel<6><<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
         K, Nc, ham, EB, static_cast<__nv_bfloat16*>(Bs));

@@ -1,23 +1,30 @@
 // Exact-slice complex GEMM on the 5th-generation tensor cores (tcgen05, TMEM).
 //
-// Same arithmetic as ozaki.cu (6 signed 7-bit digits per value, levels
-// s + t = 0, 1, 2 exact, 3..5 together, float-pair output), issued as
-// tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32, M = 128, N = 128,
-// K = 16) from shared-memory descriptors.  The four accumulation levels live
-// in tensor memory: 4 x 128 FP32 columns = the whole 512-column allocation.
+// Same number format as ozaki.cu: every value of a row (column) of an operand
+// is written on the fixed-point grid 2^(E-42) of that row's exponent E and cut
+// into six signed 7-bit digits, stored pre-scaled as BF16 planes q_s 2^(-7s);
+// digit products of level s + t = 0, 1, 2 are accumulated exactly in separate
+// FP32 accumulators, levels 3..5 together, and the four are combined into a
+// float pair.  Issued as tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 ->
+// FP32, M = 128, N = 128, K = 16) from shared-memory descriptors; the four
+// accumulation levels are 4 x 128 FP32 columns of tensor memory.
 //
-// CTA = 8 warps, one output tile of 128 rows x 64 complex columns:
-//   warp 0      allocates TMEM; lane 0 issues the MMAs and commits them;
-//   warps 1..7  digit producers: read the FP64 / FP32 / pair / pre-sliced
-//               operands, write digit planes (K-major, no-swizzle core
-//               matrices of 8 rows x 16 bytes) into one of two stage buffers;
-//   warps 4..7  after the K loop: read the four levels from TMEM
-//               (tcgen05.ld 32x32b, one TMEM lane = one output row), combine
-//               them with error-free TwoSums and write the float pairs.
-// Stage hand-off uses mbarriers: full[b] (224 producer arrivals) and empty[b]
-// (tcgen05.commit of the MMAs that read buffer b).  Every wait is bounded;
-// on a time-out the CTA records an error, drains its committed MMAs (bounded),
-// frees TMEM and returns.
+// CTA = 13 warps, one output tile of 128 rows x 64 complex columns:
+//   warps 0..7   A digit producers: thread = (row, 8 consecutive k); load the
+//                8 elements of the next stage into registers while converting
+//                the current one, write each digit plane as one 16-byte store
+//                (K-major core matrices of 8 rows x 16 bytes, no swizzle);
+//   warps 8..11  B digit producers, same per (column, 8 consecutive k), or,
+//                for a pre-sliced operand, one thread that copies the stage
+//                image with cp.async.bulk (completion on an mbarrier);
+//   warp 12      allocates TMEM; lane 0 issues the MMAs and commits them;
+//   warps 0..7   after the K loop: read the four levels from TMEM (tcgen05.ld
+//                32x32b, one TMEM lane = one output row), combine them with
+//                error-free sums and write the float pairs.
+// Stage hand-off uses mbarriers: full[b] (producer arrivals), bcopy[b] (bulk
+// copy bytes), empty[b] (tcgen05.commit of the MMAs that read buffer b).
+// Every wait is bounded; on a time-out the CTA records an error, waits
+// (bounded) for its own bulk copies and committed MMAs, frees TMEM and returns.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -37,9 +44,13 @@ constexpr int TC_TK = 16;         // complex k per stage (32 real)
 constexpr int TC_S = 6;           // digits per value
 constexpr int TC_LMAX = 5;
 constexpr int PLANE = 128 * 32 * 2;             // bytes of one digit plane (128 rows x 32 k bf16)
-constexpr int STAGE_BYTES = 2 * TC_S * PLANE;   // A and B planes of one stage
-constexpr int TC_SMEM = 2 * STAGE_BYTES + 1024; // two stages + barriers / scratch
-constexpr int N_PRODUCERS = 224;
+constexpr int HALF_STAGE = TC_S * PLANE;        // the six planes of one operand (49152 bytes)
+constexpr int STAGE_BYTES = 2 * HALF_STAGE;     // A and B planes of one stage
+constexpr int TC_SMEM = 2 * STAGE_BYTES + 1024; // two stages + alignment slack
+constexpr int TC_THREADS = 416;                 // 13 warps
+constexpr int MMA_WARP = 12;
+constexpr int A_PRODUCERS = 256;
+constexpr int B_PRODUCERS = 128;
 constexpr int ZERO_EXP = -100000;
 
 enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2, FMT_PRESLICED = 3 };
@@ -55,6 +66,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(su32(bar)) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(su32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -64,7 +80,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait without abort check (used to drain committed MMAs before freeing TMEM).
+// Bounded wait without abort check (used to drain committed MMAs and copies).
 __device__ __forceinline__ bool mbar_wait_plain(uint64_t* bar, uint32_t parity) {
     for (int it = 0; it < (1 << 20); ++it)
         if (mbar_try_wait(bar, parity)) return true;
@@ -82,6 +98,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 1-D bulk copy global -> shared, completion counted in bytes on `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(su32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
@@ -104,22 +132,16 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+// 8 consecutive TMEM columns of this warp's 32 lanes (no wait).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// ---- digit extraction (identical arithmetic to ozaki.cu) ----
+// ---- digit extraction ----
+// Fixed-point value trunc(x * 2^(42 - E)) of a double with |x| < 2^E.
 __device__ __forceinline__ long long fx64(double x, int E) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int ex = (int)((b >> 52) & 0x7ff);
@@ -129,6 +151,7 @@ __device__ __forceinline__ long long fx64(double x, int E) {
     const long long F = (sh >= 64) ? 0 : (long long)(M >> sh);
     return (b >> 63) ? -F : F;
 }
+// Fixed-point value trunc(x * 2^(42 - E)) of a float with |x| < 2^E.
 __device__ __forceinline__ long long fx32(float x, int E) {
     const unsigned b = __float_as_uint(x);
     const int ex = (int)((b >> 23) & 0xff);
@@ -142,107 +165,162 @@ __device__ __forceinline__ long long fx32(float x, int E) {
         F = (-sh >= 64) ? 0 : (long long)(M >> (-sh));
     return (b >> 31) ? -F : F;
 }
-template <int FMT>
-__device__ __forceinline__ void load_fx(const void* base, int64_t idx, int E, long long& re, long long& im) {
+
+// Six pre-scaled digits P_s = q_s 2^(-7s) of a fixed-point F (|F| < 2^42),
+// F = sum_s q_s 2^(35 - 7s).  F is split as hi 2^21 + lo (lo in [0, 2^21)),
+// each half is exact in FP32 and is cut by rounding to the nearest multiple
+// of 2^14 and 2^7; every step is exact.  |q_0| <= 128, |q_1|, |q_2|, |q_4|,
+// |q_5| <= 64, q_3 in [0, 128].
+__device__ __forceinline__ void digits_fixed(long long F, float* P) {
+    const int hi = (int)(F >> 21);
+    const int lo = (int)(F & 0x1FFFFF);
+    const float a = (float)hi * 0x1p-14f;  // [-128, 128)
+    const float d0 = rintf(a);
+    const float t1 = (a - d0) * 128.f;     // [-64, 64], a multiple of 2^-7
+    const float d1 = rintf(t1);
+    const float d2 = t1 - d1;              // q_2 2^-7
+    const float c = (float)lo * 0x1p-14f;  // [0, 128)
+    const float e3 = rintf(c);
+    const float t4 = (c - e3) * 128.f;
+    const float e4 = rintf(t4);
+    const float e5 = t4 - e4;              // q_5 2^-7
+    P[0] = d0;
+    P[1] = d1 * 0x1p-7f;
+    P[2] = d2 * 0x1p-7f;
+    P[3] = e3 * 0x1p-21f;
+    P[4] = e4 * 0x1p-28f;
+    P[5] = e5 * 0x1p-28f;
+}
+// Six pre-scaled digits of u = x 2^(7 - E) in (-128, 128) for an FP32 x:
+// q_s = round(t_s), t_{s+1} = 128 (t_s - q_s), every step exact; the sum
+// equals x rounded to the grid 2^(E-42).  |q_0| <= 128, |q_s| <= 64.
+__device__ __forceinline__ void digits_float(float u, float* P) {
+    float d = rintf(u);
+    P[0] = d;
+    float t = (u - d) * 128.f;
+    d = rintf(t);
+    P[1] = d * 0x1p-7f;
+    t = (t - d) * 128.f;
+    d = rintf(t);
+    P[2] = d * 0x1p-14f;
+    t = (t - d) * 128.f;
+    d = rintf(t);
+    P[3] = d * 0x1p-21f;
+    t = (t - d) * 128.f;
+    d = rintf(t);
+    P[4] = d * 0x1p-28f;
+    t = (t - d) * 128.f;
+    d = rintf(t);
+    P[5] = d * 0x1p-35f;
+}
+__device__ __forceinline__ float pow2f(int n) { return __int_as_float((127 + n) << 23); }  // n in [-126, 127]
+// 2^(7 - E) as s1 * s2 (each a normal float) for FP32 operands; 0 for a zero line.
+__device__ __forceinline__ void f32_scales(int E, float& s1, float& s2) {
     if (E == ZERO_EXP) {
-        re = im = 0;
+        s1 = s2 = 0.f;
         return;
     }
-    if (FMT == FMT_F64) {
-        const double2 v = reinterpret_cast<const double2*>(base)[idx];
-        re = fx64(v.x, E);
-        im = fx64(v.y, E);
-    } else if (FMT == FMT_F32) {
-        const float2 v = reinterpret_cast<const float2*>(base)[idx];
-        re = fx32(v.x, E);
-        im = fx32(v.y, E);
-    } else {
-        const float4 v = reinterpret_cast<const float4*>(base)[idx];
-        re = fx32(v.x, E) + fx32(v.y, E);
-        im = fx32(v.z, E) + fx32(v.w, E);
-    }
-}
-// Raw 16-byte (or 8-byte) element of an operand, loaded ahead of the digit work.
-template <int FMT>
-struct Raw {
-    int4 v;
-};
-template <int FMT>
-__device__ __forceinline__ Raw<FMT> load_raw(const void* base, int64_t idx) {
-    Raw<FMT> r;
-    if (FMT == FMT_F32) {
-        const int2 t = reinterpret_cast<const int2*>(base)[idx];
-        r.v = make_int4(t.x, t.y, 0, 0);
-    } else {
-        r.v = reinterpret_cast<const int4*>(base)[idx];
-    }
-    return r;
-}
-template <int FMT>
-__device__ __forceinline__ void raw_fx(const Raw<FMT>& r, int E, long long& re, long long& im) {
-    if (E == ZERO_EXP) {
-        re = im = 0;
-        return;
-    }
-    if (FMT == FMT_F64) {
-        re = fx64(__hiloint2double(r.v.y, r.v.x), E);
-        im = fx64(__hiloint2double(r.v.w, r.v.z), E);
-    } else if (FMT == FMT_F32) {
-        re = fx32(__int_as_float(r.v.x), E);
-        im = fx32(__int_as_float(r.v.y), E);
-    } else {
-        re = fx32(__int_as_float(r.v.x), E) + fx32(__int_as_float(r.v.y), E);
-        im = fx32(__int_as_float(r.v.z), E) + fx32(__int_as_float(r.v.w), E);
-    }
+    const int sh = 7 - E;  // in [-122, 155] for finite floats
+    const int a = min(sh, 127);
+    s1 = pow2f(max(a, -126));
+    s2 = pow2f(sh - a);
 }
 
-// digits of F (42 fractional bits), rounded, pre-scaled by 2^-7s
-__device__ __forceinline__ void digits(long long F, __nv_bfloat16* d) {
-#pragma unroll
-    for (int s = 0; s < TC_S; ++s) {
-        const int sh = 35 - 7 * s;
-        long long q;
-        if (sh == 0) {
-            q = F;
-        } else {
-            q = (F + (1ll << (sh - 1))) >> sh;
-            F -= q << sh;
-        }
-        d[s] = __float2bfloat16_rn((float)(int)q * __int_as_float((127 - 7 * s) << 23));
+// One element as raw bits: F64 {re, im} doubles, F32 {re, im} floats in .x/.y,
+// PAIR {re_hi, re_lo, im_hi, im_lo} floats.
+template <int FMT>
+__device__ __forceinline__ int4 ld_elem(const void* base, int64_t idx) {
+    if (FMT == FMT_F32) {
+        const int2 t = __ldg(reinterpret_cast<const int2*>(base) + idx);
+        return make_int4(t.x, t.y, 0, 0);
     }
+    return __ldg(reinterpret_cast<const int4*>(base) + idx);
+}
+template <int FMT>
+__device__ __forceinline__ void load8(const void* base, int64_t idx0, int64_t stride, int nvalid, int4 (&r)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = (i < nvalid) ? ld_elem<FMT>(base, idx0 + (int64_t)i * stride) : make_int4(0, 0, 0, 0);
+}
+// Digits of the real (part 0) or imaginary (part 1) component of one element.
+template <int FMT, int PART>
+__device__ __forceinline__ void elem_digits(const int4& r, int E, float s1, float s2, float* P) {
+    if (FMT == FMT_F32) {
+        const float x = __int_as_float(PART ? r.y : r.x);
+        digits_float((x * s1) * s2, P);
+    } else {
+        long long F = 0;
+        if (E != ZERO_EXP) {
+            if (FMT == FMT_F64)
+                F = PART ? fx64(__hiloint2double(r.w, r.z), E) : fx64(__hiloint2double(r.y, r.x), E);
+            else
+                F = PART ? fx32(__int_as_float(r.z), E) + fx32(__int_as_float(r.w), E)
+                         : fx32(__int_as_float(r.x), E) + fx32(__int_as_float(r.y), E);
+        }
+        digits_fixed(F, P);
+    }
+}
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo_k, float hi_k) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo_k, hi_k);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+// The six digit planes of one component of 8 consecutive-k elements: out[s]
+// holds 8 BF16 (k ascending) = one 16-byte row segment of a core matrix.
+template <int FMT, int PART>
+__device__ __forceinline__ void item_planes(const int4 (&r)[8], int E, float s1, float s2, uint4 (&out)[TC_S]) {
+    uint32_t pk[TC_S][4];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        float P0[TC_S], P1[TC_S];
+        elem_digits<FMT, PART>(r[i], E, s1, s2, P0);
+        elem_digits<FMT, PART>(r[i + 1], E, s1, s2, P1);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) pk[s][i >> 1] = pack_bf16x2(P0[s], P1[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < TC_S; ++s) out[s] = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+}
+__device__ __forceinline__ uint4 neg_bf16x8(uint4 v) {
+    const uint32_t m = 0x80008000u;
+    return make_uint4(v.x ^ m, v.y ^ m, v.z ^ m, v.w ^ m);
 }
 // byte offset of element (row, k') inside one digit plane (K-major core matrices)
-__device__ __forceinline__ int plane_off(int row, int kp) {
+__host__ __device__ __forceinline__ int plane_off(int row, int kp) {
     return (((row >> 3) * 4 + (kp >> 3)) << 7) + ((row & 7) << 4) + ((kp & 7) << 1);
 }
+__device__ __forceinline__ int n_valid(int K, int kfirst) { return max(0, min(8, K - kfirst)); }
 
 template <bool CONJ_A, int FMTA, int FMTB>
-__global__ void __launch_bounds__(256, 1) oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda,
-                                                       int64_t sA, const void* __restrict__ B, int64_t ldb, int64_t sB,
-                                                       const int* __restrict__ EA, const int* __restrict__ EB,
-                                                       float4* __restrict__ C, int64_t ldc, int64_t sC,
-                                                       int* __restrict__ err) {
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
+                 int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
+                 float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err) {
+    constexpr bool PRE = FMTB == FMT_PRESLICED;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
-    unsigned char* stage[2] = {base, base + STAGE_BYTES};
-    __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_done;
+    __shared__ __align__(8) uint64_t bar_full[2], bar_bcopy[2], bar_empty[2], bar_done;
     __shared__ uint32_t tmem_base_sh;
     __shared__ volatile int abort_sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t b = blockIdx.z;
-    const int row0 = blockIdx.y * TC_TM, col0 = blockIdx.x * TC_TN;
+    const int rt = rows_fast ? (int)blockIdx.x : (int)blockIdx.y;
+    const int ct = rows_fast ? (int)blockIdx.y : (int)blockIdx.x;
+    const int row0 = rt * TC_TM, col0 = ct * TC_TN;
     const int nstages = (K + TC_TK - 1) / TC_TK;
+    const uint32_t sbase = su32(base);
 
     if (tid == 0) {
-        mbar_init(&bar_full[0], N_PRODUCERS);
-        mbar_init(&bar_full[1], N_PRODUCERS);
+        const uint32_t nfull = PRE ? A_PRODUCERS : A_PRODUCERS + B_PRODUCERS;
+        mbar_init(&bar_full[0], nfull);
+        mbar_init(&bar_full[1], nfull);
+        mbar_init(&bar_bcopy[0], 1);
+        mbar_init(&bar_bcopy[1], 1);
         mbar_init(&bar_empty[0], 1);
         mbar_init(&bar_empty[1], 1);
         mbar_init(&bar_done, 1);
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == MMA_WARP) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(&tmem_base_sh))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -252,19 +330,19 @@ __global__ void __launch_bounds__(256, 1) oz_tc_kernel(int M, int Nc, int K, con
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
 
-    if (warp == 0) {
+    if (warp == MMA_WARP) {
         // ------------------------------------------------ MMA issuer (lane 0)
         if (lane == 0) {
-            int issued_any = 0;
             for (int it = 0; it < nstages; ++it) {
                 const int bi = it & 1;
-                if (!mbar_wait(&bar_full[bi], (it >> 1) & 1, &abort_sh)) {
+                const uint32_t ph = (it >> 1) & 1;
+                if (!mbar_wait(&bar_full[bi], ph, &abort_sh) || (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh))) {
                     abort_sh = 1;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t sa = su32(stage[bi]);
-                const uint32_t sb = sa + TC_S * PLANE;
+                const uint32_t sa = sbase + bi * STAGE_BYTES;
+                const uint32_t sb = sa + HALF_STAGE;
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
@@ -280,162 +358,168 @@ __global__ void __launch_bounds__(256, 1) oz_tc_kernel(int M, int Nc, int K, con
                         }
                     }
                 }
-                issued_any = 1;
                 umma_commit(&bar_empty[bi]);
             }
-            (void)issued_any;
             umma_commit(&bar_done);  // tracks every MMA issued above
         }
         __syncwarp();
-    } else {
-        // ----------------------------------------------- digit producers
-        const int p = tid - 32;  // 0 .. 223
-        for (int it = 0; it < nstages && !abort_sh; ++it) {
+    } else if (tid < A_PRODUCERS) {
+        // ------------------------------------- A digit producers (row, 8 k)
+        const int r = CONJ_A ? (tid & 127) : (tid >> 1);
+        const int g = CONJ_A ? (tid >> 7) : (tid & 1);
+        const int gi = row0 + r;
+        const bool rv = gi < M;
+        const int E = rv ? EA[b * M + gi] : ZERO_EXP;
+        float s1, s2;
+        f32_scales(E, s1, s2);
+        const int64_t kstride = CONJ_A ? lda : 1;
+        const int64_t idx0 = CONJ_A ? (b * sA + gi) : (b * sA + (int64_t)gi * lda);
+        const uint32_t o_re = plane_off(r, 8 * g), o_im = plane_off(r, 16 + 8 * g);
+        int4 nxt[8];
+        load8<FMTA>(A, idx0 + (int64_t)(8 * g) * kstride, kstride, rv ? n_valid(K, 8 * g) : 0, nxt);
+        for (int it = 0; it < nstages; ++it) {
             const int bi = it & 1;
+            int4 cur[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
+            if (it + 1 < nstages) {
+                const int kf = (it + 1) * TC_TK + 8 * g;
+                load8<FMTA>(A, idx0 + (int64_t)kf * kstride, kstride, rv ? n_valid(K, kf) : 0, nxt);
+            }
             if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
                 abort_sh = 1;
                 break;
             }
-            unsigned char* sa = stage[bi];
-            unsigned char* sb = sa + TC_S * PLANE;
-            const int k0 = it * TC_TK;
-            // A: 128 rows x 16 complex k.  All loads of the stage are issued first.
-            constexpr int PA = (TC_TM * TC_TK + N_PRODUCERS - 1) / N_PRODUCERS;
-            Raw<FMTA> ra[PA];
-            int ea_[PA];
+            if (abort_sh) break;
+            const uint32_t sa = sbase + bi * STAGE_BYTES;
+            uint4 d[TC_S];
+            item_planes<FMTA, 0>(cur, E, s1, s2, d);
 #pragma unroll
-            for (int q = 0; q < PA; ++q) {
-                const int e = p + q * N_PRODUCERS;
-                ea_[q] = ZERO_EXP;
-                ra[q].v = make_int4(0, 0, 0, 0);
-                if (e < TC_TM * TC_TK) {
-                    const int r = CONJ_A ? (e & 127) : (e >> 4);
-                    const int kk = CONJ_A ? (e >> 7) : (e & 15);
-                    const int gi = row0 + r, gk = k0 + kk;
-                    if (gi < M && gk < K) {
-                        ea_[q] = EA[b * M + gi];
-                        const int64_t idx =
-                            CONJ_A ? (b * sA + (int64_t)gk * lda + gi) : (b * sA + (int64_t)gi * lda + gk);
-                        ra[q] = load_raw<FMTA>(A, idx);
-                    }
-                }
-            }
+            for (int s = 0; s < TC_S; ++s) st_shared_v4(sa + s * PLANE + o_re, d[s]);
+            item_planes<FMTA, 1>(cur, E, s1, s2, d);
 #pragma unroll
-            for (int q = 0; q < PA; ++q) {
-                const int e = p + q * N_PRODUCERS;
-                if (e >= TC_TM * TC_TK) continue;
-                const int r = CONJ_A ? (e & 127) : (e >> 4);
-                const int kk = CONJ_A ? (e >> 7) : (e & 15);
-                long long fre, fim;
-                raw_fx<FMTA>(ra[q], ea_[q], fre, fim);
-                if (CONJ_A) fim = -fim;
-                __nv_bfloat16 dre[TC_S], dim_[TC_S];
-                digits(fre, dre);
-                digits(fim, dim_);
-                const int ore = plane_off(r, kk), oim = plane_off(r, 16 + kk);
-#pragma unroll
-                for (int s = 0; s < TC_S; ++s) {
-                    *reinterpret_cast<__nv_bfloat16*>(sa + s * PLANE + ore) = dre[s];
-                    *reinterpret_cast<__nv_bfloat16*>(sa + s * PLANE + oim) = dim_[s];
-                }
-            }
-            // B: 16 complex k x 64 complex columns -> rows n (re: j, im: 64 + j)
-            constexpr int PB = (TC_TK * TC_TN + N_PRODUCERS - 1) / N_PRODUCERS;
-            Raw<FMTB == FMT_PRESLICED ? FMT_F64 : FMTB> rb[PB];
-            int eb_[PB];
-            if (FMTB != FMT_PRESLICED) {
-#pragma unroll
-                for (int q = 0; q < PB; ++q) {
-                    const int e = p + q * N_PRODUCERS;
-                    eb_[q] = ZERO_EXP;
-                    rb[q].v = make_int4(0, 0, 0, 0);
-                    if (e < TC_TK * TC_TN) {
-                        const int j = e & 63, kk = e >> 6;
-                        const int gj = col0 + j, gk = k0 + kk;
-                        if (gj < Nc && gk < K) {
-                            eb_[q] = EB[b * Nc + gj];
-                            rb[q] = load_raw<FMTB == FMT_PRESLICED ? FMT_F64 : FMTB>(B, b * sB + (int64_t)gk * ldb + gj);
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < PB; ++q) {
-                const int e = p + q * N_PRODUCERS;
-                if (e >= TC_TK * TC_TN) continue;
-                const int j = e & 63, kk = e >> 6;
-                __nv_bfloat16 dre[TC_S], dim_[TC_S];
-                if (FMTB == FMT_PRESLICED) {
-                    const int nkc = (K + TC_TK - 1) / TC_TK;
-                    const __nv_bfloat16* src = static_cast<const __nv_bfloat16*>(B) +
-                                               ((int64_t)blockIdx.x * nkc + it) * (int64_t)TC_S * 2 * TC_TK * TC_TN;
-#pragma unroll
-                    for (int t = 0; t < TC_S; ++t) {
-                        dre[t] = src[((t * 2 + 0) * TC_TK + kk) * TC_TN + j];
-                        dim_[t] = src[((t * 2 + 1) * TC_TK + kk) * TC_TN + j];
-                    }
-                } else {
-                    long long fre, fim;
-                    raw_fx<FMTB == FMT_PRESLICED ? FMT_F64 : FMTB>(rb[q], eb_[q], fre, fim);
-                    digits(fre, dre);
-                    digits(fim, dim_);
-                }
-                const int o00 = plane_off(j, kk), o01 = plane_off(j, 16 + kk);
-                const int o10 = plane_off(64 + j, kk), o11 = plane_off(64 + j, 16 + kk);
-#pragma unroll
-                for (int t = 0; t < TC_S; ++t) {
-                    unsigned char* pl = sb + t * PLANE;
-                    *reinterpret_cast<__nv_bfloat16*>(pl + o00) = dre[t];
-                    *reinterpret_cast<__nv_bfloat16*>(pl + o01) = __hneg(dim_[t]);
-                    *reinterpret_cast<__nv_bfloat16*>(pl + o10) = dim_[t];
-                    *reinterpret_cast<__nv_bfloat16*>(pl + o11) = dre[t];
-                }
-            }
+            for (int s = 0; s < TC_S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(d[s]) : d[s]);
             fence_async_smem();  // make the generic-proxy writes visible to the tensor core
             mbar_arrive(&bar_full[bi]);
+        }
+    } else if (tid < A_PRODUCERS + B_PRODUCERS) {
+        const int q = tid - A_PRODUCERS;
+        if (PRE) {
+            // ------------------------- pre-sliced B: bulk copy of stage images
+            if (q == 0) {
+                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HALF_STAGE;
+                int last[2] = {-1, -1};
+                for (int it = 0; it < nstages; ++it) {
+                    const int bi = it & 1;
+                    if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
+                        abort_sh = 1;
+                        break;
+                    }
+                    if (abort_sh) break;
+                    mbar_arrive_tx(&bar_bcopy[bi], HALF_STAGE);
+                    bulk_g2s(sbase + bi * STAGE_BYTES + HALF_STAGE, src + (int64_t)it * HALF_STAGE, HALF_STAGE,
+                             &bar_bcopy[bi]);
+                    last[bi] = it;
+                }
+                // every copy issued has landed before the CTA can leave
+                for (int bi = 0; bi < 2; ++bi)
+                    if (last[bi] >= 0) mbar_wait_plain(&bar_bcopy[bi], (last[bi] >> 1) & 1);
+            }
+        } else {
+            // ---------------------------------- B digit producers (col, 8 k)
+            // real embedding: row j = [Re B | -Im B], row 64 + j = [Im B | Re B]
+            const int j = q & 63, g = q >> 6;
+            const int gj = col0 + j;
+            const bool cv = gj < Nc;
+            const int E = cv ? EB[b * Nc + gj] : ZERO_EXP;
+            float s1, s2;
+            f32_scales(E, s1, s2);
+            const int64_t idx0 = b * sB + gj;
+            const uint32_t o_jre = plane_off(j, 8 * g), o_jim = plane_off(j, 16 + 8 * g);
+            const uint32_t o_kre = plane_off(64 + j, 8 * g), o_kim = plane_off(64 + j, 16 + 8 * g);
+            constexpr int FB = PRE ? FMT_F64 : FMTB;
+            int4 nxt[8];
+            load8<FB>(B, idx0 + (int64_t)(8 * g) * ldb, ldb, cv ? n_valid(K, 8 * g) : 0, nxt);
+            for (int it = 0; it < nstages; ++it) {
+                const int bi = it & 1;
+                int4 cur[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
+                if (it + 1 < nstages) {
+                    const int kf = (it + 1) * TC_TK + 8 * g;
+                    load8<FB>(B, idx0 + (int64_t)kf * ldb, ldb, cv ? n_valid(K, kf) : 0, nxt);
+                }
+                if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
+                    abort_sh = 1;
+                    break;
+                }
+                if (abort_sh) break;
+                const uint32_t sb = sbase + bi * STAGE_BYTES + HALF_STAGE;
+                uint4 d[TC_S];
+                item_planes<FB, 0>(cur, E, s1, s2, d);
+#pragma unroll
+                for (int s = 0; s < TC_S; ++s) {
+                    st_shared_v4(sb + s * PLANE + o_jre, d[s]);
+                    st_shared_v4(sb + s * PLANE + o_kim, d[s]);
+                }
+                item_planes<FB, 1>(cur, E, s1, s2, d);
+#pragma unroll
+                for (int s = 0; s < TC_S; ++s) {
+                    st_shared_v4(sb + s * PLANE + o_kre, d[s]);
+                    st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(d[s]));
+                }
+                fence_async_smem();
+                mbar_arrive(&bar_full[bi]);
+            }
         }
     }
 
     // ---------------------------------------------------------- epilogue
-    if (warp >= 4) {
+    if (warp < 8) {
         bool ok = mbar_wait(&bar_done, 0, &abort_sh) && !abort_sh;
         ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld is warp-collective
         tc_fence_after();
-        const int q = warp - 4;  // TMEM lanes 32q .. 32q+31
+        const int q = warp & 3, h = warp >> 2;  // TMEM lanes 32q .. 32q+31; complex columns 32h .. 32h+31
         const int r = row0 + 32 * q + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
         if (ok) {
             const int ea = (r < M) ? EA[b * M + r] : ZERO_EXP;
-            for (int cb = 0; cb < 4; ++cb) {  // 32 real columns at a time
-                float a0[32], a1[32], a2[32], a3[32];
-                tmem_ld32(lane_addr + 0 * 128 + cb * 32, a0);
-                tmem_ld32(lane_addr + 1 * 128 + cb * 32, a1);
-                tmem_ld32(lane_addr + 2 * 128 + cb * 32, a2);
-                tmem_ld32(lane_addr + 3 * 128 + cb * 32, a3);
+            for (int cc = 0; cc < 4; ++cc) {
+                const int c0 = 32 * h + 8 * cc;
+                uint32_t v[8][8];  // [2 * level + (0 re, 1 im)][column]
+#pragma unroll
+                for (int L = 0; L < 4; ++L) {
+                    tmem_ld8(lane_addr + (uint32_t)(L * 128 + c0), v[2 * L]);
+                    tmem_ld8(lane_addr + (uint32_t)(L * 128 + TC_TN + c0), v[2 * L + 1]);
+                }
+                tmem_wait_ld();
                 if (r < M) {
 #pragma unroll
-                    for (int c = 0; c < 32; ++c) {
-                        const int cn = cb * 32 + c;
-                        const bool im = cn >= TC_TN;
-                        const int j = col0 + (im ? cn - TC_TN : cn);
+                    for (int c = 0; c < 8; ++c) {
+                        const int j = col0 + c0 + c;
                         if (j >= Nc) continue;
-                        const float s1 = a0[c] + a1[c];
-                        const float t1 = s1 - a0[c];
-                        const float e1 = (a0[c] - (s1 - t1)) + (a1[c] - t1);
-                        const float hi = s1 + a2[c];
-                        const float t2 = hi - s1;
-                        const float e2 = (s1 - (hi - t2)) + (a2[c] - t2);
-                        const float lo = (e1 + e2) + a3[c];
-                        const int eb = EB[b * Nc + j];
-                        float2 out = make_float2(0.f, 0.f);
-                        if (ea != ZERO_EXP && eb != ZERO_EXP) {
-                            int n = ea + eb - 14;
-                            n = max(-126, min(127, n));
-                            const float sc = __int_as_float((127 + n) << 23);
-                            out = make_float2(hi * sc, lo * sc);
+                        float hl[4];
+#pragma unroll
+                        for (int part = 0; part < 2; ++part) {
+                            const float a0 = __uint_as_float(v[0 + part][c]), a1 = __uint_as_float(v[2 + part][c]);
+                            const float a2 = __uint_as_float(v[4 + part][c]), a3 = __uint_as_float(v[6 + part][c]);
+                            const float s1 = a0 + a1;
+                            const float t1 = s1 - a0;
+                            const float e1 = (a0 - (s1 - t1)) + (a1 - t1);
+                            const float hi = s1 + a2;
+                            const float t2 = hi - s1;
+                            const float e2 = (s1 - (hi - t2)) + (a2 - t2);
+                            hl[2 * part] = hi;
+                            hl[2 * part + 1] = (e1 + e2) + a3;
                         }
-                        float* dst = reinterpret_cast<float*>(C + b * sC + (int64_t)r * ldc + j) + (im ? 2 : 0);
-                        *reinterpret_cast<float2*>(dst) = out;
+                        const int eb = EB[b * Nc + j];
+                        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (ea != ZERO_EXP && eb != ZERO_EXP) {
+                            const int n = max(-126, min(127, ea + eb - 14));
+                            const float sc = pow2f(n);
+                            out = make_float4(hl[0] * sc, hl[1] * sc, hl[2] * sc, hl[3] * sc);
+                        }
+                        C[b * sC + (int64_t)r * ldc + j] = out;
                     }
                 }
             }
@@ -444,11 +528,50 @@ __global__ void __launch_bounds__(256, 1) oz_tc_kernel(int M, int Nc, int K, con
     tc_fence_before();
     __syncthreads();
     if (abort_sh && tid == 0) atomicOr(err, 2);  // bit 1: a bounded wait ran out
-    if (warp == 0) {
+    if (warp == MMA_WARP) {
         if (lane == 0) mbar_wait_plain(&bar_done, 0);  // every committed MMA has finished
         __syncwarp();
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+// Stage images of the hop table for the Fourier contraction: for column tile
+// ct and stage it, the six B digit planes exactly as oz_tc_kernel's shared
+// stage holds them (HALF_STAGE bytes at (ct * nstages + it) * HALF_STAGE).
+// One thread per (column, 8 consecutive R).
+__global__ void hop_image_kernel(int K, int64_t Nc, const zc* __restrict__ ham, const int* __restrict__ EB,
+                                 unsigned char* __restrict__ img) {
+    const int nst = (K + TC_TK - 1) / TC_TK;
+    const int64_t nct = (Nc + TC_TN - 1) / TC_TN;
+    const int64_t total = nct * nst * B_PRODUCERS;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(idx % B_PRODUCERS);
+        const int64_t blk = idx / B_PRODUCERS;  // ct * nst + it
+        const int it = (int)(blk % nst);
+        const int64_t ct = blk / nst;
+        const int j = q & 63, g = q >> 6;
+        const int64_t gj = ct * TC_TN + j;
+        const bool cv = gj < Nc;
+        const int E = cv ? EB[gj] : ZERO_EXP;
+        const int kf = it * TC_TK + 8 * g;
+        int4 r[8];
+        load8<FMT_F64>(ham, (int64_t)kf * Nc + gj, Nc, cv ? n_valid(K, kf) : 0, r);
+        unsigned char* dst = img + blk * HALF_STAGE;
+        uint4 d[TC_S];
+        item_planes<FMT_F64, 0>(r, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) {
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(j, 8 * g)) = d[s];
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 16 + 8 * g)) = d[s];
+        }
+        item_planes<FMT_F64, 1>(r, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) {
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 8 * g)) = d[s];
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(j, 16 + 8 * g)) = neg_bf16x8(d[s]);
+        }
     }
 }
 
@@ -470,10 +593,10 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
         const int64_t nb = std::min<int64_t>(65535, batch - b0);
         dim3 grid((Nc + TC_TN - 1) / TC_TN, (M + TC_TM - 1) / TC_TM, (unsigned)nb);
         const size_t ea = FA == FMT_F32 ? 8 : 16;
-        const size_t eb = FB == FMT_F32 ? 8 : (FB == FMT_PRESLICED ? 0 : 16);
-        kern<<<grid, 256, TC_SMEM, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
-                                         static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
-                                         EB + (FB == FMT_PRESLICED ? 0 : b0 * Nc), C + b0 * sC, ldc, sC, err);
+        const size_t eb = FB == FMT_F32 ? 8 : 16;
+        kern<<<grid, TC_THREADS, TC_SMEM, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
+                                                static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
+                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err);
         TBG_LAUNCHED(name);
     }
     return TBG_OK;
@@ -501,20 +624,35 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
     return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: operand format combination not instantiated");
 }
 
-// Fourier contraction on tcgen05: C (M x Nc) = A (M x K FP64) . hop digit planes; EA filled by the caller.
+// Bytes of the hop-table stage images (K = nR rows of Nc = N^2 elements).
+size_t ozaki_hop_image_bytes(int K, int64_t Nc) {
+    const int64_t nst = (K + TC_TK - 1) / TC_TK, nct = (Nc + TC_TN - 1) / TC_TN;
+    return (size_t)nct * nst * HALF_STAGE;
+}
+// Build the stage images from the hop table and its column exponents EB.
+int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img) {
+    const int64_t nst = (K + TC_TK - 1) / TC_TK, nct = (Nc + TC_TN - 1) / TC_TN;
+    const int64_t total = nct * nst * B_PRODUCERS;
+    hop_image_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
+        K, Nc, ham, EB, static_cast<unsigned char*>(img));
+    TBG_LAUNCHED("hop_image_kernel");
+    return TBG_OK;
+}
+
+// Fourier contraction on tcgen05: C (M x Nc) = A (M x K FP64 phases) . hop
+// table (stage images); EA filled by the caller.  Row tiles vary fastest so
+// that the CTAs resident together share one column tile's images in L2.
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
-                     const void* Bs, float4* C, int* err) {
+                     const void* img, float4* C, int* err) {
     auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc fourier)");
+    if ((Nc + TC_TN - 1) / TC_TN > 65535 || M > 0x7fffffff)
+        return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier_tc: grid too large");
     KTimer kt(st, "ozaki_tc_fourier_kernel", 8.0 * (double)M * Nc * K);
-    for (int64_t m0 = 0; m0 < M; m0 += (int64_t)TC_TM * 65535) {
-        const int64_t mb = std::min<int64_t>(M - m0, (int64_t)TC_TM * 65535);
-        dim3 grid((unsigned)((Nc + TC_TN - 1) / TC_TN), (unsigned)((mb + TC_TM - 1) / TC_TM), 1);
-        kern<<<grid, 256, TC_SMEM, st>>>((int)mb, (int)Nc, K, A + m0 * K, K, 0, Bs, Nc, 0, EA + m0, EB, C + m0 * Nc,
-                                         Nc, 0, err);
-        TBG_LAUNCHED("ozaki_tc_fourier_kernel");
-    }
+    dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
+    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err);
+    TBG_LAUNCHED("ozaki_tc_fourier_kernel");
     return TBG_OK;
 }
 
