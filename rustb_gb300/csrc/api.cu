@@ -46,8 +46,6 @@ int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* 
                   int64_t sB, zc* C, int64_t sC);
 int berry_from_bands(cudaStream_t st, int N, int64_t batch, const zc* Bx, const zc* By, int64_t ldB,
                      const double* E, double eta, double* Omega);
-int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d);
 
 namespace {
 
@@ -247,6 +245,7 @@ struct BerryJob {
     void* fwork;
     size_t fwork_bytes;
     cc* U32;
+    float4* pairs;  // mixed: H, V_0, V_1 as float pairs (3 chunk N^2)
 };
 
 int alloc_berry(Ctx& ctx, BerryJob& J) {
@@ -266,11 +265,13 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
     J.work_bytes = 0;
     J.fwork = nullptr;
     J.fwork_bytes = 0;
+    J.pairs = nullptr;
     if (J.precision == TBG_PREC_MIXED) {
         J.work_bytes = mixed_berry_workspace_bytes(N, c);
         J.work = J.work_bytes ? ctx.alloc<unsigned char>(J.work_bytes) : nullptr;
         J.fwork_bytes = fourier_mixed_scratch_bytes(*J.m, c);
         J.fwork = ctx.alloc<unsigned char>(J.fwork_bytes);
+        J.pairs = ctx.alloc<float4>(3 * c * NN);
     }
     if (ctx.rc == TBG_OK) {
         cudaError_t e = cudaMemsetAsync(J.status_d, 0, sizeof(int), ctx.st);
@@ -283,9 +284,36 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
     ModelDev& m = *J.m;
     const int N = (int)m.nsta;
     const int64_t NN = (int64_t)N * N;
-    int rc = (J.precision == TBG_PREC_MIXED)
-                 ? fourier_mixed(m, ctx.st, nkc, J.k_d, J.dirs_d, J.H, J.V, J.fwork, J.fwork_bytes)
-                 : fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
+    int rc;
+    if (J.precision == TBG_PREC_MIXED) {
+        // H, V_0, V_1 as float pairs: from the tensor-core contraction in the
+        // lattice gauge, or (position-matrix models, nR beyond the exact
+        // contraction length) Atom-gauge FP64 converted to pairs
+        float4* P = J.pairs;
+        if (m.n_rmat == 0 && fourier_mixed_ok(m)) {
+            rc = fourier_mixed_pairs(m, ctx.st, nkc, J.k_d, J.dirs_d, P, J.fwork, J.fwork_bytes);
+            if (rc) return rc;
+        } else {
+            rc = fourier_mixed(m, ctx.st, nkc, J.k_d, J.dirs_d, J.H, J.V, P, J.fwork, J.fwork_bytes);
+            if (rc) return rc;
+            if (m.n_rmat > 0) {
+                rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
+                if (rc) return rc;
+            }
+            // V is (nkc, 2, N, N); the pairs hold the components as separate blocks
+            if ((rc = z_to_pairs(ctx.st, nkc, NN, J.H, NN, P))) return rc;
+            if ((rc = z_to_pairs(ctx.st, nkc, NN, J.V, 2 * NN, P + nkc * NN))) return rc;
+            if ((rc = z_to_pairs(ctx.st, nkc, NN, J.V + NN, 2 * NN, P + 2 * nkc * NN))) return rc;
+        }
+        if (J.spin >= 0) {
+            rc = spin_dress_pairs(ctx.st, N, m.norb, nkc, J.spin, P + nkc * NN, NN,
+                                  reinterpret_cast<float4*>(J.scratch));
+            if (rc) return rc;
+        }
+        return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
+                           J.status_d, clusters_d);
+    }
+    rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
     if (rc) return rc;
     if (m.n_rmat > 0) {
         rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
@@ -295,9 +323,6 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
         rc = spin_dress(ctx.st, N, m.norb, nkc, J.spin, J.V, 2 * NN, J.scratch);
         if (rc) return rc;
     }
-    if (J.precision == TBG_PREC_MIXED)
-        return mixed_berry(ctx.st, N, nkc, J.H, J.V, J.V + NN, 2 * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
-                           J.status_d, clusters_d);
     rc = eig_batched(ctx.st, N, nkc, J.H, J.E, J.U, nullptr, 0, J.status_d);
     if (rc) return rc;
     return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch);

@@ -150,6 +150,49 @@ __global__ void spin_dress_kernel(int N, int norb, int64_t batch, int spin, cons
     }
 }
 
+// s (one of +-1/2, +-i/2) times a float-pair complex {re_hi, re_lo, im_hi, im_lo}: exact
+__device__ __forceinline__ float4 spin_scale(float4 v, zc s) {
+    if (s.im == 0.0) {
+        const float f = (float)s.re;
+        return make_float4(v.x * f, v.y * f, v.z * f, v.w * f);
+    }
+    const float f = (float)s.im;  // i f (re + i im) = -f im + i f re
+    return make_float4(-v.z * f, -v.w * f, v.x * f, v.y * f);
+}
+
+// J = 1/2 (S V + V S) on float pairs, same index algebra as spin_dress_kernel.
+__global__ void spin_dress_pairs_kernel(int N, int norb, int64_t batch, int spin, const float4* __restrict__ V,
+                                        int64_t ldV, float4* __restrict__ J) {
+    const int NN = N * N;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= NN) return;
+    const int i = e / N, j = e - i * N;
+    int pi, pj, ppj;
+    zc si, sj;
+    spin_entry(spin, norb, i, pi, si);
+    spin_entry(spin, norb, j, pj, sj);
+    spin_entry(spin, norb, pj, ppj, sj);
+    for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
+        const float4* Vb = V + b * ldV;
+        const float4 a = spin_scale(Vb[(int64_t)pi * N + j], si);
+        const float4 c = spin_scale(Vb[(int64_t)i * N + pj], sj);
+        const float2 re = df_add(make_float2(a.x, a.y), make_float2(c.x, c.y));
+        const float2 im = df_add(make_float2(a.z, a.w), make_float2(c.z, c.w));
+        J[b * NN + e] = make_float4(0.5f * re.x, 0.5f * re.y, 0.5f * im.x, 0.5f * im.y);
+    }
+}
+
+__global__ void z_to_pairs_kernel(int64_t nb, int64_t N2, const zc* __restrict__ in, int64_t ld_in,
+                                  float4* __restrict__ out) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nb * N2;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = idx / N2, e = idx - b * N2;
+        const zc v = in[b * ld_in + e];
+        const float2 r = df_of(v.re), q = df_of(v.im);
+        out[idx] = make_float4(r.x, r.y, q.x, q.y);
+    }
+}
+
 __device__ __forceinline__ double fermi(double e, double mu, double width) {
     if (width == 0.0) return (e < mu) ? 1.0 : ((e > mu) ? 0.0 : 0.5);
     const double x = (e - mu) / width;
@@ -230,6 +273,24 @@ int spin_dress(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, zc
     // copy J back into the V_0 slots
     TBG_CUDA(cudaMemcpy2DAsync(V, sizeof(zc) * ldV, scratch, sizeof(zc) * NN, sizeof(zc) * NN, batch,
                                cudaMemcpyDeviceToDevice, st));
+    return TBG_OK;
+}
+
+int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
+                     float4* scratch) {
+    const int64_t NN = (int64_t)N * N;
+    KTimer kt(st, "spin_dress_kernel");
+    dim3 grid((unsigned)((NN + 255) / 256), (unsigned)std::min<int64_t>(batch, 65535));
+    spin_dress_pairs_kernel<<<grid, 256, 0, st>>>(N, (int)norb, batch, spin, V, ldV, scratch);
+    TBG_LAUNCHED("spin_dress_pairs_kernel");
+    TBG_CUDA(cudaMemcpy2DAsync(V, sizeof(float4) * ldV, scratch, sizeof(float4) * NN, sizeof(float4) * NN, batch,
+                               cudaMemcpyDeviceToDevice, st));
+    return TBG_OK;
+}
+
+int z_to_pairs(cudaStream_t st, int64_t nb, int64_t N2, const zc* in, int64_t ld_in, float4* out) {
+    z_to_pairs_kernel<<<grid_for(nb * N2, 256), 256, 0, st>>>(nb, N2, in, ld_in, out);
+    TBG_LAUNCHED("z_to_pairs_kernel");
     return TBG_OK;
 }
 

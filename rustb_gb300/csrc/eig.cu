@@ -195,9 +195,9 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
 template <typename T, bool A_SMEM>
 __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
-                                                   double* __restrict__ Eout, cx<T>* __restrict__ Uout,
-                                                   cx<T>* __restrict__ Awork, int* __restrict__ status, int G,
-                                                   int PB) {
+                                                   const float4* __restrict__ Hpair, double* __restrict__ Eout,
+                                                   cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
+                                                   int* __restrict__ status, int G, int PB) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     EigShared<T> sh;
     {
@@ -243,7 +243,14 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             A = Awork + (size_t)blockIdx.x * NN;
         }
         // ---------------------------------------------------------- load --
-        if (A_SMEM || sizeof(T) != sizeof(double)) {
+        if (Hpair) {
+            // float-pair input {re_hi, re_lo, im_hi, im_lo} (FP32 solver only)
+            const float4* src = Hpair + b * NN;
+            for (size_t idx = tid; idx < NN; idx += nthr) {
+                const float4 h = src[idx];
+                A[(idx / N) * LDA + idx % N] = mk<T>((T)(h.x + h.y), (T)(h.z + h.w));
+            }
+        } else if (A_SMEM || sizeof(T) != sizeof(double)) {
             const zc* src = Hin + b * NN;
             for (size_t idx = tid; idx < NN; idx += nthr) {
                 zc h = src[idx];
@@ -547,7 +554,7 @@ inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB
 
 template <typename T, bool A_SMEM>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
-                size_t work_bytes, int* status_d, const char* name, int G, int PB) {
+                size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
     auto kern = heev_kernel<T, A_SMEM>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -569,7 +576,8 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
     KTimer kt(st, name, 14.0 * (double)N * N * N * batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, E, U, reinterpret_cast<cx<T>*>(work), status_d, G, PB);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work), status_d, G,
+                                                PB);
     TBG_LAUNCHED(name);
     return TBG_OK;
 }
@@ -617,24 +625,24 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, E, nullptr, nullptr, nullptr, G, PB);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB);
     TBG_LAUNCHED("heev_kernel<double> (static scratch)");
     return TBG_OK;
 }
 
 // FP32 driver (mixed path): H preserved, U complex<float>.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d) {
+                    size_t work_bytes, int* status_d, const float4* Hpair) {
     if (batch <= 0) return TBG_OK;
     int G, PB;
     if (f32_in_smem(N)) {
         choose_g_pb<float>(N, true, 32, 64, G, PB);
         return launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
-                                        G, PB);
+                                        G, PB, Hpair);
     }
     choose_g_pb<float>(N, false, 32, 64, G, PB);
     return launch_heev<float, false>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,global>",
-                                     G, PB);
+                                     G, PB, Hpair);
 }
 
 }  // namespace tbg

@@ -337,6 +337,40 @@ __global__ void gauge_pairs_kernel(int64_t nk, int N, const float4* __restrict__
     }
 }
 
+// taup (FP64) -> float pairs
+__global__ void tau_split_kernel(int n, const double* __restrict__ taup, float2* __restrict__ tau2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tau2[i] = df_of(taup[i]);
+}
+
+// Lattice gauge, float-pair arithmetic, in place on the contraction output:
+//   V_p += i (tau_p,n - tau_p,m) H_l   (velocity.rs:602-610 before the phase).
+// The Atom-gauge phase conj(phi_m) phi_n is a diagonal unitary similarity
+// (H_atom = P^H H_l P, V_atom = P^H V_l P), so energies and band-basis
+// velocities, hence Omega, do not depend on it; the mixed path skips it.
+__global__ void tau_pairs_kernel(int64_t nk, int N, float4* __restrict__ C, const float2* __restrict__ tau2) {
+    const int64_t NN = (int64_t)N * N;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= NN) return;
+    const int mrow = e / N, ncol = e - mrow * N;
+    float2 d[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) d[p] = df_add(tau2[p * N + ncol], df_neg(tau2[p * N + mrow]));
+    for (int64_t kk = blockIdx.y; kk < nk; kk += gridDim.y) {
+        const int64_t idx = kk * NN + e;
+        const float4 h = C[idx];
+        const float2 hr = make_float2(h.x, h.y), hi = make_float2(h.z, h.w);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            float4* vp = C + (1 + p) * nk * NN + idx;
+            const float4 v = *vp;
+            const float2 vr = df_add(make_float2(v.x, v.y), df_neg(df_mul(d[p], hi)));
+            const float2 vi = df_add(make_float2(v.z, v.w), df_mul(d[p], hr));
+            *vp = make_float4(vr.x, vr.y, vi.x, vi.y);
+        }
+    }
+}
+
 std::mutex g_hop_mu;
 
 }  // namespace
@@ -347,19 +381,23 @@ int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, in
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
                   const void* Bs, float4* C, int* err);
 
+bool fourier_mixed_ok(const ModelDev& m) { return m.nR <= ozaki_fourier_max_k(); }
+
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
-    const size_t N = (size_t)m.nsta, NN = N * N, nR = (size_t)m.nR;
-    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) + 3 * NN * sizeof(float4)) +
-           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 9 * 256;
+    const size_t N = (size_t)m.nsta, nR = (size_t)m.nR;
+    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int)) + 2 * nR * sizeof(double) +
+           2 * N * sizeof(double) + 2 * N * sizeof(float2) + 10 * 256;
 }
 
-int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H, zc* V,
-                  void* scratch, size_t scratch_bytes) {
-    if (nk <= 0) return TBG_OK;
+namespace {
+
+// Phases and the tensor-core contraction: C (3 nk N^2 float pairs) = lattice-
+// gauge H, V_0, V_1 without the orbital-position term.  orbph (nk, N) and
+// taup (2, N) are left in the scratch for the gauge step.
+int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, float4* C,
+                       void* scratch, zc** orbph_out, double** taup_out, float2** tau2_out) {
     const int N = (int)m.nsta, nR = (int)m.nR;
     const int64_t NN = (int64_t)N * N;
-    if (nR > ozaki_fourier_max_k() || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
-        return fourier_direct(m, st, nk, k_d, TBG_GAUGE_ATOM, 2, dirs_d, H, V, NN, 2 * NN);
     {
         std::lock_guard<std::mutex> lk(g_hop_mu);
         if (!m.hop_slices) {
@@ -391,8 +429,8 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
     zc* orbph = static_cast<zc*>(take(sizeof(zc) * nk * N));
     double* coef = static_cast<double*>(take(sizeof(double) * 2 * nR));
     double* taup = static_cast<double*>(take(sizeof(double) * 2 * N));
+    float2* tau2 = static_cast<float2*>(take(sizeof(float2) * 2 * N));
     int* EA = static_cast<int*>(take(sizeof(int) * 3 * nk));
-    float4* C = static_cast<float4*>(take(sizeof(float4) * 3 * nk * NN));
     int* err = static_cast<int*>(take(sizeof(int)));
     {
         KTimer kt(st, "phases_kernel");
@@ -405,7 +443,8 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
         const int64_t t2 = nk * (int64_t)nR;
         phases3_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
             nk, m.dim, k_d, nR, m.hamR_d, coef, ph3);
-        count_launch(3);
+        tau_split_kernel<<<(2 * N + 255) / 256, 256, 0, st>>>(2 * N, taup, tau2);
+        count_launch(4);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_error(e, "phases");
     }
@@ -413,12 +452,49 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
     if (rc) return rc;
     rc = ozaki_fourier(st, 3 * nk, NN, nR, ph3, EA, m.hop_EB, m.hop_slices, C, err);
     if (rc) return rc;
-    {
-        KTimer kt(st, "gauge_pairs_kernel");
-        gauge_pairs_kernel<<<(unsigned)std::min<int64_t>((nk * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
-            nk, N, C, orbph, taup, H, V);
-        TBG_LAUNCHED("gauge_pairs_kernel");
-    }
+    *orbph_out = orbph;
+    *taup_out = taup;
+    *tau2_out = tau2;
+    return TBG_OK;
+}
+
+}  // namespace
+
+int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H, zc* V,
+                  float4* C, void* scratch, size_t scratch_bytes) {
+    if (nk <= 0) return TBG_OK;
+    const int N = (int)m.nsta;
+    const int64_t NN = (int64_t)N * N;
+    if (!fourier_mixed_ok(m) || !C || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
+        return fourier_direct(m, st, nk, k_d, TBG_GAUGE_ATOM, 2, dirs_d, H, V, NN, 2 * NN);
+    zc* orbph;
+    double* taup;
+    float2* tau2;
+    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2);
+    if (rc) return rc;
+    KTimer kt(st, "gauge_pairs_kernel");
+    gauge_pairs_kernel<<<(unsigned)std::min<int64_t>((nk * NN + 255) / 256, 152 * 64), 256, 0, st>>>(nk, N, C, orbph,
+                                                                                                  taup, H, V);
+    TBG_LAUNCHED("gauge_pairs_kernel");
+    return TBG_OK;
+}
+
+int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
+                        float4* C, void* scratch, size_t scratch_bytes) {
+    if (nk <= 0) return TBG_OK;
+    if (!fourier_mixed_ok(m) || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
+        return set_error(TBG_E_UNSUPPORTED, "fourier_mixed_pairs: nR beyond the exact contraction length");
+    const int N = (int)m.nsta;
+    const int64_t NN = (int64_t)N * N;
+    zc* orbph;
+    double* taup;
+    float2* tau2;
+    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2);
+    if (rc) return rc;
+    KTimer kt(st, "tau_pairs_kernel");
+    dim3 grid((unsigned)((NN + 255) / 256), (unsigned)std::min<int64_t>(nk, 65535));
+    tau_pairs_kernel<<<grid, 256, 0, st>>>(nk, N, C, tau2);
+    TBG_LAUNCHED("tau_pairs_kernel");
     return TBG_OK;
 }
 

@@ -1,10 +1,11 @@
-// Mixed-precision eigenpairs: FP32 eigensolve followed by an Ogita-Aishima
-// refinement sweep in FP64 with Rayleigh-Ritz on near-degenerate clusters.
+// Mixed path: FP32 eigensolve, one Ogita-Aishima refinement sweep and the
+// velocity rotation, with every FP64-class product on the tensor cores
+// (exact-slice BF16 GEMM, float-pair results).
 //
 // For an approximate eigenvector matrix X of the Hermitian H (Ogita & Aishima,
 // "Iterative refinement for symmetric eigenvalue decomposition", 2018):
 //   R = I - X^H X,  S = X^H H X,
-//   lambda_i = Re S_ii / (1 - Re R_ii),
+//   lambda_i = Re S_ii / (1 - Re R_ii) = Re S_ii / Re (X^H X)_ii,
 //   F_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i)   for separated pairs,
 //   F_ij = R_ij / 2                                        inside a cluster,
 //   X <- X (I + F).
@@ -12,6 +13,14 @@
 // is resolved by Rayleigh-Ritz: the projected matrix
 //   S~ = S_c + (R_c S_c + S_c R_c) / 2
 // is diagonalised (complex Jacobi, FP64) and F_c = (I + R_c/2) W - I.
+//
+// Precision split: lambda (the refined eigenvalues) in FP64 from the float
+// pairs; the separated-pair entries of F are a first-order correction of the
+// size of the FP32 eigenvector error and are formed in FP32 from the pair sums
+// (their own relative accuracy only needs to be ~1e-7); cluster blocks in
+// FP64.  Omega is summed in float-pair arithmetic: the FP64 pipe of the part
+// is a small fraction of its FP32 rate, and the band-basis velocities carry
+// about 2^-43 relative accuracy, which float pairs (~2^-48) preserve.
 
 #include <cuda_runtime.h>
 
@@ -22,24 +31,19 @@
 
 namespace tbg {
 
-int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* A, int64_t sA, const zc* B,
-                  int64_t sB, zc* C, int64_t sC);
-int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d);
+int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
+                int64_t sC, int* EA, int* EB);
+int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+bool ozaki_use_tc();
+size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
 
 namespace {
 
 constexpr int kMaxCluster = 8;
-
-__global__ void widen_kernel(int64_t n, const cc* __restrict__ a, zc* __restrict__ b) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        b[i] = mk((double)a[i].re, (double)a[i].im);
-}
-
-__global__ void add_kernel(int64_t n, zc* __restrict__ x, const zc* __restrict__ t) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        x[i] = x[i] + t[i];
-}
+enum { F64 = 0, F32 = 1, PAIR = 2 };
 
 // Small complex Hermitian eigenproblem (c <= kMaxCluster) by cyclic Jacobi,
 // single thread.  A (c x c, row-major) is destroyed; W gets the eigenvectors
@@ -105,22 +109,29 @@ __device__ void jacobi_small(int c, zc* A, zc* W, double* w) {
     }
 }
 
-// One CTA per matrix: R (in/out: becomes F), S; E out.
-__global__ void __launch_bounds__(256) oa_kernel(int N, int64_t batch, zc* __restrict__ R, const zc* __restrict__ S,
-                                                 double* __restrict__ E, int64_t* __restrict__ clusters) {
+__device__ __forceinline__ zc pair_z(float4 v) { return mk((double)v.x + (double)v.y, (double)v.z + (double)v.w); }
+__device__ __forceinline__ zc widen(cc v) { return mk((double)v.re, (double)v.im); }
+
+// One CTA per matrix.  XX = X^H X and S = X^H H X as float pairs -> refined
+// eigenvalues E (FP64) and the update F (FP32 complex).
+__global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, const float4* __restrict__ XX,
+                                                       const float4* __restrict__ S, double* __restrict__ E,
+                                                       cc* __restrict__ F, int64_t* __restrict__ clusters) {
     extern __shared__ double smem[];
-    double* lam = smem;                                  // N
-    int* cstart = reinterpret_cast<int*>(lam + N);       // N
+    double* lam = smem;                                   // N
+    float* lamf = reinterpret_cast<float*>(lam + N);      // N
+    int* cstart = reinterpret_cast<int*>(lamf + N);       // N
     __shared__ double red[32];
-    __shared__ double s_tnorm;
-    const int64_t NN = (int64_t)N * N;
+    const int NN = N * N;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
-        zc* Rb = R + b * NN;
-        const zc* Sb = S + b * NN;
+        const float4* XXb = XX + b * NN;
+        const float4* Sb = S + b * NN;
+        cc* Fb = F + b * NN;
         double mx = 0.0;
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            const double l = Sb[(int64_t)i * N + i].re / (1.0 - Rb[(int64_t)i * N + i].re);
+            const double l = pair_z(Sb[i * N + i]).re / pair_z(XXb[i * N + i]).re;
             lam[i] = l;
+            lamf[i] = (float)l;
             mx = fmax(mx, fabs(l));
         }
         for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -129,7 +140,6 @@ __global__ void __launch_bounds__(256) oa_kernel(int N, int64_t batch, zc* __res
         if (threadIdx.x == 0) {
             double t = 0.0;
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w]);
-            s_tnorm = t;
             // clusters: runs of consecutive (sorted) eigenvalues with gaps <= delta
             const double delta = 1e-3 * fmax(t, 1e-300);
             int start = 0;
@@ -146,22 +156,25 @@ __global__ void __launch_bounds__(256) oa_kernel(int N, int64_t batch, zc* __res
             if (ncl && clusters) atomicAdd(reinterpret_cast<unsigned long long*>(clusters), (unsigned long long)ncl);
         }
         __syncthreads();
-        // F for separated pairs / diagonal; cluster blocks get R/2 first
-        for (int64_t idx = threadIdx.x; idx < NN; idx += blockDim.x) {
-            const int i = (int)(idx / N), j = (int)(idx % N);
-            const zc r = Rb[idx];
-            zc f;
+        // F for separated pairs (FP32); R/2 inside clusters and on the diagonal
+        for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
+            const int i = idx / N, j = idx - i * N;
+            const float4 x4 = XXb[idx];
+            float fr, fi;
             if (cstart[i] == cstart[j]) {
-                f = mk(0.5 * r.re, 0.5 * r.im);
+                fr = (i == j) ? 0.5f * ((1.f - x4.x) - x4.y) : -0.5f * (x4.x + x4.y);
+                fi = -0.5f * (x4.z + x4.w);
             } else {
-                const zc s = Sb[idx];
-                const double den = lam[j] - lam[i];
-                f = mk((s.re + lam[j] * r.re) / den, (s.im + lam[j] * r.im) / den);
+                const float4 s4 = Sb[idx];
+                const float lj = lamf[j];
+                const float den = (float)(lam[j] - lam[i]);
+                fr = ((s4.x + s4.y) - lj * (x4.x + x4.y)) / den;
+                fi = ((s4.z + s4.w) - lj * (x4.z + x4.w)) / den;
             }
-            Rb[idx] = f;  // each element read then written by the same thread
+            Fb[idx] = mk(fr, fi);
         }
         __syncthreads();
-        // Rayleigh-Ritz on clusters (one thread per cluster)
+        // Rayleigh-Ritz on clusters (one thread per cluster, FP64)
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
             if (cstart[i] != i) continue;
             int c = 1;
@@ -172,12 +185,12 @@ __global__ void __launch_bounds__(256) oa_kernel(int N, int64_t batch, zc* __res
             // S~ = S_c + (R_c S_c + S_c R_c)/2, with R_c = 2 F_c (F_c holds R_c/2 now)
             for (int p = 0; p < c; ++p)
                 for (int q = 0; q < c; ++q) {
-                    zc acc = Sb[(int64_t)(i + p) * N + (i + q)];
+                    zc acc = pair_z(Sb[(i + p) * N + (i + q)]);
                     for (int t = 0; t < c; ++t) {
-                        const zc fpt = Rb[(int64_t)(i + p) * N + (i + t)];
-                        const zc stq = Sb[(int64_t)(i + t) * N + (i + q)];
-                        const zc spt = Sb[(int64_t)(i + p) * N + (i + t)];
-                        const zc ftq = Rb[(int64_t)(i + t) * N + (i + q)];
+                        const zc fpt = widen(Fb[(i + p) * N + (i + t)]);
+                        const zc stq = pair_z(Sb[(i + t) * N + (i + q)]);
+                        const zc spt = pair_z(Sb[(i + p) * N + (i + t)]);
+                        const zc ftq = widen(Fb[(i + t) * N + (i + q)]);
                         acc = acc + fpt * stq + spt * ftq;
                     }
                     A[p * c + q] = acc;
@@ -195,172 +208,29 @@ __global__ void __launch_bounds__(256) oa_kernel(int N, int64_t batch, zc* __res
             for (int p = 0; p < c; ++p)
                 for (int q = 0; q < c; ++q) {
                     zc acc = W[p * c + q];
-                    for (int t = 0; t < c; ++t) acc = acc + Rb[(int64_t)(i + p) * N + (i + t)] * W[t * c + q];
+                    for (int t = 0; t < c; ++t) acc = acc + widen(Fb[(i + p) * N + (i + t)]) * W[t * c + q];
                     if (p == q) acc.re -= 1.0;
                     Fn[p * c + q] = acc;
                 }
             for (int p = 0; p < c; ++p) {
-                for (int q = 0; q < c; ++q) Rb[(int64_t)(i + p) * N + (i + q)] = Fn[p * c + q];
+                for (int q = 0; q < c; ++q) Fb[(i + p) * N + (i + q)] = mk((float)Fn[p * c + q].re, (float)Fn[p * c + q].im);
                 lam[i + p] = w[p];
             }
             // rows outside the cluster: F_{t,c} <- F_{t,c} W
             for (int t = 0; t < N; ++t) {
                 if (t >= i && t < i + c) continue;
                 zc row[kMaxCluster];
-                for (int q = 0; q < c; ++q) row[q] = Rb[(int64_t)t * N + i + q];
+                for (int q = 0; q < c; ++q) row[q] = widen(Fb[t * N + i + q]);
                 for (int q = 0; q < c; ++q) {
                     zc acc = mk(0.0, 0.0);
                     for (int u = 0; u < c; ++u) acc = acc + row[u] * W[u * c + q];
-                    Rb[(int64_t)t * N + i + q] = acc;
+                    Fb[t * N + i + q] = mk((float)acc.re, (float)acc.im);
                 }
             }
         }
         __syncthreads();
         for (int i = threadIdx.x; i < N; i += blockDim.x) E[b * N + i] = lam[i];
         __syncthreads();
-    }
-}
-
-// Restore ascending order of E (with the columns of X) after refinement.
-__global__ void sort_pairs_kernel(int N, int64_t batch, double* __restrict__ E, zc* __restrict__ X,
-                                  zc* __restrict__ tmp) {
-    extern __shared__ double sm2[];
-    double* e = sm2;
-    int* perm = reinterpret_cast<int*>(e + N);
-    __shared__ int s_sorted;
-    const int64_t NN = (int64_t)N * N;
-    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
-        if (threadIdx.x == 0) s_sorted = 1;
-        __syncthreads();
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            e[i] = E[b * N + i];
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < N - 1; i += blockDim.x)
-            if (e[i + 1] < e[i]) s_sorted = 0;
-        __syncthreads();
-        if (s_sorted) continue;
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            int rank = 0;
-            for (int j = 0; j < N; ++j) rank += (e[j] < e[i]) || (e[j] == e[i] && j < i);
-            perm[rank] = i;
-        }
-        __syncthreads();
-        zc* Xb = X + b * NN;
-        zc* Tb = tmp + b * NN;
-        for (int64_t idx = threadIdx.x; idx < NN; idx += blockDim.x) Tb[idx] = Xb[idx];
-        __syncthreads();
-        for (int64_t idx = threadIdx.x; idx < NN; idx += blockDim.x) {
-            const int r = (int)(idx / N), c = (int)(idx % N);
-            Xb[idx] = Tb[(int64_t)r * N + perm[c]];
-        }
-        for (int i = threadIdx.x; i < N; i += blockDim.x) E[b * N + i] = e[perm[i]];
-        __syncthreads();
-    }
-}
-
-__global__ void eye_minus_kernel(int N, int64_t batch, zc* __restrict__ R) {
-    const int64_t NN = (int64_t)N * N;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < batch * NN;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int e = (int)(idx % NN);
-        zc r = R[idx];
-        r.re = -r.re;
-        r.im = -r.im;
-        if (e / N == e % N) r.re += 1.0;
-        R[idx] = r;
-    }
-}
-
-inline unsigned blocks(int64_t total) {
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152LL * 64));
-}
-
-}  // namespace
-
-size_t mixed_workspace_bytes(int N, int64_t batch) {
-    // U32 + R + S + HX (per k) + FP32 eigensolver global workspace
-    const size_t NN = (size_t)N * N;
-    return (size_t)batch * NN * (sizeof(cc) + 3 * sizeof(zc)) + eig_workspace_bytes(N, batch, 1) + 1024;
-}
-
-// H (FP64, preserved), E out (FP64), U out (FP64 eigenvectors in columns).
-int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, void* work,
-                     size_t work_bytes, int* status_d, int64_t* clusters_d) {
-    if (batch <= 0) return TBG_OK;
-    const size_t NN = (size_t)N * N;
-    if (work_bytes < mixed_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
-    unsigned char* p = static_cast<unsigned char*>(work);
-    cc* U32 = reinterpret_cast<cc*>(p);
-    p += batch * NN * sizeof(cc);
-    zc* R = reinterpret_cast<zc*>(p);
-    p += batch * NN * sizeof(zc);
-    zc* S = reinterpret_cast<zc*>(p);
-    p += batch * NN * sizeof(zc);
-    zc* HX = reinterpret_cast<zc*>(p);
-    p += batch * NN * sizeof(zc);
-    void* eigw = p;
-    const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
-    int rc = eig_batched_f32(st, N, batch, const_cast<zc*>(H), E, U32, eigw, eigw_bytes, status_d);
-    if (rc) return rc;
-    widen_kernel<<<blocks(batch * NN), 256, 0, st>>>(batch * NN, U32, U);
-    TBG_LAUNCHED("widen_kernel");
-    // R = I - X^H X ; S = X^H (H X)
-    if ((rc = zgemm_batched(st, N, batch, true, U, NN, U, NN, R, NN))) return rc;
-    eye_minus_kernel<<<blocks(batch * NN), 256, 0, st>>>(N, batch, R);
-    TBG_LAUNCHED("eye_minus_kernel");
-    if ((rc = zgemm_batched(st, N, batch, false, H, NN, U, NN, HX, NN))) return rc;
-    if ((rc = zgemm_batched(st, N, batch, true, U, NN, HX, NN, S, NN))) return rc;
-    const size_t smem = sizeof(double) * N + sizeof(int) * N;
-    {
-    KTimer kt(st, "oa_kernel");
-    oa_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, R, S, E, clusters_d);
-    TBG_LAUNCHED("oa_kernel");
-    }
-    // X <- X + X F   (HX reused as the product buffer)
-    if ((rc = zgemm_batched(st, N, batch, false, U, NN, R, NN, HX, NN))) return rc;
-    add_kernel<<<blocks(batch * NN), 256, 0, st>>>(batch * NN, U, HX);
-    TBG_LAUNCHED("add_kernel");
-    sort_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, E, U, S);
-    TBG_LAUNCHED("sort_pairs_kernel");
-    return TBG_OK;
-}
-
-}  // namespace tbg
-
-// ===========================================================================
-// Mixed path on the tensor cores: FP32 eigensolve, Ogita-Aishima refinement
-// and the velocity rotation with the exact-slice BF16 GEMM.
-// ===========================================================================
-namespace tbg {
-
-int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
-                const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
-                int64_t sC, int* EA, int* EB);
-int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
-                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
-bool ozaki_use_tc();
-size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
-
-namespace {
-
-enum { F64 = 0, F32 = 1, PAIR = 2 };
-
-// pair -> FP64 complex, optionally as I - X (for R = I - X^H X)
-__global__ void pairs_to_z_kernel(int N, int64_t batch, const float4* __restrict__ in, zc* __restrict__ out,
-                                  int eye_minus) {
-    const int64_t NN = (int64_t)N * N;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < batch * NN;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const float4 v = in[i];
-        double re = (double)v.x + (double)v.y, im = (double)v.z + (double)v.w;
-        if (eye_minus) {
-            const int e = (int)(i % NN);
-            re = ((e / N == e % N) ? 1.0 : 0.0) - re;
-            im = -im;
-        }
-        out[i] = mk(re, im);
     }
 }
 
@@ -374,35 +244,49 @@ __global__ void xprime_kernel(int64_t n, const cc* __restrict__ X, const float4*
     }
 }
 
-// Omega_n = sum_{m != n} -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2) from
-// float-pair band-basis velocities; one warp per row n.
-__global__ void berry_pairs_kernel(int N, int64_t batch, const float4* __restrict__ Bx, const float4* __restrict__ By,
-                                   const double* __restrict__ E, double eta2, double* __restrict__ Omega) {
-    const int lane = threadIdx.x & 31;
-    const int64_t NN = (int64_t)N * N;
-    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t w = gw; w < batch * N; w += nw) {
-        const int64_t b = w / N;
-        const int n = (int)(w % N);
-        const float4* bx = Bx + b * NN + (int64_t)n * N;
-        const float4* by = By + b * NN;
-        const double* Eb = E + b * N;
-        const double en = Eb[n];
-        double s = 0.0;
-        for (int m = lane; m < N; m += 32) {
-            if (m == n) continue;
-            const float4 x = bx[m];
-            const float4 y = by[(int64_t)m * N + n];
-            const double xr = (double)x.x + (double)x.y, xi = (double)x.z + (double)x.w;
-            const double yr = (double)y.x + (double)y.y, yi = (double)y.z + (double)y.w;
-            const double im = xr * yi + xi * yr;
-            const double de = en - Eb[m];
-            s += -2.0 * im / (de * de + eta2);
-        }
+__device__ __forceinline__ float2 df_warp_sum(float2 s) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) Omega[b * N + n] = s;
+    for (int o = 16; o > 0; o >>= 1)
+        s = df_add(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+    return s;
+}
+
+// Omega_n = sum_{m != n} -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2)
+// (traits.rs:181-195) from float-pair band-basis velocities, in float-pair
+// arithmetic.  By is Hermitian, so By[m,n] = conj(By[n,m]) and both operands
+// are read along row n.  One warp per row n; E of the matrix as pairs in
+// shared memory.
+__global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, const float4* __restrict__ Bx,
+                                                       const float4* __restrict__ By, const double* __restrict__ E,
+                                                       float2 eta2, double* __restrict__ Omega) {
+    extern __shared__ float2 e2s[];  // N
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int NN = N * N;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) e2s[i] = df_of(E[b * N + i]);
+        __syncthreads();
+        for (int n = warp; n < N; n += nw) {
+            const float4* bx = Bx + b * NN + n * N;
+            const float4* by = By + b * NN + n * N;
+            const float2 en = e2s[n];
+            float2 s = make_float2(0.f, 0.f);
+            for (int m = lane; m < N; m += 32) {
+                if (m == n) continue;
+                const float4 x = bx[m];
+                const float4 y = by[m];
+                // Im(x conj(y)) = x_im y_re - x_re y_im
+                const float2 t1 = df_mul(make_float2(x.z, x.w), make_float2(y.x, y.y));
+                const float2 t2 = df_mul(make_float2(x.x, x.y), make_float2(y.z, y.w));
+                const float2 num = df_add(t1, df_neg(t2));
+                const float2 de = df_add(en, df_neg(e2s[m]));
+                const float2 den = df_add(df_mul(de, de), eta2);
+                const float2 q = df_div(num, den);
+                s = df_add(s, make_float2(-2.f * q.x, -2.f * q.y));
+            }
+            s = df_warp_sum(s);
+            if (lane == 0) Omega[b * N + n] = df_to_double(s);
+        }
     }
 }
 
@@ -443,13 +327,13 @@ inline unsigned nblk(int64_t total) {
 
 size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     const size_t NN = (size_t)N * N;
-    // X (cc) + 5 pair buffers + R, S (zc) + exponents + FP32 solver workspace
-    return (size_t)batch * NN * (sizeof(cc) + 5 * sizeof(float4) + 2 * sizeof(zc)) +
-           ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) + 4096;
+    // X and F (cc) + 5 pair buffers + exponents + FP32 solver workspace
+    return (size_t)batch * NN * (2 * sizeof(cc) + 5 * sizeof(float4)) + ozaki_exp_bytes(batch, N, N) +
+           eig_workspace_bytes(N, batch, 1) + 4096;
 }
 
-// H (FP64, preserved), Vx/Vy (FP64, stride ldV) -> E (refined, ascending), Omega.
-int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx, const zc* Vy, int64_t ldV,
+// H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega.
+int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
                 int64_t* clusters_d) {
     if (batch <= 0) return TBG_OK;
@@ -462,46 +346,39 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx
         return q;
     };
     cc* X = static_cast<cc*>(take(sizeof(cc) * batch * NN));
+    cc* F = static_cast<cc*>(take(sizeof(cc) * batch * NN));
     float4* bA = static_cast<float4*>(take(sizeof(float4) * batch * NN));
     float4* bB = static_cast<float4*>(take(sizeof(float4) * batch * NN));
     float4* bC = static_cast<float4*>(take(sizeof(float4) * batch * NN));
     float4* bD = static_cast<float4*>(take(sizeof(float4) * batch * NN));
     float4* bE = static_cast<float4*>(take(sizeof(float4) * batch * NN));
-    zc* Rz = static_cast<zc*>(take(sizeof(zc) * batch * NN));
-    zc* Sz = static_cast<zc*>(take(sizeof(zc) * batch * NN));
     int* EA = static_cast<int*>(take(ozaki_exp_bytes(batch, N, N)));
     int* EB = EA + batch * N;
     const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
     void* eigw = take(eigw_bytes);
     // FP64-class products: tcgen05 form unless the mma.sync form is selected
-    auto hp = [&](bool conj_a, int fa, int fb, const void* A, int64_t sA, const void* B, int64_t sB,
-                  float4* C) -> int {
+    auto hp = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C) -> int {
         if (ozaki_use_tc())
-            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, sA, B, N, sB, C, N, NN, EA, EB, status_d);
-        return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, sA, B, N, sB, C, N, NN, EA, EB);
+            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB, status_d);
+        return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB);
     };
     int rc;
-    // 1. FP32 eigenpairs
-    if ((rc = eig_batched_f32(st, N, batch, const_cast<zc*>(H), E, X, eigw, eigw_bytes, status_d))) return rc;
-    // 2. R = I - X^H X, S = X^H (H X)   (FP64-class, tensor cores)
-    if ((rc = hp(true, F32, F32, X, NN, X, NN, bA))) return rc;
-    if ((rc = hp(false, F64, F32, H, NN, X, NN, bB))) return rc;
-    if ((rc = hp(true, F32, PAIR, X, NN, bB, NN, bC))) return rc;
-    {
-        KTimer kt(st, "pairs_to_z_kernel");
-        pairs_to_z_kernel<<<nblk(batch * NN), 256, 0, st>>>(N, batch, bA, Rz, 1);
-        pairs_to_z_kernel<<<nblk(batch * NN), 256, 0, st>>>(N, batch, bC, Sz, 0);
-        count_launch(2);
-    }
-    // 3. Ogita-Aishima update F (into Rz) and refined eigenvalues
+    // 1. FP32 eigenpairs of H
+    if ((rc = eig_batched_f32(st, N, batch, nullptr, E, X, eigw, eigw_bytes, status_d, H))) return rc;
+    // 2. X^H X and S = X^H (H X)   (FP64-class, tensor cores)
+    if ((rc = hp(true, F32, F32, X, X, bA))) return rc;
+    if ((rc = hp(false, PAIR, F32, H, X, bB))) return rc;
+    if ((rc = hp(true, F32, PAIR, X, bB, bC))) return rc;
+    // 3. Ogita-Aishima update F and refined eigenvalues
     {
         KTimer kt(st, "oa_kernel");
-        const size_t smem = sizeof(double) * N + sizeof(int) * N;
-        oa_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, Rz, Sz, E, clusters_d);
+        const size_t smem = sizeof(double) * N + sizeof(float) * N + sizeof(int) * N;
+        oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, bC, E, F,
+                                                                                        clusters_d);
         TBG_LAUNCHED("oa_kernel");
     }
     // 4. X' = X + X F  (float pair: hi = X, lo = X F)
-    if ((rc = ozaki_zgemm(st, false, false, F32, F64, batch, N, N, N, X, N, NN, Rz, N, NN, bE, N, NN, EA, EB)))
+    if ((rc = ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB)))
         return rc;
     {
         KTimer kt(st, "xprime_kernel");
@@ -509,15 +386,19 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx
         TBG_LAUNCHED("xprime_kernel");
     }
     // 5. band-basis velocities B = X'^H V X'
-    if ((rc = hp(false, F64, PAIR, Vx, ldV, bA, NN, bB))) return rc;
-    if ((rc = hp(false, F64, PAIR, Vy, ldV, bA, NN, bC))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, NN, bB, NN, bD))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, NN, bC, NN, bE))) return rc;
+    if ((rc = hp(false, PAIR, PAIR, Vx, bA, bB))) return rc;
+    if ((rc = hp(false, PAIR, PAIR, Vy, bA, bC))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bB, bD))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bC, bE))) return rc;
     // 6. Omega
     {
         KTimer kt(st, "berry_kernel");
-        berry_pairs_kernel<<<nblk(batch * N * 32), 256, 0, st>>>(N, batch, bD, bE, E, eta * eta, Om);
-        TBG_LAUNCHED("berry_pairs_kernel");
+        const double e2 = eta * eta;
+        const float hi = (float)e2;
+        const float2 eta2 = make_float2(hi, (float)(e2 - (double)hi));
+        berry_df_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, sizeof(float2) * N, st>>>(N, batch, bD, bE,
+                                                                                                    E, eta2, Om);
+        TBG_LAUNCHED("berry_df_kernel");
     }
     sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 2 * sizeof(double) * N, st>>>(N, batch, E,
                                                                                                       Om);

@@ -402,11 +402,11 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
     EXP_CASE(false, FMT_F64, FMT_F64)
     EXP_CASE(true, FMT_F64, FMT_F64)
     EXP_CASE(true, FMT_F32, FMT_F32)
-    EXP_CASE(false, FMT_F64, FMT_F32)
+    EXP_CASE(false, FMT_PAIR, FMT_F32)
     EXP_CASE(true, FMT_F32, FMT_PAIR)
-    EXP_CASE(false, FMT_F64, FMT_PAIR)
+    EXP_CASE(false, FMT_PAIR, FMT_PAIR)
     EXP_CASE(true, FMT_PAIR, FMT_PAIR)
-    EXP_CASE(false, FMT_F32, FMT_F64)
+    EXP_CASE(false, FMT_F32, FMT_F32)
 #undef EXP_CASE
     return set_error(TBG_E_UNSUPPORTED, "ozaki_exp_launch: format combination");
 }
@@ -548,12 +548,12 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
     // combinations used by the mixed path and by the unit test
     OZ_CASE(true, false, FMT_F64, FMT_F64)
     OZ_CASE(true, true, FMT_F64, FMT_F64)
-    OZ_CASE(true, true, FMT_F32, FMT_F32)   // X^H X
-    OZ_CASE(true, false, FMT_F64, FMT_F32)  // H X
-    OZ_CASE(true, true, FMT_F32, FMT_PAIR)  // X^H (H X)
-    OZ_CASE(true, false, FMT_F64, FMT_PAIR) // V X'
-    OZ_CASE(true, true, FMT_PAIR, FMT_PAIR) // X'^H (V X')
-    OZ_CASE(false, false, FMT_F32, FMT_F64) // X F
+    OZ_CASE(true, true, FMT_F32, FMT_F32)    // X^H X
+    OZ_CASE(true, false, FMT_PAIR, FMT_F32)  // H X
+    OZ_CASE(true, true, FMT_F32, FMT_PAIR)   // X^H (H X)
+    OZ_CASE(true, false, FMT_PAIR, FMT_PAIR) // V X'
+    OZ_CASE(true, true, FMT_PAIR, FMT_PAIR)  // X'^H (V X')
+    OZ_CASE(false, false, FMT_F32, FMT_F32)  // X F
     OZ_CASE(false, false, FMT_F64, FMT_F64)
 #undef OZ_CASE
     return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm: operand format combination not instantiated");

@@ -613,13 +613,13 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
         return launch_tc<CJ, FA, FB>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,          \
                                      "ozaki_tc_kernel<high>", work);
-    TC_CASE(false, FMT_F64, FMT_F64)
-    TC_CASE(true, FMT_F64, FMT_F64)
-    TC_CASE(true, FMT_F32, FMT_F32)
-    TC_CASE(false, FMT_F64, FMT_F32)
-    TC_CASE(true, FMT_F32, FMT_PAIR)
-    TC_CASE(false, FMT_F64, FMT_PAIR)
-    TC_CASE(true, FMT_PAIR, FMT_PAIR)
+    TC_CASE(false, FMT_F64, FMT_F64)   // unit test
+    TC_CASE(true, FMT_F64, FMT_F64)    // unit test
+    TC_CASE(true, FMT_F32, FMT_F32)    // X^H X
+    TC_CASE(false, FMT_PAIR, FMT_F32)  // H X
+    TC_CASE(true, FMT_F32, FMT_PAIR)   // X^H (H X)
+    TC_CASE(false, FMT_PAIR, FMT_PAIR) // V X'
+    TC_CASE(true, FMT_PAIR, FMT_PAIR)  // X'^H (V X')
 #undef TC_CASE
     return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: operand format combination not instantiated");
 }

@@ -68,6 +68,40 @@ __host__ __device__ __forceinline__ void fma_cjx(cx<T>& acc, cx<T> a, cx<T> b) {
 typedef cx<double> zc;
 typedef cx<float> cc;
 
+// ---------------------------------------------------- float-pair arithmetic --
+// Values hi + lo held as two floats (about 48 significant bits).  Error-free
+// transformations: TwoSum (Knuth) and TwoProduct through FMA.  Used where the
+// FP64 pipe would otherwise bound an elementwise kernel.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float2 s = df_two_sum(a.x, b.x);
+    return df_two_sum(s.x, s.y + (a.y + b.y));
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_two_sum(p, e);
+}
+// a / b: quotient estimate, one correction step with the exact remainder
+__device__ __forceinline__ float2 df_div(float2 a, float2 b) {
+    const float q1 = a.x / b.x;
+    const float2 r = df_add(a, df_neg(df_mul(make_float2(q1, 0.f), b)));
+    const float q2 = (r.x + r.y) / b.x;
+    return df_two_sum(q1, q2);
+}
+__device__ __forceinline__ float2 df_of(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
 // -------------------------------------------------------------- model data --
 struct ModelDev {
     int dim = 0, spin = 0;
@@ -146,9 +180,16 @@ bool fourier_mesh_supported(const ModelDev& m);
 // (exact-slice BF16 contraction), Atom gauge, FP64 outputs H (nk, N, N) and
 // V (nk, 2, N, N).  Falls back to fourier_direct when nR exceeds the exact
 // contraction length.
+// C (3 nk N^2 float pairs) is the contraction output buffer.
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk);
+bool fourier_mixed_ok(const ModelDev& m);
 int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, zc* H,
-                  zc* V, void* scratch, size_t scratch_bytes);
+                  zc* V, float4* C, void* scratch, size_t scratch_bytes);
+// Same contraction, left in C as float pairs in the lattice gauge with the
+// orbital-position term added to V_0, V_1 (blocks [0,nk), [nk,2nk), [2nk,3nk)
+// of N^2 elements).  Requires fourier_mixed_ok(m).
+int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
+                        float4* C, void* scratch, size_t scratch_bytes);
 
 // Batched Hermitian eigensolver: A (batch, N, N) FP64 input (destroyed),
 // E (batch, N) ascending, U (batch, N, N) eigenvectors in columns (may be
@@ -184,16 +225,20 @@ int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* kl
 constexpr int kSmallMaxN = 8;
 
 // ------------------------------------------------------------- mixed path --
-int mixed_eig_refine(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U,
-                     void* work, size_t work_bytes, int* status_d, int64_t* clusters_d);
-size_t mixed_workspace_bytes(int N, int64_t batch);
+// FP32 solver: H (FP64) or, when Hpair is given, float pairs
+// {re_hi, re_lo, im_hi, im_lo} (batch stride N*N); U32 eigenvectors in columns.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d);
-// Mixed path end to end: FP32 eigensolve, refinement and rotation on the
-// tensor cores -> refined E (ascending) and Omega.
+                    size_t work_bytes, int* status_d, const float4* Hpair = nullptr);
+// FP32 eigensolve, refinement and rotation on the tensor cores: H, Vx, Vy as
+// float pairs (batch stride N*N) -> refined E (ascending) and Omega.
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);
-int mixed_berry(cudaStream_t st, int N, int64_t batch, const zc* H, const zc* Vx, const zc* Vy, int64_t ldV,
+int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
                 int64_t* clusters_d);
+// Spin-current dressing of float-pair velocities (V_0 blocks, batch stride ldV).
+int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
+                     float4* scratch);
+// FP64 complex -> float pairs: out[b N2 + e] = in[b ld_in + e], b < nb, e < N2.
+int z_to_pairs(cudaStream_t st, int64_t nb, int64_t N2, const zc* in, int64_t ld_in, float4* out);
 
 }  // namespace tbg
