@@ -178,6 +178,53 @@ int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begi
                         const double* mu, double T, double eta, int spin,
                         int precision, double* sums_out, tbg_report* report);
 
+/* ------------------------------------------- asynchronous batch queue --- */
+
+/* Jobs run on library-owned worker threads, each call on its own CUDA stream,
+ * so jobs of different models and sizes overlap on the GPU.  The reference
+ * runs the same methods concurrently from rayon workers
+ * (src/response/linear/mod.rs:198-202, src/solve_ham.rs:327-332); a Rust
+ * caller uses these entry points to keep many batch calls in flight. */
+typedef enum {
+  TBG_JOB_HALL = 0,      /* tbg_hall_conductivity: out0 = sigma (nmu)         */
+  TBG_JOB_BANDS = 1,     /* tbg_solve_band: out0 = E (nk, nsta)               */
+  TBG_JOB_BERRY = 2,     /* tbg_berry_curvature: out0 = Omega, out1 = E       */
+  TBG_JOB_OCCUPIED = 3   /* tbg_occupied_berry_curvature: out0 (nk), mu[0]    */
+} tbg_job_kind;
+
+typedef struct tbg_job {
+  int kind;                 /* tbg_job_kind */
+  const tbg_model* model;
+  const int64_t* kmesh;     /* HALL: (dim) */
+  int64_t nk;               /* BANDS, BERRY, OCCUPIED */
+  const double* k;          /* (nk, dim) */
+  const double* dirs2;      /* (2, dim) */
+  int64_t nmu;
+  const double* mu;         /* (nmu); OCCUPIED uses mu[0] */
+  double T, eta;
+  int spin, precision;
+  double* out0;
+  double* out1;
+} tbg_job;
+
+/* Queue a job.  The descriptor, kmesh, dirs2 and mu are copied; k and the
+ * outputs must stay valid until the job is reported done.  The job runs on
+ * the device current in the calling thread.  *ticket identifies it. */
+int tbg_batch_submit(const tbg_job* job, int64_t* ticket);
+
+/* Non-blocking: *done = 1 once the job finished, *status = its tbg_status
+ * (and tbg_last_error in this thread holds its message).  A ticket is
+ * released by the call that reports it done; an unknown ticket is
+ * TBG_E_INVALID_ARGUMENT. */
+int tbg_batch_poll(int64_t ticket, int* done, int* status);
+
+/* Block until the job finished; *status as for tbg_batch_poll.  Releases the
+ * ticket. */
+int tbg_batch_wait(int64_t ticket, int* status);
+
+/* Number of worker threads (default 4; applies to workers not yet started). */
+int tbg_batch_set_workers(int n);
+
 /* ------------------------------------------------ no-allocation variant --- */
 
 /* Size of the fixed device scratch array used by tbg_eigvalsh_noalloc. */

@@ -42,6 +42,28 @@ class TbgReport(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class TbgJob(ctypes.Structure):
+    """``tbg_job`` of the asynchronous batch queue."""
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("model", ctypes.c_void_p),
+        ("kmesh", _c_int64_p),
+        ("nk", ctypes.c_int64),
+        ("k", _c_double_p),
+        ("dirs2", _c_double_p),
+        ("nmu", ctypes.c_int64),
+        ("mu", _c_double_p),
+        ("T", ctypes.c_double),
+        ("eta", ctypes.c_double),
+        ("spin", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("out0", _c_double_p),
+        ("out1", _c_double_p),
+    ]
+
+
+JOB_HALL, JOB_BANDS, JOB_BERRY, JOB_OCCUPIED = 0, 1, 2, 3
+
 # (name, restype, argtypes) for every symbol include/tbgpu.h declares.
 SIGNATURES = [
     ("tbg_model_create", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
@@ -79,6 +101,10 @@ SIGNATURES = [
                                               ctypes.c_int, ctypes.c_int]),
     ("tbg_eigvalsh_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p]),
+    ("tbg_batch_submit", ctypes.c_int, [ctypes.POINTER(TbgJob), _c_int64_p]),
+    ("tbg_batch_poll", ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    ("tbg_batch_wait", ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
+    ("tbg_batch_set_workers", ctypes.c_int, [ctypes.c_int]),
     ("tbg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     ("tbg_version", ctypes.c_char_p, []),
     ("tbg_kernel_launch_count", ctypes.c_int64, [ctypes.c_int]),

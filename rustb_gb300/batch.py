@@ -183,3 +183,90 @@ def _gpu_name() -> str:
         return r.stdout.strip() or "GPU"
     except Exception:
         return "GPU"
+
+
+# --------------------------------------------------- native asynchronous queue
+class AsyncJob:
+    """A job queued on the library's own worker threads (``tbg_batch_submit``).
+
+    Holds the input and output arrays until the job is reported done."""
+
+    def __init__(self, lib, ticket: int, keep: tuple, result):
+        self._lib = lib
+        self.ticket = ticket
+        self._keep = keep
+        self._result = result
+        self._status = None
+
+    def _finish(self, status: int):
+        self._status = status
+        _lib.check(status, self._lib)
+        return self._result()
+
+    def poll(self):
+        """None while running, else the result (raises the job's error)."""
+        if self._status is not None:
+            return self._finish(self._status)
+        done, st = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(self._lib.tbg_batch_poll(self.ticket, ctypes.byref(done), ctypes.byref(st)), self._lib)
+        return self._finish(st.value) if done.value else None
+
+    def wait(self):
+        if self._status is not None:
+            return self._finish(self._status)
+        st = ctypes.c_int(0)
+        _lib.check(self._lib.tbg_batch_wait(self.ticket, ctypes.byref(st)), self._lib)
+        return self._finish(st.value)
+
+
+def _submit(job, keep, result) -> AsyncJob:
+    lib = _lib.load()
+    t = ctypes.c_int64(0)
+    _lib.check(lib.tbg_batch_submit(ctypes.byref(job), ctypes.byref(t)), lib)
+    return AsyncJob(lib, t.value, keep + (job,), result)
+
+
+def submit_hall(model: Model, p: Parameters, precision=Precision.FP64) -> AsyncJob:
+    """Asynchronous ``hall_conductivity`` (Direct); wait() -> conductivity (nmu)."""
+    p.validate_rank2(model.dim)
+    km = np.ascontiguousarray(p.kmesh, dtype=np.int64)
+    d = _lib.as_f64(p.direction)
+    mu = _lib.as_f64(p.mu)
+    out = np.empty(len(mu))
+    job = _lib.TbgJob(kind=_lib.JOB_HALL, model=model.device_handle(), kmesh=_lib.iptr(km), dirs2=_lib.dptr(d),
+                      nmu=len(mu), mu=_lib.dptr(mu), T=float(p.T[0]), eta=float(p.eta), spin=spin_code(p.spin),
+                      precision=int(precision), out0=_lib.dptr(out))
+    return _submit(job, (km, d, mu, out), lambda: out)
+
+
+def submit_bands(model: Model, k) -> AsyncJob:
+    """Asynchronous ``solve_band_all_parallel``; wait() -> E (nk, nsta)."""
+    k = _lib.as_f64(np.atleast_2d(k))
+    E = np.empty((k.shape[0], model.nsta))
+    job = _lib.TbgJob(kind=_lib.JOB_BANDS, model=model.device_handle(), nk=k.shape[0], k=_lib.dptr(k),
+                      out0=_lib.dptr(E))
+    return _submit(job, (k, E), lambda: E)
+
+
+def submit_berry(model: Model, k, p: Parameters, precision=Precision.FP64) -> AsyncJob:
+    """Asynchronous band-resolved Berry curvature; wait() -> (Omega, E)."""
+    k = _lib.as_f64(np.atleast_2d(k))
+    d = _lib.as_f64(p.direction)
+    Om = np.empty((k.shape[0], model.nsta))
+    E = np.empty((k.shape[0], model.nsta))
+    job = _lib.TbgJob(kind=_lib.JOB_BERRY, model=model.device_handle(), nk=k.shape[0], k=_lib.dptr(k),
+                      dirs2=_lib.dptr(d), eta=float(p.eta), spin=spin_code(p.spin), precision=int(precision),
+                      out0=_lib.dptr(Om), out1=_lib.dptr(E))
+    return _submit(job, (k, d, Om, E), lambda: (Om, E))
+
+
+def submit_occupied(model: Model, k, p: Parameters, precision=Precision.FP64) -> AsyncJob:
+    """Asynchronous occupied Berry curvature at mu = p.mu[0]; wait() -> (nk,)."""
+    k = _lib.as_f64(np.atleast_2d(k))
+    d = _lib.as_f64(p.direction)
+    mu = _lib.as_f64(p.mu)
+    out = np.empty(k.shape[0])
+    job = _lib.TbgJob(kind=_lib.JOB_OCCUPIED, model=model.device_handle(), nk=k.shape[0], k=_lib.dptr(k),
+                      dirs2=_lib.dptr(d), nmu=len(mu), mu=_lib.dptr(mu), T=float(p.T[0]), eta=float(p.eta),
+                      spin=spin_code(p.spin), precision=int(precision), out0=_lib.dptr(out))
+    return _submit(job, (k, d, mu, out), lambda: out)

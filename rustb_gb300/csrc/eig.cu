@@ -552,13 +552,27 @@ inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB
     PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 1))));
 }
 
+// The dynamic shared-memory limit is a per-function attribute shared by every
+// host thread; it is set once to the device's opt-in maximum (a per-call value
+// would race with concurrent calls on other matrix sizes).
+template <typename K>
+int allow_max_smem(K kern, size_t need) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (need > (size_t)optin) return set_error(TBG_E_UNSUPPORTED, "eigensolver: shared memory beyond the device limit");
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
+    return TBG_OK;
+}
+
 template <typename T, bool A_SMEM>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
                 size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
     auto kern = heev_kernel<T, A_SMEM>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
+    if (int rc = allow_max_smem(kern, smem)) return rc;
+    cudaError_t e;
     int dev = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -616,8 +630,8 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     choose_g_pb<double>(N, false, 16, 16, G, PB);
     const size_t smem = eig_smem_bytes<double>(N, false, G, PB);
     auto kern = heev_kernel<double, false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(heev)");
+    if (int rc = allow_max_smem(kern, smem)) return rc;
+    cudaError_t e;
     int dev = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

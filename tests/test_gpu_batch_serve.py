@@ -55,3 +55,66 @@ def test_server_results_equal_alone_and_in_the_mix():
             assert a == b
     lat = srv.latencies()
     assert len(lat) == len(reqs) and np.all(lat > 0)
+
+
+def test_concurrent_calls_on_different_band_counts():
+    """Threads solving models of different sizes at once (each size launches
+    the eigensolver with a different shared-memory footprint)."""
+    import concurrent.futures as cf
+
+    sizes = [(2, 40), (2, 100), (3, 64), (2, 200), (2, 256), (3, 24)]
+    models = [W.random_model(dim, n, False, 1, seed=700 + i) for i, (dim, n) in enumerate(sizes)]
+    rng = np.random.default_rng(11)
+    ks = [rng.uniform(0, 1, (48, m.dim)) for m in models]
+    params = [Parameters(kmesh=(1,) * m.dim, direction=np.eye(m.dim)[:2], mu=[0.0]) for m in models]
+    alone = [m.berry_curvature_on(k, p, Precision.MIXED) for m, k, p in zip(models, ks, params)]
+
+    def run(i):
+        return [models[i].berry_curvature_on(ks[i], params[i], Precision.MIXED) for _ in range(3)]
+
+    with cf.ThreadPoolExecutor(len(models)) as ex:
+        out = list(ex.map(run, range(len(models))))
+    for a, rs in zip(alone, out):
+        for r in rs:
+            assert all(np.array_equal(x, y) for x, y in zip(a, r))
+
+
+def test_native_async_queue_matches_synchronous_calls():
+    from rustb_gb300 import errors
+
+    models = [W.random_model(2, 6, True, 1, seed=810), W.random_model(3, 40, False, 1, seed=811),
+              W.random_model(2, 128, False, 1, seed=812)]
+    rng = np.random.default_rng(5)
+    jobs, expect = [], []
+    for i, m in enumerate(models):
+        dirs = np.eye(m.dim)[:2]
+        ph = Parameters(kmesh=(4,) * m.dim, direction=dirs, mu=[-0.1, 0.0, 0.2])
+        k = rng.uniform(0, 1, (37, m.dim))
+        pb = Parameters(kmesh=(1,) * m.dim, direction=dirs, mu=[0.05])
+        for prec in (Precision.FP64, Precision.MIXED):
+            jobs.append(batch.submit_hall(m, ph, prec))
+            expect.append(m.hall_conductivity(ph, prec).conductivity)
+            jobs.append(batch.submit_berry(m, k, pb, prec))
+            expect.append(m.berry_curvature_on(k, pb, prec))
+            jobs.append(batch.submit_occupied(m, k, pb, prec))
+            expect.append(m.occupied_berry_curvature_on(k, pb, prec))
+        jobs.append(batch.submit_bands(m, k))
+        expect.append(m.solve_band_all_parallel(k))
+    # poll the first job until done, wait for the rest
+    first = None
+    while first is None:
+        first = jobs[0].poll()
+    got = [first] + [j.wait() for j in jobs[1:]]
+    for g, e in zip(got, expect):
+        if isinstance(e, tuple):
+            assert all(np.array_equal(x, y) for x, y in zip(g, e))
+        else:
+            assert np.array_equal(g, e)
+    # a job that fails reports its status and message through wait()
+    bad = Parameters(kmesh=(4, 4), direction=np.eye(2), mu=[0.0])
+    j = batch.submit_hall(models[0], bad, precision=7)
+    with pytest.raises(errors.TbError):
+        j.wait()
+    lib = batch._lib.load()
+    st = batch.ctypes.c_int(0)
+    assert lib.tbg_batch_wait(123456789, batch.ctypes.byref(st)) == 9  # unknown ticket
