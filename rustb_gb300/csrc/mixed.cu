@@ -37,6 +37,9 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
                    int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
+                       const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
+                       int* err);
 bool ozaki_use_tc();
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
 
@@ -378,8 +381,9 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         TBG_LAUNCHED("oa_kernel");
     }
     // 4. X' = X + X F  (float pair: hi = X, lo = X F)
-    if ((rc = ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB)))
-        return rc;
+    rc = ozaki_use_tc() ? ozaki_zgemm_tc_low(st, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB, status_d)
+                        : ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB);
+    if (rc) return rc;
     {
         KTimer kt(st, "xprime_kernel");
         xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, X, bE, bA);

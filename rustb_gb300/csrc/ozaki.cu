@@ -416,6 +416,9 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
                    int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
                      const void* Bs, float4* C, int* err);
+int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
+                       const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
+                       int* err);
 
 // tcgen05 kernels are used unless TBG_OZAKI_MMA_SYNC=1 (the mma.sync form).
 bool ozaki_use_tc() {
@@ -583,7 +586,16 @@ extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int
         int* derr = nullptr;
         cudaMalloc(&derr, sizeof(int));
         cudaMemset(derr, 0, sizeof(int));
-        if (use_tc && high)
+        if (use_tc && !high && !conj_a) {
+            // LOW class on tcgen05 takes FP32 operands: round the inputs once
+            std::vector<float> a32((size_t)2 * ar * ac * batch), b32((size_t)2 * K * Nc * batch);
+            for (size_t i = 0; i < a32.size(); ++i) a32[i] = (float)A[i];
+            for (size_t i = 0; i < b32.size(); ++i) b32[i] = (float)B[i];
+            cudaMemcpy(dA, a32.data(), sizeof(float) * a32.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(dB, b32.data(), sizeof(float) * b32.size(), cudaMemcpyHostToDevice);
+            rc = ozaki_zgemm_tc_low(st, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
+                                    static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr);
+        } else if (use_tc && high)
             rc = ozaki_zgemm_tc(st, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
                                 static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr);
         else

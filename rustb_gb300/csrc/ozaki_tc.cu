@@ -41,12 +41,18 @@ namespace {
 constexpr int TC_TM = 128;        // output rows
 constexpr int TC_TN = 64;         // complex output columns (128 real)
 constexpr int TC_TK = 16;         // complex k per stage (32 real)
-constexpr int TC_S = 6;           // digits per value
-constexpr int TC_LMAX = 5;
+constexpr int TC_S = 6;           // digits per value (HIGH precision class)
 constexpr int PLANE = 128 * 32 * 2;             // bytes of one digit plane (128 rows x 32 k bf16)
 constexpr int HALF_STAGE = TC_S * PLANE;        // the six planes of one operand (49152 bytes)
-constexpr int STAGE_BYTES = 2 * HALF_STAGE;     // A and B planes of one stage
-constexpr int TC_SMEM = 2 * STAGE_BYTES + 1024; // two stages + alignment slack
+// Precision classes: S digits per value, digit pairs s + t <= LMAX, NLEV TMEM
+// accumulators (levels below NLEV - 1 each exact in their own, the rest merged).
+//   HIGH: S = 6, LMAX = 5, NLEV = 4  (about 2^-43 of the product scale)
+//   LOW : S = 3, LMAX = 2, NLEV = 1  (about 2^-21; for small corrections)
+template <int S> struct Class;
+template <> struct Class<6> { static constexpr int LMAX = 5, NLEV = 4, MIN_CTAS = 1; };
+template <> struct Class<3> { static constexpr int LMAX = 2, NLEV = 1, MIN_CTAS = 2; };
+constexpr int tc_smem_bytes(int S) { return 2 * 2 * S * PLANE + 1024; }  // two stages of A and B planes + slack
+constexpr int TC_SMEM = tc_smem_bytes(TC_S);
 constexpr int TC_THREADS = 416;                 // 13 warps
 constexpr int MMA_WARP = 12;
 constexpr int A_PRODUCERS = 256;
@@ -265,19 +271,20 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo_k, float hi_k) {
 }
 // The six digit planes of one component of 8 consecutive-k elements: out[s]
 // holds 8 BF16 (k ascending) = one 16-byte row segment of a core matrix.
-template <int FMT, int PART>
-__device__ __forceinline__ void item_planes(const int4 (&r)[8], int E, float s1, float s2, uint4 (&out)[TC_S]) {
-    uint32_t pk[TC_S][4];
+// The leading S of the six digits are kept (S = 3: the value truncated to 21 bits).
+template <int FMT, int PART, int S>
+__device__ __forceinline__ void item_planes(const int4 (&r)[8], int E, float s1, float s2, uint4 (&out)[S]) {
+    uint32_t pk[S][4];
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
         float P0[TC_S], P1[TC_S];
         elem_digits<FMT, PART>(r[i], E, s1, s2, P0);
         elem_digits<FMT, PART>(r[i + 1], E, s1, s2, P1);
 #pragma unroll
-        for (int s = 0; s < TC_S; ++s) pk[s][i >> 1] = pack_bf16x2(P0[s], P1[s]);
+        for (int s = 0; s < S; ++s) pk[s][i >> 1] = pack_bf16x2(P0[s], P1[s]);
     }
 #pragma unroll
-    for (int s = 0; s < TC_S; ++s) out[s] = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+    for (int s = 0; s < S; ++s) out[s] = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
 }
 __device__ __forceinline__ uint4 neg_bf16x8(uint4 v) {
     const uint32_t m = 0x80008000u;
@@ -289,12 +296,16 @@ __host__ __device__ __forceinline__ int plane_off(int row, int kp) {
 }
 __device__ __forceinline__ int n_valid(int K, int kfirst) { return max(0, min(8, K - kfirst)); }
 
-template <bool CONJ_A, int FMTA, int FMTB>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <bool CONJ_A, int FMTA, int FMTB, int S>
+__global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
                  int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
                  float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
+    constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
+    constexpr int HS = S * PLANE;             // planes of one operand in a stage
+    constexpr int SB = 2 * HS;                // stage bytes
+    constexpr uint32_t TMEM_COLS = NLEV * 128;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
     __shared__ __align__(8) uint64_t bar_full[2], bar_bcopy[2], bar_empty[2], bar_done;
@@ -321,7 +332,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == MMA_WARP) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(&tmem_base_sh))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base_sh)),
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -341,19 +353,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t sa = sbase + bi * STAGE_BYTES;
-                const uint32_t sb = sa + HALF_STAGE;
+                const uint32_t sa = sbase + bi * SB;
+                const uint32_t sb = sa + HS;
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
-                    for (int t = 0; t < TC_S; ++t) {
+                    for (int t = 0; t < S; ++t) {
 #pragma unroll
-                        for (int s = 0; s < TC_S; ++s) {
-                            if (s + t > TC_LMAX) continue;
-                            const int lv = (s + t) < 3 ? (s + t) : 3;
+                        for (int s = 0; s < S; ++s) {
+                            if (s + t > LMAX) continue;
+                            const int lv = (s + t) < NLEV - 1 ? (s + t) : NLEV - 1;
                             const uint64_t ad = smem_desc(sa + s * PLANE + ks * 256, 128, 512);
                             const uint64_t bd = smem_desc(sb + t * PLANE + ks * 256, 128, 512);
-                            const uint32_t acc = (it == 0 && ks == 0 && t == 0 && s <= 3) ? 0u : 1u;
+                            // the first product into each accumulator overwrites it
+                            const uint32_t acc = (it == 0 && ks == 0 && t == 0 && s <= NLEV - 1) ? 0u : 1u;
                             umma(tmem + (uint32_t)(lv * 128), ad, bd, acc);
                         }
                     }
@@ -391,14 +404,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 break;
             }
             if (abort_sh) break;
-            const uint32_t sa = sbase + bi * STAGE_BYTES;
-            uint4 d[TC_S];
-            item_planes<FMTA, 0>(cur, E, s1, s2, d);
+            const uint32_t sa = sbase + bi * SB;
+            uint4 d[S];
+            item_planes<FMTA, 0, S>(cur, E, s1, s2, d);
 #pragma unroll
-            for (int s = 0; s < TC_S; ++s) st_shared_v4(sa + s * PLANE + o_re, d[s]);
-            item_planes<FMTA, 1>(cur, E, s1, s2, d);
+            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_re, d[s]);
+            item_planes<FMTA, 1, S>(cur, E, s1, s2, d);
 #pragma unroll
-            for (int s = 0; s < TC_S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(d[s]) : d[s]);
+            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(d[s]) : d[s]);
             fence_async_smem();  // make the generic-proxy writes visible to the tensor core
             mbar_arrive(&bar_full[bi]);
         }
@@ -407,7 +420,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (PRE) {
             // ------------------------- pre-sliced B: bulk copy of stage images
             if (q == 0) {
-                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HALF_STAGE;
+                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HS;
                 int last[2] = {-1, -1};
                 for (int it = 0; it < nstages; ++it) {
                     const int bi = it & 1;
@@ -416,9 +429,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         break;
                     }
                     if (abort_sh) break;
-                    mbar_arrive_tx(&bar_bcopy[bi], HALF_STAGE);
-                    bulk_g2s(sbase + bi * STAGE_BYTES + HALF_STAGE, src + (int64_t)it * HALF_STAGE, HALF_STAGE,
-                             &bar_bcopy[bi]);
+                    mbar_arrive_tx(&bar_bcopy[bi], HS);
+                    bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HS, HS, &bar_bcopy[bi]);
                     last[bi] = it;
                 }
                 // every copy issued has landed before the CTA can leave
@@ -454,17 +466,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 }
                 if (abort_sh) break;
-                const uint32_t sb = sbase + bi * STAGE_BYTES + HALF_STAGE;
-                uint4 d[TC_S];
-                item_planes<FB, 0>(cur, E, s1, s2, d);
+                const uint32_t sb = sbase + bi * SB + HS;
+                uint4 d[S];
+                item_planes<FB, 0, S>(cur, E, s1, s2, d);
 #pragma unroll
-                for (int s = 0; s < TC_S; ++s) {
+                for (int s = 0; s < S; ++s) {
                     st_shared_v4(sb + s * PLANE + o_jre, d[s]);
                     st_shared_v4(sb + s * PLANE + o_kim, d[s]);
                 }
-                item_planes<FB, 1>(cur, E, s1, s2, d);
+                item_planes<FB, 1, S>(cur, E, s1, s2, d);
 #pragma unroll
-                for (int s = 0; s < TC_S; ++s) {
+                for (int s = 0; s < S; ++s) {
                     st_shared_v4(sb + s * PLANE + o_kre, d[s]);
                     st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(d[s]));
                 }
@@ -486,9 +498,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int ea = (r < M) ? EA[b * M + r] : ZERO_EXP;
             for (int cc = 0; cc < 4; ++cc) {
                 const int c0 = 32 * h + 8 * cc;
-                uint32_t v[8][8];  // [2 * level + (0 re, 1 im)][column]
+                uint32_t v[2 * NLEV][8];  // [2 * level + (0 re, 1 im)][column]
 #pragma unroll
-                for (int L = 0; L < 4; ++L) {
+                for (int L = 0; L < NLEV; ++L) {
                     tmem_ld8(lane_addr + (uint32_t)(L * 128 + c0), v[2 * L]);
                     tmem_ld8(lane_addr + (uint32_t)(L * 128 + TC_TN + c0), v[2 * L + 1]);
                 }
@@ -501,6 +513,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         float hl[4];
 #pragma unroll
                         for (int part = 0; part < 2; ++part) {
+                            if (NLEV == 1) {
+                                hl[2 * part] = __uint_as_float(v[part][c]);
+                                hl[2 * part + 1] = 0.f;
+                                continue;
+                            }
                             const float a0 = __uint_as_float(v[0 + part][c]), a1 = __uint_as_float(v[2 + part][c]);
                             const float a2 = __uint_as_float(v[4 + part][c]), a3 = __uint_as_float(v[6 + part][c]);
                             const float s1 = a0 + a1;
@@ -532,7 +549,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) mbar_wait_plain(&bar_done, 0);  // every committed MMA has finished
         __syncwarp();
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
     }
 }
 
@@ -560,13 +577,13 @@ __global__ void hop_image_kernel(int K, int64_t Nc, const zc* __restrict__ ham, 
         load8<FMT_F64>(ham, (int64_t)kf * Nc + gj, Nc, cv ? n_valid(K, kf) : 0, r);
         unsigned char* dst = img + blk * HALF_STAGE;
         uint4 d[TC_S];
-        item_planes<FMT_F64, 0>(r, E, 0.f, 0.f, d);
+        item_planes<FMT_F64, 0, TC_S>(r, E, 0.f, 0.f, d);
 #pragma unroll
         for (int s = 0; s < TC_S; ++s) {
             *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(j, 8 * g)) = d[s];
             *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 16 + 8 * g)) = d[s];
         }
-        item_planes<FMT_F64, 1>(r, E, 0.f, 0.f, d);
+        item_planes<FMT_F64, 1, TC_S>(r, E, 0.f, 0.f, d);
 #pragma unroll
         for (int s = 0; s < TC_S; ++s) {
             *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 8 * g)) = d[s];
@@ -581,12 +598,13 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
                      const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, int* EA, int* EB);
 
 // tcgen05 form of ozaki_zgemm for the HIGH precision class.
-template <bool CJ, int FA, int FB>
+template <bool CJ, int FA, int FB, int S>
 static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                      const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                      int* err, const char* name, double work) {
-    auto kern = oz_tc_kernel<CJ, FA, FB>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    auto kern = oz_tc_kernel<CJ, FA, FB, S>;
+    constexpr int smem = tc_smem_bytes(S);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc)");
     KTimer kt(st, name, work);
     for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
@@ -594,7 +612,7 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
         dim3 grid((Nc + TC_TN - 1) / TC_TN, (M + TC_TM - 1) / TC_TM, (unsigned)nb);
         const size_t ea = FA == FMT_F32 ? 8 : 16;
         const size_t eb = FB == FMT_F32 ? 8 : 16;
-        kern<<<grid, TC_THREADS, TC_SMEM, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
+        kern<<<grid, TC_THREADS, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
                                                 static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
                                                 EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err);
         TBG_LAUNCHED(name);
@@ -611,8 +629,8 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
     const double work = 8.0 * (double)M * Nc * K * batch;
 #define TC_CASE(CJ, FA, FB)                                                                                          \
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
-        return launch_tc<CJ, FA, FB>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,          \
-                                     "ozaki_tc_kernel<high>", work);
+        return launch_tc<CJ, FA, FB, TC_S>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,    \
+                                           "ozaki_tc_kernel<high>", work);
     TC_CASE(false, FMT_F64, FMT_F64)   // unit test
     TC_CASE(true, FMT_F64, FMT_F64)    // unit test
     TC_CASE(true, FMT_F32, FMT_F32)    // X^H X
@@ -622,6 +640,18 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
     TC_CASE(true, FMT_PAIR, FMT_PAIR)  // X'^H (V X')
 #undef TC_CASE
     return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: operand format combination not instantiated");
+}
+
+// tcgen05 form of the LOW precision class (3 x 3 digits, one FP32 accumulator):
+// C = A B for FP32 A and B, e.g. the correction X F of the refinement.
+int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
+                       const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
+                       int* err) {
+    if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc_low: K > 256");
+    int rc = ozaki_exp_launch(st, false, FMT_F32, FMT_F32, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
+    if (rc) return rc;
+    return launch_tc<false, FMT_F32, FMT_F32, 3>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,
+                                                 "ozaki_tc_kernel<low>", 8.0 * (double)M * Nc * K * batch);
 }
 
 // Bytes of the hop-table stage images (K = nR rows of Nc = N^2 elements).
@@ -644,7 +674,7 @@ int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, co
 // that the CTAs resident together share one column tile's images in L2.
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
                      const void* img, float4* C, int* err) {
-    auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED>;
+    auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED, TC_S>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc fourier)");
     if ((Nc + TC_TN - 1) / TC_TN > 65535 || M > 0x7fffffff)

@@ -58,14 +58,15 @@ def test_ozaki_high_precision(conj_a, M, Nc, K, use_tc):
     assert err.max() < 1e-12, err.max()
 
 
-def test_ozaki_low_precision_and_zeros():
+@pytest.mark.parametrize("use_tc", [0, 1], ids=["mma_sync", "tcgen05"])
+def test_ozaki_low_precision_and_zeros(use_tc):
     lib = _lib.load()
     rng = np.random.default_rng(3)
     A = rng.standard_normal((2, 64, 64)) + 1j * rng.standard_normal((2, 64, 64))
     B = rng.standard_normal((2, 64, 64)) + 1j * rng.standard_normal((2, 64, 64))
     A[0, 5, :] = 0.0  # an all-zero row
     ref = A @ B
-    C = ozaki(lib, A, B, False, False)
+    C = ozaki(lib, A, B, False, False, use_tc)
     scale = np.abs(A).max() * np.abs(B).max() * 64
     assert np.abs(C - ref).max() / scale < 1e-5
     assert np.all(C[0, 5, :] == 0.0)
