@@ -9,10 +9,13 @@
 //      opposite to Re(alpha) (no cancellation).  v_j is kept in row j of A.
 //   2. Eigenvalues of T by Sturm-count bisection, one thread per eigenvalue
 //      (ascending by construction, absolute accuracy ~ eps * ||T||).
-//   3. Eigenvectors of T by inverse iteration (tridiagonal LU with partial
-//      pivoting, three iterations), eigenvalues closer than 1e-3 ||T|| form a
-//      cluster whose vectors are computed by one thread with modified
-//      Gram-Schmidt against the earlier members.
+//   3. Eigenvectors of T: for eigenvalues farther than 1e-3 ||T|| from their
+//      neighbours, the twisted factorisation of T - lambda I (Fernando 1997;
+//      one top-down and one bottom-up pivot sweep, no pivoting branches, no
+//      iteration); eigenvalues closer than that form a cluster whose vectors
+//      are computed by one thread by inverse iteration (tridiagonal LU with
+//      partial pivoting) with modified Gram-Schmidt against the earlier
+//      members.
 //   4. Back-transformation U = H_0 H_1 ... H_{N-2} Z in column panels.
 //
 // Output: E ascending (double), U with eigenvectors in columns (row-major).
@@ -162,6 +165,75 @@ __device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ 
     }
 }
 
+// Eigenvector of the symmetric tridiagonal (d, e) for an isolated eigenvalue
+// lam by the twisted factorisation of T - lam I (Fernando, "On computing an
+// eigenvector of a tridiagonal matrix", 1997): stationary (top-down) pivots
+// D+ and progressive (bottom-up) pivots D-, twist index r at the smallest
+// |gamma_k| = |D+_k + D-_k - (d_k - lam)|, then z_r = 1 and
+//   z_i = -e_i z_{i+1} / D+_i (i < r),   z_{i+1} = -e_i z_i / D-_{i+1} (i >= r).
+// Pivots smaller than pert are replaced by -pert.  Dp holds N values with
+// stride G, followed by the N values of D- (same stride).  Writes the
+// normalised (real) vector to u[i * ldu]; returns false if it is not finite.
+template <typename T>
+__device__ bool twisted_vector(int N, const T* __restrict__ d, const T* __restrict__ e, const T* __restrict__ e2,
+                               T lam, T pert, T* __restrict__ Dp, int G, cx<T>* __restrict__ u, int ldu) {
+    T* Dm = Dp + (size_t)N * G;
+    T p = d[0] - lam;
+    if (fabs(p) < pert) p = -pert;
+    Dp[0] = p;
+    for (int i = 0; i < N - 1; ++i) {
+        p = (d[i + 1] - lam) - Lim<T>::div(e2[i], p);
+        if (fabs(p) < pert) p = -pert;
+        Dp[(size_t)(i + 1) * G] = p;
+    }
+    T q = d[N - 1] - lam;
+    if (fabs(q) < pert) q = -pert;
+    Dm[(size_t)(N - 1) * G] = q;
+    int r = N - 1;
+    T best = fabs(p + q - (d[N - 1] - lam));
+    for (int i = N - 1; i >= 1; --i) {
+        q = (d[i - 1] - lam) - Lim<T>::div(e2[i - 1], q);
+        if (fabs(q) < pert) q = -pert;
+        Dm[(size_t)(i - 1) * G] = q;
+        const T g = fabs(Dp[(size_t)(i - 1) * G] + q - (d[i - 1] - lam));
+        if (g < best) {
+            best = g;
+            r = i - 1;
+        }
+    }
+    // the vector, in place: z_i (i < r) over D+, z_i (i > r) over D-
+    T z = 1, amax = 1;
+#pragma unroll 4
+    for (int i = r - 1; i >= 0; --i) {
+        const T ratio = Lim<T>::div(e[i], Dp[(size_t)i * G]);
+        z = -ratio * z;
+        Dp[(size_t)i * G] = z;
+        amax = max(amax, fabs(z));
+    }
+    z = 1;
+#pragma unroll 4
+    for (int i = r; i < N - 1; ++i) {
+        const T ratio = Lim<T>::div(e[i], Dm[(size_t)(i + 1) * G]);
+        z = -ratio * z;
+        Dm[(size_t)(i + 1) * G] = z;
+        amax = max(amax, fabs(z));
+    }
+    if (!(amax < T(INFINITY))) return false;  // also NaN
+    const T sc = T(1) / amax;
+    T nrm = 0;
+    for (int i = 0; i < N; ++i) {
+        const T v = (i < r ? Dp[(size_t)i * G] : (i == r ? T(1) : Dm[(size_t)i * G])) * sc;
+        nrm += v * v;
+    }
+    if (!(nrm > T(0))) return false;
+    const T inv = sc / sqrt(nrm);
+    for (int i = 0; i < N; ++i) {
+        const T v = (i < r ? Dp[(size_t)i * G] : (i == r ? T(1) : Dm[(size_t)i * G])) * inv;
+        u[(size_t)i * ldu] = mk<T>(v, T(0));
+    }
+    return true;
+}
+
 template <typename T>
 struct EigShared {
     cx<T>* A;   // N*N (shared or global)
@@ -174,7 +246,7 @@ struct EigShared {
     cx<T>* w;   // N
     T* red;     // 64
     T* scratch; // inverse iteration: 4*N*G ; back-transform panel: N*PB complex
-    int* flags; // 4
+    int* flags; // 4 + N: status flags, then per-eigenvalue "left to inverse iteration" marks
 };
 
 template <typename T>
@@ -187,7 +259,7 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
     size_t s2 = sizeof(cx<T>) * (size_t)(N + 4) * PB;
     b += std::max(s1, s2);
-    b += 16;
+    b += sizeof(int) * (4 + (size_t)N);  // flags + per-eigenvalue redo marks
     return b;
 }
 
@@ -435,16 +507,32 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             continue;
         }
 
-        // ------------------------------------------- inverse iteration --
+        // ------------------------------------------ eigenvectors of T --
         cx<T>* U = Uout + b * NN;
         const T ctol = T(1e-3) * max(tnorm, Lim<T>::tiny());
         const T pert = max(Lim<T>::eps() * tnorm, pivmin);
+        int* redo = sh.flags + 4;
+        // (1) isolated eigenvalues: twisted factorisation, 2N scratch values
+        //     each, 2G at a time
+        for (int g0 = 0; g0 < N; g0 += 2 * G) {
+            if (tid < 2 * G && g0 + tid < N) {
+                const int i = g0 + tid;
+                const bool iso = (i == 0 || sh.lam[i] - sh.lam[i - 1] > ctol) &&
+                                 (i == N - 1 || sh.lam[i + 1] - sh.lam[i] > ctol);
+                redo[i] = iso ? !twisted_vector<T>(N, sh.d, sh.e, sh.e2, sh.lam[i], pert, sh.scratch + tid, 2 * G,
+                                                   U + i, N)
+                              : 1;
+            }
+            __syncthreads();
+        }
+        // (2) clusters (and any vector the twisted pass could not form): inverse
+        //     iteration with Gram-Schmidt against the earlier cluster members
         for (int g0 = 0; g0 < N; g0 += G) {
             const int t = tid;
             if (t < G && g0 + t < N) {
                 const int i = g0 + t;
                 const bool first = (i == 0) || (sh.lam[i] - sh.lam[i - 1] > ctol);
-                if (first) {
+                if (first && redo[i]) {
                     int c1 = i;
                     while (c1 + 1 < N && sh.lam[c1 + 1] - sh.lam[c1] <= ctol) ++c1;
                     T* x = sh.scratch + t;
