@@ -249,6 +249,8 @@ struct EigShared {
     int* flags; // 4 + N: status flags, then per-eigenvalue "left to inverse iteration" marks
 };
 
+constexpr int BT_NB = 16;  // reflectors per block of the blocked back-transformation
+
 template <typename T>
 __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB) {
     size_t b = 0;
@@ -257,10 +259,161 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     b += sizeof(cx<T>) * 3 * (size_t)N;
     b += sizeof(T) * 64;
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-    size_t s2 = sizeof(cx<T>) * (size_t)(N + 4) * PB;
+    // back-transform: blocked (matrix in shared memory): panel N x PB, Y (BT_NB x PB), Gram and T;
+    // otherwise a column-major panel with stride N + 4
+    size_t s2 = a_smem ? sizeof(cx<T>) * ((size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB)
+                       : sizeof(cx<T>) * (size_t)(N + 4) * PB;
     b += std::max(s1, s2);
     b += sizeof(int) * (4 + (size_t)N);  // flags + per-eigenvalue redo marks
     return b;
+}
+
+// U <- H_0 H_1 ... H_{N-2} U with H_j = I - tau_j v_j v_j^H (v_j in row j of
+// A from column j+1, v_j[j+1] = 1), in compact-WY blocks of BT_NB reflectors:
+// H_{j0} ... H_{j1-1} = I - V T V^H with T^{-1} = diag(1/tau) + striu(V^H V)
+// (Joffrain, Low, Quintana-Orti, van de Geijn, Van Zee, "Accumulating
+// Householder transformations, revisited", 2006).  Blocks are applied
+// last-first to panels of PB columns of U held row-major in shared memory:
+//   Y = V^H P;  Y <- T Y by back-substitution with T^{-1}, per column:
+//   y_i = tau_i (y_i - sum_{l>i} G_il y_l)  (tau_i = 0 gives y_i = 0);
+//   P <- P - V Y in 4 x 4 register tiles.
+// work: P (N x PB), Y (BT_NB x PB), G (BT_NB x BT_NB).
+template <typename T>
+__device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__ A, const cx<T>* __restrict__ tau,
+                                       cx<T>* __restrict__ U, cx<T>* __restrict__ work, int PB) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    cx<T>* P = work;
+    cx<T>* Y = P + (size_t)N * PB;
+    cx<T>* G = Y + (size_t)BT_NB * PB;
+    if (N < 2) return;
+    for (int c0 = 0; c0 < N; c0 += PB) {
+        const int pw = min(PB, N - c0);
+        for (int idx = tid; idx < N * pw; idx += nthr) {
+            const int r = idx / pw, c = idx - r * pw;
+            P[(size_t)r * PB + c] = U[(size_t)r * N + c0 + c];
+        }
+        __syncthreads();
+        for (int j0 = ((N - 2) / BT_NB) * BT_NB; j0 >= 0; j0 -= BT_NB) {
+            const int nb = min(BT_NB, N - 1 - j0);
+            const int k0 = j0 + 1;        // first row touched by the block
+            const int kf = min(N, j0 + BT_NB + 1);  // from here on every v_i of the block is unmasked
+            // Gram G(l, i) = v_l^H v_i for l < i < nb (zero elsewhere)
+            for (int e = tid; e < BT_NB * BT_NB; e += nthr) {
+                const int l = e / BT_NB, i = e - l * BT_NB;
+                cx<T> acc = mk<T>(0, 0);
+                if (l < i && i < nb) {
+                    const cx<T>* vl = A + (size_t)(j0 + l) * LDA;
+                    const cx<T>* vi = A + (size_t)(j0 + i) * LDA;
+                    cx<T> q[4] = {mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0)};
+                    for (int kk = j0 + i + 1; kk < N; kk += 4) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if (kk + u < N) fma_cjx(q[u], vl[kk + u], vi[kk + u]);
+                    }
+                    acc = (q[0] + q[1]) + (q[2] + q[3]);
+                }
+                G[e] = acc;
+            }
+            // Y = V^H P: item (ig, c) computes rows ig and ig + 8
+            for (int it = tid; it < 8 * pw; it += nthr) {
+                const int ig = it / pw, c = it - ig * pw;
+                const int i0 = ig, i1 = ig + 8;
+                cx<T> y0 = mk<T>(0, 0), y1 = mk<T>(0, 0);
+                if (i0 < nb) {
+                    const cx<T>* v0 = A + (size_t)(j0 + i0) * LDA;
+                    const bool h1 = i1 < nb;
+                    const cx<T>* v1 = A + (size_t)(j0 + (h1 ? i1 : i0)) * LDA;
+                    for (int k = k0; k < kf; ++k) {  // rows where part of the block is still zero
+                        const cx<T> pk = P[(size_t)k * PB + c];
+                        if (k > j0 + i0) fma_cjx(y0, v0[k], pk);
+                        if (h1 && k > j0 + i1) fma_cjx(y1, v1[k], pk);
+                    }
+                    // eight interleaved partial sums: shorter FP32 accumulation chains
+                    // (error and latency) than one running sum over the column
+                    cx<T> p0[8], p1[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) p0[u] = p1[u] = mk<T>(0, 0);
+                    for (int kk = kf; kk < N; kk += 8) {
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int k = kk + u;
+                            if (k < N) {
+                                const cx<T> pk = P[(size_t)k * PB + c];
+                                fma_cjx(p0[u], v0[k], pk);
+                                if (h1) fma_cjx(p1[u], v1[k], pk);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int w = 4; w > 0; w >>= 1)
+#pragma unroll
+                        for (int u = 0; u < w; ++u) {
+                            p0[u] = p0[u] + p0[u + w];
+                            p1[u] = p1[u] + p1[u + w];
+                        }
+                    y0 = y0 + p0[0];
+                    y1 = y1 + p1[0];
+                }
+                Y[i0 * PB + c] = y0;
+                Y[i1 * PB + c] = y1;
+            }
+            __syncthreads();
+            // Y <- T Y: back-substitution with T^{-1} = diag(1/tau) + striu(G), per column
+            for (int c = tid; c < pw; c += nthr) {
+                cx<T> y[BT_NB];
+#pragma unroll
+                for (int i = 0; i < BT_NB; ++i) y[i] = Y[i * PB + c];
+#pragma unroll
+                for (int i = BT_NB - 1; i >= 0; --i) {
+                    cx<T> s = y[i];
+#pragma unroll
+                    for (int l = i + 1; l < BT_NB; ++l) s = s - G[i * BT_NB + l] * y[l];
+                    y[i] = (i < nb) ? tau[j0 + i] * s : mk<T>(0, 0);
+                }
+#pragma unroll
+                for (int i = 0; i < BT_NB; ++i) Y[i * PB + c] = y[i];
+            }
+            __syncthreads();
+            // P <- P - V Y: item (rg, cg) updates rows k0 + 4 rg .. +3, columns cg + 16 q
+            const int nrg = (N - k0 + 3) / 4;
+            for (int it = tid; it < nrg * 16; it += nthr) {
+                const int rg = it >> 4, cg = it & 15;
+                const int kb = k0 + 4 * rg;
+                cx<T> acc[4][4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[a][q] = mk<T>(0, 0);
+                for (int l = 0; l < nb; ++l) {
+                    const cx<T>* vl = A + (size_t)(j0 + l) * LDA;
+                    cx<T> v[4], y[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) v[a] = (kb + a < N && kb + a > j0 + l) ? vl[kb + a] : mk<T>(0, 0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) y[q] = Y[l * PB + min(cg + 16 * q, PB - 1)];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) fma_cx(acc[a][q], v[a], y[q]);
+                }
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    if (kb + a >= N) continue;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int c = cg + 16 * q;
+                        if (c < pw) P[(size_t)(kb + a) * PB + c] = P[(size_t)(kb + a) * PB + c] - acc[a][q];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        for (int idx = tid; idx < N * pw; idx += nthr) {
+            const int r = idx / pw, c = idx - r * pw;
+            U[(size_t)r * N + c0 + c] = P[(size_t)r * PB + c];
+        }
+        __syncthreads();
+    }
 }
 
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
@@ -295,8 +448,10 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         sh.red = reinterpret_cast<T*>(p);
         p += sizeof(T) * 64;
         sh.scratch = reinterpret_cast<T*>(p);
-        size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-        size_t s2 = sizeof(cx<T>) * (size_t)(N + 4) * PB;
+        // same layout as eig_smem_bytes
+        const size_t s1 = sizeof(T) * 4 * (size_t)N * G;
+        const size_t s2 = A_SMEM ? sizeof(cx<T>) * ((size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB)
+                                 : sizeof(cx<T>) * (size_t)(N + 4) * PB;
         p += std::max(s1, s2);
         sh.flags = reinterpret_cast<int*>(p);
     }
@@ -583,6 +738,12 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         __syncthreads();
 
         // ----------------------------------------------- back-transform --
+        if constexpr (A_SMEM) {
+            back_transform_blocked<T>(N, LDA, A, sh.tau, U, reinterpret_cast<cx<T>*>(sh.scratch), PB);
+            if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
+            __syncthreads();
+            continue;
+        }
         // Panel P holds PB columns of U, column-major with stride N + 4.  Column
         // c belongs to the 8 threads 8c .. 8c+7 (rows interleaved), which apply
         // every reflector to it without block barriers.
@@ -637,7 +798,13 @@ inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB
     const size_t fixed = eig_smem_bytes<T>(N, a_smem, 0, 0);
     const size_t left = budget > fixed ? budget - fixed : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
-    PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 1))));
+    if (a_smem) {
+        const size_t fix2 = sizeof(cx<T>) * 2 * BT_NB * BT_NB;
+        const size_t l2 = left > fix2 ? left - fix2 : 0;
+        PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, l2 / (sizeof(cx<T>) * (size_t)(N + BT_NB))));
+    } else {
+        PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 4))));
+    }
 }
 
 // The dynamic shared-memory limit is a per-function attribute shared by every
