@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <vector>
 
 #include "tbgpu_internal.cuh"
 
@@ -242,7 +243,8 @@ struct EigShared {
     T* e2;      // N
     T* lam;     // N
     cx<T>* tau; // N
-    cx<T>* v;   // N
+    cx<T>* v;   // N  (reflector of even steps)
+    cx<T>* v2;  // N  (reflector of odd steps)
     cx<T>* w;   // N
     T* red;     // 64
     T* scratch; // inverse iteration: 4*N*G ; back-transform panel: N*PB complex
@@ -256,7 +258,7 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     size_t b = 0;
     if (a_smem) b += sizeof(cx<T>) * (size_t)N * (N + 4);  // rows padded to N + 4 (bank spread)
     b += sizeof(T) * 4 * (size_t)N;
-    b += sizeof(cx<T>) * 3 * (size_t)N;
+    b += sizeof(cx<T>) * 4 * (size_t)N;  // tau, v, v2, w
     b += sizeof(T) * 64;
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
     // back-transform: blocked (matrix in shared memory): panel N x PB, Y (BT_NB x PB), Gram and T;
@@ -435,6 +437,8 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         p += sizeof(cx<T>) * N;
         sh.v = reinterpret_cast<cx<T>*>(p);
         p += sizeof(cx<T>) * N;
+        sh.v2 = reinterpret_cast<cx<T>*>(p);
+        p += sizeof(cx<T>) * N;
         sh.w = reinterpret_cast<cx<T>*>(p);
         p += sizeof(cx<T>) * N;
         sh.d = reinterpret_cast<T*>(p);
@@ -488,52 +492,61 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         __syncthreads();
 
         // ------------------------------------------------- tridiagonalise --
+        // Only the upper triangle is kept (row i from column i on): A22 v reads
+        // row i right of the diagonal and column i above it.  Warp 0 updates
+        // row j+1 first and forms the reflector of step j+1 from it while the
+        // other warps update the rest of the trailing matrix; reflectors of
+        // consecutive steps alternate between two buffers.
+        // reflector by warp 0 from row jr: H^H [alpha; x] = [beta; 0]
+        auto make_reflector = [&](int jr, cx<T>* vout) {
+            const int mr = N - 1 - jr;
+            cx<T>* rowj = A + (size_t)jr * LDA + (jr + 1);  // row jr, columns jr+1.. = conj(column jr)
+            T part = 0;
+            for (int i = 1 + lane; i < mr; i += 32) part += abs2(rowj[i]);
+            const T xnorm2 = warp_sum(part);
+            const cx<T> alpha = conj(rowj[0]);
+            cx<T> tau, scal;
+            T beta;
+            if (xnorm2 == T(0) && alpha.im == T(0)) {
+                tau = mk<T>(0, 0);
+                scal = mk<T>(0, 0);
+                beta = alpha.re;
+            } else {
+                const T nrm = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xnorm2);
+                beta = (alpha.re >= T(0)) ? -nrm : nrm;
+                tau = mk<T>((beta - alpha.re) / beta, -alpha.im / beta);
+                const cx<T> den = mk<T>(alpha.re - beta, alpha.im);
+                const T dd = den.re * den.re + den.im * den.im;
+                scal = mk<T>(den.re / dd, -den.im / dd);
+            }
+            for (int i = lane; i < mr; i += 32) {
+                const cx<T> vi = (i == 0) ? mk<T>(1, 0) : conj(rowj[i]) * scal;
+                vout[i] = vi;
+                rowj[i] = vi;  // keep v_jr in row jr for the back-transformation
+            }
+            if (lane == 0) {
+                sh.tau[jr] = tau;
+                sh.e[jr] = beta;
+                sh.d[jr] = A[(size_t)jr * LDA + jr].re;
+            }
+        };
+        if (N > 1 && warp == 0) make_reflector(0, sh.v);
+        __syncthreads();
         for (int j = 0; j < N - 1; ++j) {
             const int m = N - 1 - j;
-            cx<T>* rowj = A + (size_t)j * LDA + (j + 1);  // row j, columns j+1.. = conj(column j)
-            // reflector by warp 0: H_j^H [alpha; x] = [beta; 0]
-            if (warp == 0) {
-                T part = 0;
-                for (int i = 1 + lane; i < m; i += 32) part += abs2(rowj[i]);
-                const T xnorm2 = warp_sum(part);
-                const cx<T> alpha = conj(rowj[0]);
-                cx<T> tau, scal;
-                T beta;
-                if (xnorm2 == T(0) && alpha.im == T(0)) {
-                    tau = mk<T>(0, 0);
-                    scal = mk<T>(0, 0);
-                    beta = alpha.re;
-                } else {
-                    const T nrm = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xnorm2);
-                    beta = (alpha.re >= T(0)) ? -nrm : nrm;
-                    tau = mk<T>((beta - alpha.re) / beta, -alpha.im / beta);
-                    const cx<T> den = mk<T>(alpha.re - beta, alpha.im);
-                    const T dd = den.re * den.re + den.im * den.im;
-                    scal = mk<T>(den.re / dd, -den.im / dd);
-                }
-                for (int i = lane; i < m; i += 32) {
-                    const cx<T> vi = (i == 0) ? mk<T>(1, 0) : conj(rowj[i]) * scal;
-                    sh.v[i] = vi;
-                    rowj[i] = vi;  // keep v_j in row j for the back-transformation
-                }
-                if (lane == 0) {
-                    sh.tau[j] = tau;
-                    sh.e[j] = beta;
-                    sh.d[j] = A[(size_t)j * LDA + j].re;
-                }
-            }
-            __syncthreads();
+            const cx<T>* v = (j & 1) ? sh.v2 : sh.v;
             const cx<T> tau = sh.tau[j];
-            if (tau.re == T(0) && tau.im == T(0)) continue;
+            const size_t o22 = (size_t)(j + 1) * LDA + (j + 1);  // A22(0, 0)
             // w = tau * A22 v: four threads per row, two-level butterfly; partial of w^H v
             cx<T> dpart = mk<T>(0, 0);
             {
                 const int q = tid & 3;
                 const unsigned gm = 0xFu << (lane & 28);
                 for (int i = tid >> 2; i < m; i += nthr >> 2) {
-                    const cx<T>* row = A + (size_t)(j + 1 + i) * LDA + (j + 1);
+                    const cx<T>* row = A + o22 + (size_t)i * LDA;  // row[l] = A22(i, l), l >= i
                     cx<T> acc = mk<T>(0, 0);
-                    for (int l = q; l < m; l += 4) fma_cx(acc, row[l], sh.v[l]);
+                    for (int l = i + q; l < m; l += 4) fma_cx(acc, row[l], v[l]);
+                    for (int l = q; l < i; l += 4) fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);  // conj(A22(l, i))
                     acc.re += __shfl_xor_sync(gm, acc.re, 1);
                     acc.im += __shfl_xor_sync(gm, acc.im, 1);
                     acc.re += __shfl_xor_sync(gm, acc.re, 2);
@@ -541,7 +554,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                     if (q == 0) {
                         const cx<T> wi = tau * acc;
                         sh.w[i] = wi;
-                        fma_cjx(dpart, wi, sh.v[i]);
+                        fma_cjx(dpart, wi, v[i]);
                     }
                 }
                 dpart.re = warp_sum(dpart.re);
@@ -557,17 +570,27 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                 dp.re += sh.red[w2];
                 dp.im += sh.red[32 + w2];
             }
-            // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H
+            // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H (upper triangle)
             const cx<T> alpha2 = T(-0.5) * (tau * dp);
-            for (int i = warp; i < m; i += nwarps) {
-                cx<T>* row = A + (size_t)(j + 1 + i) * LDA + (j + 1);
-                const cx<T> vi = sh.v[i];
+            auto update_row = [&](int i) {
+                cx<T>* row = A + o22 + (size_t)i * LDA;
+                const cx<T> vi = v[i];
                 const cx<T> wi = sh.w[i] + alpha2 * vi;
-                for (int l = lane; l < m; l += 32) {
-                    const cx<T> vl = sh.v[l];
+                for (int l = i + lane; l < m; l += 32) {
+                    const cx<T> vl = v[l];
                     const cx<T> wl = sh.w[l] + alpha2 * vl;
                     row[l] = row[l] - mulc(vi, wl) - mulc(wi, vl);
                 }
+            };
+            if (warp == 0) {
+                update_row(0);
+                if (nwarps == 1)
+                    for (int i = 1; i < m; ++i) update_row(i);
+                __syncwarp();
+                if (m >= 2) make_reflector(j + 1, (j & 1) ? sh.v : sh.v2);
+            } else {
+                for (int i = warp; i < m; i += nwarps - 1) update_row(i);  // rows 1 .. m-1 over warps 1 ..
+
             }
             __syncthreads();
         }
@@ -915,3 +938,40 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 }
 
 }  // namespace tbg
+
+// Internal test hook (not part of the public header): FP32 eigenpairs of nk
+// host complex-double matrices (n x n) -> E (nk, n) and U (nk, n, n) complex
+// double (eigenvectors in columns), for checks of the solver's own accuracy.
+extern "C" int tbg_internal_eig_f32(int n, int64_t nk, const double* H, double* E, double* U) {
+    using namespace tbg;
+    const size_t NN = (size_t)n * n;
+    void *dH = nullptr, *dE = nullptr, *dU = nullptr, *dW = nullptr, *dS = nullptr;
+    const size_t wb = eig_workspace_bytes(n, nk, 1);
+    int rc = TBG_OK;
+    if (cudaMalloc(&dH, 16 * NN * nk) || cudaMalloc(&dE, 8 * n * nk) || cudaMalloc(&dU, 8 * NN * nk) ||
+        cudaMalloc(&dS, sizeof(int)) || (wb && cudaMalloc(&dW, wb)))
+        rc = set_error(TBG_E_OOM, "eig test alloc");
+    if (!rc) {
+        cudaMemcpy(dH, H, 16 * NN * nk, cudaMemcpyHostToDevice);
+        cudaMemset(dS, 0, sizeof(int));
+        rc = eig_batched_f32(0, n, nk, static_cast<zc*>(dH), static_cast<double*>(dE), static_cast<cc*>(dU), dW, wb,
+                             static_cast<int*>(dS));
+        cudaError_t e = cudaDeviceSynchronize();
+        if (!rc && e != cudaSuccess) rc = cuda_error(e, "eig test");
+    }
+    if (!rc) {
+        std::vector<cc> u(NN * nk);
+        cudaMemcpy(E, dE, 8 * n * nk, cudaMemcpyDeviceToHost);
+        cudaMemcpy(u.data(), dU, 8 * NN * nk, cudaMemcpyDeviceToHost);
+        for (size_t i = 0; i < u.size(); ++i) {
+            U[2 * i] = u[i].re;
+            U[2 * i + 1] = u[i].im;
+        }
+    }
+    cudaFree(dH);
+    cudaFree(dE);
+    cudaFree(dU);
+    cudaFree(dS);
+    cudaFree(dW);
+    return rc;
+}
