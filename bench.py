@@ -148,13 +148,25 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
     return 24.0 * nR * N * N + 46.0 * N ** 3
 
 
-def kernel_roofline(timing: dict, peaks: dict) -> dict | None:
+# DRAM bytes per unit of work of a kernel family, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the bench's 128-band model:
+# heev_kernel<float,smem>: 169.3 MB for one launch over 512 matrices
+# (profiles/heev_f32_random3d_b512.md).  The traffic of a bench launch is this
+# figure times the matrices that launch processes.
+DRAM_BYTES_PER_MATRIX = {"heev_kernel<float,smem>": 169.3e6 / 512}
+
+
+def kernel_roofline(timing: dict, peaks: dict, units: int = 0) -> dict | None:
     """Roofline entry for the kernel family with the largest device time:
     achieved = its algorithmic flops / its device time (CUDA events around
-    every launch, on the launching stream)."""
+    every launch, on the launching stream).  units = matrices (k-points) the
+    timed launches of the family processed, for the per-launch traffic."""
     if not timing:
         return None
     name, (launches, ms, work) = max(timing.items(), key=lambda kv: kv[1][1])
+    traffic = None
+    if name in DRAM_BYTES_PER_MATRIX and units and launches:
+        traffic = DRAM_BYTES_PER_MATRIX[name] * units / launches
     if name.startswith("heev_kernel<float") or name.startswith("fp32"):
         bound, peak, src = "fp32", peaks["fp32_tflops"], "FP32 FMA loop on this GPU (tbg_measure_fma_peaks)"
     elif name.startswith("ozaki"):
@@ -167,7 +179,8 @@ def kernel_roofline(timing: dict, peaks: dict) -> dict | None:
         bound, peak, src = "fp64", peaks["fp64_tflops"], "FP64 FMA loop on this GPU (tbg_measure_fma_peaks)"
     achieved = work / (ms / 1e3) / 1e12 if ms > 0 and work > 0 else None
     return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
+            "traffic_unit": "bytes per launch (DRAM read + write, ncu per-matrix figure x matrices per launch)",
             "kernel": name, "launches": launches, "avg_launch_ms": ms / max(launches, 1),
             "peak_source": src}
 
@@ -337,7 +350,7 @@ def main():
         fp64_val = fs / t_fp64
         acc = {"ahc_partial_rel_err_mixed_vs_fp64": float(abs(mixed_sum[0] - plain_sum[0]) / abs(plain_sum[0])),
                "sample": f"flat k indices [0, {fs}) of the 64^3 mesh"}
-        roof_line = kernel_roofline(timing, peaks)
+        roof_line = kernel_roofline(timing, peaks, units=done)
         cpu = None
         if not args.no_cpu_baseline:
             from oracle import build_port
