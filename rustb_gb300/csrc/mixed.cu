@@ -36,12 +36,14 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
                 int64_t sC, int* EA, int* EB);
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
-                       int* err);
+                       int* err, bool exps_ready = false);
 bool ozaki_use_tc();
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
+int ozaki_line_exps(cudaStream_t st, int fmt, bool cols, int64_t batch, int lines, int K, const void* X, int64_t ld,
+                    int64_t sX, int* E);
 
 namespace {
 
@@ -330,9 +332,9 @@ inline unsigned nblk(int64_t total) {
 
 size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     const size_t NN = (size_t)N * N;
-    // X and F (cc) + 5 pair buffers + exponents + FP32 solver workspace
-    return (size_t)batch * NN * (2 * sizeof(cc) + 5 * sizeof(float4)) + ozaki_exp_bytes(batch, N, N) +
-           eig_workspace_bytes(N, batch, 1) + 4096;
+    // X and F (cc) + 5 pair buffers + line exponents (10 operand sides) + FP32 solver workspace
+    return (size_t)batch * NN * (2 * sizeof(cc) + 5 * sizeof(float4)) + sizeof(int) * 10 * (size_t)batch * N +
+           ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) + 4096;
 }
 
 // H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega.
@@ -357,21 +359,33 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     float4* bE = static_cast<float4*>(take(sizeof(float4) * batch * NN));
     int* EA = static_cast<int*>(take(ozaki_exp_bytes(batch, N, N)));
     int* EB = EA + batch * N;
+    // tcgen05 form: the exponents of each operand side are scanned once and
+    // shared by the products that use it
+    int* ex = static_cast<int*>(take(sizeof(int) * 10 * (size_t)batch * N));
+    auto slot = [&](int i) { return ex + (size_t)i * batch * N; };
+    enum { XC, HR, HXC, XR, FC, XPC, VXR, VYR, BXC, BYC };
+    const bool tc = ozaki_use_tc();
+    auto exps = [&](int fmt, bool cols, const void* M, int s) -> int {
+        return tc ? ozaki_line_exps(st, fmt, cols, batch, N, N, M, N, NN, slot(s)) : TBG_OK;
+    };
     const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
     void* eigw = take(eigw_bytes);
     // FP64-class products: tcgen05 form unless the mma.sync form is selected
-    auto hp = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C) -> int {
-        if (ozaki_use_tc())
-            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB, status_d);
+    auto hp = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb) -> int {
+        if (tc)
+            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, slot(sa),
+                                  slot(sb), status_d, true);
         return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB);
     };
     int rc;
     // 1. FP32 eigenpairs of H
     if ((rc = eig_batched_f32(st, N, batch, nullptr, E, X, eigw, eigw_bytes, status_d, H))) return rc;
     // 2. X^H X and S = X^H (H X)   (FP64-class, tensor cores)
-    if ((rc = hp(true, F32, F32, X, X, bA))) return rc;
-    if ((rc = hp(false, PAIR, F32, H, X, bB))) return rc;
-    if ((rc = hp(true, F32, PAIR, X, bB, bC))) return rc;
+    if ((rc = exps(F32, true, X, XC)) || (rc = exps(PAIR, false, H, HR))) return rc;
+    if ((rc = hp(true, F32, F32, X, X, bA, XC, XC))) return rc;
+    if ((rc = hp(false, PAIR, F32, H, X, bB, HR, XC))) return rc;
+    if ((rc = exps(PAIR, true, bB, HXC))) return rc;
+    if ((rc = hp(true, F32, PAIR, X, bB, bC, XC, HXC))) return rc;
     // 3. Ogita-Aishima update F and refined eigenvalues
     {
         KTimer kt(st, "oa_kernel");
@@ -381,8 +395,9 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         TBG_LAUNCHED("oa_kernel");
     }
     // 4. X' = X + X F  (float pair: hi = X, lo = X F)
-    rc = ozaki_use_tc() ? ozaki_zgemm_tc_low(st, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB, status_d)
-                        : ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB);
+    if ((rc = exps(F32, false, X, XR)) || (rc = exps(F32, true, F, FC))) return rc;
+    rc = tc ? ozaki_zgemm_tc_low(st, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, slot(XR), slot(FC), status_d, true)
+            : ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB);
     if (rc) return rc;
     {
         KTimer kt(st, "xprime_kernel");
@@ -390,10 +405,13 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         TBG_LAUNCHED("xprime_kernel");
     }
     // 5. band-basis velocities B = X'^H V X'
-    if ((rc = hp(false, PAIR, PAIR, Vx, bA, bB))) return rc;
-    if ((rc = hp(false, PAIR, PAIR, Vy, bA, bC))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, bB, bD))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, bC, bE))) return rc;
+    if ((rc = exps(PAIR, true, bA, XPC)) || (rc = exps(PAIR, false, Vx, VXR)) || (rc = exps(PAIR, false, Vy, VYR)))
+        return rc;
+    if ((rc = hp(false, PAIR, PAIR, Vx, bA, bB, VXR, XPC))) return rc;
+    if ((rc = hp(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC))) return rc;
+    if ((rc = exps(PAIR, true, bB, BXC)) || (rc = exps(PAIR, true, bC, BYC))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bB, bD, XPC, BXC))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bC, bE, XPC, BYC))) return rc;
     // 6. Omega
     {
         KTimer kt(st, "berry_kernel");

@@ -135,36 +135,65 @@ __device__ __forceinline__ float mag_of(const void* base, int64_t idx) {
     return 0.f;
 }
 
-// Exponents: EA[b][i] for rows of op(A) (conj: columns of A), EB[b][j] for
-// columns of B.  One warp per (b, line).
-template <int FMTA, int FMTB, bool CONJ_A>
-__global__ void oz_exp_kernel(int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
-                              const void* B, int64_t ldb, int64_t sB, int* EA, int* EB) {
+// Row exponents of a row-major operand (one warp per row, lanes along the row)
+// and column exponents (one thread per column, rows walked in order, so a
+// warp reads 32 consecutive elements of a row at a time).
+template <int FMT>
+__global__ void row_exps_kernel(int64_t batch, int M, int K, const void* A, int64_t lda, int64_t sA, int* E) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t per = (int64_t)M + Nc;
-    for (int64_t w = gw; w < batch * per; w += nw) {
-        const int64_t b = w / per;
-        const int line = (int)(w % per);
+    for (int64_t w = gw; w < batch * M; w += nw) {
+        const int64_t b = w / M;
+        const int r = (int)(w % M);
         float m = 0.f;
-        if (line < M) {
-            for (int k = lane; k < K; k += 32) {
-                const int64_t idx = CONJ_A ? (b * sA + (int64_t)k * lda + line) : (b * sA + (int64_t)line * lda + k);
-                m = fmaxf(m, mag_of<FMTA>(A, idx));
-            }
-        } else {
-            const int j = line - M;
-            for (int k = lane; k < K; k += 32) m = fmaxf(m, mag_of<FMTB>(B, b * sB + (int64_t)k * ldb + j));
-        }
+        for (int k = lane; k < K; k += 32) m = fmaxf(m, mag_of<FMT>(A, b * sA + (int64_t)r * lda + k));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) {
-            if (line < M)
-                EA[b * M + line] = exp_of_max(m);
-            else
-                EB[b * Nc + (line - M)] = exp_of_max(m);
+        if (lane == 0) E[w] = exp_of_max(m);
+    }
+}
+template <int FMT>
+__global__ void col_exps_kernel(int64_t batch, int Ncols, int K, const void* B, int64_t ldb, int64_t sB, int* E) {
+    const int64_t nchunk = (Ncols + blockDim.x - 1) / blockDim.x;
+    for (int64_t w = blockIdx.x; w < batch * nchunk; w += gridDim.x) {
+        const int64_t b = w / nchunk;
+        const int j = (int)(w % nchunk) * blockDim.x + threadIdx.x;
+        if (j >= Ncols) continue;
+        float m0 = 0.f, m1 = 0.f;
+        int k = 0;
+        for (; k + 1 < K; k += 2) {
+            m0 = fmaxf(m0, mag_of<FMT>(B, b * sB + (int64_t)k * ldb + j));
+            m1 = fmaxf(m1, mag_of<FMT>(B, b * sB + (int64_t)(k + 1) * ldb + j));
         }
+        if (k < K) m0 = fmaxf(m0, mag_of<FMT>(B, b * sB + (int64_t)k * ldb + j));
+        E[b * Ncols + j] = exp_of_max(fmaxf(m0, m1));
+    }
+}
+
+template <int FMT>
+int line_exps(cudaStream_t st, bool cols, int64_t batch, int lines, int K, const void* X, int64_t ld, int64_t sX,
+              int* E) {
+    if (cols) {
+        const int64_t work = batch * ((lines + 127) / 128);
+        col_exps_kernel<FMT><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(work, 152 * 16)), 128, 0, st>>>(
+            batch, lines, K, X, ld, sX, E);
+    } else {
+        const int64_t warps = batch * lines;
+        row_exps_kernel<FMT><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((warps * 32 + 255) / 256, 152 * 64)),
+                                256, 0, st>>>(batch, lines, K, X, ld, sX, E);
+    }
+    TBG_LAUNCHED("oz_exp_kernel");
+    return TBG_OK;
+}
+
+int exps_of(cudaStream_t st, int fmt, bool cols, int64_t batch, int lines, int K, const void* X, int64_t ld,
+            int64_t sX, int* E) {
+    switch (fmt) {
+        case FMT_F64: return line_exps<FMT_F64>(st, cols, batch, lines, K, X, ld, sX, E);
+        case FMT_F32: return line_exps<FMT_F32>(st, cols, batch, lines, K, X, ld, sX, E);
+        case FMT_PAIR: return line_exps<FMT_PAIR>(st, cols, batch, lines, K, X, ld, sX, E);
+        default: return set_error(TBG_E_UNSUPPORTED, "exponents: operand format");
     }
 }
 
@@ -353,12 +382,8 @@ __global__ void __launch_bounds__(256, 1) oz_gemm_kernel(int M, int Nc, int K, c
 template <int SA, int SB, int LMAX, bool CONJ_A, int FMTA, int FMTB>
 int launch_oz(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
               const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB) {
-    {
-        const int64_t lines = batch * (M + Nc);
-        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((lines * 32 + 255) / 256, 152 * 64));
-        oz_exp_kernel<FMTA, FMTB, CONJ_A><<<blocks, 256, 0, st>>>(batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
-        TBG_LAUNCHED("oz_exp_kernel");
-    }
+    if (int rc = exps_of(st, FMTA, CONJ_A, batch, M, K, A, lda, sA, EA)) return rc;
+    if (int rc = exps_of(st, FMTB, true, batch, Nc, K, B, ldb, sB, EB)) return rc;
     const size_t smem = sizeof(__nv_bfloat16) * OZ_PAD * (SA * OZ_TM + SB * 2 * OZ_TN);
     auto kern = oz_gemm_kernel<SA, SB, LMAX, CONJ_A, FMTA, FMTB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -387,38 +412,32 @@ int launch_oz(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* 
 
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc) { return sizeof(int) * (size_t)batch * (M + Nc) + 256; }
 
+// Exponents of the rows (cols = false: rows of a row-major X with leading
+// dimension ld) or columns (cols = true) of `batch` operands of `lines` lines
+// and K elements each, in the given format.
+int ozaki_line_exps(cudaStream_t st, int fmt, bool cols, int64_t batch, int lines, int K, const void* X, int64_t ld,
+                    int64_t sX, int* E) {
+    return exps_of(st, fmt, cols, batch, lines, K, X, ld, sX, E);
+}
+
 // Row / column exponents for any operand format combination (shared by the
 // mma.sync and tcgen05 forms).
 int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                      const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, int* EA, int* EB) {
-    const int64_t lines = batch * (M + Nc);
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((lines * 32 + 255) / 256, 152 * 64));
-#define EXP_CASE(CJ, FA, FB)                                                                              \
-    if (conj_a == CJ && fmt_a == FA && fmt_b == FB) {                                                     \
-        oz_exp_kernel<FA, FB, CJ><<<blocks, 256, 0, st>>>(batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB); \
-        TBG_LAUNCHED("oz_exp_kernel");                                                                    \
-        return TBG_OK;                                                                                    \
-    }
-    EXP_CASE(false, FMT_F64, FMT_F64)
-    EXP_CASE(true, FMT_F64, FMT_F64)
-    EXP_CASE(true, FMT_F32, FMT_F32)
-    EXP_CASE(false, FMT_PAIR, FMT_F32)
-    EXP_CASE(true, FMT_F32, FMT_PAIR)
-    EXP_CASE(false, FMT_PAIR, FMT_PAIR)
-    EXP_CASE(true, FMT_PAIR, FMT_PAIR)
-    EXP_CASE(false, FMT_F32, FMT_F32)
-#undef EXP_CASE
-    return set_error(TBG_E_UNSUPPORTED, "ozaki_exp_launch: format combination");
+    // rows of op(A): rows of A, or (conj) columns of A; columns of B
+    int rc = exps_of(st, fmt_a, conj_a, batch, M, K, A, lda, sA, EA);
+    if (rc) return rc;
+    return exps_of(st, fmt_b, true, batch, Nc, K, B, ldb, sB, EB);
 }
 
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err);
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false);
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
                      const void* Bs, float4* C, int* err);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
-                       int* err);
+                       int* err, bool exps_ready = false);
 
 // tcgen05 kernels are used unless TBG_OZAKI_MMA_SYNC=1 (the mma.sync form).
 bool ozaki_use_tc() {

@@ -620,12 +620,16 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
     return TBG_OK;
 }
 
+// With exps_ready the caller has filled EA (rows of op(A)) and EB (columns of
+// B) already, e.g. once for an operand shared by several products.
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err) {
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready) {
     if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: K > 256");
-    int rc = ozaki_exp_launch(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
-    if (rc) return rc;
+    if (!exps_ready) {
+        int rc = ozaki_exp_launch(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
+        if (rc) return rc;
+    }
     const double work = 8.0 * (double)M * Nc * K * batch;
 #define TC_CASE(CJ, FA, FB)                                                                                          \
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
@@ -646,10 +650,12 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
 // C = A B for FP32 A and B, e.g. the correction X F of the refinement.
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
-                       int* err) {
+                       int* err, bool exps_ready) {
     if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc_low: K > 256");
-    int rc = ozaki_exp_launch(st, false, FMT_F32, FMT_F32, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
-    if (rc) return rc;
+    if (!exps_ready) {
+        int rc = ozaki_exp_launch(st, false, FMT_F32, FMT_F32, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
+        if (rc) return rc;
+    }
     return launch_tc<false, FMT_F32, FMT_F32, 3>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,
                                                  "ozaki_tc_kernel<low>", 8.0 * (double)M * Nc * K * batch);
 }
