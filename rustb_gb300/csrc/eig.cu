@@ -7,8 +7,8 @@
 //      (unblocked, full storage).  The reflector H_j = I - tau_j v_j v_j^H is
 //      chosen so that H_j^H [alpha; x] = [beta; 0] with real beta of sign
 //      opposite to Re(alpha) (no cancellation).  v_j is kept in row j of A.
-//   2. Eigenvalues of T by Sturm-count bisection, one thread per eigenvalue
-//      (ascending by construction, absolute accuracy ~ eps * ||T||).
+//   2. Eigenvalues of T by Sturm-count multisection, a few threads per
+//      eigenvalue (ascending by construction, absolute accuracy ~ eps ||T||).
 //   3. Eigenvectors of T: for eigenvalues farther than 1e-3 ||T|| from their
 //      neighbours, the twisted factorisation of T - lambda I (Fernando 1997;
 //      one top-down and one bottom-up pivot sweep, no pivoting branches, no
@@ -655,26 +655,48 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             }
         }
         const T atol = T(2) * Lim<T>::eps() * tnorm + T(2) * pivmin;
-        for (int i = tid; i < N; i += nthr) {
-            T a = lo_g, c = hi_g;
-            for (int it = 0; it < 200; ++it) {
-                const T mid = T(0.5) * (a + c);
-                if (c - a <= atol + T(2) * Lim<T>::eps() * max(fabs(a), fabs(c))) break;
-                if (sturm_count<T>(N, sh.d, sh.e2, mid, pivmin) <= i)
-                    a = mid;
-                else
-                    c = mid;
-            }
-            T lam = T(0.5) * (a + c);
-            // an isolated diagonal entry inside the final bracket is the exact eigenvalue
-            for (int j = 0; j < N; ++j) {
-                const bool iso = (j == 0 || sh.e[j - 1] == T(0)) && (j == N - 1 || sh.e[j] == T(0));
-                if (iso && sh.d[j] >= a && sh.d[j] <= c) {
-                    lam = sh.d[j];
-                    break;
+        // Multisection: S threads (a power of two, S N <= threads) share one
+        // eigenvalue; each round they evaluate the Sturm count at the S inner
+        // points of S + 1 equal subintervals and keep the one holding it.
+        {
+            int S = 1;
+            while (S < 8 && 2 * S * N <= nthr) S *= 2;
+            const int passes = (N * S + nthr - 1) / nthr;  // uniform over the CTA
+            for (int ps = 0; ps < passes; ++ps) {
+                const int idx = ps * nthr + tid;
+                const int i = idx / S, q = idx - (idx / S) * S;
+                const int gbase = (lane / S) * S;
+                const unsigned gmask = (S == 32) ? 0xffffffffu : ((1u << S) - 1u);
+                T a = lo_g, c = hi_g;
+                bool done = i >= N;
+                for (int it = 0; it < 200; ++it) {
+                    done = done || (c - a <= atol + T(2) * Lim<T>::eps() * max(fabs(a), fabs(c)));
+                    if (__all_sync(0xffffffffu, done)) break;
+                    const T h = (c - a) / T(S + 1);
+                    const T x = a + T(q + 1) * h;
+                    const bool above = !done && sturm_count<T>(N, sh.d, sh.e2, x, pivmin) > i;
+                    const unsigned g = (__ballot_sync(0xffffffffu, above) >> gbase) & gmask;
+                    if (!done) {
+                        const int qs = g ? __ffs(g) - 1 : S;  // first inner point above the eigenvalue
+                        const T na = (qs == 0) ? a : a + T(qs) * h;
+                        const T nc = (qs == S) ? c : a + T(qs + 1) * h;
+                        a = na;
+                        c = nc;
+                    }
+                }
+                if (i < N && q == 0) {
+                    T lam = T(0.5) * (a + c);
+                    // an isolated diagonal entry inside the final bracket is the exact eigenvalue
+                    for (int j = 0; j < N; ++j) {
+                        const bool iso = (j == 0 || sh.e[j - 1] == T(0)) && (j == N - 1 || sh.e[j] == T(0));
+                        if (iso && sh.d[j] >= a && sh.d[j] <= c) {
+                            lam = sh.d[j];
+                            break;
+                        }
+                    }
+                    sh.lam[i] = lam;
                 }
             }
-            sh.lam[i] = lam;
         }
         __syncthreads();
         if (Eout) {
