@@ -544,9 +544,21 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                 const unsigned gm = 0xFu << (lane & 28);
                 for (int i = tid >> 2; i < m; i += nthr >> 2) {
                     const cx<T>* row = A + o22 + (size_t)i * LDA;  // row[l] = A22(i, l), l >= i
-                    cx<T> acc = mk<T>(0, 0);
-                    for (int l = i + q; l < m; l += 4) fma_cx(acc, row[l], v[l]);
-                    for (int l = q; l < i; l += 4) fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);  // conj(A22(l, i))
+                    // two partial sums per part: independent load/FMA chains
+                    cx<T> acc = mk<T>(0, 0), acc2 = mk<T>(0, 0);
+                    int l = i + q;
+                    for (; l + 4 < m; l += 8) {
+                        fma_cx(acc, row[l], v[l]);
+                        fma_cx(acc2, row[l + 4], v[l + 4]);
+                    }
+                    if (l < m) fma_cx(acc, row[l], v[l]);
+                    l = q;
+                    for (; l + 4 < i; l += 8) {  // conj(A22(l, i)) from the column above the diagonal
+                        fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);
+                        fma_cjx(acc2, A[o22 + (size_t)(l + 4) * LDA + i], v[l + 4]);
+                    }
+                    if (l < i) fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);
+                    acc = acc + acc2;
                     acc.re += __shfl_xor_sync(gm, acc.re, 1);
                     acc.im += __shfl_xor_sync(gm, acc.im, 1);
                     acc.re += __shfl_xor_sync(gm, acc.re, 2);
