@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "tbgpu_internal.cuh"
 
@@ -314,20 +315,36 @@ __global__ void phases3_kernel(int64_t nk, int dim, const double* __restrict__ k
 
 // Atom gauge and tau term from the lattice-gauge float-pair sums:
 //   H = conj(phi_m) H_l phi_n,  V_p = (V_l,p + i (tau_p,n - tau_p,m) H_l) conj(phi_m) phi_n
-__global__ void gauge_pairs_kernel(int64_t nk, int N, const float4* __restrict__ C, const zc* __restrict__ orbph,
-                                   const double* __restrict__ taup, zc* __restrict__ H, zc* __restrict__ V) {
+// Contraction output C, component c (0: H, 1, 2: V_p) of k-point kk, element
+// (m, n): full N x N columns, or only the upper triangle (packed row by row);
+// then the lower triangle is the conjugate of its mirror (H and V_p are Hermitian).
+__host__ __device__ __forceinline__ int64_t upper_index(int N, int m, int n) {
+    return (int64_t)m * N - (int64_t)m * (m - 1) / 2 + (n - m);
+}
+__device__ __forceinline__ float4 c_elem(const float4* __restrict__ C, bool packed, int64_t nk, int N, int c,
+                                         int64_t kk, int m, int n) {
+    if (!packed) return C[(c * nk + kk) * (int64_t)N * N + (int64_t)m * N + n];
+    const int64_t np = (int64_t)N * (N + 1) / 2;
+    if (m <= n) return C[(c * nk + kk) * np + upper_index(N, m, n)];
+    const float4 v = C[(c * nk + kk) * np + upper_index(N, n, m)];
+    return make_float4(v.x, v.y, -v.z, -v.w);
+}
+
+__global__ void gauge_pairs_kernel(int64_t nk, int N, const float4* __restrict__ C, bool packed,
+                                   const zc* __restrict__ orbph, const double* __restrict__ taup, zc* __restrict__ H,
+                                   zc* __restrict__ V) {
     const int64_t NN = (int64_t)N * N;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nk * NN;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t kk = idx / NN;
         const int e = (int)(idx % NN), mrow = e / N, ncol = e % N;
-        const float4 h4 = C[idx];
+        const float4 h4 = c_elem(C, packed, nk, N, 0, kk, mrow, ncol);
         const zc hl = mk((double)h4.x + (double)h4.y, (double)h4.z + (double)h4.w);
         const zc g = cmul(orbph[kk * N + mrow], orbph[kk * N + ncol]);
         H[idx] = hl * g;
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-            const float4 v4 = C[(1 + p) * nk * NN + idx];
+            const float4 v4 = c_elem(C, packed, nk, N, 1 + p, kk, mrow, ncol);
             zc v = mk((double)v4.x + (double)v4.y, (double)v4.z + (double)v4.w);
             const double diff = taup[p * N + ncol] - taup[p * N + mrow];
             v.re -= diff * hl.im;
@@ -371,13 +388,41 @@ __global__ void tau_pairs_kernel(int64_t nk, int N, float4* __restrict__ C, cons
     }
 }
 
+// Packed upper-triangle contraction output -> full float-pair H, V_0, V_1
+// (P: blocks [0, nk), [nk, 2nk), [2nk, 3nk) of N^2 elements) with the
+// orbital-position term V_p += i (tau_p,n - tau_p,m) H, in float-pair arithmetic.
+__global__ void unpack_tau_kernel(int64_t nk, int N, const float4* __restrict__ Cp, const float2* __restrict__ tau2,
+                                  float4* __restrict__ P) {
+    const int64_t NN = (int64_t)N * N;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= NN) return;
+    const int mrow = e / N, ncol = e - mrow * N;
+    float2 d[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) d[p] = df_add(tau2[p * N + ncol], df_neg(tau2[p * N + mrow]));
+    for (int64_t kk = blockIdx.y; kk < nk; kk += gridDim.y) {
+        const float4 h = c_elem(Cp, true, nk, N, 0, kk, mrow, ncol);
+        P[kk * NN + e] = h;
+        const float2 hr = make_float2(h.x, h.y), hi = make_float2(h.z, h.w);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float4 v = c_elem(Cp, true, nk, N, 1 + p, kk, mrow, ncol);
+            const float2 vr = df_add(make_float2(v.x, v.y), df_neg(df_mul(d[p], hi)));
+            const float2 vi = df_add(make_float2(v.z, v.w), df_mul(d[p], hr));
+            P[((1 + p) * nk + kk) * NN + e] = make_float4(vr.x, vr.y, vi.x, vi.y);
+        }
+    }
+}
+
 std::mutex g_hop_mu;
 
 }  // namespace
 
 int ozaki_fourier_max_k();
 size_t ozaki_hop_slices_bytes(int K, int64_t Nc);
-int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs);
+int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
+                           int64_t ncols);
+bool ozaki_use_tc();
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
                   const void* Bs, float4* C, int* err);
 
@@ -385,8 +430,9 @@ bool fourier_mixed_ok(const ModelDev& m) { return m.nR <= ozaki_fourier_max_k();
 
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
     const size_t N = (size_t)m.nsta, nR = (size_t)m.nR;
-    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int)) + 2 * nR * sizeof(double) +
-           2 * N * sizeof(double) + 2 * N * sizeof(float2) + 10 * 256;
+    // phases, orbital phases, exponents; the packed (upper-triangle) contraction output
+    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) + 3 * (N * (N + 1) / 2) * sizeof(float4)) +
+           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 2 * N * sizeof(float2) + 10 * 256;
 }
 
 namespace {
@@ -394,29 +440,69 @@ namespace {
 // Phases and the tensor-core contraction: C (3 nk N^2 float pairs) = lattice-
 // gauge H, V_0, V_1 without the orbital-position term.  orbph (nk, N) and
 // taup (2, N) are left in the scratch for the gauge step.
-int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, float4* C,
-                       void* scratch, zc** orbph_out, double** taup_out, float2** tau2_out) {
+// With the tcgen05 kernels the contraction covers only the upper-triangle
+// elements (m <= n) of H and V_p, which are Hermitian: N(N+1)/2 columns, written
+// packed to *Cg in the scratch; otherwise all N^2 columns are written to C.
+__global__ void gather_exps_kernel(int64_t n, const int* __restrict__ idx, const int* __restrict__ src,
+                                   int* __restrict__ dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[idx[i]];
+}
+
+int build_hop_table(ModelDev& m, cudaStream_t st) {
     const int N = (int)m.nsta, nR = (int)m.nR;
-    const int64_t NN = (int64_t)N * N;
+    const int64_t NN = (int64_t)N * N, NP = (int64_t)N * (N + 1) / 2;
+    const bool packed = ozaki_use_tc();
+    const int64_t ncols = packed ? NP : NN;
+    void* bs = nullptr;
+    int *eb_full = nullptr, *eb = nullptr, *colmap = nullptr;
+    int rc = TBG_OK;
+    if (cudaMalloc(&bs, ozaki_hop_slices_bytes(nR, ncols)) != cudaSuccess ||
+        cudaMalloc(&eb_full, sizeof(int) * NN) != cudaSuccess ||
+        (packed && (cudaMalloc(&eb, sizeof(int) * NP) != cudaSuccess ||
+                    cudaMalloc(&colmap, sizeof(int) * NP) != cudaSuccess)))
+        rc = set_error(TBG_E_OOM, "hop table digit planes");
+    if (!rc && packed) {
+        std::vector<int> cm((size_t)NP);
+        for (int a = 0; a < N; ++a)
+            for (int b = a; b < N; ++b) cm[(size_t)upper_index(N, a, b)] = a * N + b;
+        if (cudaMemcpy(colmap, cm.data(), sizeof(int) * NP, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = set_error(TBG_E_CUDA, "hop table column map");
+    }
+    if (!rc) rc = ozaki_build_hop_slices(st, nR, NN, m.ham, eb_full, bs, packed ? colmap : nullptr, ncols);
+    if (!rc && packed) {
+        gather_exps_kernel<<<(unsigned)std::min<int64_t>((NP + 255) / 256, 1024), 256, 0, st>>>(NP, colmap, eb_full,
+                                                                                                  eb);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_error(e, "hop table exponents");
+    }
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_error(e, "hop table digit planes");
+    }
+    cudaFree(colmap);
+    if (rc) {
+        cudaFree(bs);
+        cudaFree(eb_full);
+        cudaFree(eb);
+        return rc;
+    }
+    if (packed) cudaFree(eb_full);
+    m.hop_slices = bs;
+    m.hop_EB = packed ? eb : eb_full;
+    m.hop_packed = packed;
+    return TBG_OK;
+}
+
+int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d, float4* C,
+                       void* scratch, zc** orbph_out, double** taup_out, float2** tau2_out, float4** Cg_out) {
+    const int N = (int)m.nsta, nR = (int)m.nR;
+    const int64_t NN = (int64_t)N * N, NP = (int64_t)N * (N + 1) / 2;
     {
         std::lock_guard<std::mutex> lk(g_hop_mu);
         if (!m.hop_slices) {
-            void* bs = nullptr;
-            int* eb = nullptr;
-            TBG_CUDA(cudaMalloc(&bs, ozaki_hop_slices_bytes(nR, NN)));
-            if (cudaMalloc(&eb, sizeof(int) * NN) != cudaSuccess) {
-                cudaFree(bs);
-                return set_error(TBG_E_OOM, "hop table digit planes");
-            }
-            int rc = ozaki_build_hop_slices(st, nR, NN, m.ham, eb, bs);
-            cudaError_t e = cudaStreamSynchronize(st);
-            if (rc || e != cudaSuccess) {
-                cudaFree(bs);
-                cudaFree(eb);
-                return rc ? rc : cuda_error(e, "hop table digit planes");
-            }
-            m.hop_slices = bs;
-            m.hop_EB = eb;
+            int rc = build_hop_table(m, st);
+            if (rc) return rc;
         }
     }
     unsigned char* p = static_cast<unsigned char*>(scratch);
@@ -432,6 +518,8 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     float2* tau2 = static_cast<float2*>(take(sizeof(float2) * 2 * N));
     int* EA = static_cast<int*>(take(sizeof(int) * 3 * nk));
     int* err = static_cast<int*>(take(sizeof(int)));
+    float4* Cpk = static_cast<float4*>(take(sizeof(float4) * 3 * nk * NP));
+    float4* Cg = m.hop_packed ? Cpk : C;
     {
         KTimer kt(st, "phases_kernel");
         const int total = 2 * (nR + N);
@@ -450,8 +538,9 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     }
     int rc = cudaMemsetAsync(err, 0, sizeof(int), st) == cudaSuccess ? TBG_OK : set_error(TBG_E_CUDA, "memset");
     if (rc) return rc;
-    rc = ozaki_fourier(st, 3 * nk, NN, nR, ph3, EA, m.hop_EB, m.hop_slices, C, err);
+    rc = ozaki_fourier(st, 3 * nk, m.hop_packed ? NP : NN, nR, ph3, EA, m.hop_EB, m.hop_slices, Cg, err);
     if (rc) return rc;
+    *Cg_out = Cg;
     *orbph_out = orbph;
     *taup_out = taup;
     *tau2_out = tau2;
@@ -470,11 +559,12 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
     zc* orbph;
     double* taup;
     float2* tau2;
-    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2);
+    float4* Cg;
+    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2, &Cg);
     if (rc) return rc;
     KTimer kt(st, "gauge_pairs_kernel");
-    gauge_pairs_kernel<<<(unsigned)std::min<int64_t>((nk * NN + 255) / 256, 152 * 64), 256, 0, st>>>(nk, N, C, orbph,
-                                                                                                  taup, H, V);
+    gauge_pairs_kernel<<<(unsigned)std::min<int64_t>((nk * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
+        nk, N, Cg, m.hop_packed, orbph, taup, H, V);
     TBG_LAUNCHED("gauge_pairs_kernel");
     return TBG_OK;
 }
@@ -489,12 +579,18 @@ int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* 
     zc* orbph;
     double* taup;
     float2* tau2;
-    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2);
+    float4* Cg;
+    int rc = fourier_mixed_gemm(m, st, nk, k_d, dirs_d, C, scratch, &orbph, &taup, &tau2, &Cg);
     if (rc) return rc;
     KTimer kt(st, "tau_pairs_kernel");
     dim3 grid((unsigned)((NN + 255) / 256), (unsigned)std::min<int64_t>(nk, 65535));
-    tau_pairs_kernel<<<grid, 256, 0, st>>>(nk, N, C, tau2);
-    TBG_LAUNCHED("tau_pairs_kernel");
+    if (m.hop_packed) {
+        unpack_tau_kernel<<<grid, 256, 0, st>>>(nk, N, Cg, tau2, C);
+        TBG_LAUNCHED("unpack_tau_kernel");
+    } else {
+        tau_pairs_kernel<<<grid, 256, 0, st>>>(nk, N, C, tau2);
+        TBG_LAUNCHED("tau_pairs_kernel");
+    }
     return TBG_OK;
 }
 

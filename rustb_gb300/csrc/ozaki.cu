@@ -509,7 +509,8 @@ __global__ void row_exp_kernel(int64_t M, int K, const zc* __restrict__ A, int64
 int ozaki_fourier_max_k() { return 408; }
 
 size_t ozaki_hop_image_bytes(int K, int64_t Nc);
-int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img);
+int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img,
+                          const int* colmap, int64_t ldh);
 
 // Bytes of the hop table's digit planes in the layout of the selected kernel
 // (tcgen05 stage images, or the mma.sync slice layout).
@@ -519,12 +520,15 @@ size_t ozaki_hop_slices_bytes(int K, int64_t Nc) {
     return sizeof(__nv_bfloat16) * (size_t)nct * nkc * 6 * 2 * OZ_TK * OZ_TN;
 }
 
-// Build the digit planes of the hop table (K = nR rows of Nc = N^2 elements).
-int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs) {
+// Build the digit planes of the hop table (K = nR rows of Nc = N^2 elements);
+// EB gets the exponent of every table element.  The tcgen05 images cover the
+// ncols elements listed in colmap (all Nc when colmap is null).
+int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
+                           int64_t ncols) {
     KTimer kt(st, "hop_slice_kernel");
     hop_exp_kernel<<<(unsigned)std::min<int64_t>((Nc * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(K, Nc, ham, EB);
     TBG_LAUNCHED("hop_exp_kernel");
-    if (ozaki_use_tc()) return ozaki_hop_image_launch(st, K, Nc, ham, EB, Bs);
+    if (ozaki_use_tc()) return ozaki_hop_image_launch(st, K, colmap ? ncols : Nc, ham, EB, Bs, colmap, Nc);
     const int64_t total = ((Nc + OZ_TN - 1) / OZ_TN) * ((K + OZ_TK - 1) / OZ_TK) * OZ_TK * OZ_TN;
     hop_slice_kernel<6><<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
         K, Nc, ham, EB, static_cast<__nv_bfloat16*>(Bs));

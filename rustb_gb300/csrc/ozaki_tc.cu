@@ -557,8 +557,10 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
 // ct and stage it, the six B digit planes exactly as oz_tc_kernel's shared
 // stage holds them (HALF_STAGE bytes at (ct * nstages + it) * HALF_STAGE).
 // One thread per (column, 8 consecutive R).
+// Column gj of the contraction is matrix element colmap[gj] of the hop table
+// (identity when colmap is null); rows of the table are ldh elements apart.
 __global__ void hop_image_kernel(int K, int64_t Nc, const zc* __restrict__ ham, const int* __restrict__ EB,
-                                 unsigned char* __restrict__ img) {
+                                 unsigned char* __restrict__ img, const int* __restrict__ colmap, int64_t ldh) {
     const int nst = (K + TC_TK - 1) / TC_TK;
     const int64_t nct = (Nc + TC_TN - 1) / TC_TN;
     const int64_t total = nct * nst * B_PRODUCERS;
@@ -571,10 +573,11 @@ __global__ void hop_image_kernel(int K, int64_t Nc, const zc* __restrict__ ham, 
         const int j = q & 63, g = q >> 6;
         const int64_t gj = ct * TC_TN + j;
         const bool cv = gj < Nc;
-        const int E = cv ? EB[gj] : ZERO_EXP;
+        const int64_t el = cv ? (colmap ? (int64_t)colmap[gj] : gj) : 0;
+        const int E = cv ? EB[el] : ZERO_EXP;
         const int kf = it * TC_TK + 8 * g;
         int4 r[8];
-        load8<FMT_F64>(ham, (int64_t)kf * Nc + gj, Nc, cv ? n_valid(K, kf) : 0, r);
+        load8<FMT_F64>(ham, (int64_t)kf * ldh + el, ldh, cv ? n_valid(K, kf) : 0, r);
         unsigned char* dst = img + blk * HALF_STAGE;
         uint4 d[TC_S];
         item_planes<FMT_F64, 0, TC_S>(r, E, 0.f, 0.f, d);
@@ -666,11 +669,14 @@ size_t ozaki_hop_image_bytes(int K, int64_t Nc) {
     return (size_t)nct * nst * HALF_STAGE;
 }
 // Build the stage images from the hop table and its column exponents EB.
-int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img) {
+// Nc columns (matrix elements colmap[0 .. Nc) of a table with ldh elements per row,
+// or the first Nc elements when colmap is null); EB per table element.
+int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, const int* EB, void* img,
+                          const int* colmap, int64_t ldh) {
     const int64_t nst = (K + TC_TK - 1) / TC_TK, nct = (Nc + TC_TN - 1) / TC_TN;
     const int64_t total = nct * nst * B_PRODUCERS;
     hop_image_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
-        K, Nc, ham, EB, static_cast<unsigned char*>(img));
+        K, Nc, ham, EB, static_cast<unsigned char*>(img), colmap, ldh);
     TBG_LAUNCHED("hop_image_kernel");
     return TBG_OK;
 }

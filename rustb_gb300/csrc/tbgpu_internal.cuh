@@ -123,7 +123,8 @@ struct ModelDev {
     int device = 0;
     // digit planes of the hop table for the tensor-core Fourier sum (built lazily)
     void* hop_slices = nullptr;
-    int* hop_EB = nullptr;
+    int* hop_EB = nullptr;         // per contraction column
+    bool hop_packed = false;       // columns = upper-triangle elements (m <= n) only
 };
 
 // ------------------------------------------------------------------ errors --
