@@ -142,24 +142,38 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
         for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w]);
-            // clusters: runs of consecutive (sorted) eigenvalues with gaps <= delta
-            const double delta = 1e-3 * fmax(t, 1e-300);
-            int start = 0;
-            int64_t ncl = 0;
-            cstart[0] = 0;
-            for (int i = 1; i < N; ++i) {
-                if (fabs(lam[i] - lam[i - 1]) > delta) {
-                    if (i - start > 1) ++ncl;
-                    start = i;
-                }
-                cstart[i] = start;
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w]);
+        // clusters: runs of consecutive (sorted) eigenvalues with gaps <= delta.
+        // cstart[i] = the last run start at or before i: a block max-scan of
+        // (i if a run starts at i), over chunks of blockDim.x indices.
+        const double delta = 1e-3 * fmax(t, 1e-300);
+        __shared__ int wscan[32];
+        __shared__ int carry;
+        if (threadIdx.x == 0) carry = 0;
+        int ncl = 0;
+        for (int i0 = 0; i0 < N; i0 += blockDim.x) {
+            const int i = i0 + threadIdx.x;
+            const bool start = i < N && (i == 0 || fabs(lam[i] - lam[i - 1]) > delta);
+            const bool next_start = i + 1 >= N || fabs(lam[i + 1] - lam[i]) > delta;
+            int v = start ? i : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if ((threadIdx.x & 31) >= o) v = max(v, u);
             }
-            if (N - start > 1) ++ncl;
-            if (ncl && clusters) atomicAdd(reinterpret_cast<unsigned long long*>(clusters), (unsigned long long)ncl);
+            __syncthreads();
+            if ((threadIdx.x & 31) == 31) wscan[threadIdx.x >> 5] = v;
+            __syncthreads();
+            for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) v = max(v, wscan[w]);
+            v = max(v, carry);
+            if (i < N) cstart[i] = v;
+            // a run of length > 1 starts at i
+            ncl += __syncthreads_count(start && i < N && !next_start);
+            if (threadIdx.x == blockDim.x - 1) carry = v;
         }
+        if (threadIdx.x == 0 && ncl && clusters)
+            atomicAdd(reinterpret_cast<unsigned long long*>(clusters), (unsigned long long)ncl);
         __syncthreads();
         // F for separated pairs (FP32); R/2 inside clusters and on the diagonal
         for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
@@ -172,9 +186,10 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
             } else {
                 const float4 s4 = Sb[idx];
                 const float lj = lamf[j];
-                const float den = (float)(lam[j] - lam[i]);
-                fr = ((s4.x + s4.y) - lj * (x4.x + x4.y)) / den;
-                fi = ((s4.z + s4.w) - lj * (x4.z + x4.w)) / den;
+                // |den| > 1e-3 max|lambda|: the fast reciprocal is accurate to a few ulp
+                const float rden = __frcp_rn((float)(lam[j] - lam[i]));
+                fr = ((s4.x + s4.y) - lj * (x4.x + x4.y)) * rden;
+                fi = ((s4.z + s4.w) - lj * (x4.z + x4.w)) * rden;
             }
             Fb[idx] = mk(fr, fi);
         }
