@@ -172,52 +172,50 @@ __device__ __forceinline__ long long fx32(float x, int E) {
     return (b >> 31) ? -F : F;
 }
 
+// r rounded to the nearest multiple of 2^k (ties to even) by adding and
+// subtracting 1.5 * 2^(23 + k); exact for |r| < 2^(22 + k).
+constexpr double pow2c(int e) { return e == 0 ? 1.0 : (e > 0 ? 2.0 * pow2c(e - 1) : 0.5 * pow2c(e + 1)); }
+template <int K>
+__device__ __forceinline__ float round_to_pow2(float r) {
+    constexpr float C = (float)(1.5 * pow2c(23 + K));
+    return __fsub_rn(__fadd_rn(r, C), C);
+}
+
 // Six pre-scaled digits P_s = q_s 2^(-7s) of a fixed-point F (|F| < 2^42),
 // F = sum_s q_s 2^(35 - 7s).  F is split as hi 2^21 + lo (lo in [0, 2^21)),
 // each half is exact in FP32 and is cut by rounding to the nearest multiple
-// of 2^14 and 2^7; every step is exact.  |q_0| <= 128, |q_1|, |q_2|, |q_4|,
-// |q_5| <= 64, q_3 in [0, 128].
+// of the digit weight; every step is exact.  |q_0| <= 128, |q_1|, |q_2|,
+// |q_4|, |q_5| <= 64, q_3 in [0, 128].
 __device__ __forceinline__ void digits_fixed(long long F, float* P) {
     const int hi = (int)(F >> 21);
     const int lo = (int)(F & 0x1FFFFF);
     const float a = (float)hi * 0x1p-14f;  // [-128, 128)
-    const float d0 = rintf(a);
-    const float t1 = (a - d0) * 128.f;     // [-64, 64], a multiple of 2^-7
-    const float d1 = rintf(t1);
-    const float d2 = t1 - d1;              // q_2 2^-7
-    const float c = (float)lo * 0x1p-14f;  // [0, 128)
-    const float e3 = rintf(c);
-    const float t4 = (c - e3) * 128.f;
-    const float e4 = rintf(t4);
-    const float e5 = t4 - e4;              // q_5 2^-7
-    P[0] = d0;
-    P[1] = d1 * 0x1p-7f;
-    P[2] = d2 * 0x1p-7f;
-    P[3] = e3 * 0x1p-21f;
-    P[4] = e4 * 0x1p-28f;
-    P[5] = e5 * 0x1p-28f;
+    P[0] = round_to_pow2<0>(a);
+    const float r = __fsub_rn(a, P[0]);    // a multiple of 2^-14, |r| <= 1/2
+    P[1] = round_to_pow2<-7>(r);
+    P[2] = __fsub_rn(r, P[1]);              // q_2 2^-14
+    const float c = (float)lo * 0x1p-35f;  // [0, 2^-14)
+    P[3] = round_to_pow2<-21>(c);
+    const float r2 = __fsub_rn(c, P[3]);
+    P[4] = round_to_pow2<-28>(r2);
+    P[5] = __fsub_rn(r2, P[4]);             // q_5 2^-35
 }
 // Six pre-scaled digits of u = x 2^(7 - E) in (-128, 128) for an FP32 x:
-// q_s = round(t_s), t_{s+1} = 128 (t_s - q_s), every step exact; the sum
-// equals x rounded to the grid 2^(E-42).  |q_0| <= 128, |q_s| <= 64.
+// P_s = u_s rounded to a multiple of 2^(-7s), u_{s+1} = u_s - P_s, every step
+// exact; the sum equals x rounded to the grid 2^(E-42).  |q_0| <= 128,
+// |q_s| <= 64.
 __device__ __forceinline__ void digits_float(float u, float* P) {
-    float d = rintf(u);
-    P[0] = d;
-    float t = (u - d) * 128.f;
-    d = rintf(t);
-    P[1] = d * 0x1p-7f;
-    t = (t - d) * 128.f;
-    d = rintf(t);
-    P[2] = d * 0x1p-14f;
-    t = (t - d) * 128.f;
-    d = rintf(t);
-    P[3] = d * 0x1p-21f;
-    t = (t - d) * 128.f;
-    d = rintf(t);
-    P[4] = d * 0x1p-28f;
-    t = (t - d) * 128.f;
-    d = rintf(t);
-    P[5] = d * 0x1p-35f;
+    P[0] = round_to_pow2<0>(u);
+    float r = __fsub_rn(u, P[0]);
+    P[1] = round_to_pow2<-7>(r);
+    r = __fsub_rn(r, P[1]);
+    P[2] = round_to_pow2<-14>(r);
+    r = __fsub_rn(r, P[2]);
+    P[3] = round_to_pow2<-21>(r);
+    r = __fsub_rn(r, P[3]);
+    P[4] = round_to_pow2<-28>(r);
+    r = __fsub_rn(r, P[4]);
+    P[5] = round_to_pow2<-35>(r);
 }
 __device__ __forceinline__ float pow2f(int n) { return __int_as_float((127 + n) << 23); }  // n in [-126, 127]
 // 2^(7 - E) as s1 * s2 (each a normal float) for FP32 operands; 0 for a zero line.
