@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-/* Status codes.  Codes 1..9 map 1:1 onto TbError variants (src/error.rs). */
+/* Status codes.  Codes 1..11 map 1:1 onto TbError variants (src/error.rs). */
 enum tbg_status {
     TBG_OK = 0,
     TBG_E_KVECTOR_LENGTH = 1,             /* TbError::KVectorLengthMismatch */
@@ -44,6 +44,8 @@ enum tbg_status {
     TBG_E_INVALID_DIMENSION = 7,          /* TbError::InvalidDimension */
     TBG_E_INVALID_MODEL = 8,              /* TbError::InvalidModelInvariant */
     TBG_E_INVALID_ARGUMENT = 9,           /* conditions on which Rustb panics */
+    TBG_E_INVALID_ENERGY_RANGE = 10,      /* TbError::InvalidEnergyRange */
+    TBG_E_INVALID_DOS_PARAMETER = 11,     /* TbError::InvalidDosParameter */
     TBG_E_CUDA = 20,                      /* CUDA runtime failure */
     TBG_E_NOCONV = 21,                    /* eigensolver did not converge */
     TBG_E_TIMEOUT = 22,                   /* a bounded device wait ran out */
@@ -177,6 +179,39 @@ int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begi
                         int64_t k_count, const double* dirs2, int64_t nmu,
                         const double* mu, double T, double eta, int spin,
                         int precision, double* sums_out, tbg_report* report);
+
+/* Band-resolved quantum geometry at nk k-points: the tensor
+ *   G_n = sum_{m != n} v^a_nm v^b_mn / ((E_n - E_m)^2 + eta^2)
+ * with dirs2 (2, dim) rows = a, b; metric_out = Re G_n, berry_out = -2 Im G_n,
+ * E_out (may be NULL) the band energies, all (nk, nsta).  Charge current
+ * (no spin dressing).
+ * Replaces: QuantumGeometry::quantum_geometry_at / quantum_geometry_on
+ * (src/quantum_geometry.rs:88-138, kernel quantum_geometry_at_impl
+ * quantum_geometry.rs:149-193). */
+int tbg_quantum_geometry(const tbg_model* m, int64_t nk, const double* k,
+                         const double* dirs2, double eta, int precision,
+                         double* metric_out, double* berry_out, double* E_out);
+
+/* Occupation-weighted quantum geometry, Direct integration over the uniform
+ * mesh kmesh[dim]: per mu_j,
+ *   metric_out[j] = sum_k sum_n g_n f(E_n, mu_j) / nk / det(lat),
+ *   berry_out[j]  = sum_k sum_n Omega_n f(E_n, mu_j) / nk / det(lat).
+ * Replaces: Model::quantum_geometry with Integration::Direct
+ * (src/quantum_geometry.rs:196-240). */
+int tbg_quantum_geometry_mesh(const tbg_model* m, const int64_t* kmesh,
+                              const double* dirs2, int64_t nmu, const double* mu,
+                              double T, double eta, int precision,
+                              double* metric_out, double* berry_out,
+                              tbg_report* report);
+
+/* Density of states with Gaussian smearing on the uniform mesh kmesh[dim]:
+ * E_out[i] = E_min + i (E_max - E_min) / (E_n - 1) (E_out may be NULL) and
+ *   dos_out[i] = 1/nk sum_{k,n} exp(-((E_i - E_nk) / sigma)^2 / 2) / sigma / sqrt(2 pi),
+ * band energies in FP64.  Errors: E_min >= E_max -> INVALID_ENERGY_RANGE;
+ * E_n == 0 or sigma not finite and positive -> INVALID_DOS_PARAMETER.
+ * Replaces: Model::dos (src/model_physics.rs:179-230). */
+int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max,
+            int64_t E_n, double sigma, double* E_out, double* dos_out);
 
 /* ------------------------------------------- asynchronous batch queue --- */
 

@@ -32,7 +32,7 @@ def scipy_openblas() -> str:
 
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", os.path.join(HERE, "cpu_port.c"), "-o", LIB, "-ldl", "-lm"]
+    cmd = ["gcc", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", os.path.join(HERE, "cpu_port.c"), "-o", LIB, "-ldl", "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"gcc failed:\n{r.stderr}")
@@ -61,6 +61,10 @@ def load():
                                        ctypes.c_int64, ctypes.c_int64, dp, dp, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, dp, ctypes.c_double, ctypes.c_int, dp, dp, dp]
         lib.port_hall_sums.restype = ctypes.c_int
+        lib.port_dos.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ip, dp, ip,
+                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_int, dp]
+        lib.port_dos.restype = ctypes.c_int
         _port = lib
     return _port
 
@@ -96,3 +100,23 @@ def hall_sums(model, directions, mu, T=0.0, eta=1e-3, spin=-1, kmesh=None, k0=0,
     if rc != 0:
         raise RuntimeError(f"zheev info={rc}")
     return (S, Om, E) if want_bands else S
+
+
+def dos_sums(model, kmesh, E_min, E_max, E_n, sigma, k0=0, nk=None, threads=None):
+    """Unnormalised DOS sums (E_n) over mesh points [k0, k0 + nk) from the C port."""
+    lib = load()
+    ham = np.ascontiguousarray(model.ham).view(np.float64)
+    hamR = np.ascontiguousarray(model.hamR, dtype=np.int64)
+    orb = np.ascontiguousarray(model.orb, dtype=np.float64)
+    km = np.ascontiguousarray(kmesh, dtype=np.int64)
+    if nk is None:
+        nk = int(np.prod(km))
+    acc = np.zeros(int(E_n))
+    threads = threads or os.cpu_count() or 1
+    rc = lib.port_dos(model.dim, int(model.spin), model.norb, model.nR, _dp(ham),
+                      hamR.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _dp(orb),
+                      km.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(k0), int(nk), int(E_n),
+                      float(E_min), float(E_max), float(sigma), int(threads), _dp(acc))
+    if rc != 0:
+        raise RuntimeError(f"zheev info={rc}")
+    return acc

@@ -9,6 +9,7 @@
  *   U^T V U*            src/response/traits.rs:177-180 (two zgemm per direction)
  *   Omega_n             src/response/traits.rs:181-195
  *   occupation sums     src/response/linear/mod.rs:204-223, src/thermodynamics.rs:100-118
+ * and the density of states of Model::dos (src/model_physics.rs:179-230).
  * The BLAS/LAPACK routines are taken at run time from the OpenBLAS that scipy
  * bundles (the routines Rustb's openblas backend links).  k-points run in
  * parallel under OpenMP with single-threaded BLAS, as Rustb's rayon
@@ -16,6 +17,9 @@
  */
 #include <dlfcn.h>
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -259,5 +263,112 @@ int port_hall_sums(int dim, int spin_model, int norb, int nR, const double* ham,
     free(Rcart);
     free(tau);
     free(taucart);
+    return err;
+}
+
+/* H(k) in the Atom gauge (src/velocity.rs Fourier sum, then conj(phi_m) phi_n),
+ * as berry_one builds it.  u: 2 nR, phi: 2 N scratch. */
+static void ham_one(int dim, int N, int nR, const double* ham, const int64_t* hamR, const double* tau,
+                    const double* k, double* H, double* u, double* phi) {
+    const size_t NN = (size_t)N * N;
+    const int one = 1, nn = (int)NN;
+    memset(H, 0, sizeof(double) * 2 * NN);
+    for (int r = 0; r < nR; ++r) {
+        double s = (double)hamR[r * dim] * k[0];
+        if (dim > 1) s += (double)hamR[r * dim + 1] * k[1];
+        if (dim > 2) s += (double)hamR[r * dim + 2] * k[2];
+        u[2 * r] = cos(2.0 * M_PI * s);
+        u[2 * r + 1] = sin(2.0 * M_PI * s);
+        p_zaxpy(&nn, u + 2 * r, ham + 2 * NN * r, &one, H, &one);
+    }
+    for (int s = 0; s < N; ++s) {
+        double t = tau[3 * s] * k[0];
+        if (dim > 1) t += tau[3 * s + 1] * k[1];
+        if (dim > 2) t += tau[3 * s + 2] * k[2];
+        phi[2 * s] = cos(2.0 * M_PI * t);
+        phi[2 * s + 1] = sin(2.0 * M_PI * t);
+    }
+    for (int m = 0; m < N; ++m)
+        for (int n = 0; n < N; ++n) {
+            const size_t e = (size_t)m * N + n;
+            double gr = phi[2 * m] * phi[2 * n] + phi[2 * m + 1] * phi[2 * n + 1];
+            double gi = phi[2 * m] * phi[2 * n + 1] - phi[2 * m + 1] * phi[2 * n];
+            double hr = H[2 * e], hi = H[2 * e + 1];
+            H[2 * e] = hr * gr - hi * gi;
+            H[2 * e + 1] = hr * gi + hi * gr;
+        }
+}
+
+/* Model::dos (src/model_physics.rs:179-230) on the mesh points [k0, k0 + nk)
+ * (gen_kmesh order): band energies by zheev JOBZ='N' (solve_band_onek,
+ * src/solve_ham.rs:52-62), then, as the reference's fold does, every energy
+ * against every one of the E_n grid points:
+ *   A = (E_i - x) / sigma;  acc[i] += exp(-A^2 / 2) / sigma / sqrt(2 pi).
+ * acc (E_n) receives the sum over the range (not divided by nk); threads keep
+ * private accumulators that are added in thread order at the end.  Returns 0
+ * or the first non-zero LAPACK info. */
+int port_dos(int dim, int spin_model, int norb, int nR, const double* ham, const int64_t* hamR, const double* orb,
+             const int64_t* kmesh, int64_t k0, int64_t nk, int64_t E_n, double E_min, double E_max, double sigma,
+             int nthreads, double* acc) {
+    const int N = spin_model ? 2 * norb : norb;
+    const size_t NN = (size_t)N * N;
+    double* tau = (double*)calloc((size_t)N * 3, sizeof(double));
+    for (int s = 0; s < N; ++s)
+        for (int d = 0; d < dim; ++d) tau[3 * s + d] = orb[(s % norb) * dim + d];
+    const double step = E_n > 1 ? (E_max - E_min) / (double)(E_n - 1) : 0.0;
+    const double sigma0 = 1.0 / sigma, pi0 = 1.0 / sqrt(2.0 * M_PI);
+    double* Eg = (double*)malloc(sizeof(double) * E_n);
+    for (int64_t i = 0; i < E_n; ++i) Eg[i] = E_min + step * (double)i;
+    double* parts = (double*)calloc((size_t)nthreads * E_n, sizeof(double));
+    int err = 0;
+#pragma omp parallel num_threads(nthreads)
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        double* mine = parts + (size_t)tid * E_n;
+        const int lwork = 66 * N;
+        double* H = (double*)malloc(sizeof(double) * (2 * NN + 2 * (size_t)nR + 2 * (size_t)N + 2 * (size_t)lwork +
+                                                      3 * (size_t)N + (size_t)N));
+        double* u = H + 2 * NN;
+        double* phi = u + 2 * nR;
+        double* work = phi + 2 * N;
+        double* rwork = work + 2 * lwork;
+        double* E = rwork + 3 * N;
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t t = 0; t < nk; ++t) {
+            double k[3] = {0, 0, 0};
+            const int64_t idx = k0 + t;
+            const int64_t n0 = kmesh[0], n1 = dim > 1 ? kmesh[1] : 1, n2 = dim > 2 ? kmesh[2] : 1;
+            if (dim == 1) k[0] = (double)idx / (double)n0;
+            if (dim == 2) { k[0] = (double)(idx / n1) / (double)n0; k[1] = (double)(idx % n1) / (double)n1; }
+            if (dim == 3) {
+                k[0] = (double)(idx / (n1 * n2)) / (double)n0;
+                k[1] = (double)((idx / n2) % n1) / (double)n1;
+                k[2] = (double)(idx % n2) / (double)n2;
+            }
+            ham_one(dim, N, nR, ham, hamR, tau, k, H, u, phi);
+            int info = 0, n = N;
+            p_zheev("N", "L", &n, H, &n, E, work, &lwork, rwork, &info, 1, 1);
+            if (info) {
+#pragma omp critical
+                err = info;
+            }
+            for (int b = 0; b < N; ++b) {
+                const double x = E[b];
+                for (int64_t i = 0; i < E_n; ++i) {
+                    const double A = (Eg[i] - x) * sigma0;
+                    mine[i] += exp(-A * A / 2.0) * sigma0 * pi0;
+                }
+            }
+        }
+        free(H);
+    }
+    for (int t = 0; t < nthreads; ++t)
+        for (int64_t i = 0; i < E_n; ++i) acc[i] += parts[(size_t)t * E_n + i];
+    free(parts);
+    free(Eg);
+    free(tau);
     return err;
 }

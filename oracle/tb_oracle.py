@@ -292,6 +292,89 @@ def hall_conductivity(model, kmesh, directions, mu_list, T=0.0, eta=1e-3, spin=-
 
 
 # --------------------------------------------------------------------------
+# Quantum geometry (src/quantum_geometry.rs) and density of states
+# (src/model_physics.rs)
+# --------------------------------------------------------------------------
+
+def quantum_geometry_at(model, k, directions, eta: float = 1e-3):
+    """``quantum_geometry_at_impl`` (src/quantum_geometry.rs:149-193).
+
+    (V, H) = gen_v_projected(k, Atom, direction)                      :154-155
+    (E, U) = eigh(H)                                                  :156
+    Ab = U^T V_0 U*, Bb = U^T V_1 U*                                  :157-163
+    K = Ab o Bb^T; G_n = sum_{m != n} K_nm / ((E_n - E_m)^2 + eta^2)  :164-184
+    metric_n = Re G_n, Omega_n = -2 Im G_n                            :185-186
+    Charge current only: the spin field of the parameters is ignored.
+    Returns (metric, Omega, E).
+    """
+    V, H = gen_v_projected(model, np.asarray(k, dtype=np.float64), 1, directions)
+    E, W = eigh(H)
+    Ab = W.conj().T @ V[0] @ W
+    Bb = W.conj().T @ V[1] @ W
+    K = Ab * Bb.T
+    dE = E[:, None] - E[None, :]
+    T = K / (dE * dE + eta * eta)
+    np.fill_diagonal(T, 0.0)
+    G = T.sum(axis=1)
+    return G.real.copy(), -2.0 * G.imag, E
+
+
+def quantum_geometry_on(model, k_list, directions, eta: float = 1e-3):
+    """``quantum_geometry_on`` (src/quantum_geometry.rs:104-138): per k-point,
+    returns (metric, Omega, E), each (nk, nsta)."""
+    k_list = np.atleast_2d(np.asarray(k_list, dtype=np.float64))
+    g = np.empty((k_list.shape[0], model.nsta))
+    om = np.empty_like(g)
+    E = np.empty_like(g)
+    for i, k in enumerate(k_list):
+        g[i], om[i], E[i] = quantum_geometry_at(model, k, directions, eta)
+    return g, om, E
+
+
+def quantum_geometry(model, kmesh, directions, mu_list, T=0.0, eta=1e-3):
+    """``Model::quantum_geometry`` with Integration::Direct
+    (src/quantum_geometry.rs:196-240): per mu,
+    sum_k sum_n value_n f(E_n, mu) / nk / det(lat) for the metric and Omega."""
+    k = gen_kmesh(kmesh)
+    g, om, E = quantum_geometry_on(model, k, directions, eta)
+    det = float(np.linalg.det(model.lat))
+    mu_list = np.atleast_1d(np.asarray(mu_list, dtype=np.float64))
+    return (hall_from_bands(g, E, mu_list, T, k.shape[0], det),
+            hall_from_bands(om, E, mu_list, T, k.shape[0], det))
+
+
+def dos_energies(E_min: float, E_max: float, E_n: int) -> np.ndarray:
+    """``Array1::linspace(E_min, E_max, E_n)`` as ndarray 0.17 yields it
+    (src/model_physics.rs:210): start + i * step, step = (end - start) / (n - 1)
+    (0 for n == 1) -- the last point is not forced to E_max."""
+    step = (E_max - E_min) / float(E_n - 1) if E_n > 1 else 0.0
+    return E_min + step * np.arange(E_n, dtype=np.float64)
+
+
+def dos_from_bands(eigs, E_min: float, E_max: float, E_n: int, sigma: float, nk: int, chunk: int = 4096):
+    """The Gaussian sum of ``Model::dos`` (src/model_physics.rs:206-227):
+    A = (E - x) / sigma, f = exp(-A^2 / 2) / sigma / sqrt(2 pi), summed over
+    every band energy x, divided by nk."""
+    E = dos_energies(E_min, E_max, E_n)
+    sigma0 = 1.0 / sigma
+    pi0 = 1.0 / np.sqrt(2.0 * np.pi)
+    x = np.asarray(eigs, dtype=np.float64).reshape(-1)
+    acc = np.zeros(E_n)
+    for c0 in range(0, x.size, chunk):
+        A = (E[None, :] - x[c0:c0 + chunk, None]) * sigma0
+        acc += (np.exp(-A * A / 2.0) * sigma0 * pi0).sum(axis=0)
+    return E, acc / float(nk)
+
+
+def dos(model, kmesh, E_min: float, E_max: float, E_n: int, sigma: float):
+    """``Model::dos`` (src/model_physics.rs:179-230): band energies on the
+    uniform mesh (gen_kmesh order), then the Gaussian sum."""
+    k = gen_kmesh(kmesh)
+    eigs = solve_band_all(model, k)
+    return dos_from_bands(eigs, E_min, E_max, E_n, sigma, k.shape[0])
+
+
+# --------------------------------------------------------------------------
 # Wilson loop (used only to pin the Kubo formula, src/geometry.rs:156-215)
 # --------------------------------------------------------------------------
 

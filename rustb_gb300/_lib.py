@@ -94,6 +94,14 @@ SIGNATURES = [
                                            _c_double_p, ctypes.c_int64, _c_double_p, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int, ctypes.c_int, _c_double_p,
                                            ctypes.POINTER(TbgReport)]),
+    ("tbg_quantum_geometry", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p,
+                                            ctypes.c_double, ctypes.c_int, _c_double_p, _c_double_p,
+                                            _c_double_p]),
+    ("tbg_quantum_geometry_mesh", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p, ctypes.c_int64,
+                                                 _c_double_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 _c_double_p, _c_double_p, ctypes.POINTER(TbgReport)]),
+    ("tbg_dos", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                               ctypes.c_double, _c_double_p, _c_double_p]),
     ("tbg_measure_fma_peaks", ctypes.c_int, [_c_double_p, _c_double_p]),
     ("tbg_set_device", ctypes.c_int, [ctypes.c_int]),
     ("tbg_kernel_timing_enable", ctypes.c_int, [ctypes.c_int]),

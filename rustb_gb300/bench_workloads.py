@@ -11,6 +11,9 @@
 * ``serve``     -- resident models, Poisson arrivals of (model, k-list of
                    1-4096 points, observable) requests at 20-100 % of the
                    measured peak; p50 / p99 latency per load.
+* ``dos``       -- Model::dos of the reference's benchmark model (two-band
+                   honeycomb, -3..3 eV, 500 bins, sigma 1e-2) on a
+                   1000 x 1000 mesh; a step is the whole mesh.
 
 Each prints one JSON line in the bench.py format.  The CPU baseline of each
 (``--impl reference``) is the C port of the reference path on the host cores.
@@ -53,7 +56,8 @@ def _cpu_port(model, dirs, mu, kmesh, k0, nk, threads=None):
 def run(args, rank, world, local):
     if rank != 0 and args.impl == "reference":
         return 0
-    fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench}[args.workload]
+    fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench,
+          "dos": dos_bench}[args.workload]
     return fn(args, rank, world, local)
 
 
@@ -263,4 +267,70 @@ def serve_bench(args, rank, world, local):
     p99_80 = loads["80%"]["p99_ms"]
     _line(args, world, "p99 latency (serving, 80% load)", p99_80, "ms", p99_80, "f32 eigensolve + exact-slice tensor products",
           cfg, {"loads": loads, "peak_requests_per_s": peak_req, "peak_k_pts_per_s": peak_k})
+    return 0
+
+
+# --------------------------------------------------------------------- dos --
+DOS_METRIC = "k-pts/s (Model::dos: band energies + Gaussian sum)"
+
+
+def _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, nk, threads=None):
+    from oracle import build_port
+
+    build_port.load()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    build_port.dos_sums(model, mesh, E_min, E_max, E_n, sigma, 0, nk, threads=threads)
+    return nk / (time.perf_counter() - t0), threads
+
+
+def dos_bench(args, rank, world, local):
+    model = W.honeycomb_small()
+    mesh = (1000, 1000)
+    nk = mesh[0] * mesh[1]
+    E_min, E_max, E_n, sigma = -3.0, 3.0, 500, 1e-2
+    cfg = {"workload": "Model::dos, two-band honeycomb (onsite -0.7/+0.7, t=-1), 1000x1000 mesh, "
+                       "E in [-3, 3] with 500 points, sigma = 1e-2", "k_mesh": list(mesh), "E_n": E_n,
+           "sigma": sigma}
+    sample = 40000
+    if args.impl == "reference":
+        val, thr = _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, sample)
+        _line(args, world, DOS_METRIC, val, "k-pts/s", nk / val * 1e3, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "k-pts/s", "cores": thr, "kind": "port",
+                                                     "sample": f"the first {sample} k-points of the mesh"},
+               "e2e": {"value": val, "unit": "k-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    for _ in range(args.warmup):
+        model.dos(mesh, E_min, E_max, E_n, sigma)
+    lib.tbg_kernel_timing_enable(1)
+    _lib.kernel_timing(reset=True)
+    l0 = lib.tbg_kernel_launch_count(0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        E, d = model.dos(mesh, E_min, E_max, E_n, sigma)
+    wall = time.perf_counter() - t0
+    launches = lib.tbg_kernel_launch_count(0) - l0
+    lib.tbg_kernel_timing_enable(0)
+    timing = _lib.kernel_timing(reset=True)
+    t_dev = sum(v[1] for v in timing.values()) / 1e3
+    # whole call with the model resident: launches, the device work and the read-back
+    val = args.steps * nk * world / wall
+    # e2e: model upload, the whole mesh and the DOS read-back per step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m2 = W.honeycomb_small()
+        m2.dos(mesh, E_min, E_max, E_n, sigma)
+        m2._invalidate()
+    e2e = args.steps * nk / (time.perf_counter() - t0)
+    cpu, thr = _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, sample)
+    _line(args, world, DOS_METRIC, val, "k-pts/s", wall / args.steps * 1e3, "f64", cfg,
+          {"gpu_launches": int(launches), "states_integral": float(d.sum() * (E[1] - E[0])),
+           "kernel_ms_per_step": t_dev / args.steps * 1e3,
+           "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in timing.items()},
+           "cpu_baseline": {"value": cpu, "unit": "k-pts/s", "cores": thr, "kind": "port",
+                            "sample": f"the first {sample} k-points of the mesh"},
+           "e2e": {"value": e2e, "unit": "k-pts/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
+                   "d2h_bytes_per_step": 8 * E_n}})
     return 0

@@ -19,7 +19,10 @@ OUT_DIR = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(OUT_DIR, "libtbgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+# Host code keeps IEEE evaluation order (no a*b+c contraction into FMA, which
+# gcc does by default on aarch64), as the Rust reference does.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr"] + ARCH
 
 
 def nvcc() -> str:

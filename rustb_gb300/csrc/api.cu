@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -246,6 +247,8 @@ struct BerryJob {
     size_t fwork_bytes;
     cc* U32;
     float4* pairs;  // mixed: H, V_0, V_1 as float pairs (3 chunk N^2)
+    bool want_metric;
+    double* Met;  // quantum metric (chunk, N) when want_metric
 };
 
 int alloc_berry(Ctx& ctx, BerryJob& J) {
@@ -258,6 +261,7 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
     J.scratch = ctx.alloc<zc>(c * NN);
     J.E = ctx.alloc<double>(c * N);
     J.Om = ctx.alloc<double>(c * N);
+    J.Met = J.want_metric ? ctx.alloc<double>(c * N) : nullptr;
     J.status_d = ctx.alloc<int>(1);
     J.Hcopy = nullptr;
     J.U32 = nullptr;
@@ -311,7 +315,7 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
             if (rc) return rc;
         }
         return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
-                           J.status_d, clusters_d);
+                           J.status_d, clusters_d, J.Met);
     }
     rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
     if (rc) return rc;
@@ -325,7 +329,7 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
     }
     rc = eig_batched(ctx.st, N, nkc, J.H, J.E, J.U, nullptr, 0, J.status_d);
     if (rc) return rc;
-    return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch);
+    return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch, J.Met);
 }
 
 }  // namespace
@@ -580,7 +584,7 @@ int tbg_solve(const tbg_model* m, int64_t nk, const double* k, double* E_out, do
 
 static int berry_common(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, int spin, double eta,
                         int precision, double* Omega_out, double* E_out, int nmu, const double* mu, double T,
-                        double* occ_out) {
+                        double* occ_out, double* Met_out = nullptr) {
     int rc = check_model(m);
     if (rc) return rc;
     const ModelDev& M = m->d;
@@ -600,6 +604,7 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
+    J.want_metric = Met_out != nullptr;
     J.chunk = choose_chunk(nk, sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 15 : 5) + 64 * N +
                                    (precision == TBG_PREC_MIXED ? 48 * (int64_t)M.nR : 0));
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
@@ -617,8 +622,11 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
         TBG_CUDA(cudaMemcpyAsync(J.k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
         if (small) {
             if ((rc = small_fused(M, ctx.st, nkc, J.k_d, 0, nullptr, dirs_d, spin, eta, occ_out ? nmu : 0, mu_d, width,
-                                  J.Om, J.E, occ_out ? S : nullptr)))
+                                  J.Om, J.E, occ_out ? S : nullptr, J.Met)))
                 return rc;
+            if (Met_out)
+                TBG_CUDA(cudaMemcpyAsync(Met_out + c0 * N, J.Met, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost,
+                                         ctx.st));
             if (Omega_out)
                 TBG_CUDA(cudaMemcpyAsync(Omega_out + c0 * N, J.Om, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost,
                                          ctx.st));
@@ -630,6 +638,8 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
             continue;
         }
         if ((rc = run_berry_chunk(ctx, J, nkc, nullptr))) return rc;
+        if (Met_out)
+            TBG_CUDA(cudaMemcpyAsync(Met_out + c0 * N, J.Met, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
         if (Omega_out)
             TBG_CUDA(cudaMemcpyAsync(Omega_out + c0 * N, J.Om, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
         if (E_out)
@@ -661,7 +671,7 @@ int tbg_occupied_berry_curvature(const tbg_model* m, int64_t nk, const double* k
 
 static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, int64_t k_count, bool whole,
                      const double* dirs2, int64_t nmu, const double* mu, double T, double eta, int spin,
-                     int precision, double* out, tbg_report* report) {
+                     int precision, double* out, tbg_report* report, double* metric_out = nullptr) {
     int rc = check_model(m);
     if (rc) return rc;
     const ModelDev& M = m->d;
@@ -691,6 +701,7 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
         return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
     if (!out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    const bool met = metric_out != nullptr;
     precision = effective_precision(M, precision);
     const double det = lattice_det(M.lat, M.dim);
     if (whole && (det == 0.0 || !std::isfinite(det)))
@@ -708,20 +719,25 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     J.spin = spin;
     J.eta = eta;
     J.precision = precision;
+    J.want_metric = met;
     J.chunk = choose_chunk(std::max<int64_t>(k_count, 1),
-                           sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 15 : 5) + 64 * N + 8 * nmu +
+                           sizeof(zc) * NN * (precision == TBG_PREC_MIXED ? 15 : 5) + 64 * N + 16 * nmu +
                                (precision == TBG_PREC_MIXED ? 48 * (int64_t)M.nR : 0));
     double* dirs_d = ctx.alloc<double>(2 * M.dim);
     J.dirs_d = dirs_d;
     double* mu_d = ctx.alloc<double>(nmu);
     double* S = ctx.alloc<double>(J.chunk * nmu);
     double* acc = ctx.alloc<double>(2 * nmu);
+    // metric: occupation sums and running compensated totals
+    double* SG = met ? ctx.alloc<double>(J.chunk * nmu) : nullptr;
+    double* accg = met ? ctx.alloc<double>(2 * nmu) : nullptr;
     int64_t* clusters_d = ctx.alloc<int64_t>(1);
     if (ctx.rc) return ctx.rc;
     if ((rc = alloc_berry(ctx, J))) return rc;
     TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
     TBG_CUDA(cudaMemcpyAsync(mu_d, mu, sizeof(double) * nmu, cudaMemcpyHostToDevice, ctx.st));
     TBG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 2 * nmu, ctx.st));
+    if (met) TBG_CUDA(cudaMemsetAsync(accg, 0, sizeof(double) * 2 * nmu, ctx.st));
     TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
     const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
@@ -730,19 +746,23 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
         const int64_t nkc = std::min(J.chunk, k_count - c0);
         if (small) {
             if ((rc = small_fused(M, ctx.st, nkc, nullptr, k_begin + c0, kmesh, dirs_d, spin, eta, (int)nmu, mu_d,
-                                  width, nullptr, nullptr, S)))
+                                  width, nullptr, nullptr, S, nullptr, SG)))
                 return rc;
         } else {
             kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(k_begin + c0, nkc, M.dim, n0, n1, n2, J.k_d);
             TBG_LAUNCHED("kmesh_kernel");
             if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
             if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
+            if (met && (rc = occupation_sums(ctx.st, N, nkc, J.Met, J.E, (int)nmu, mu_d, width, SG))) return rc;
         }
         if ((rc = kahan_column_sums(ctx.st, nkc, (int)nmu, S, acc))) return rc;
+        if (met && (rc = kahan_column_sums(ctx.st, nkc, (int)nmu, SG, accg))) return rc;
     }
-    std::vector<double> acc_h(2 * nmu);
+    std::vector<double> acc_h(2 * nmu), accg_h(met ? 2 * nmu : 0);
     int64_t clusters_h = 0;
     TBG_CUDA(cudaMemcpyAsync(acc_h.data(), acc, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, ctx.st));
+    if (met)
+        TBG_CUDA(cudaMemcpyAsync(accg_h.data(), accg, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, ctx.st));
     TBG_CUDA(cudaMemcpyAsync(&clusters_h, clusters_d, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.st));
     cudaEventRecord(ev1, ctx.st);
     if (ctx.sync("tbg_hall_conductivity")) return ctx.rc;
@@ -750,6 +770,10 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     for (int64_t j = 0; j < nmu; ++j) {
         const double s = acc_h[2 * j] - acc_h[2 * j + 1];
         out[j] = whole ? s / (double)nk / det : s;
+        if (met) {
+            const double g = accg_h[2 * j] - accg_h[2 * j + 1];
+            metric_out[j] = whole ? g / (double)nk / det : g;
+        }
     }
     if (report) {
         float ms = 0.f;
@@ -779,6 +803,90 @@ int tbg_hall_sums_range(const tbg_model* m, const int64_t* kmesh, int64_t k_begi
                         int precision, double* sums_out, tbg_report* report) {
     return hall_impl(m, kmesh, k_begin, k_count, false, dirs2, nmu, mu, T, eta, spin, precision, sums_out,
                      report);
+}
+
+int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max, int64_t E_n, double sigma,
+            double* E_out, double* dos_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    // model_physics.rs:187-205 order: energy range, bin count, width; then gen_kmesh
+    if (E_min >= E_max)
+    {
+        char msg[96];
+        std::snprintf(msg, sizeof(msg), "Invalid energy range: min=%.17g, max=%.17g", E_min, E_max);
+        return set_error(TBG_E_INVALID_ENERGY_RANGE, msg);
+    }
+    if (E_n <= 0)
+        return set_error(TBG_E_INVALID_DOS_PARAMETER, "E_n: number of energy bins must be at least 1");
+    if (!std::isfinite(sigma) || sigma <= 0.0)
+        return set_error(TBG_E_INVALID_DOS_PARAMETER, "sigma: Gaussian smearing width must be finite and positive");
+    if (!kmesh) return set_error(TBG_E_INVALID_ARGUMENT, "null k-mesh");
+    int64_t nk = 1;
+    for (int d = 0; d < M.dim; ++d) {
+        if (kmesh[d] <= 0) return set_error(TBG_E_INVALID_KMESH, "Invalid k-point mesh dimensions");
+        nk *= kmesh[d];
+    }
+    if (E_n > (int64_t(1) << 30)) return set_error(TBG_E_UNSUPPORTED, "E_n > 2^30 is not supported");
+    if (!dos_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    // ndarray linspace: E_i = E_min + i step, step = (E_max - E_min) / (E_n - 1)
+    const double step = E_n > 1 ? (E_max - E_min) / (double)(E_n - 1) : 0.0;
+    if (E_out)
+        for (int64_t i = 0; i < E_n; ++i) E_out[i] = E_min + step * (double)i;
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    const bool small = N <= kSmallMaxN;
+    Ctx ctx;
+    const int64_t chunk = choose_chunk(nk, (small ? 0 : sizeof(zc) * NN) + 16 * N + 64);
+    const int slices = dos_slices(E_n, chunk * N);
+    double* k_d = small ? nullptr : ctx.alloc<double>(chunk * M.dim);
+    zc* H = small ? nullptr : ctx.alloc<zc>(chunk * NN);
+    double* E = ctx.alloc<double>(chunk * N);
+    double* dirs_d = small ? ctx.alloc<double>(2 * M.dim) : nullptr;
+    double* part = ctx.alloc<double>((int64_t)slices * E_n);
+    double* acc = ctx.alloc<double>(2 * E_n);
+    int* status_d = ctx.alloc<int>(1);
+    if (ctx.rc) return ctx.rc;
+    TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
+    TBG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 2 * E_n, ctx.st));
+    if (dirs_d) TBG_CUDA(cudaMemsetAsync(dirs_d, 0, sizeof(double) * 2 * M.dim, ctx.st));
+    const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
+    for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
+        const int64_t nkc = std::min(chunk, nk - c0);
+        if (small) {
+            // the fused small-model kernel returns the band energies alongside its (unused) curvature
+            if ((rc = small_fused(M, ctx.st, nkc, nullptr, c0, kmesh, dirs_d, -1, 0.0, 0, nullptr, 0.0, nullptr, E,
+                                  nullptr)))
+                return rc;
+        } else {
+            kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, M.dim, n0, n1, n2, k_d);
+            TBG_LAUNCHED("kmesh_kernel");
+            if ((rc = fourier_direct(M, ctx.st, nkc, k_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0))) return rc;
+            if ((rc = eig_batched(ctx.st, N, nkc, H, E, nullptr, nullptr, 0, status_d))) return rc;
+        }
+        if ((rc = dos_accumulate(ctx.st, nkc * N, E, E_n, E_min, step, sigma, part, slices, acc))) return rc;
+    }
+    std::vector<double> acc_h(2 * E_n);
+    TBG_CUDA(cudaMemcpyAsync(acc_h.data(), acc, sizeof(double) * 2 * E_n, cudaMemcpyDeviceToHost, ctx.st));
+    if (ctx.sync("tbg_dos")) return ctx.rc;
+    if ((rc = check_status(status_d, ctx.st))) return rc;
+    for (int64_t i = 0; i < E_n; ++i) dos_out[i] = (acc_h[2 * i] - acc_h[2 * i + 1]) / (double)nk;
+    return TBG_OK;
+}
+
+int tbg_quantum_geometry(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, double eta,
+                         int precision, double* metric_out, double* berry_out, double* E_out) {
+    if (nk > 0 && (!metric_out || !berry_out)) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    // the quantum-geometry kernel always uses the charge current (spin ignored)
+    return berry_common(m, nk, k, dirs2, -1, eta, precision, berry_out, E_out, 0, nullptr, 0.0, nullptr,
+                        metric_out);
+}
+
+int tbg_quantum_geometry_mesh(const tbg_model* m, const int64_t* kmesh, const double* dirs2, int64_t nmu,
+                              const double* mu, double T, double eta, int precision, double* metric_out,
+                              double* berry_out, tbg_report* report) {
+    if (!metric_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    return hall_impl(m, kmesh, 0, 0, true, dirs2, nmu, mu, T, eta, -1, precision, berry_out, report, metric_out);
 }
 
 }  // extern "C"

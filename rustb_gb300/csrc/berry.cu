@@ -86,9 +86,12 @@ __global__ void __launch_bounds__(256) zgemm_batched_kernel(int N, const zc* __r
 }
 
 // Omega_n = sum_{m != n} -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2), one warp per row n.
+// With MET, also the quantum metric g_n = sum_{m != n} Re(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2)
+// (src/quantum_geometry.rs:160-187: the real part of the same tensor).
+template <bool MET>
 __global__ void berry_kernel(int N, int64_t batch, const zc* __restrict__ Bx, const zc* __restrict__ By,
                              int64_t ldB, const double* __restrict__ E, double eta2,
-                             double* __restrict__ Omega) {
+                             double* __restrict__ Omega, double* __restrict__ Met) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -99,18 +102,26 @@ __global__ void berry_kernel(int N, int64_t batch, const zc* __restrict__ Bx, co
         const zc* by = By + b * ldB;
         const double* Eb = E + b * N;
         const double en = Eb[n];
-        double s = 0.0;
+        double s = 0.0, g = 0.0;
         for (int m = lane; m < N; m += 32) {
             if (m == n) continue;
             const zc kx = bx[m];
             const zc ky = by[(int64_t)m * N + n];
             const double im = kx.re * ky.im + kx.im * ky.re;
             const double de = en - Eb[m];
-            s += -2.0 * im / (de * de + eta2);
+            const double den = de * de + eta2;
+            s += -2.0 * im / den;
+            if (MET) g += (kx.re * ky.re - kx.im * ky.im) / den;
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) Omega[b * N + n] = s;
+        for (int o = 16; o > 0; o >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (MET) g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        if (lane == 0) {
+            Omega[b * N + n] = s;
+            if (MET) Met[b * N + n] = g;
+        }
     }
 }
 
@@ -294,9 +305,21 @@ int z_to_pairs(cudaStream_t st, int64_t nb, int64_t N2, const zc* in, int64_t ld
     return TBG_OK;
 }
 
-// Bx = U^H (Vx U), By = U^H (Vy U) written over Vx / Vy, then Omega.
+static int launch_berry(cudaStream_t st, int N, int64_t batch, const zc* Bx, const zc* By, int64_t ldB, const double* E,
+                  double eta, double* Omega, double* Met) {
+    KTimer kt(st, "berry_kernel");
+    const unsigned g = grid_for(batch * N * 32, 256);
+    if (Met)
+        berry_kernel<true><<<g, 256, 0, st>>>(N, batch, Bx, By, ldB, E, eta * eta, Omega, Met);
+    else
+        berry_kernel<false><<<g, 256, 0, st>>>(N, batch, Bx, By, ldB, E, eta * eta, Omega, nullptr);
+    TBG_LAUNCHED("berry_kernel");
+    return TBG_OK;
+}
+
+// Bx = U^H (Vx U), By = U^H (Vy U) written over Vx / Vy, then Omega (and the metric when Met is given).
 int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* Vx, const zc* Vy, int64_t ldV,
-                 const double* E, double eta, double* Omega, zc* scratch) {
+                 const double* E, double eta, double* Omega, zc* scratch, double* Met) {
     const int64_t NN = (int64_t)N * N;
     zc* Vxm = const_cast<zc*>(Vx);
     zc* Vym = const_cast<zc*>(Vy);
@@ -309,18 +332,12 @@ int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* V
     if (rc) return rc;
     rc = zgemm_batched(st, N, batch, true, U, NN, scratch, NN, Vym, ldV);
     if (rc) return rc;
-    KTimer kt(st, "berry_kernel");
-    berry_kernel<<<grid_for(batch * N * 32, 256), 256, 0, st>>>(N, batch, Vx, Vy, ldV, E, eta * eta, Omega);
-    TBG_LAUNCHED("berry_kernel");
-    return TBG_OK;
+    return launch_berry(st, N, batch, Vx, Vy, ldV, E, eta, Omega, Met);
 }
 
 int berry_from_bands(cudaStream_t st, int N, int64_t batch, const zc* Bx, const zc* By, int64_t ldB,
                      const double* E, double eta, double* Omega) {
-    KTimer kt(st, "berry_kernel");
-    berry_kernel<<<grid_for(batch * N * 32, 256), 256, 0, st>>>(N, batch, Bx, By, ldB, E, eta * eta, Omega);
-    TBG_LAUNCHED("berry_kernel");
-    return TBG_OK;
+    return launch_berry(st, N, batch, Bx, By, ldB, E, eta, Omega, nullptr);
 }
 
 int occupation_sums(cudaStream_t st, int N, int64_t batch, const double* Omega, const double* E, int nmu,

@@ -276,9 +276,11 @@ __device__ __forceinline__ float2 df_warp_sum(float2 s) {
 // arithmetic.  By is Hermitian, so By[m,n] = conj(By[n,m]) and both operands
 // are read along row n.  One warp per row n; E of the matrix as pairs in
 // shared memory.
+template <bool MET>
 __global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, const float4* __restrict__ Bx,
                                                        const float4* __restrict__ By, const double* __restrict__ E,
-                                                       float2 eta2, double* __restrict__ Omega) {
+                                                       float2 eta2, double* __restrict__ Omega,
+                                                       double* __restrict__ Met) {
     extern __shared__ float2 e2s[];  // N
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int NN = N * N;
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, con
             const float4* bx = Bx + b * NN + n * N;
             const float4* by = By + b * NN + n * N;
             const float2 en = e2s[n];
-            float2 s = make_float2(0.f, 0.f);
+            float2 s = make_float2(0.f, 0.f), g = make_float2(0.f, 0.f);
             for (int m = lane; m < N; m += 32) {
                 if (m == n) continue;
                 const float4 x = bx[m];
@@ -303,18 +305,31 @@ __global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, con
                 const float2 den = df_add(df_mul(de, de), eta2);
                 const float2 q = df_div(num, den);
                 s = df_add(s, make_float2(-2.f * q.x, -2.f * q.y));
+                if (MET) {
+                    // Re(x conj(y)) = x_re y_re + x_im y_im
+                    const float2 r = df_add(df_mul(make_float2(x.x, x.y), make_float2(y.x, y.y)),
+                                            df_mul(make_float2(x.z, x.w), make_float2(y.z, y.w)));
+                    g = df_add(g, df_div(r, den));
+                }
             }
             s = df_warp_sum(s);
-            if (lane == 0) Omega[b * N + n] = df_to_double(s);
+            if (MET) g = df_warp_sum(g);
+            if (lane == 0) {
+                Omega[b * N + n] = df_to_double(s);
+                if (MET) Met[b * N + n] = df_to_double(g);
+            }
         }
     }
 }
 
-// Keep E ascending (with Omega) after refinement; a no-op when already sorted.
-__global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, double* __restrict__ Om) {
+// Keep E ascending (with Omega and, when given, the metric) after refinement;
+// a no-op when already sorted.
+__global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, double* __restrict__ Om,
+                                 double* __restrict__ Met) {
     extern __shared__ double sm3[];
     double* e = sm3;
     double* o = sm3 + N;
+    double* g = sm3 + 2 * N;
     __shared__ int s_sorted;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         if (threadIdx.x == 0) s_sorted = 1;
@@ -322,6 +337,7 @@ __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, d
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
             e[i] = E[b * N + i];
             o[i] = Om[b * N + i];
+            if (Met) g[i] = Met[b * N + i];
         }
         __syncthreads();
         for (int i = threadIdx.x; i < N - 1; i += blockDim.x)
@@ -333,6 +349,7 @@ __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, d
                 for (int j = 0; j < N; ++j) rank += (e[j] < e[i]) || (e[j] == e[i] && j < i);
                 E[b * N + rank] = e[i];
                 Om[b * N + rank] = o[i];
+                if (Met) Met[b * N + rank] = g[i];
             }
         }
         __syncthreads();
@@ -352,10 +369,11 @@ size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
            ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) + 4096;
 }
 
-// H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega.
+// H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega and, when Met is
+// not null, the quantum metric.
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d) {
+                int64_t* clusters_d, double* Met) {
     if (batch <= 0) return TBG_OK;
     const int64_t NN = (int64_t)N * N;
     if (work_bytes < mixed_berry_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
@@ -433,12 +451,15 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         const double e2 = eta * eta;
         const float hi = (float)e2;
         const float2 eta2 = make_float2(hi, (float)(e2 - (double)hi));
-        berry_df_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, sizeof(float2) * N, st>>>(N, batch, bD, bE,
-                                                                                                    E, eta2, Om);
+        const unsigned g = (unsigned)std::min<int64_t>(batch, 152 * 8);
+        if (Met)
+            berry_df_kernel<true><<<g, 256, sizeof(float2) * N, st>>>(N, batch, bD, bE, E, eta2, Om, Met);
+        else
+            berry_df_kernel<false><<<g, 256, sizeof(float2) * N, st>>>(N, batch, bD, bE, E, eta2, Om, nullptr);
         TBG_LAUNCHED("berry_df_kernel");
     }
-    sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 2 * sizeof(double) * N, st>>>(N, batch, E,
-                                                                                                      Om);
+    sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 3 * sizeof(double) * N, st>>>(N, batch, E,
+                                                                                                      Om, Met);
     TBG_LAUNCHED("sort_e_om_kernel");
     return TBG_OK;
 }

@@ -3,7 +3,8 @@
 // registers / local memory, FP64:
 //   H, V_0, V_1 by the Fourier sum over R with the Atom gauge and tau term
 //   (src/velocity.rs:538-622), optional spin dressing (traits.rs:170-175),
-//   eigenpairs by cyclic complex Jacobi, U^H V U, Omega_n, and the
+//   eigenpairs by cyclic complex Jacobi, U^H V U, Omega_n (and optionally
+//   the quantum metric, src/quantum_geometry.rs:160-187), and the
 //   occupation sums per chemical potential (linear/mod.rs:204-223).
 // For nsta <= 8 the per-k work is a few thousand flops, so one launch covers
 // tens of thousands of k-points and the batched per-matrix kernels would be
@@ -32,10 +33,11 @@ __device__ __forceinline__ double fermi_s(double e, double mu, double width) {
 // Cyclic complex Jacobi on the Hermitian NM x NM (active N) matrix A; W gets
 // the eigenvectors in columns.  Rotation: G = diag(1, e^{-i phi}) [[c,-s],[s,c]]
 // with e^{i phi} = a_pq / |a_pq|, tan 2 theta = 2 |a_pq| / (a_pp - a_qq).
-template <int NM>
+template <int NM, bool WANT_W>
 __device__ void jacobi(int N, zc (&A)[NM][NM], zc (&W)[NM][NM]) {
-    for (int i = 0; i < NM; ++i)
-        for (int j = 0; j < NM; ++j) W[i][j] = mk(i == j ? 1.0 : 0.0, 0.0);
+    if (WANT_W)
+        for (int i = 0; i < NM; ++i)
+            for (int j = 0; j < NM; ++j) W[i][j] = mk(i == j ? 1.0 : 0.0, 0.0);
     for (int sweep = 0; sweep < 40; ++sweep) {
         double off = 0.0, dia = 0.0;
         for (int i = 0; i < N; ++i)
@@ -71,22 +73,24 @@ __device__ void jacobi(int N, zc (&A)[NM][NM], zc (&W)[NM][NM]) {
                 A[q][p] = mk(0.0, 0.0);
                 A[p][p].im = 0.0;
                 A[q][q].im = 0.0;
-                for (int k = 0; k < N; ++k) {
-                    const zc wkp = W[k][p], wkq = emi * W[k][q];
-                    W[k][p] = cs * wkp + sn * wkq;
-                    W[k][q] = cs * wkq - sn * wkp;
-                }
+                if (WANT_W)
+                    for (int k = 0; k < N; ++k) {
+                        const zc wkp = W[k][p], wkq = emi * W[k][q];
+                        W[k][p] = cs * wkp + sn * wkq;
+                        W[k][q] = cs * wkq - sn * wkp;
+                    }
             }
     }
 }
 
-template <int NM>
+// VALS: band energies only (E_out); no velocities, eigenvectors or curvature.
+template <int NM, bool VALS>
 __global__ void __launch_bounds__(128) small_fused_kernel(
     int N, int norb, int dim, int nR, int64_t nk, const double* __restrict__ klist, int64_t k0, int64_t n0,
     int64_t n1, int64_t n2, const zc* __restrict__ ham, const int* __restrict__ hamR, const double* __restrict__ Rcart,
     const double* __restrict__ tau, const double* __restrict__ taucart, const double* __restrict__ dirs, int spin,
     double eta, int nmu, const double* __restrict__ mu, double width, double* __restrict__ Om_out,
-    double* __restrict__ E_out, double* __restrict__ S_out) {
+    double* __restrict__ E_out, double* __restrict__ S_out, double* __restrict__ Met_out, double* __restrict__ SM_out) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nk) return;
     double kv[3] = {0.0, 0.0, 0.0};
@@ -118,6 +122,12 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
         double sn, cs;
         sincos(kTwoPiS * s, &sn, &cs);
         const zc u = mk(cs, sn);
+        const zc* hr = ham + (int64_t)r * N * N;
+        if (VALS) {
+            for (int i = 0; i < N; ++i)
+                for (int j = 0; j < N; ++j) H[i][j] = H[i][j] + u * hr[i * N + j];
+            continue;
+        }
         const double* rc = Rcart + 3 * r;
         double c0 = w0[0] * rc[0], c1 = w1[0] * rc[0];
         if (dim > 1) {
@@ -128,7 +138,6 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
             c0 += w0[2] * rc[2];
             c1 += w1[2] * rc[2];
         }
-        const zc* hr = ham + (int64_t)r * N * N;
         for (int i = 0; i < N; ++i)
             for (int j = 0; j < N; ++j) {
                 const zc tt = u * hr[i * N + j];
@@ -148,6 +157,7 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
         double sn, cs;
         sincos(kTwoPiS * a, &sn, &cs);
         ph[s] = mk(cs, sn);
+        if (VALS) continue;
         const double* tc = taucart + 3 * s;
         double p0 = w0[0] * tc[0], p1 = w1[0] * tc[0];
         if (dim > 1) {
@@ -165,12 +175,16 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
         for (int n = 0; n < N; ++n) {
             const zc g = cmul(ph[m], ph[n]);
             const zc hl = H[m][n];
+            if (VALS) {
+                H[m][n] = hl * g;
+                continue;
+            }
             const double d0 = tp0[n] - tp0[m], d1 = tp1[n] - tp1[m];
             V0[m][n] = (V0[m][n] + mk(-d0 * hl.im, d0 * hl.re)) * g;
             V1[m][n] = (V1[m][n] + mk(-d1 * hl.im, d1 * hl.re)) * g;
             H[m][n] = hl * g;
         }
-    if (spin >= 0) {  // J = 1/2 (S V0 + V0 S), S = sigma (x) I / 2
+    if (!VALS && spin >= 0) {  // J = 1/2 (S V0 + V0 S), S = sigma (x) I / 2
         zc J[NM][NM];
         for (int i = 0; i < N; ++i)
             for (int j = 0; j < N; ++j) {
@@ -200,7 +214,7 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
             for (int j = 0; j < N; ++j) V0[i][j] = J[i][j];
     }
     zc W[NM][NM];
-    jacobi<NM>(N, H, W);
+    jacobi<NM, !VALS>(N, H, W);
     double E[NM];
     int ord[NM];
     for (int i = 0; i < N; ++i) {
@@ -215,6 +229,10 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
             --j;
         }
         ord[j + 1] = oi;
+    }
+    if (VALS) {
+        for (int i = 0; i < N; ++i) E_out[t * N + i] = E[ord[i]];
+        return;
     }
     // band-basis velocities B = W^H V W (H reused as scratch)
     zc Bx[NM][NM], By[NM][NM];
@@ -234,26 +252,36 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
             By[a][b] = sy;
         }
     const double eta2 = eta * eta;
-    double Om[NM];
+    const bool met = Met_out || SM_out;
+    double Om[NM], G[NM];
     for (int a = 0; a < N; ++a) {
-        double v = 0.0;
+        double v = 0.0, g = 0.0;
         for (int b = 0; b < N; ++b) {
             if (a == b) continue;
             const double im = Bx[a][b].re * By[b][a].im + Bx[a][b].im * By[b][a].re;
             const double de = E[a] - E[b];
-            v += -2.0 * im / (de * de + eta2);
+            const double den = de * de + eta2;
+            v += -2.0 * im / den;
+            if (met) g += (Bx[a][b].re * By[b][a].re - Bx[a][b].im * By[b][a].im) / den;
         }
         Om[a] = v;
+        G[a] = g;
     }
     for (int i = 0; i < N; ++i) {
         if (Om_out) Om_out[t * N + i] = Om[ord[i]];
         if (E_out) E_out[t * N + i] = E[ord[i]];
+        if (Met_out) Met_out[t * N + i] = G[ord[i]];
     }
     if (S_out) {
         for (int j = 0; j < nmu; ++j) {
-            double s = 0.0;
-            for (int i = 0; i < N; ++i) s += Om[ord[i]] * fermi_s(E[ord[i]], mu[j], width);
+            double s = 0.0, sg = 0.0;
+            for (int i = 0; i < N; ++i) {
+                const double f = fermi_s(E[ord[i]], mu[j], width);
+                s += Om[ord[i]] * f;
+                sg += G[ord[i]] * f;
+            }
             S_out[t * nmu + j] = s;
+            if (SM_out) SM_out[t * nmu + j] = sg;
         }
     }
 }
@@ -262,17 +290,27 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
 
 int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* klist_d, int64_t k0,
                 const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
-                double width, double* Om, double* E, double* S) {
+                double width, double* Om, double* E, double* S, double* Met, double* SM) {
     if (nk <= 0) return TBG_OK;
     const int N = (int)m.nsta;
     const int64_t n0 = kmesh ? kmesh[0] : 1, n1 = (kmesh && m.dim > 1) ? kmesh[1] : 1,
                   n2 = (kmesh && m.dim > 2) ? kmesh[2] : 1;
     const unsigned blocks = (unsigned)((nk + 127) / 128);
     KTimer kt(st, "small_fused_kernel");
-#define SMALL_LAUNCH(NM)                                                                                          \
-    small_fused_kernel<NM><<<blocks, 128, 0, st>>>(N, (int)m.norb, m.dim, (int)m.nR, nk, klist_d, k0, n0, n1, n2, \
-                                                   m.ham, m.hamR_d, m.Rcart_d, m.tau_d, m.taucart_d, dirs_d, spin,  \
-                                                   eta, nmu, mu_d, width, Om, E, S)
+    // energies only when nothing else is asked for
+    const bool vals = !Om && !S && !Met && !SM;
+    if (vals && !E) return TBG_OK;
+#define SMALL_LAUNCH(NM)                                                                                             \
+    do {                                                                                                             \
+        if (vals)                                                                                                    \
+            small_fused_kernel<NM, true><<<blocks, 128, 0, st>>>(                                                    \
+                N, (int)m.norb, m.dim, (int)m.nR, nk, klist_d, k0, n0, n1, n2, m.ham, m.hamR_d, m.Rcart_d, m.tau_d, \
+                m.taucart_d, dirs_d, spin, eta, nmu, mu_d, width, Om, E, S, Met, SM);                               \
+        else                                                                                                         \
+            small_fused_kernel<NM, false><<<blocks, 128, 0, st>>>(                                                   \
+                N, (int)m.norb, m.dim, (int)m.nR, nk, klist_d, k0, n0, n1, n2, m.ham, m.hamR_d, m.Rcart_d, m.tau_d, \
+                m.taucart_d, dirs_d, spin, eta, nmu, mu_d, width, Om, E, S, Met, SM);                               \
+    } while (0)
     if (N <= 2)
         SMALL_LAUNCH(2);
     else if (N <= 4)

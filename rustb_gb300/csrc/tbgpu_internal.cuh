@@ -205,9 +205,10 @@ int spin_dress(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, zc
                zc* scratch);
 
 // Rotation into the eigenbasis + band-resolved Berry curvature:
-// Omega (batch, N) from U (batch, N, N), Vx/Vy (batch strided), E.
+// Omega (batch, N) from U (batch, N, N), Vx/Vy (batch strided), E; the
+// quantum metric (batch, N) too when Met is not null.
 int berry_rotate(cudaStream_t st, int N, int64_t batch, const zc* U, const zc* Vx, const zc* Vy,
-                 int64_t ldV, const double* E, double eta, double* Omega, zc* scratch);
+                 int64_t ldV, const double* E, double eta, double* Omega, zc* scratch, double* Met = nullptr);
 
 // Occupation-weighted sums: per k and per mu -> S (batch, nmu).
 int occupation_sums(cudaStream_t st, int N, int64_t batch, const double* Omega, const double* E,
@@ -222,8 +223,15 @@ int kahan_column_sums(cudaStream_t st, int64_t nk, int nmu, const double* S, dou
 // null, the mesh points [k0, k0 + nk) of kmesh.
 int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* klist_d, int64_t k0,
                 const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
-                double width, double* Om, double* E, double* S);
+                double width, double* Om, double* E, double* S, double* Met = nullptr, double* SM = nullptr);
 constexpr int kSmallMaxN = 8;
+
+// Gaussian-smeared DOS: add the terms of count band energies ev (device) to
+// the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds
+// slices * E_n doubles; slices from dos_slices(E_n, chunk energies).
+int dos_slices(int64_t E_n, int64_t count);
+int dos_accumulate(cudaStream_t st, int64_t count, const double* ev, int64_t E_n, double E_min, double step,
+                   double sigma, double* part, int slices, double* acc);
 
 // ------------------------------------------------------------- mixed path --
 // FP32 solver: H (FP64) or, when Hpair is given, float pairs
@@ -235,7 +243,7 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d);
+                int64_t* clusters_d, double* Met = nullptr);
 // Spin-current dressing of float-pair velocities (V_0 blocks, batch stride ldV).
 int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
                      float4* scratch);

@@ -20,6 +20,8 @@ TBG_E_LINALG = 6
 TBG_E_INVALID_DIMENSION = 7
 TBG_E_INVALID_MODEL = 8
 TBG_E_INVALID_ARGUMENT = 9
+TBG_E_INVALID_ENERGY_RANGE = 10
+TBG_E_INVALID_DOS_PARAMETER = 11
 TBG_E_CUDA = 20
 TBG_E_NOCONV = 21
 TBG_E_TIMEOUT = 22
@@ -85,6 +87,18 @@ class InvalidModel(TbError):
     code = TBG_E_INVALID_MODEL
 
 
+class InvalidEnergyRange(TbError):
+    """``TbError::InvalidEnergyRange`` (model_physics.rs:187-192)."""
+
+    code = TBG_E_INVALID_ENERGY_RANGE
+
+
+class InvalidDosParameter(TbError):
+    """``TbError::InvalidDosParameter`` (model_physics.rs:193-204)."""
+
+    code = TBG_E_INVALID_DOS_PARAMETER
+
+
 class TbPanic(TbError):
     """A condition on which the reference panics (assert!/todo!)."""
 
@@ -107,6 +121,8 @@ _BY_CODE = {
     TBG_E_INVALID_DIMENSION: InvalidDimension,
     TBG_E_INVALID_MODEL: InvalidModel,
     TBG_E_INVALID_ARGUMENT: TbPanic,
+    TBG_E_INVALID_ENERGY_RANGE: InvalidEnergyRange,
+    TBG_E_INVALID_DOS_PARAMETER: InvalidDosParameter,
     TBG_E_CUDA: DeviceError,
     TBG_E_NOCONV: DeviceError,
     TBG_E_TIMEOUT: DeviceError,

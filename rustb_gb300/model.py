@@ -8,8 +8,8 @@ spin decoration follows ``update_hamiltonian!`` / ``add_hamiltonian!``
 (model_build.rs:43-118: sigma_y writes +i t to [i+N, j] and -i t to [i, j+N]).
 
 The k-mesh methods (``gen_ham``, ``gen_v``, ``gen_v_projected``, the ``Solve``
-family, the ``BerryCurvature`` family and ``hall_conductivity``) run on the
-GPU through ``libtbgpu.so``; the model's arrays are uploaded once and kept
+family, the ``BerryCurvature`` family, ``hall_conductivity``, the
+``QuantumGeometry`` family and ``dos``) run on the GPU through ``libtbgpu.so``; the model's arrays are uploaded once and kept
 resident until the model is modified.
 """
 
@@ -20,8 +20,9 @@ import ctypes
 import numpy as np
 
 from . import _lib, errors
-from .params import (Gauge, HallConductivityResult, BandBerryCurvature, Integration, Parameters,
-                     Precision, SpinDirection, spin_code, validate_broadening,
+from .params import (Gauge, HallConductivityResult, BandBerryCurvature, BandQuantumGeometry, Integration,
+                     Parameters, Precision, QuantumGeometryMap, QuantumGeometryResult, SpinDirection,
+                     spin_code, validate_broadening,
                      validate_chemical_potentials, validate_direction_matrix, validate_temperature)
 
 
@@ -373,3 +374,86 @@ class Model:
         if report is not None:
             report.update(rep.as_dict())
         return HallConductivityResult(chemical_potentials=params.mu.copy(), conductivity=sigma)
+
+    # ------------------------------------------------------- QuantumGeometry
+    def quantum_geometry_on(self, k_points, params: Parameters, precision=Precision.FP64) -> QuantumGeometryMap:
+        """``QuantumGeometry::quantum_geometry_on`` (src/quantum_geometry.rs:104-138):
+        band-resolved metric, Berry curvature and energies, each (nk, nsta)."""
+        k = np.asarray(k_points, dtype=np.float64)
+        if k.ndim != 2 or k.shape[1] != self.dim:
+            raise errors.DimensionMismatch(
+                f"quantum geometry k-points: expected {self.dim}, got {k.shape[-1] if k.ndim else 0}")
+        validate_direction_matrix(params.direction, 2, self.dim)
+        validate_broadening(params.eta)
+        k = np.ascontiguousarray(k)
+        nk = k.shape[0]
+        g = np.empty((nk, self.nsta))
+        om = np.empty((nk, self.nsta))
+        E = np.empty((nk, self.nsta))
+        d = _lib.as_f64(params.direction)
+        lib = _lib.load()
+        _lib.check(lib.tbg_quantum_geometry(self.device_handle(), nk, _lib.dptr(k), _lib.dptr(d),
+                                            float(params.eta), int(precision), _lib.dptr(g), _lib.dptr(om),
+                                            _lib.dptr(E)), lib)
+        return QuantumGeometryMap(metric=g, berry_curvature=om, energies=E)
+
+    def quantum_geometry_at(self, k, params: Parameters, precision=Precision.FP64) -> BandQuantumGeometry:
+        """``QuantumGeometry::quantum_geometry_at`` (src/quantum_geometry.rs:88-102)."""
+        k = np.asarray(k, dtype=np.float64).reshape(-1)
+        if len(k) != self.dim:
+            raise errors.KVectorLengthMismatch(f"expected {self.dim}, actual {len(k)}")
+        r = self.quantum_geometry_on(k[None, :], params, precision)
+        return BandQuantumGeometry(metric=r.metric[0], berry_curvature=r.berry_curvature[0], energies=r.energies[0])
+
+    def quantum_geometry(self, params: Parameters, precision=Precision.FP64,
+                         report: dict | None = None) -> QuantumGeometryResult:
+        """``Model::quantum_geometry`` (src/quantum_geometry.rs:196-240), Direct
+        integration; EnergyCut is rejected as in the reference, Simplex is not
+        provided by the GPU library."""
+        params.validate_rank2(self.dim)
+        if params.integration == Integration.EnergyCut:
+            raise errors.InvalidResponseParameter(
+                "integration: quantum_geometry supports Integration::Direct or Simplex, not EnergyCut")
+        if params.integration == Integration.Simplex:
+            if self.dim == 1:
+                raise errors.InvalidDimension(f"dimension {self.dim} is not supported; supported: [2, 3]")
+            raise errors.TbPanic("Integration::Simplex is not provided by the GPU library")
+        kmesh = np.ascontiguousarray(np.asarray(params.kmesh, dtype=np.int64))
+        mu = _lib.as_f64(params.mu)
+        d = _lib.as_f64(params.direction)
+        g = np.empty(len(mu))
+        om = np.empty(len(mu))
+        rep = _lib.TbgReport()
+        lib = _lib.load()
+        _lib.check(lib.tbg_quantum_geometry_mesh(self.device_handle(), _lib.iptr(kmesh), _lib.dptr(d), len(mu),
+                                                 _lib.dptr(mu), float(params.T[0]), float(params.eta),
+                                                 int(precision), _lib.dptr(g), _lib.dptr(om), ctypes.byref(rep)),
+                   lib)
+        if report is not None:
+            report.update(rep.as_dict())
+        return QuantumGeometryResult(chemical_potentials=params.mu.copy(), metric=g, berry_curvature=om)
+
+    # ------------------------------------------------------------------- DOS
+    def dos(self, k_mesh, E_min: float, E_max: float, E_n: int, sigma: float):
+        """``Model::dos`` (src/model_physics.rs:179-230): Gaussian-smeared
+        density of states on the uniform mesh; returns ``(energies, dos)``."""
+        E_min = float(E_min)
+        E_max = float(E_max)
+        sigma = float(sigma)
+        if E_min >= E_max:
+            raise errors.InvalidEnergyRange(f"Invalid energy range: min={E_min}, max={E_max}")
+        if int(E_n) <= 0:
+            raise errors.InvalidDosParameter("E_n: number of energy bins must be at least 1")
+        if not np.isfinite(sigma) or sigma <= 0.0:
+            raise errors.InvalidDosParameter("sigma: Gaussian smearing width must be finite and positive")
+        kmesh = np.ascontiguousarray(np.asarray(k_mesh, dtype=np.int64).reshape(-1))
+        if kmesh.size == 0 or np.any(kmesh <= 0):
+            raise errors.InvalidKmeshDimensions(f"Invalid k-point mesh dimensions: {kmesh.tolist()}")
+        if kmesh.size != self.dim:
+            raise errors.TbPanic(f"k-mesh has {kmesh.size} entries, the model has dimension {self.dim}")
+        E = np.empty(int(E_n))
+        out = np.empty(int(E_n))
+        lib = _lib.load()
+        _lib.check(lib.tbg_dos(self.device_handle(), _lib.iptr(kmesh), E_min, E_max, int(E_n), sigma,
+                               _lib.dptr(E), _lib.dptr(out)), lib)
+        return E, out

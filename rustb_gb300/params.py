@@ -176,3 +176,32 @@ class HallConductivityResult:
 
     chemical_potentials: np.ndarray
     conductivity: np.ndarray
+
+
+@dataclass
+class BandQuantumGeometry:
+    """``BandQuantumGeometry`` (src/quantum_geometry.rs:30-39)."""
+
+    metric: np.ndarray
+    berry_curvature: np.ndarray
+    energies: np.ndarray
+
+
+@dataclass
+class QuantumGeometryMap:
+    """``QuantumGeometryMap`` (src/quantum_geometry.rs:41-50): each (nk, nsta)."""
+
+    metric: np.ndarray
+    berry_curvature: np.ndarray
+    energies: np.ndarray
+
+
+@dataclass
+class QuantumGeometryResult:
+    """``QuantumGeometryResult`` (src/quantum_geometry.rs:52-63); ``diagnostics``
+    is set by Simplex integration only, which this library does not provide."""
+
+    chemical_potentials: np.ndarray
+    metric: np.ndarray
+    berry_curvature: np.ndarray
+    diagnostics: object = None

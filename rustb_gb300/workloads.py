@@ -14,6 +14,9 @@
   the batched uneven workload draws its models from it.
 * :func:`supercell_2d` -- 1024-orbital square supercell, R in {-1,0,1}^2,
   t_ij(R) = exp(-d_ij/0.8) (N(0,1)+iN(0,1))/sqrt2, onsite U(-0.5, 0.5).
+* :func:`honeycomb_small` -- the two-band honeycomb model Rustb's benchmarks
+  use for ``dos`` (benches/bench_main.rs:15-25): lattice [1,0],[1/2,sqrt3/2],
+  orbitals (1/3,1/3),(2/3,2/3), onsite -0.7/+0.7, t = -1 on R = (0,0),(-1,0),(0,-1).
 
 Hopping tables are stored the way ``add_hop`` stores them: R = 0 first, then
 each R immediately followed by -R with H(-R) = H(R)^dagger.
@@ -29,6 +32,16 @@ import numpy as np
 from .model import Model
 
 SEED_SPINFUL_3D = 20260101
+
+
+def honeycomb_small() -> Model:
+    s3 = math.sqrt(3.0)
+    model = Model.tb_model([[1.0, 0.0], [0.5, s3 / 2.0]], [[1.0 / 3.0, 1.0 / 3.0], [2.0 / 3.0, 2.0 / 3.0]],
+                           spin=False)
+    model.set_onsite([-0.7, 0.7])
+    for R in [(0, 0), (-1, 0), (0, -1)]:
+        model.add_hop(-1.0, 0, 1, R)
+    return model
 
 
 def haldane_200(t1=-1.0, t2=0.15, m=0.2) -> Model:

@@ -69,3 +69,41 @@ def kane_mele(t=-1.0, soc=-0.06, rashba=0.0) -> Model:
         m.add_hop(-rashba * 1j * r0[1], 1, 1, R, SpinDirection.X)
         m.add_hop(-rashba * 1j * r0[0], 1, 1, R, SpinDirection.Y)
     return m
+
+
+def qwz_2d(mass=-1.0) -> Model:
+    """qwz_model (src/quantum_geometry.rs:298-315)."""
+    m = Model.tb_model(np.eye(2), [[0.0, 0.0], [0.0, 0.0]])
+    m.add_onsite([mass, -mass])
+    m.add_hop(-0.5j, 0, 1, (1, 0))
+    m.add_hop(0.5j, 0, 1, (-1, 0))
+    m.add_hop(-0.5, 0, 1, (0, 1))
+    m.add_hop(0.5, 0, 1, (0, -1))
+    for R in [(1, 0), (-1, 0), (0, 1), (0, -1)]:
+        m.add_hop(0.5, 0, 0, R)
+        m.add_hop(-0.5, 1, 1, R)
+    return m
+
+
+def massive_dirac() -> Model:
+    """massive_dirac_model (src/quantum_geometry.rs:287-296): onsite -0.5, 0.5, no hopping."""
+    m = Model.tb_model(np.eye(2), [[0.0, 0.0], [0.0, 0.0]])
+    m.set_onsite([-0.5, 0.5])
+    return m
+
+
+def bench_small() -> Model:
+    """build_small (benches/bench_main.rs:15-25): honeycomb, onsite -0.7 / 0.7, t = -1."""
+    m = Model.tb_model(HEX_LAT, HEX_ORB)
+    m.set_onsite([-0.7, 0.7])
+    for R in [(0, 0), (-1, 0), (0, -1)]:
+        m.add_hop(-1.0, 0, 1, R)
+    return m
+
+
+def flat_bands(energies, dim=2) -> Model:
+    """Orbitals with on-site energies only: k-independent bands at ``energies``."""
+    n = len(energies)
+    m = Model.tb_model(np.eye(dim), np.zeros((n, dim)))
+    m.set_onsite(list(energies))
+    return m
