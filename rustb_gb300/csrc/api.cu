@@ -837,7 +837,10 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
     const int64_t NN = (int64_t)N * N;
     const bool small = N <= kSmallMaxN;
     Ctx ctx;
-    const int64_t chunk = choose_chunk(nk, (small ? 0 : sizeof(zc) * NN) + 16 * N + 64);
+    // the fused small-model kernel has no batch limit: one chunk of up to 2^21 k-points
+    const int64_t chunk = small ? std::max<int64_t>(1, std::min<int64_t>({nk, int64_t(1) << 21,
+                                                                          chunk_budget_bytes() / (16 * N + 64)}))
+                                : choose_chunk(nk, sizeof(zc) * NN + 16 * N + 64);
     const int slices = dos_slices(E_n, chunk * N);
     double* k_d = small ? nullptr : ctx.alloc<double>(chunk * M.dim);
     zc* H = small ? nullptr : ctx.alloc<zc>(chunk * NN);
@@ -854,7 +857,7 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
     for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
         const int64_t nkc = std::min(chunk, nk - c0);
         if (small) {
-            // the fused small-model kernel returns the band energies alongside its (unused) curvature
+            // the fused small-model kernel in its energies-only form (no velocities or eigenvectors)
             if ((rc = small_fused(M, ctx.st, nkc, nullptr, c0, kmesh, dirs_d, -1, 0.0, 0, nullptr, 0.0, nullptr, E,
                                   nullptr)))
                 return rc;

@@ -149,7 +149,8 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
     // Atom gauge + tau term
     zc ph[NM];
     double tp0[NM], tp1[NM];
-    for (int s = 0; s < N; ++s) {
+    // energies only: the Atom-gauge phase is a unitary similarity and leaves them unchanged
+    for (int s = 0; s < (VALS ? 0 : N); ++s) {
         const double* ts = tau + 3 * s;
         double a = ts[0] * kv[0];
         if (dim > 1) a += ts[1] * kv[1];
@@ -157,7 +158,6 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
         double sn, cs;
         sincos(kTwoPiS * a, &sn, &cs);
         ph[s] = mk(cs, sn);
-        if (VALS) continue;
         const double* tc = taucart + 3 * s;
         double p0 = w0[0] * tc[0], p1 = w1[0] * tc[0];
         if (dim > 1) {
@@ -171,14 +171,10 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
         tp0[s] = p0;
         tp1[s] = p1;
     }
-    for (int m = 0; m < N; ++m)
+    for (int m = 0; m < (VALS ? 0 : N); ++m)
         for (int n = 0; n < N; ++n) {
             const zc g = cmul(ph[m], ph[n]);
             const zc hl = H[m][n];
-            if (VALS) {
-                H[m][n] = hl * g;
-                continue;
-            }
             const double d0 = tp0[n] - tp0[m], d1 = tp1[n] - tp1[m];
             V0[m][n] = (V0[m][n] + mk(-d0 * hl.im, d0 * hl.re)) * g;
             V1[m][n] = (V1[m][n] + mk(-d1 * hl.im, d1 * hl.re)) * g;
