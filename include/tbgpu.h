@@ -204,6 +204,14 @@ int tbg_quantum_geometry_mesh(const tbg_model* m, const int64_t* kmesh,
                               double* metric_out, double* berry_out,
                               tbg_report* report);
 
+/* FP64 band energies (ascending) at every point of the uniform mesh
+ * kmesh[dim], gen_kmesh order (first dimension outermost) -> E_out (nk, nsta).
+ * Replaces: solve_band_all_parallel(&gen_kmesh(k_mesh)) as the mesh consumers
+ * call it -- Model::dos (src/model_physics.rs:206-207), write_bxsf and
+ * show_fermi_surface (src/fermi_surface.rs:454-463, 848-900), write_spin_frmsf
+ * (fermi_surface.rs:637-666). */
+int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out);
+
 /* Density of states with Gaussian smearing on the uniform mesh kmesh[dim]:
  * E_out[i] = E_min + i (E_max - E_min) / (E_n - 1) (E_out may be NULL) and
  *   dos_out[i] = 1/nk sum_{k,n} exp(-((E_i - E_nk) / sigma)^2 / 2) / sigma / sqrt(2 pi),

@@ -8,11 +8,12 @@ C-ABI of ``include/tbgpu.h``; this package is the host-side mirror of Rustb's
 """
 
 from .errors import TbError
+from .fermi import write_spin_frmsf
 from .model import Model
 from .params import (BandBerryCurvature, BandQuantumGeometry, Gauge, HallConductivityResult, Integration,
                      Parameters, Precision, QuantumGeometryMap, QuantumGeometryResult, SpinDirection)
 
 __all__ = ["Model", "Parameters", "Gauge", "SpinDirection", "Integration", "Precision",
            "BandBerryCurvature", "HallConductivityResult", "BandQuantumGeometry", "QuantumGeometryMap",
-           "QuantumGeometryResult", "TbError"]
+           "QuantumGeometryResult", "TbError", "write_spin_frmsf"]
 __version__ = "0.1.0"

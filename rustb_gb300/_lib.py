@@ -100,6 +100,7 @@ SIGNATURES = [
     ("tbg_quantum_geometry_mesh", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p, ctypes.c_int64,
                                                  _c_double_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                                  _c_double_p, _c_double_p, ctypes.POINTER(TbgReport)]),
+    ("tbg_bands_mesh", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p]),
     ("tbg_dos", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                ctypes.c_double, _c_double_p, _c_double_p]),
     ("tbg_measure_fma_peaks", ctypes.c_int, [_c_double_p, _c_double_p]),

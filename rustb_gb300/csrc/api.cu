@@ -332,6 +332,68 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
     return berry_rotate(ctx.st, N, nkc, J.U, J.V, J.V + NN, 2 * NN, J.E, J.eta, J.Om, J.scratch, J.Met);
 }
 
+// FP64 band energies (ascending) on chunks of the uniform mesh, gen_kmesh
+// order: the energies-only fused kernel for nsta <= 8, else the Fourier sum in
+// the Atom gauge and the batched eigensolve (values only) -- the path of
+// solve_band_all_parallel(gen_kmesh(..)) (src/solve_ham.rs:52-62, 94-107).
+struct MeshEnergies {
+    const ModelDev* M = nullptr;
+    const int64_t* kmesh = nullptr;
+    bool small = false;
+    int64_t chunk = 0;
+    double* k_d = nullptr;
+    zc* H = nullptr;
+    double* E = nullptr;  // (chunk, nsta)
+    double* dirs_d = nullptr;
+    int* status_d = nullptr;
+
+    int init(Ctx& ctx, const ModelDev& m, const int64_t* km, int64_t nk, int64_t extra_per_k = 0) {
+        M = &m;
+        kmesh = km;
+        const int N = (int)m.nsta;
+        const int64_t NN = (int64_t)N * N;
+        small = N <= kSmallMaxN;
+        // the fused small-model kernel has no batch limit: one chunk of up to 2^21 k-points
+        chunk = small ? std::max<int64_t>(1, std::min<int64_t>({nk, int64_t(1) << 21,
+                                                                chunk_budget_bytes() / (16 * N + 64 + extra_per_k)}))
+                      : choose_chunk(nk, sizeof(zc) * NN + 16 * N + 64 + extra_per_k);
+        k_d = small ? nullptr : ctx.alloc<double>(chunk * m.dim);
+        H = small ? nullptr : ctx.alloc<zc>(chunk * NN);
+        E = ctx.alloc<double>(chunk * N);
+        dirs_d = small ? ctx.alloc<double>(2 * m.dim) : nullptr;
+        status_d = ctx.alloc<int>(1);
+        if (ctx.rc) return ctx.rc;
+        TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
+        if (dirs_d) TBG_CUDA(cudaMemsetAsync(dirs_d, 0, sizeof(double) * 2 * m.dim, ctx.st));
+        return TBG_OK;
+    }
+
+    int run(Ctx& ctx, int64_t c0, int64_t nkc) {
+        const int N = (int)M->nsta;
+        const int64_t NN = (int64_t)N * N;
+        if (small)  // energies-only form: no velocities or eigenvectors
+            return small_fused(*M, ctx.st, nkc, nullptr, c0, kmesh, dirs_d, -1, 0.0, 0, nullptr, 0.0, nullptr, E,
+                               nullptr);
+        const int64_t n0 = kmesh[0], n1 = M->dim > 1 ? kmesh[1] : 1, n2 = M->dim > 2 ? kmesh[2] : 1;
+        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, M->dim, n0, n1, n2, k_d);
+        TBG_LAUNCHED("kmesh_kernel");
+        int rc = fourier_direct(*M, ctx.st, nkc, k_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0);
+        if (rc) return rc;
+        return eig_batched(ctx.st, N, nkc, H, E, nullptr, nullptr, 0, status_d);
+    }
+};
+
+int check_kmesh(const ModelDev& M, const int64_t* kmesh, int64_t* nk_out) {
+    if (!kmesh) return set_error(TBG_E_INVALID_ARGUMENT, "null k-mesh");
+    int64_t nk = 1;
+    for (int d = 0; d < M.dim; ++d) {
+        if (kmesh[d] <= 0) return set_error(TBG_E_INVALID_KMESH, "Invalid k-point mesh dimensions");
+        nk *= kmesh[d];
+    }
+    *nk_out = nk;
+    return TBG_OK;
+}
+
 }  // namespace
 }  // namespace tbg
 
@@ -821,12 +883,8 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
         return set_error(TBG_E_INVALID_DOS_PARAMETER, "E_n: number of energy bins must be at least 1");
     if (!std::isfinite(sigma) || sigma <= 0.0)
         return set_error(TBG_E_INVALID_DOS_PARAMETER, "sigma: Gaussian smearing width must be finite and positive");
-    if (!kmesh) return set_error(TBG_E_INVALID_ARGUMENT, "null k-mesh");
-    int64_t nk = 1;
-    for (int d = 0; d < M.dim; ++d) {
-        if (kmesh[d] <= 0) return set_error(TBG_E_INVALID_KMESH, "Invalid k-point mesh dimensions");
-        nk *= kmesh[d];
-    }
+    int64_t nk = 0;
+    if ((rc = check_kmesh(M, kmesh, &nk))) return rc;
     if (E_n > (int64_t(1) << 30)) return set_error(TBG_E_UNSUPPORTED, "E_n > 2^30 is not supported");
     if (!dos_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
     // ndarray linspace: E_i = E_min + i step, step = (E_max - E_min) / (E_n - 1)
@@ -834,47 +892,46 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
     if (E_out)
         for (int64_t i = 0; i < E_n; ++i) E_out[i] = E_min + step * (double)i;
     const int N = (int)M.nsta;
-    const int64_t NN = (int64_t)N * N;
-    const bool small = N <= kSmallMaxN;
     Ctx ctx;
-    // the fused small-model kernel has no batch limit: one chunk of up to 2^21 k-points
-    const int64_t chunk = small ? std::max<int64_t>(1, std::min<int64_t>({nk, int64_t(1) << 21,
-                                                                          chunk_budget_bytes() / (16 * N + 64)}))
-                                : choose_chunk(nk, sizeof(zc) * NN + 16 * N + 64);
-    const int slices = dos_slices(E_n, chunk * N);
-    double* k_d = small ? nullptr : ctx.alloc<double>(chunk * M.dim);
-    zc* H = small ? nullptr : ctx.alloc<zc>(chunk * NN);
-    double* E = ctx.alloc<double>(chunk * N);
-    double* dirs_d = small ? ctx.alloc<double>(2 * M.dim) : nullptr;
+    MeshEnergies me;
+    if ((rc = me.init(ctx, M, kmesh, nk))) return rc;
+    const int slices = dos_slices(E_n, me.chunk * N);
     double* part = ctx.alloc<double>((int64_t)slices * E_n);
     double* acc = ctx.alloc<double>(2 * E_n);
-    int* status_d = ctx.alloc<int>(1);
     if (ctx.rc) return ctx.rc;
-    TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
     TBG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 2 * E_n, ctx.st));
-    if (dirs_d) TBG_CUDA(cudaMemsetAsync(dirs_d, 0, sizeof(double) * 2 * M.dim, ctx.st));
-    const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
-    for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
-        const int64_t nkc = std::min(chunk, nk - c0);
-        if (small) {
-            // the fused small-model kernel in its energies-only form (no velocities or eigenvectors)
-            if ((rc = small_fused(M, ctx.st, nkc, nullptr, c0, kmesh, dirs_d, -1, 0.0, 0, nullptr, 0.0, nullptr, E,
-                                  nullptr)))
-                return rc;
-        } else {
-            kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, M.dim, n0, n1, n2, k_d);
-            TBG_LAUNCHED("kmesh_kernel");
-            if ((rc = fourier_direct(M, ctx.st, nkc, k_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0))) return rc;
-            if ((rc = eig_batched(ctx.st, N, nkc, H, E, nullptr, nullptr, 0, status_d))) return rc;
-        }
-        if ((rc = dos_accumulate(ctx.st, nkc * N, E, E_n, E_min, step, sigma, part, slices, acc))) return rc;
+    for (int64_t c0 = 0; c0 < nk; c0 += me.chunk) {
+        const int64_t nkc = std::min(me.chunk, nk - c0);
+        if ((rc = me.run(ctx, c0, nkc))) return rc;
+        if ((rc = dos_accumulate(ctx.st, nkc * N, me.E, E_n, E_min, step, sigma, part, slices, acc))) return rc;
     }
     std::vector<double> acc_h(2 * E_n);
     TBG_CUDA(cudaMemcpyAsync(acc_h.data(), acc, sizeof(double) * 2 * E_n, cudaMemcpyDeviceToHost, ctx.st));
     if (ctx.sync("tbg_dos")) return ctx.rc;
-    if ((rc = check_status(status_d, ctx.st))) return rc;
+    if ((rc = check_status(me.status_d, ctx.st))) return rc;
     for (int64_t i = 0; i < E_n; ++i) dos_out[i] = (acc_h[2 * i] - acc_h[2 * i + 1]) / (double)nk;
     return TBG_OK;
+}
+
+int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    int64_t nk = 0;
+    if ((rc = check_kmesh(M, kmesh, &nk))) return rc;
+    if (!E_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    const int N = (int)M.nsta;
+    Ctx ctx;
+    MeshEnergies me;
+    if ((rc = me.init(ctx, M, kmesh, nk))) return rc;
+    for (int64_t c0 = 0; c0 < nk; c0 += me.chunk) {
+        const int64_t nkc = std::min(me.chunk, nk - c0);
+        if ((rc = me.run(ctx, c0, nkc))) return rc;
+        TBG_CUDA(cudaMemcpyAsync(E_out + c0 * N, me.E, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+        if (ctx.sync("tbg_bands_mesh")) return ctx.rc;
+    }
+    if ((rc = check_status(me.status_d, ctx.st))) return rc;
+    return ctx.sync("tbg_bands_mesh");
 }
 
 int tbg_quantum_geometry(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, double eta,

@@ -457,3 +457,23 @@ class Model:
         _lib.check(lib.tbg_dos(self.device_handle(), _lib.iptr(kmesh), E_min, E_max, int(E_n), sigma,
                                _lib.dptr(E), _lib.dptr(out)), lib)
         return E, out
+
+    # ----------------------------------------------------------- band meshes
+    def solve_band_mesh(self, k_mesh) -> np.ndarray:
+        """``solve_band_all_parallel(&gen_kmesh(k_mesh))`` (src/solve_ham.rs:94-107,
+        src/kpoints.rs:49-87) in one device call: energies (nk, nsta)."""
+        from . import fermi
+
+        return fermi.bands_mesh(self, k_mesh)
+
+    def write_bxsf(self, k_mesh, e_fermi: float, filename: str) -> str:
+        """``BxsfExport::write_bxsf`` (src/fermi_surface.rs:454-546)."""
+        from . import fermi
+
+        return fermi.write_bxsf(self, k_mesh, e_fermi, filename)
+
+    def rec_lat(self) -> np.ndarray:
+        """``Model::rec_lat`` (src/model.rs:679-687)."""
+        from . import fermi
+
+        return fermi.rec_lat(self.lat)

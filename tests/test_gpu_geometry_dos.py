@@ -193,3 +193,71 @@ def test_quantum_geometry_c_abi_errors():
     res = np.empty(2)
     assert lib.tbg_quantum_geometry_mesh(h, _lib.iptr(km), _lib.dptr(d), 1, _lib.dptr(mu), 0.0, 1e-3, 0,
                                          _lib.dptr(res[:1]), _lib.dptr(res[1:]), None) == errors.TBG_E_INVALID_KMESH
+
+
+# ------------------------------------------------------------ band meshes --
+@pytest.mark.parametrize("name,build,kmesh", [
+    ("haldane", M.haldane, [9, 7]),
+    ("kane_mele", lambda: M.kane_mele(rashba=0.05), [5, 6]),
+    ("random12", lambda: W.random_model(2, 12, False, 1, seed=309), [6, 4]),
+    ("qwz3d", M.qwz_stacked_3d, [4, 3, 5]),
+    ("random3d_s9", lambda: W.random_model(3, 9, True, 1, seed=310), [3, 2, 4]),
+])
+def test_bands_mesh_matches_oracle(name, build, kmesh):
+    model = build()
+    E = model.solve_band_mesh(kmesh)
+    ref = O.solve_band_all(model, O.gen_kmesh(kmesh))
+    scale = max(np.max(np.abs(ref)), 1.0)
+    assert E.shape == ref.shape
+    assert np.max(np.abs(E - ref)) <= 1e-10 * scale
+    # the k-list path gives the same energies
+    E2 = model.solve_band_all_parallel(O.gen_kmesh(kmesh))
+    assert np.max(np.abs(E - E2)) <= 1e-12 * scale
+
+
+def _parse_bxsf(path):
+    lines = open(path, encoding="utf-8").read().split("\n")
+    i = lines.index("  BEGIN_BANDGRID_3D_band_energies")
+    nb = int(lines[i + 1])
+    dims = [int(v) for v in lines[i + 2].split()]
+    vals = []
+    for ln in lines[i + 7:]:
+        if ln.startswith("    BAND:") or not ln.strip() or ln.strip().startswith("END"):
+            continue
+        vals += [float(v) for v in ln.split()]
+    return nb, dims, np.array(vals).reshape(nb, -1).T
+
+
+def test_write_bxsf_round_trip(tmp_path):
+    model = W.random_model(3, 5, False, 1, seed=311)
+    km = [3, 4, 12]
+    path = model.write_bxsf(km, 0.25, str(tmp_path / "bands"))
+    assert path.endswith(".bxsf")
+    nb, dims, E = _parse_bxsf(path)
+    assert nb == model.nsta and dims == km
+    ref = O.solve_band_all(model, O.gen_kmesh(km))
+    assert np.allclose(E, ref, rtol=2e-10, atol=1e-12)  # 10 decimals in the file
+    text = open(path, encoding="utf-8").read()
+    assert "  Fermi Energy: 0.250000000000\n" in text
+
+
+def test_write_spin_frmsf(tmp_path):
+    from rustb_gb300 import write_spin_frmsf
+
+    up = W.random_model(3, 3, False, 1, seed=312)
+    dn = W.random_model(3, 3, False, 1, seed=313)
+    dn.lat = up.lat.copy()
+    km = [2, 3, 4]
+    path = write_spin_frmsf(up, dn, km, 0.1, str(tmp_path / "spin"))
+    lines = open(path).read().split("\n")
+    assert lines[0] == "2 3 4" and lines[1] == "1" and lines[2] == "6"
+    vals = np.array([float(v) for ln in lines[6:] for v in ln.split()])
+    nk = 24
+    energies, colors = vals[:6 * nk], vals[6 * nk:]
+    eu = O.solve_band_all(up, O.gen_kmesh(km)) - 0.1
+    ed = O.solve_band_all(dn, O.gen_kmesh(km)) - 0.1
+    ref = np.concatenate([eu, ed], axis=1).T.reshape(-1)
+    assert np.allclose(energies, ref, rtol=2e-10, atol=1e-12)
+    assert np.array_equal(colors, np.where(np.arange(6 * nk) // nk < 3, 1.0, -1.0))
+    with pytest.raises(errors.TbPanic):
+        write_spin_frmsf(up, W.random_model(3, 4, False, 1, seed=314), km, 0.0, str(tmp_path / "bad"))
