@@ -284,6 +284,41 @@ def _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, nk, threads=None):
     return nk / (time.perf_counter() - t0), threads
 
 
+# ncu: DRAM bytes of one dos_kernel launch over the whole 1000 x 1000 mesh
+# (one chunk; profiles/dos_kernel_honeycomb_1000x1000.md)
+DOS_KERNEL_DRAM_BYTES = 16.02e6
+
+
+def _dos_roofline(lib, model, mesh, E_min, E_max, E_n, sigma, timing):
+    """dos_kernel against the FP64 pipe.  Work unit: one in-window Gaussian term
+    (|E_i - x| <= 38.6 sigma, the terms that are non-zero in FP64); the table
+    method needs at least 3 FP64 operations per term (two recurrence multiplies,
+    one add into the bin), so the peak is the measured FP64 FMA issue rate / 3."""
+    import ctypes
+
+    if "dos_kernel" not in timing:
+        return None
+    launches, ms, _ = timing["dos_kernel"]
+    ev = model.solve_band_mesh(mesh).reshape(-1)
+    step = (E_max - E_min) / (E_n - 1)
+    w = 38.6 * sigma
+    lo = np.clip(np.ceil((ev - w - E_min) / step), 0, E_n - 1)
+    hi = np.clip(np.floor((ev + w - E_min) / step), 0, E_n - 1)
+    inside = (ev + w >= E_min) & (ev - w <= E_min + step * (E_n - 1))
+    terms = float(np.sum(np.where(inside, hi - lo + 1, 0)))
+    p64 = ctypes.c_double(0.0)
+    p32 = ctypes.c_double(0.0)
+    lib.tbg_measure_fma_peaks(ctypes.byref(p64), ctypes.byref(p32))
+    avg_s = ms / 1e3 / max(launches, 1)
+    achieved = terms / avg_s / 1e9
+    peak = p64.value * 1e12 / 2.0 / 3.0 / 1e9
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "Gterms/s",
+            "frac": achieved / peak if peak > 0 else None, "traffic": DOS_KERNEL_DRAM_BYTES,
+            "traffic_unit": "bytes per launch (ncu dram read + write)", "kernel": "dos_kernel",
+            "terms_per_launch": terms, "avg_launch_ms": avg_s * 1e3,
+            "peak_source": "FP64 FMA loop on this GPU (tbg_measure_fma_peaks) / 2 flops / 3 ops per term"}
+
+
 def dos_bench(args, rank, world, local):
     model = W.honeycomb_small()
     mesh = (1000, 1000)
@@ -326,7 +361,8 @@ def dos_bench(args, rank, world, local):
     e2e = args.steps * nk / (time.perf_counter() - t0)
     cpu, thr = _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, sample)
     _line(args, world, DOS_METRIC, val, "k-pts/s", wall / args.steps * 1e3, "f64", cfg,
-          {"gpu_launches": int(launches), "states_integral": float(d.sum() * (E[1] - E[0])),
+          {"roofline": _dos_roofline(lib, model, mesh, E_min, E_max, E_n, sigma, timing),
+           "gpu_launches": int(launches), "states_integral": float(d.sum() * (E[1] - E[0])),
            "kernel_ms_per_step": t_dev / args.steps * 1e3,
            "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in timing.items()},
            "cpu_baseline": {"value": cpu, "unit": "k-pts/s", "cores": thr, "kind": "port",
