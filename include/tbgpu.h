@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-/* Status codes.  Codes 1..11 map 1:1 onto TbError variants (src/error.rs). */
+/* Status codes.  Codes 1..13 map 1:1 onto TbError variants (src/error.rs). */
 enum tbg_status {
     TBG_OK = 0,
     TBG_E_KVECTOR_LENGTH = 1,             /* TbError::KVectorLengthMismatch */
@@ -46,6 +46,8 @@ enum tbg_status {
     TBG_E_INVALID_ARGUMENT = 9,           /* conditions on which Rustb panics */
     TBG_E_INVALID_ENERGY_RANGE = 10,      /* TbError::InvalidEnergyRange */
     TBG_E_INVALID_DOS_PARAMETER = 11,     /* TbError::InvalidDosParameter */
+    TBG_E_FILE_PARSE = 12,                /* TbError::FileParse */
+    TBG_E_FILE_OPEN = 13,                 /* TbError::FileCreation (a file that cannot be opened) */
     TBG_E_CUDA = 20,                      /* CUDA runtime failure */
     TBG_E_NOCONV = 21,                    /* eigensolver did not converge */
     TBG_E_TIMEOUT = 22,                   /* a bounded device wait ran out */
@@ -220,6 +222,34 @@ int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out);
  * Replaces: Model::dos (src/model_physics.rs:179-230). */
 int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max,
             int64_t E_n, double sigma, double* E_out, double* dos_out);
+
+/* ------------------------------------------------------ Wannier90 input --- */
+
+/* Native reader of Wannier90 tight-binding tables (host side; the result is
+ * uploaded with tbg_model_create / tbg_model_set_rmatrix).  Together with the
+ * seedname.win / _centres.xyz parsing of the host mirror it replaces
+ * Wannier90::from_hr and Model::from_hr_with_rmatrix
+ * (src/wannier90.rs:49-1219).  Call order as the reference reads the files:
+ * tbg_w90_read_hr, (win / xyz on the host), tbg_w90_read_r when the model
+ * carries a position matrix, tbg_w90_apply_wsvec (no-op when the file is
+ * absent), tbg_w90_hermitize_rmatrix; then tbg_w90_info / tbg_w90_copy. */
+typedef struct tbg_w90 tbg_w90;
+
+/* seedname_hr.dat -> ham (nR, nsta, nsta) complex with R = 0 first, hamR (nR, 3);
+ * zero_energy is subtracted from the R = 0 diagonal (wannier90.rs:85-245). */
+int tbg_w90_read_hr(const char* hr_path, double zero_energy, tbg_w90** out);
+/* seedname_r.dat -> rmatrix (nR, 3, nsta, nsta) aligned with hamR
+ * (wannier90.rs:771-880); TBG_E_FILE_OPEN when the file is missing. */
+int tbg_w90_read_r(tbg_w90* h, const char* r_path);
+/* seedname_wsvec.dat Wigner-Seitz refolding (wannier90.rs:882-1142);
+ * *applied = 0 and TBG_OK when the file does not exist. */
+int tbg_w90_apply_wsvec(tbg_w90* h, const char* ws_path, int* applied);
+/* rmatrix(R) <- (rmatrix(R) + rmatrix(-R)^dagger) / 2 (wannier90.rs:1146-1167). */
+int tbg_w90_hermitize_rmatrix(tbg_w90* h);
+int tbg_w90_info(const tbg_w90* h, int64_t* nsta, int64_t* nR, int* has_r);
+/* Copies into caller arrays sized from tbg_w90_info (any may be NULL). */
+int tbg_w90_copy(const tbg_w90* h, double* ham, int64_t* hamR, double* rmatrix);
+int tbg_w90_free(tbg_w90* h);
 
 /* ------------------------------------------- asynchronous batch queue --- */
 

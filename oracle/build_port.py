@@ -65,6 +65,8 @@ def load():
                                  ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_int, dp]
         lib.port_dos.restype = ctypes.c_int
+        lib.port_read_hr.argtypes = [ctypes.c_char_p, ctypes.c_double, dp, ctypes.c_int64]
+        lib.port_read_hr.restype = ctypes.c_int64
         _port = lib
     return _port
 
@@ -120,3 +122,13 @@ def dos_sums(model, kmesh, E_min, E_max, E_n, sigma, k0=0, nk=None, threads=None
     if rc != 0:
         raise RuntimeError(f"zheev info={rc}")
     return acc
+
+
+def read_hr(path, nvalues):
+    """The reference's line-by-line _hr.dat reading on one thread (timing baseline)."""
+    lib = load()
+    out = np.empty(2 * int(nvalues))
+    n = lib.port_read_hr(path.encode(), 0.0, _dp(out), out.size)
+    if n < 0:
+        raise RuntimeError("malformed _hr.dat")
+    return out[: 2 * n].view(np.complex128)

@@ -372,3 +372,71 @@ int port_dos(int dim, int spin_model, int norb, int nR, const double* ham, const
     free(tau);
     return err;
 }
+
+/* Wannier90 _hr.dat as from_hr reads it (src/wannier90.rs:85-245), on one
+ * thread: every line kept, then the values taken by position (tokens 5 and 6
+ * of each data line) and divided by the block's weight.  ham_out receives the
+ * n_R blocks in file order (n_R, nsta, nsta) complex, transposed as the
+ * reference stores them.  Returns n_R * nsta^2, or -1 on a malformed file. */
+int64_t port_read_hr(const char* path, double zero_energy, double* ham_out, int64_t cap_values) {
+    FILE* f = fopen(path, "r");
+    if (!f) return -1;
+    size_t nl = 0, capl = 1024;
+    char** lines = (char**)malloc(sizeof(char*) * capl);
+    char* buf = NULL;
+    size_t bl = 0;
+    ssize_t got;
+    while ((got = getline(&buf, &bl, f)) >= 0) {
+        if (nl == capl) {
+            capl *= 2;
+            lines = (char**)realloc(lines, sizeof(char*) * capl);
+        }
+        lines[nl++] = strdup(buf);
+    }
+    free(buf);
+    fclose(f);
+    int64_t result = -1;
+    if (nl >= 3) {
+        const long nsta = strtol(lines[1], NULL, 10), n_R = strtol(lines[2], NULL, 10);
+        long* w = (long*)malloc(sizeof(long) * (n_R > 0 ? n_R : 1));
+        long nw = 0;
+        size_t n_line = 0;
+        for (size_t i = 3; i < nl; ++i) {
+            if (strchr(lines[i], '.')) {
+                n_line = i;
+                break;
+            }
+            char* p = lines[i];
+            char* e;
+            for (long v = strtol(p, &e, 10); e != p; v = strtol(p, &e, 10)) {
+                if (nw < n_R) w[nw++] = v;
+                p = e;
+            }
+        }
+        const int64_t NN = (int64_t)nsta * nsta;
+        if (nsta > 0 && nw >= n_R && n_line + (size_t)(n_R * NN) <= nl && n_R * NN * 2 <= cap_values) {
+            for (long r = 0; r < n_R; ++r)
+                for (long a = 0; a < nsta; ++a)
+                    for (long b = 0; b < nsta; ++b) {
+                        char* p = lines[n_line + r * NN + a * nsta + b];
+                        char* e;
+                        for (int t = 0; t < 5; ++t) {
+                            strtod(p, &e);
+                            p = e;
+                        }
+                        const double re = strtod(p, &e);
+                        p = e;
+                        const double im = strtod(p, &e);
+                        double* o = ham_out + 2 * (r * NN + b * nsta + a);
+                        o[0] = re / (double)w[r];
+                        o[1] = im / (double)w[r];
+                    }
+            (void)zero_energy;
+            result = n_R * NN;
+        }
+        free(w);
+    }
+    for (size_t i = 0; i < nl; ++i) free(lines[i]);
+    free(lines);
+    return result;
+}

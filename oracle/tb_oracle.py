@@ -393,3 +393,128 @@ def berry_loop(model, k_loop, occ):
     for a, b in zip(vecs[:-1], vecs[1:]):
         prod = prod @ (a.conj().T @ b)
     return -np.angle(np.linalg.det(prod))
+
+
+# --------------------------------------------------------------------------
+# Wannier90 tight-binding tables (src/wannier90.rs), line by line
+# --------------------------------------------------------------------------
+
+def _w90_lines(path):
+    with open(path, "rb") as f:
+        text = f.read().decode("utf-8")
+    lines = text.split("\n")
+    if lines and lines[-1] == "":
+        lines.pop()
+    return [ln[:-1] if ln.endswith("\r") else ln for ln in lines]
+
+
+def w90_read_hr(path, zero_energy=0.0):
+    """_hr.dat as ``from_hr`` reads it (src/wannier90.rs:85-245): returns
+    (ham (nR, nsta, nsta) c128 with R = 0 first, hamR (nR, 3), weights)."""
+    reads = _w90_lines(path)
+    nsta = int(reads[1].strip())
+    n_R = int(reads[2].strip())
+    weights = []
+    n_line = 0
+    for i in range(3, len(reads)):
+        if "." in reads[i]:
+            n_line = i
+            break
+        weights += [int(x) for x in reads[i].split()]
+    ham = [np.zeros((nsta, nsta), dtype=np.complex128)]
+    hamR = [(0, 0, 0)]
+    for i in range(n_R):
+        first = reads[i * nsta * nsta + n_line].split()
+        R = (int(first[0]), int(first[1]), int(first[2]))
+        m = np.zeros((nsta, nsta), dtype=np.complex128)
+        for ind_i in range(nsta):
+            for ind_j in range(nsta):
+                tok = reads[i * nsta * nsta + ind_i * nsta + ind_j + n_line].split()
+                m[ind_j, ind_i] = complex(float(tok[5]), float(tok[6])) / float(weights[i])
+        if R == (0, 0, 0):
+            ham[0] = m
+        else:
+            ham.append(m)
+            hamR.append(R)
+    ham = np.array(ham)
+    for i in range(nsta):
+        ham[0, i, i] -= zero_energy
+    return ham, np.array(hamR, dtype=np.int64), weights
+
+
+def _find_R(hamR, R):
+    for r in range(len(hamR)):
+        if tuple(hamR[r]) == tuple(R):
+            return r
+    return None
+
+
+def w90_read_r(path, hamR, weights, nsta):
+    """_r.dat (src/wannier90.rs:771-880): rmatrix (nR, 3, nsta, nsta) aligned with hamR."""
+    reads = _w90_lines(path)
+    n_R = int(reads[2].strip())
+    rm = np.zeros((len(hamR), 3, nsta, nsta), dtype=np.complex128)
+    for i in range(n_R):
+        first = reads[i * nsta * nsta + 3].split()
+        index = _find_R(hamR, (int(first[0]), int(first[1]), int(first[2])))
+        if index is None:
+            raise KeyError("R vector not found in Hamiltonian")
+        for ind_i in range(nsta):
+            for ind_j in range(nsta):
+                tok = reads[i * nsta * nsta + ind_i * nsta + ind_j + 3].split()
+                for r in range(3):
+                    rm[index, r, ind_j, ind_i] = complex(float(tok[5 + 2 * r]), float(tok[6 + 2 * r])) / float(weights[i])
+    return rm
+
+
+def w90_apply_wsvec(path, ham, hamR, rm=None):
+    """_wsvec.dat refolding (src/wannier90.rs:882-1142)."""
+    reads = _w90_lines(path)
+    nsta = ham.shape[1]
+    new_R = [(0, 0, 0)]
+    new_ham = [np.zeros((nsta, nsta), dtype=np.complex128)]
+    new_rm = [np.zeros((3, nsta, nsta), dtype=np.complex128)] if rm is not None else None
+    i = 0
+    while i < len(reads) - 1:
+        i += 1
+        tok = reads[i].split()
+        R = (int(tok[0]), int(tok[1]), int(tok[2]))
+        ii, jj = int(tok[3]) - 1, int(tok[4]) - 1
+        i += 1
+        weight = int(reads[i].split()[0])
+        index = _find_R(hamR, R)
+        if index is None:
+            raise KeyError("R vector not found in Hamiltonian")
+        hop = ham[index, ii, jj] / float(weight)
+        hx = rm[index, :, ii, jj] / float(weight) if rm is not None else None
+        for _ in range(weight):
+            i += 1
+            t = reads[i].split()
+            nR = (R[0] + int(t[0]), R[1] + int(t[1]), R[2] + int(t[2]))
+            j = _find_R(new_R, nR)
+            if j is None:
+                new_R.append(nR)
+                new_ham.append(np.zeros((nsta, nsta), dtype=np.complex128))
+                if rm is not None:
+                    new_rm.append(np.zeros((3, nsta, nsta), dtype=np.complex128))
+                j = len(new_R) - 1
+            new_ham[j][ii, jj] += hop
+            if rm is not None:
+                new_rm[j][:, ii, jj] += hx
+    return (np.array(new_ham), np.array(new_R, dtype=np.int64),
+            np.array(new_rm) if rm is not None else None)
+
+
+def w90_hermitize_rmatrix(rm, hamR):
+    """(src/wannier90.rs:1146-1167): every R row but the last, in place."""
+    nsta = rm.shape[2]
+    for r in range(len(hamR) - 1):
+        q = _find_R(hamR, tuple(-x for x in hamR[r]))
+        if q is None:
+            raise KeyError("Missing Hermitian conjugate")
+        for i in range(nsta):
+            for j in range(nsta):
+                for c in range(3):
+                    rm[r, c, i, j] = (rm[r, c, i, j] + np.conj(rm[q, c, j, i])) / 2.0
+                    rm[q, c, j, i] = np.conj(rm[r, c, i, j])
+    return rm

@@ -14,6 +14,9 @@
 * ``dos``       -- Model::dos of the reference's benchmark model (two-band
                    honeycomb, -3..3 eV, 500 bins, sigma 1e-2) on a
                    1000 x 1000 mesh; a step is the whole mesh.
+* ``w90``       -- Wannier90 loading: a 64-orbital, 125-R seedname_hr.dat
+                   (512 000 lines, Wannier90's 5I5,2F12.6 format) read into a
+                   device-resident model; a step is one load.
 
 Each prints one JSON line in the bench.py format.  The CPU baseline of each
 (``--impl reference``) is the C port of the reference path on the host cores.
@@ -57,7 +60,7 @@ def run(args, rank, world, local):
     if rank != 0 and args.impl == "reference":
         return 0
     fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench,
-          "dos": dos_bench}[args.workload]
+          "dos": dos_bench, "w90": w90_bench}[args.workload]
     return fn(args, rank, world, local)
 
 
@@ -370,3 +373,118 @@ def dos_bench(args, rank, world, local):
            "e2e": {"value": e2e, "unit": "k-pts/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
                    "d2h_bytes_per_step": 8 * E_n}})
     return 0
+
+
+# --------------------------------------------------------------------- w90 --
+W90_METRIC = "MB/s (Wannier90 _hr.dat -> device-resident model)"
+
+
+def write_w90_dataset(d: str, seed_name: str, model) -> int:
+    """Write ``model``'s tables as seedname_hr.dat (unit weights, Wannier90's
+    5I5,2F12.6 lines, column-major blocks) plus a minimal .win; returns the
+    _hr.dat size in bytes."""
+    os.makedirs(d, exist_ok=True)
+    n, nR = model.nsta, model.nR
+    head = f"written for the w90 workload\n{n:12d}\n{nR:12d}\n"
+    w = ["".join(f"{1:5d}" for _ in range(min(15, nR - i))) for i in range(0, nR, 15)]
+    jj, ii = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")  # j outer, i inner
+    rows = []
+    for r in range(nR):
+        R = model.hamR[r]
+        h = model.ham[r][ii.reshape(-1), jj.reshape(-1)]
+        block = np.empty((n * n, 7))
+        block[:, 0:3] = R
+        block[:, 3] = ii.reshape(-1) + 1
+        block[:, 4] = jj.reshape(-1) + 1
+        block[:, 5] = h.real
+        block[:, 6] = h.imag
+        rows.append(block)
+    path = os.path.join(d, seed_name + "_hr.dat")
+    with open(path, "w") as f:
+        f.write(head + "\n".join(w) + "\n")
+        np.savetxt(f, np.concatenate(rows), fmt="%5d%5d%5d%5d%5d%12.6f%12.6f")
+    lat = model.lat
+    win = ["begin unit_cell_cart", "Ang"] + [" ".join(f"{x:.10f}" for x in lat[i]) for i in range(3)]
+    win += ["end unit_cell_cart", "", "begin projections", "Fe:" + ",".join(["s"] * n), "end projections", "",
+            "begin atoms_frac", "Fe 0.0 0.0 0.0", "end atoms_frac"]
+    with open(os.path.join(d, seed_name + ".win"), "w") as f:
+        f.write("\n".join(win) + "\n")
+    return os.path.getsize(path)
+
+
+def w90_bench(args, rank, world, local):
+    import ctypes
+    import shutil
+    import tempfile
+
+    from .model import Model
+
+    src = W.random_model(3, 64, False, 2, seed=20260107)
+    cfg = {"workload": "Wannier90 seedname_hr.dat of a random 64-orbital model, R in {-2..2}^3 (125 R, "
+                       "512 000 lines, 5I5,2F12.6) + .win, loaded to a device-resident model",
+           "nsta": src.nsta, "n_R": src.nR}
+    tmp = tempfile.mkdtemp(prefix="w90_")
+    try:
+        size = write_w90_dataset(tmp, "bench", src)
+        mb = size / 1e6
+        hr = os.path.join(tmp, "bench_hr.dat")
+
+        def port_once():
+            from oracle import build_port
+
+            build_port.load()
+            t0 = time.perf_counter()
+            build_port.read_hr(hr, src.nR * src.nsta ** 2)
+            return mb / (time.perf_counter() - t0)
+
+        if args.impl == "reference":
+            vals = [port_once() for _ in range(max(1, args.steps))]
+            val = float(np.median(vals))
+            _line(args, world, W90_METRIC, val, "MB/s", mb / val * 1e3, "f64", cfg,
+                  {"impl": "reference", "cpu_baseline": {"value": val, "unit": "MB/s", "cores": 1, "kind": "port",
+                                                         "sample": f"the whole {mb:.1f} MB _hr.dat"},
+                   "e2e": {"value": val, "unit": "MB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+            return 0
+        lib = _lib.load()
+        lib.tbg_set_device(local)
+
+        def tables_once():
+            # native table reader + upload of the tables (the device-resident part)
+            h = ctypes.c_void_p()
+            t0 = time.perf_counter()
+            _lib.check(lib.tbg_w90_read_hr(hr.encode(), 0.0, ctypes.byref(h)), lib)
+            nsta, nR = ctypes.c_int64(), ctypes.c_int64()
+            lib.tbg_w90_info(h, ctypes.byref(nsta), ctypes.byref(nR), None)
+            ham = np.empty((nR.value, nsta.value, nsta.value), dtype=np.complex128)
+            hamR = np.empty((nR.value, 3), dtype=np.int64)
+            lib.tbg_w90_copy(h, _lib.dptr(ham.view(np.float64)), _lib.iptr(hamR), None)
+            lib.tbg_w90_free(h)
+            m = Model(src.lat, np.zeros((nsta.value, 3)), False, ham=ham, hamR=hamR)
+            m.device_handle()
+            lib.tbg_set_device(local)
+            dt = time.perf_counter() - t0
+            m._invalidate()
+            return dt
+
+        for _ in range(args.warmup):
+            tables_once()
+        t = [tables_once() for _ in range(args.steps)]
+        val = args.steps * mb * world / sum(t)
+        # e2e: Model.from_hr (hr + win), then the upload, per step
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m = Model.from_hr(tmp + "/", "bench", 0.0)
+            m.device_handle()
+            m._invalidate()
+        e2e = args.steps * mb / (time.perf_counter() - t0)
+        cpu = port_once()
+        _line(args, world, W90_METRIC, val, "MB/s", sum(t) / args.steps * 1e3, "f64", cfg,
+              {"roofline": None, "bound": "host parse (all host threads) + one H2D copy of the tables",
+               "gpu_launches": 0, "threads": os.cpu_count(),
+               "cpu_baseline": {"value": cpu, "unit": "MB/s", "cores": 1, "kind": "port",
+                                "sample": f"the whole {mb:.1f} MB _hr.dat, line by line on one thread"},
+               "e2e": {"value": e2e, "unit": "MB/s", "h2d_bytes_per_step": int(src.ham.nbytes + src.hamR.nbytes),
+                       "d2h_bytes_per_step": 0}})
+        return 0
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)

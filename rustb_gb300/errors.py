@@ -22,6 +22,8 @@ TBG_E_INVALID_MODEL = 8
 TBG_E_INVALID_ARGUMENT = 9
 TBG_E_INVALID_ENERGY_RANGE = 10
 TBG_E_INVALID_DOS_PARAMETER = 11
+TBG_E_FILE_PARSE = 12
+TBG_E_FILE_OPEN = 13
 TBG_E_CUDA = 20
 TBG_E_NOCONV = 21
 TBG_E_TIMEOUT = 22
@@ -99,6 +101,26 @@ class InvalidDosParameter(TbError):
     code = TBG_E_INVALID_DOS_PARAMETER
 
 
+class FileParse(TbError):
+    """``TbError::FileParse`` (error.rs:63-64): malformed Wannier90 input."""
+
+    code = TBG_E_FILE_PARSE
+
+
+class FileCreation(TbError):
+    """``TbError::FileCreation`` (error.rs:78-79): an input file cannot be opened."""
+
+    code = TBG_E_FILE_OPEN
+
+
+class InvalidOrbitalProjection(TbError):
+    """``TbError::InvalidOrbitalProjection`` (error.rs:66-67), raised by the host .win parser."""
+
+
+class Other(TbError):
+    """``TbError::Other`` (e.g. the Wannier90 spin mismatch, wannier90.rs:538-544)."""
+
+
 class TbPanic(TbError):
     """A condition on which the reference panics (assert!/todo!)."""
 
@@ -123,6 +145,8 @@ _BY_CODE = {
     TBG_E_INVALID_ARGUMENT: TbPanic,
     TBG_E_INVALID_ENERGY_RANGE: InvalidEnergyRange,
     TBG_E_INVALID_DOS_PARAMETER: InvalidDosParameter,
+    TBG_E_FILE_PARSE: FileParse,
+    TBG_E_FILE_OPEN: FileCreation,
     TBG_E_CUDA: DeviceError,
     TBG_E_NOCONV: DeviceError,
     TBG_E_TIMEOUT: DeviceError,

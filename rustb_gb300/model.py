@@ -477,3 +477,24 @@ class Model:
         from . import fermi
 
         return fermi.rec_lat(self.lat)
+
+    # ------------------------------------------------------------- Wannier90
+    @classmethod
+    def from_hr(cls, path: str, file_name: str, zero_energy: float = 0.0, spin: bool | None = None,
+                with_rmatrix: bool = False) -> "Model":
+        """``Wannier90::from_hr`` (src/wannier90.rs:49-1203); see ``rustb_gb300.wannier90``."""
+        from . import wannier90
+
+        return wannier90.from_hr(path, file_name, zero_energy, spin, with_rmatrix)
+
+    @classmethod
+    def from_hr_with_rmatrix(cls, path: str, file_name: str, zero_energy: float = 0.0,
+                             spin: bool | None = None) -> "Model":
+        """``Model::from_hr_with_rmatrix`` (src/wannier90.rs:1208-1219)."""
+        from . import wannier90
+
+        return wannier90.from_hr_with_rmatrix(path, file_name, zero_energy, spin)
+
+    def natom(self) -> int:
+        """Number of atoms (set by the Wannier90 loader; 0 for hand-built models)."""
+        return len(getattr(self, "atoms", []) or [])

@@ -104,7 +104,7 @@ def test_status_codes_map_to_error_classes():
 
 def _header_symbols():
     text = open(os.path.join(ROOT, "include", "tbgpu.h")).read()
-    return sorted(set(re.findall(r"\b(tbg_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(tbg_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_and_binding_agree():
