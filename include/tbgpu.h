@@ -223,6 +223,20 @@ int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out);
 int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max,
             int64_t E_n, double sigma, double* E_out, double* dos_out);
 
+/* Wilson loops over n_loops closed k-paths kvec (n_loops, n_k, dim); each
+ * path's last point must equal its first up to an integer vector G (the
+ * eigenvectors there are the first point's times exp(-2 pi i G . tau)).
+ * occ (n_occ) are the occupied band indices (n_occ <= 48).
+ * mode 0: out (n_loops, n_occ) = -arg of the eigenvalues of the product of the
+ *         unitary (U V^dagger) parts of the overlap matrices, ascending per loop;
+ *         replaces Berry::berry_loop (src/geometry.rs:156-215) and, through the
+ *         loops the caller builds, berry_flux / berry_phase / wannier_centre
+ *         (geometry.rs:272-420).
+ * mode 1: out (n_loops) = -arg det of the product of the raw overlaps;
+ *         replaces Berry::berry_loop_det (geometry.rs:217-270). */
+int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const double* kvec,
+                     int64_t n_occ, const int64_t* occ, int mode, double* out);
+
 /* ------------------------------------------------------ Wannier90 input --- */
 
 /* Native reader of Wannier90 tight-binding tables (host side; the result is

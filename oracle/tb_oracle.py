@@ -518,3 +518,66 @@ def w90_hermitize_rmatrix(rm, hamR):
                     rm[r, c, i, j] = (rm[r, c, i, j] + np.conj(rm[q, c, j, i])) / 2.0
                     rm[q, c, j, i] = np.conj(rm[r, c, i, j])
     return rm
+
+
+# --------------------------------------------------------------------------
+# Wilson loops (src/geometry.rs:156-420), with the loop's periodic gauge
+# --------------------------------------------------------------------------
+
+def _loop_overlaps(model, k_loop, occ):
+    """Overlap matrices <u_i(k_t)|u_j(k_t+1)> along the loop; the last point's
+    eigenvectors are the first point's times exp(-2 pi i G . tau)
+    (geometry.rs:160-196)."""
+    k_loop = np.atleast_2d(np.asarray(k_loop, dtype=np.float64))
+    n_k = k_loop.shape[0]
+    diff = k_loop[-1] - k_loop[0]
+    if np.any(np.abs(diff - np.round(diff)) > 1e-9):
+        raise ValueError("the end of this loop must differ from the beginning by an integer grid vector")
+    tau = orb_states(model)
+    _, U = solve_all(model, k_loop)                       # rows = eigenvectors
+    U = U.copy()
+    U[n_k - 1] = U[0] * np.exp(-2j * np.pi * (tau @ diff))[None, :]
+    ev = U[:, occ, :]                                     # (n_k, n_occ, nsta)
+    return [ev[t].conj() @ ev[t + 1].T for t in range(n_k - 1)]
+
+
+def wilson_loop(model, k_loop, occ):
+    """``berry_loop`` (geometry.rs:156-215): product of the unitary parts U V^H
+    of the overlaps, -arg of its eigenvalues; sorted ascending here."""
+    prod = np.eye(len(occ), dtype=np.complex128)
+    for O in _loop_overlaps(model, k_loop, occ):
+        u, _, vh = np.linalg.svd(O)
+        prod = prod @ (u @ vh)
+    return np.sort(-np.angle(np.linalg.eigvals(prod)))
+
+
+def wilson_loop_det(model, k_loop, occ):
+    """``berry_loop_det`` (geometry.rs:217-270): -arg det of the raw product."""
+    prod = np.eye(len(occ), dtype=np.complex128)
+    for O in _loop_overlaps(model, k_loop, occ):
+        prod = prod @ O
+    return float(-np.angle(np.linalg.det(prod)))
+
+
+def berry_flux(model, occ, k_start, dir_1, dir_2, nk1, nk2):
+    """``berry_flux`` (geometry.rs:272-339): plaquette Wilson loops, (nk1, nk2, n_occ)."""
+    ks, d1, d2 = (np.asarray(v, dtype=np.float64) for v in (k_start, dir_1, dir_2))
+    out = np.empty((nk1, nk2, len(occ)))
+    dx, dy = 1.0 / nk1, 1.0 / nk2
+    for i in range(nk1):
+        for j in range(nk2):
+            i0, j0 = i / nk1, j / nk2
+            loop = [ks + i0 * d1 + j0 * d2, ks + (i0 + dx) * d1 + j0 * d2, ks + (i0 + dx) * d1 + (j0 + dy) * d2,
+                    ks + i0 * d1 + (j0 + dy) * d2, ks + i0 * d1 + j0 * d2]
+            out[i, j] = wilson_loop(model, np.array(loop), occ)
+    return out
+
+
+def wannier_centre(model, occ, k_start, dir_1, dir_2, nk1, nk2):
+    """``wannier_centre`` (geometry.rs:360-420): (n_occ, nk1), sorted per loop."""
+    ks, d1, d2 = (np.asarray(v, dtype=np.float64) for v in (k_start, dir_1, dir_2))
+    out = np.empty((nk1, len(occ)))
+    for i in range(nk1):
+        loop = np.array([ks + d1 * float(i) / float(nk1 - 1) + d2 * float(j) / float(nk2 - 1) for j in range(nk2)])
+        out[i] = wilson_loop(model, loop, occ)
+    return out.T

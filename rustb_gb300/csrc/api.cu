@@ -211,6 +211,9 @@ int check_status(int* status_d, cudaStream_t st) {
     if (e != cudaSuccess) return cuda_error(e, "status readback");
     if (h & 1) return set_error(TBG_E_NOCONV, "eigensolver input contains NaN or Inf");
     if (h & 2) return set_error(TBG_E_TIMEOUT, "a bounded device wait ran out in a tensor-core kernel");
+    if (h & 4)
+        return set_error(TBG_E_NOCONV,
+                         "Wilson loop: an overlap matrix is singular (the occupied bands touch others on the loop)");
     return TBG_OK;
 }
 
@@ -932,6 +935,78 @@ int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out) {
     }
     if ((rc = check_status(me.status_d, ctx.st))) return rc;
     return ctx.sync("tbg_bands_mesh");
+}
+
+int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const double* kvec, int64_t n_occ,
+                     const int64_t* occ, int mode, double* out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    if (mode != 0 && mode != 1) return set_error(TBG_E_INVALID_ARGUMENT, "mode must be 0 (berry_loop) or 1 (det)");
+    if (n_loops < 0 || n_k < 1 || n_occ < 0) return set_error(TBG_E_INVALID_ARGUMENT, "negative size or empty loop");
+    if (n_loops == 0) return TBG_OK;
+    if (!kvec || !out || (n_occ > 0 && !occ)) return set_error(TBG_E_INVALID_ARGUMENT, "null argument");
+    const int N = (int)M.nsta, dim = M.dim;
+    // geometry.rs:160-170: the loop must close modulo an integer vector (else the reference panics)
+    for (int64_t l = 0; l < n_loops; ++l)
+        for (int d = 0; d < dim; ++d) {
+            const double diff = kvec[(l * n_k + n_k - 1) * dim + d] - kvec[(l * n_k) * dim + d];
+            if (!(std::fabs(diff - std::round(diff)) <= 1e-9))
+                return set_error(TBG_E_INVALID_ARGUMENT,
+                                 "wrong, the end of this loop must differ from the beginning by an integer grid vector");
+        }
+    for (int64_t i = 0; i < n_occ; ++i)
+        if (occ[i] < 0 || occ[i] >= N) return set_error(TBG_E_INVALID_ARGUMENT, "occupied band index out of bounds");
+    if (n_occ > kWilsonMaxOcc) return set_error(TBG_E_UNSUPPORTED, "Wilson loops support at most 48 occupied bands");
+    const int svd = mode == 0;
+    if (n_occ == 0) {  // empty product: det 1 (phase 0); no eigenphases
+        if (!svd)
+            for (int64_t l = 0; l < n_loops; ++l) out[l] = 0.0;
+        return TBG_OK;
+    }
+    const int T = (int)(n_k - 1);
+    const int64_t NN = (int64_t)N * N;
+    // loops per chunk: eigenpairs at T points per loop plus the loop workspace
+    const int64_t per_loop = (int64_t)std::max(T, 1) * (sizeof(zc) * NN * 2 + 8 * N + 8 * dim) +
+                             (int64_t)wilson_workspace_bytes(N, 1, (int)n_k, (int)n_occ) + 8 * n_k * dim;
+    int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_loops, chunk_budget_bytes() / per_loop));
+    chunk = std::min<int64_t>(chunk, std::max<int64_t>(1, 65535 / std::max(T, 1)));
+    Ctx ctx;
+    double* kv_d = ctx.alloc<double>(chunk * n_k * dim);
+    double* kp_d = ctx.alloc<double>(chunk * std::max(T, 1) * dim);
+    zc* H = ctx.alloc<zc>(chunk * std::max(T, 1) * NN);
+    zc* U = ctx.alloc<zc>(chunk * std::max(T, 1) * NN);
+    double* E = ctx.alloc<double>(chunk * std::max(T, 1) * N);
+    int* occ_d = ctx.alloc<int>(n_occ);
+    const size_t wb = wilson_workspace_bytes(N, chunk, (int)n_k, (int)n_occ);
+    void* work = ctx.alloc<unsigned char>(wb);
+    double* out_d = ctx.alloc<double>(chunk * (svd ? n_occ : 1));
+    int* status_d = ctx.alloc<int>(1);
+    if (ctx.rc) return ctx.rc;
+    std::vector<int> occ32(occ, occ + n_occ);
+    TBG_CUDA(cudaMemcpyAsync(occ_d, occ32.data(), sizeof(int) * n_occ, cudaMemcpyHostToDevice, ctx.st));
+    TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
+    for (int64_t l0 = 0; l0 < n_loops; l0 += chunk) {
+        const int64_t nl = std::min(chunk, n_loops - l0);
+        TBG_CUDA(cudaMemcpyAsync(kv_d, kvec + l0 * n_k * dim, sizeof(double) * nl * n_k * dim,
+                                 cudaMemcpyHostToDevice, ctx.st));
+        if (T > 0) {
+            // the loop points k_0 .. k_{T-1} (k_T is k_0 up to the gauge phase)
+            TBG_CUDA(cudaMemcpy2DAsync(kp_d, sizeof(double) * T * dim, kv_d, sizeof(double) * n_k * dim,
+                                       sizeof(double) * T * dim, nl, cudaMemcpyDeviceToDevice, ctx.st));
+            const int64_t np = nl * T;
+            if ((rc = fourier_direct(M, ctx.st, np, kp_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0))) return rc;
+            if ((rc = eig_batched(ctx.st, N, np, H, E, U, nullptr, 0, status_d))) return rc;
+        }
+        if ((rc = wilson_from_vectors(ctx.st, M, nl, (int)n_k, kv_d, U, (int)n_occ, occ_d, svd, out_d, work, wb,
+                                      status_d)))
+            return rc;
+        TBG_CUDA(cudaMemcpyAsync(out + l0 * (svd ? n_occ : 1), out_d, sizeof(double) * nl * (svd ? n_occ : 1),
+                                 cudaMemcpyDeviceToHost, ctx.st));
+        if (ctx.sync("tbg_wilson_loops")) return ctx.rc;
+    }
+    if ((rc = check_status(status_d, ctx.st))) return rc;
+    return ctx.sync("tbg_wilson_loops");
 }
 
 int tbg_quantum_geometry(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, double eta,

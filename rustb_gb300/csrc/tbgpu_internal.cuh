@@ -229,6 +229,13 @@ constexpr int kSmallMaxN = 8;
 // Gaussian-smeared DOS: add the terms of count band energies ev (device) to
 // the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds
 // slices * E_n doubles; slices from dos_slices(E_n, chunk energies).
+// Wilson loops from the eigenvectors at the loop points (see wilson.cu).
+constexpr int kWilsonMaxOcc = 48;
+size_t wilson_workspace_bytes(int N, int64_t n_loops, int n_k, int n_occ);
+int wilson_from_vectors(cudaStream_t st, const ModelDev& m, int64_t n_loops, int n_k, const double* kv_d, const zc* U,
+                        int n_occ, const int* occ_d, int svd, double* out, void* work, size_t work_bytes,
+                        int* status_d);
+
 int dos_slices(int64_t E_n, int64_t count);
 int dos_accumulate(cudaStream_t st, int64_t count, const double* ev, int64_t E_n, double E_min, double step,
                    double sigma, double* part, int slices, double* acc);

@@ -498,3 +498,79 @@ class Model:
     def natom(self) -> int:
         """Number of atoms (set by the Wannier90 loader; 0 for hand-built models)."""
         return len(getattr(self, "atoms", []) or [])
+
+    # ----------------------------------------------------------- Wilson loops
+    def _wilson(self, kvec3: np.ndarray, occ, mode: int) -> np.ndarray:
+        kv = np.ascontiguousarray(np.asarray(kvec3, dtype=np.float64))
+        n_loops, n_k = kv.shape[0], kv.shape[1]
+        occ_a = np.ascontiguousarray(np.asarray(list(occ), dtype=np.int64).reshape(-1))
+        out = np.empty((n_loops, occ_a.size) if mode == 0 else (n_loops,))
+        lib = _lib.load()
+        _lib.check(lib.tbg_wilson_loops(self.device_handle(), n_loops, n_k, _lib.dptr(kv), occ_a.size,
+                                        _lib.iptr(occ_a) if occ_a.size else None, int(mode), _lib.dptr(out)), lib)
+        return out
+
+    def _check_loop(self, kvec):
+        k = np.asarray(kvec, dtype=np.float64)
+        if k.ndim != 2 or k.shape[1] != self.dim or k.shape[0] < 1:
+            raise errors.TbPanic(f"k-loop must have shape (n_k, {self.dim})")
+        return k
+
+    def berry_loop(self, kvec, occ) -> np.ndarray:
+        """``Berry::berry_loop`` (src/geometry.rs:156-215): -arg of the eigenvalues
+        of the product of the unitary parts of the overlap matrices along the
+        closed loop ``kvec`` (n_k, dim); ascending (the reference's order is
+        LAPACK zgeev's)."""
+        k = self._check_loop(kvec)
+        return self._wilson(k[None], occ, 0)[0]
+
+    def berry_loop_det(self, kvec, occ) -> float:
+        """``Berry::berry_loop_det`` (src/geometry.rs:217-270)."""
+        k = self._check_loop(kvec)
+        return float(self._wilson(k[None], occ, 1)[0])
+
+    def berry_flux(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int) -> np.ndarray:
+        """``Berry::berry_flux`` (src/geometry.rs:272-339): Wilson loop around
+        every plaquette of the (nk1, nk2) mesh spanned by dir_1, dir_2 from
+        k_start; (nk1, nk2, n_occ), each plaquette's phases ascending."""
+        ks, d1, d2 = (np.asarray(v, dtype=np.float64).reshape(-1) for v in (k_start, dir_1, dir_2))
+        for name, v in (("k_start", ks), ("dir_1", d1), ("dir_2", d2)):
+            if v.size != self.dim:
+                raise errors.TbPanic(f"Wrong!, the {name}'s length is {v.size} but dim_r is {self.dim}, it's not equal!")
+        if nk1 < 1 or nk2 < 1:
+            raise errors.TbPanic(f"Wrong!, nk1 and nk2 must be at least 1, but nk1={nk1} and nk2={nk2}")
+        loops = np.empty((nk1 * nk2, 5, self.dim))
+        dx, dy = 1.0 / nk1, 1.0 / nk2
+        for i in range(nk1):
+            for j in range(nk2):
+                i0, j0 = i / nk1, j / nk2
+                r = loops[i * nk2 + j]
+                r[0] = ks + i0 * d1 + j0 * d2
+                r[1] = ks + (i0 + dx) * d1 + j0 * d2
+                r[2] = ks + (i0 + dx) * d1 + (j0 + dy) * d2
+                r[3] = ks + i0 * d1 + (j0 + dy) * d2
+                r[4] = ks + i0 * d1 + j0 * d2
+        occ = list(occ)
+        return self._wilson(loops, occ, 0).reshape(nk1, nk2, len(occ))
+
+    def berry_phase(self, occ, kvec) -> np.ndarray:
+        """``Berry::berry_phase`` (src/geometry.rs:341-358): one loop per
+        ``kvec[i]`` (nk1, nk2, dim); returns (n_occ, nk1), each column sorted."""
+        kv = np.asarray(kvec, dtype=np.float64)
+        return self._wilson(kv, occ, 0).T.copy()
+
+    def wannier_centre(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int) -> np.ndarray:
+        """``Berry::wannier_centre`` (src/geometry.rs:360-420): loops along dir_2
+        at nk1 positions along dir_1 (both ends included); (n_occ, nk1)."""
+        ks, d1, d2 = (np.asarray(v, dtype=np.float64).reshape(-1) for v in (k_start, dir_1, dir_2))
+        for name, v in (("k_start", ks), ("dir_1", d1), ("dir_2", d2)):
+            if v.size != self.dim:
+                raise errors.TbPanic(f"Wrong!, the {name}'s length is {v.size} but dim_r is {self.dim}, it's not equal!")
+        if nk1 < 2 or nk2 < 2:
+            raise errors.TbPanic(f"Wrong!, nk1 and nk2 must be at least 2 for a finite-difference k-mesh, but "
+                                 f"nk1={nk1} and nk2={nk2}")
+        kv = np.empty((nk1, nk2, self.dim))
+        for i in range(nk1):
+            for j in range(nk2):
+                kv[i, j] = ks + d1 * float(i) / float(nk1 - 1) + d2 * float(j) / float(nk2 - 1)
+        return self._wilson(kv, occ, 0).T.copy()
