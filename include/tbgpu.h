@@ -226,7 +226,7 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
 /* Wilson loops over n_loops closed k-paths kvec (n_loops, n_k, dim); each
  * path's last point must equal its first up to an integer vector G (the
  * eigenvectors there are the first point's times exp(-2 pi i G . tau)).
- * occ (n_occ) are the occupied band indices (n_occ <= 48).
+ * occ (n_occ) are the occupied band indices (n_occ <= 64).
  * mode 0: out (n_loops, n_occ) = -arg of the eigenvalues of the product of the
  *         unitary (U V^dagger) parts of the overlap matrices, ascending per loop;
  *         replaces Berry::berry_loop (src/geometry.rs:156-215) and, through the

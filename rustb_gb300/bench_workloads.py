@@ -14,6 +14,9 @@
 * ``dos``       -- Model::dos of the reference's benchmark model (two-band
                    honeycomb, -3..3 eV, 500 bins, sigma 1e-2) on a
                    1000 x 1000 mesh; a step is the whole mesh.
+* ``wilson``    -- hybrid Wannier centres (Berry::wannier_centre) of a random
+                   spinful 2D model with 64 bands, 32 occupied, 64 loops of
+                   64 points; a step is the whole set of loops.
 * ``w90``       -- Wannier90 loading: a 64-orbital, 125-R seedname_hr.dat
                    (512 000 lines, Wannier90's 5I5,2F12.6 format) read into a
                    device-resident model; a step is one load.
@@ -60,7 +63,7 @@ def run(args, rank, world, local):
     if rank != 0 and args.impl == "reference":
         return 0
     fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench,
-          "dos": dos_bench, "w90": w90_bench}[args.workload]
+          "dos": dos_bench, "w90": w90_bench, "wilson": wilson_bench}[args.workload]
     return fn(args, rank, world, local)
 
 
@@ -488,3 +491,78 @@ def w90_bench(args, rank, world, local):
         return 0
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
+
+
+# ------------------------------------------------------------------ wilson --
+WILSON_METRIC = "Wilson loops/s (wannier_centre: eigenvectors, overlaps, unitary factors, eigenphases)"
+
+
+def wilson_bench(args, rank, world, local):
+    from oracle import tb_oracle as O
+
+    model = W.random_model(2, 32, True, 1, seed=20260108)
+    occ = list(range(32))
+    nk1 = nk2 = 64
+    cfg = {"workload": "Berry::wannier_centre of a random spinful 2D model (32 orbitals, 64 bands, R in "
+                       "{-1,0,1}^2), occupied bands 0..31, 64 loops along k2 of 64 points", "nsta": model.nsta,
+           "n_occ": len(occ), "loops": nk1, "points_per_loop": nk2}
+    sample = 2
+
+    def cpu_once():
+        t0 = time.perf_counter()
+        for i in range(sample):
+            loop = np.array([[i / (nk1 - 1), j / (nk2 - 1)] for j in range(nk2)])
+            O.wilson_loop(model, loop, occ)
+        return sample / (time.perf_counter() - t0)
+
+    if args.impl == "reference":
+        val = cpu_once()
+        _line(args, world, WILSON_METRIC, val, "loops/s", 1e3 / val, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "loops/s", "cores": 1, "kind": "port",
+                                                     "sample": f"{sample} of the loops (numpy + LAPACK per loop)"},
+               "e2e": {"value": val, "unit": "loops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    args0 = (occ, [0.0, 0.0], [1.0, 0.0], [0.0, 1.0], nk1, nk2)
+    for _ in range(args.warmup):
+        model.wannier_centre(*args0)
+    lib.tbg_kernel_timing_enable(1)
+    _lib.kernel_timing(reset=True)
+    l0 = lib.tbg_kernel_launch_count(0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        wcc = model.wannier_centre(*args0)
+    wall = time.perf_counter() - t0
+    launches = lib.tbg_kernel_launch_count(0) - l0
+    lib.tbg_kernel_timing_enable(0)
+    timing = _lib.kernel_timing(reset=True)
+    val = args.steps * nk1 * world / wall
+    # e2e: model upload + the loops + the centres read back, per step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m2 = W.random_model(2, 32, True, 1, seed=20260108)
+        m2.wannier_centre(*args0)
+        m2._invalidate()
+    e2e = args.steps * nk1 / (time.perf_counter() - t0)
+    # roofline: the kernel family with the largest device time, against the FP64 pipe
+    name, (ln, ms, work) = max(timing.items(), key=lambda kv: kv[1][1])
+    import ctypes
+
+    p64 = ctypes.c_double(0.0)
+    p32 = ctypes.c_double(0.0)
+    lib.tbg_measure_fma_peaks(ctypes.byref(p64), ctypes.byref(p32))
+    ach = work / (ms / 1e3) / 1e12 if work > 0 and ms > 0 else None
+    roof = {"bound": "fp64", "achieved": ach, "peak": p64.value, "unit": "TFLOP/s",
+            "frac": ach / p64.value if ach and p64.value else None, "traffic": None, "kernel": name,
+            "launches": ln, "avg_launch_ms": ms / max(ln, 1),
+            "peak_source": "FP64 FMA loop on this GPU (tbg_measure_fma_peaks); 14 N^3 flops per eigensolve"}
+    cpu = cpu_once()
+    _line(args, world, WILSON_METRIC, val, "loops/s", wall / args.steps * 1e3, "f64", cfg,
+          {"roofline": roof, "gpu_launches": int(launches), "wcc_shape": list(wcc.shape),
+           "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in timing.items()},
+           "cpu_baseline": {"value": cpu, "unit": "loops/s", "cores": 1, "kind": "port",
+                            "sample": f"{sample} of the loops (numpy + LAPACK per loop, one thread)"},
+           "e2e": {"value": e2e, "unit": "loops/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
+                   "d2h_bytes_per_step": int(wcc.nbytes)}})
+    return 0

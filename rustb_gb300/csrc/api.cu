@@ -957,7 +957,7 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
         }
     for (int64_t i = 0; i < n_occ; ++i)
         if (occ[i] < 0 || occ[i] >= N) return set_error(TBG_E_INVALID_ARGUMENT, "occupied band index out of bounds");
-    if (n_occ > kWilsonMaxOcc) return set_error(TBG_E_UNSUPPORTED, "Wilson loops support at most 48 occupied bands");
+    if (n_occ > kWilsonMaxOcc) return set_error(TBG_E_UNSUPPORTED, "Wilson loops support at most 64 occupied bands");
     const int svd = mode == 0;
     if (n_occ == 0) {  // empty product: det 1 (phase 0); no eigenphases
         if (!svd)

@@ -230,7 +230,7 @@ constexpr int kSmallMaxN = 8;
 // the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds
 // slices * E_n doubles; slices from dos_slices(E_n, chunk energies).
 // Wilson loops from the eigenvectors at the loop points (see wilson.cu).
-constexpr int kWilsonMaxOcc = 48;
+constexpr int kWilsonMaxOcc = 64;
 size_t wilson_workspace_bytes(int N, int64_t n_loops, int n_k, int n_occ);
 int wilson_from_vectors(cudaStream_t st, const ModelDev& m, int64_t n_loops, int n_k, const double* kv_d, const zc* U,
                         int n_occ, const int* occ_d, int svd, double* out, void* work, size_t work_bytes,

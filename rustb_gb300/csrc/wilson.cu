@@ -9,12 +9,12 @@
 // Atom-gauge H(k_t) (solve_all, src/solve_ham.rs:110-184).
 //
 // GB300 form: one block per segment forms O_t from the eigenvector columns
-// (L2-resident); one block per loop takes each O_t to its unitary factor by
-// the Newton-Schulz iteration X <- X (3 - X^dagger X) / 2 (the singular values
-// of an overlap of orthonormal sets lie in (0, 1], where it converges
+// (L2-resident) and, in another launch, takes it to its unitary factor by the
+// Newton-Schulz iteration X <- X (3 - X^dagger X) / 2 (the singular values of
+// an overlap of orthonormal sets lie in (0, 1], where it converges
 // quadratically; a bounded number of steps, a singular overlap -- the gap
-// closing on the path -- is reported) and multiplies the chain in shared
-// memory.  P is unitary, so its eigenvectors are those of the Hermitian
+// closing on the path -- is reported); one block per loop multiplies the
+// chain in shared memory.  P is unitary, so its eigenvectors are those of the Hermitian
 // Re(e^{-i phi} P) = (e^{-i phi} P + e^{i phi} P^dagger) / 2 (eigenvalues
 // cos(theta - phi), distinct unless theta_i + theta_j = 2 phi): that matrix
 // goes through the batched Hermitian eigensolver for two angles phi, and
@@ -89,73 +89,77 @@ __device__ void smem_mm(int n, const zc* A, const zc* B, zc* C) {
     }
 }
 
-// P[l] = prod_t (unitary factor of O[l][t])  (svd) or prod_t O[l][t]  (det).
-__global__ void __launch_bounds__(256) wl_chain_kernel(int n, int T, int svd, const zc* __restrict__ O,
-                                                       zc* __restrict__ P, int* __restrict__ status) {
+// O[seg] <- its unitary factor U V^dagger, one block per segment, by the
+// Newton-Schulz iteration: stop when X is unitary to rounding, or one step
+// after the error fell below 1e-8 (that step squares it).
+__global__ void __launch_bounds__(256) wl_polar_kernel(int n, zc* __restrict__ O, int* __restrict__ status) {
     extern __shared__ zc wsm[];
     zc* X = wsm;
     zc* Y = X + n * n;
     zc* Z = Y + n * n;
-    zc* Pc = Z + n * n;
     __shared__ double s_err;
-    __shared__ int s_fail;
+    const int nn = n * n;
+    zc* Ot = O + (int64_t)blockIdx.x * nn;
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) X[e] = Ot[e];
+    __syncthreads();
+    double err = 1.0;
+    for (int it = 0; it < kMaxNS; ++it) {
+        // Y = X^dagger X
+        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+            const int i = e / n, j = e % n;
+            zc s = mk(0.0, 0.0);
+            for (int k = 0; k < n; ++k) fma_cjx(s, X[k * n + i], X[k * n + j]);
+            Y[e] = s;
+        }
+        if (threadIdx.x == 0) s_err = 0.0;
+        __syncthreads();
+        double m = 0.0;
+        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+            const double dr = Y[e].re - ((e / n == e % n) ? 1.0 : 0.0);
+            m = fmax(m, fabs(dr) + fabs(Y[e].im));
+        }
+        // block max (non-negative doubles order like their bit patterns)
+        atomicMax(reinterpret_cast<unsigned long long*>(&s_err), (unsigned long long)__double_as_longlong(m));
+        __syncthreads();
+        err = s_err;
+        if (err <= 4e-16 * n) break;  // uniform: every thread read the same s_err
+        // Y <- (3 I - Y) / 2, X <- X Y
+        for (int e = threadIdx.x; e < nn; e += blockDim.x)
+            Y[e] = mk(((e / n == e % n) ? 1.5 : 0.0) - 0.5 * Y[e].re, -0.5 * Y[e].im);
+        __syncthreads();
+        smem_mm(n, X, Y, Z);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nn; e += blockDim.x) X[e] = Z[e];
+        __syncthreads();
+        if (err <= 1e-8) {
+            err = 0.0;
+            break;
+        }
+    }
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) Ot[e] = X[e];
+    if (threadIdx.x == 0 && err > 1e-8) atomicOr(status, 4);
+}
+
+// P[l] = O[l][0] ... O[l][T-1] (unitary factors in SVD mode, raw overlaps in det mode).
+__global__ void __launch_bounds__(256) wl_chain_kernel(int n, int T, const zc* __restrict__ O, zc* __restrict__ P) {
+    extern __shared__ zc wsm[];
+    zc* X = wsm;
+    zc* Z = X + n * n;
+    zc* Pc = Z + n * n;
     const int64_t l = blockIdx.x;
     const int nn = n * n;
     for (int e = threadIdx.x; e < nn; e += blockDim.x) Pc[e] = mk((e / n == e % n) ? 1.0 : 0.0, 0.0);
-    if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
     for (int t = 0; t < T; ++t) {
         const zc* Ot = O + (l * T + t) * (int64_t)nn;
         for (int e = threadIdx.x; e < nn; e += blockDim.x) X[e] = Ot[e];
         __syncthreads();
-        if (svd) {
-            // Newton-Schulz: stop when X is unitary to rounding, or one step after
-            // the error fell below 1e-8 (that step squares it)
-            double err = 1.0;
-            for (int it = 0; it < kMaxNS; ++it) {
-                // Y = X^dagger X
-                for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-                    const int i = e / n, j = e % n;
-                    zc s = mk(0.0, 0.0);
-                    for (int k = 0; k < n; ++k) fma_cjx(s, X[k * n + i], X[k * n + j]);
-                    Y[e] = s;
-                }
-                if (threadIdx.x == 0) s_err = 0.0;
-                __syncthreads();
-                double m = 0.0;
-                for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-                    const double dr = Y[e].re - ((e / n == e % n) ? 1.0 : 0.0);
-                    m = fmax(m, fabs(dr) + fabs(Y[e].im));
-                }
-                // block max (non-negative doubles order like their bit patterns)
-                atomicMax(reinterpret_cast<unsigned long long*>(&s_err), (unsigned long long)__double_as_longlong(m));
-                __syncthreads();
-                err = s_err;
-                if (err <= 4e-16 * n) break;  // uniform: every thread read the same s_err
-                // Y <- (3 I - Y) / 2, X <- X Y
-                for (int e = threadIdx.x; e < nn; e += blockDim.x)
-                    Y[e] = mk(((e / n == e % n) ? 1.5 : 0.0) - 0.5 * Y[e].re, -0.5 * Y[e].im);
-                __syncthreads();
-                smem_mm(n, X, Y, Z);
-                __syncthreads();
-                for (int e = threadIdx.x; e < nn; e += blockDim.x) X[e] = Z[e];
-                __syncthreads();
-                if (err <= 1e-8) {
-                    err = 0.0;
-                    break;
-                }
-            }
-            if (threadIdx.x == 0 && err > 1e-8) s_fail = 1;
-            __syncthreads();
-        }
-        // Pc <- Pc X
-        smem_mm(n, Pc, X, Z);
+        smem_mm(n, Pc, X, Z);  // Pc <- Pc X
         __syncthreads();
         for (int e = threadIdx.x; e < nn; e += blockDim.x) Pc[e] = Z[e];
         __syncthreads();
     }
     for (int e = threadIdx.x; e < nn; e += blockDim.x) P[l * nn + e] = Pc[e];
-    if (threadIdx.x == 0 && s_fail) atomicOr(status, 4);
 }
 
 // Hz[l] = (e^{-i phi} P + e^{i phi} P^dagger) / 2
@@ -264,12 +268,12 @@ int wl_allow_smem(K kern, size_t need) {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, kern);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncGetAttributes(wl_chain_kernel)");
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncGetAttributes(wilson kernel)");
     // static and dynamic shared memory together stay within the opt-in limit
     const int dyn_max = optin - (int)fa.sharedSizeBytes;
     if (need > (size_t)dyn_max) return set_error(TBG_E_UNSUPPORTED, "Wilson loop: too many occupied bands");
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_max);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(wl_chain_kernel)");
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(wilson kernel)");
     return TBG_OK;
 }
 
@@ -279,7 +283,7 @@ inline unsigned nblk(int64_t total) {
 
 }  // namespace
 
-size_t wilson_chain_smem(int n_occ) { return sizeof(zc) * 4 * (size_t)n_occ * n_occ; }
+size_t wilson_chain_smem(int n_occ) { return sizeof(zc) * 3 * (size_t)n_occ * n_occ; }
 
 // kv_d: (n_loops, n_k, dim) k-points; U: eigenvectors at points t < n_k - 1 of
 // every loop, (n_loops * (n_k - 1), N, N).  out: (n_loops, n_occ) or (n_loops).
@@ -311,11 +315,17 @@ int wilson_from_vectors(cudaStream_t st, const ModelDev& m, int64_t n_loops, int
         wl_overlap_kernel<<<(unsigned)(n_loops * T), 256, 0, st>>>(N, n_occ, T, U, occ_d, endph, O);
         TBG_LAUNCHED("wl_overlap_kernel");
     }
+    const size_t smem = wilson_chain_smem(n_occ);
+    if (svd && T > 0) {
+        KTimer kt(st, "wl_polar_kernel");
+        if (int rc = wl_allow_smem(wl_polar_kernel, smem)) return rc;
+        wl_polar_kernel<<<(unsigned)(n_loops * T), 256, smem, st>>>(n_occ, O, status_d);
+        TBG_LAUNCHED("wl_polar_kernel");
+    }
     {
         KTimer kt(st, "wl_chain_kernel");
-        const size_t smem = wilson_chain_smem(n_occ);
         if (int rc = wl_allow_smem(wl_chain_kernel, smem)) return rc;
-        wl_chain_kernel<<<(unsigned)n_loops, 256, smem, st>>>(n_occ, T, svd, O, P, status_d);
+        wl_chain_kernel<<<(unsigned)n_loops, 256, smem, st>>>(n_occ, T, O, P);
         TBG_LAUNCHED("wl_chain_kernel");
     }
     if (!svd) {

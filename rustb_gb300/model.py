@@ -539,17 +539,17 @@ class Model:
                 raise errors.TbPanic(f"Wrong!, the {name}'s length is {v.size} but dim_r is {self.dim}, it's not equal!")
         if nk1 < 1 or nk2 < 1:
             raise errors.TbPanic(f"Wrong!, nk1 and nk2 must be at least 1, but nk1={nk1} and nk2={nk2}")
-        loops = np.empty((nk1 * nk2, 5, self.dim))
+        # element-wise the same operations in the same order as geometry.rs:309-326
         dx, dy = 1.0 / nk1, 1.0 / nk2
-        for i in range(nk1):
-            for j in range(nk2):
-                i0, j0 = i / nk1, j / nk2
-                r = loops[i * nk2 + j]
-                r[0] = ks + i0 * d1 + j0 * d2
-                r[1] = ks + (i0 + dx) * d1 + j0 * d2
-                r[2] = ks + (i0 + dx) * d1 + (j0 + dy) * d2
-                r[3] = ks + i0 * d1 + (j0 + dy) * d2
-                r[4] = ks + i0 * d1 + j0 * d2
+        i0 = (np.arange(nk1, dtype=np.float64) / nk1)[:, None, None]
+        j0 = (np.arange(nk2, dtype=np.float64) / nk2)[None, :, None]
+        loops = np.empty((nk1, nk2, 5, self.dim))
+        loops[:, :, 0] = ks + i0 * d1 + j0 * d2
+        loops[:, :, 1] = ks + (i0 + dx) * d1 + j0 * d2
+        loops[:, :, 2] = ks + (i0 + dx) * d1 + (j0 + dy) * d2
+        loops[:, :, 3] = ks + i0 * d1 + (j0 + dy) * d2
+        loops[:, :, 4] = ks + i0 * d1 + j0 * d2
+        loops = loops.reshape(nk1 * nk2, 5, self.dim)
         occ = list(occ)
         return self._wilson(loops, occ, 0).reshape(nk1, nk2, len(occ))
 
@@ -569,8 +569,8 @@ class Model:
         if nk1 < 2 or nk2 < 2:
             raise errors.TbPanic(f"Wrong!, nk1 and nk2 must be at least 2 for a finite-difference k-mesh, but "
                                  f"nk1={nk1} and nk2={nk2}")
-        kv = np.empty((nk1, nk2, self.dim))
-        for i in range(nk1):
-            for j in range(nk2):
-                kv[i, j] = ks + d1 * float(i) / float(nk1 - 1) + d2 * float(j) / float(nk2 - 1)
+        # element-wise as geometry.rs:398-403: k_start + dir_1 * i / (nk1 - 1) + dir_2 * j / (nk2 - 1)
+        fi = np.arange(nk1, dtype=np.float64)[:, None, None]
+        fj = np.arange(nk2, dtype=np.float64)[None, :, None]
+        kv = ks + d1 * fi / float(nk1 - 1) + d2 * fj / float(nk2 - 1)
         return self._wilson(kv, occ, 0).T.copy()

@@ -47,6 +47,7 @@ CASES = [
     ("kane_mele", lambda: M.kane_mele(rashba=0.1), [0, 1]),
     ("random12", lambda: W.random_model(2, 12, False, 1, seed=401), [0, 1, 2, 3, 4]),
     ("random3d_s8", lambda: W.random_model(3, 8, True, 1, seed=402), list(range(7))),
+    ("random2d_s32_occ60", lambda: W.random_model(2, 32, True, 1, seed=405), list(range(60))),
     ("qwz3d", M.qwz_stacked_3d, [0]),
 ]
 
@@ -112,6 +113,6 @@ def test_wilson_errors():
         m.berry_loop(np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]]), [2])
     with pytest.raises(errors.TbPanic):
         m.wannier_centre([0], [0.0, 0.0], [1.0, 0.0], [0.0, 1.0], 1, 5)
-    big = W.random_model(2, 60, False, 1, seed=404)
-    with pytest.raises(errors.TbPanic):  # more than 48 occupied bands
-        big.berry_loop(np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]]), list(range(50)))
+    big = W.random_model(2, 70, False, 1, seed=404)
+    with pytest.raises(errors.TbPanic):  # more than 64 occupied bands
+        big.berry_loop(np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]]), list(range(66)))
