@@ -170,6 +170,21 @@ int tbg_hall_conductivity(const tbg_model* m, const int64_t* kmesh,
                           double T, double eta, int spin, int precision,
                           double* sigma_out, tbg_report* report);
 
+/* Anomalous / spin Hall conductivity with Integration::EnergyCut on the
+ * uniform mesh kmesh[dim] (dim 2 or 3; mu sorted ascending): eigenpairs and
+ * K_nm = v^a_nm v^b_mn at every mesh point, bands tracked by eigenvector
+ * overlap, each triangle (2D, both diagonals) or tetrahedron (3D) cut at every
+ * mu -- vertex-averaged Omega where a band is fully occupied, quadrature of
+ * the interpolated Kubo term on the occupied part where it is partly occupied
+ * -- and, for T > 0, the thermal convolution of the zero-width result.
+ * sigma_out[j] / det(lat).  FP64.
+ * Replaces: Model::hall_conductivity with Integration::EnergyCut
+ * (src/response/linear/mod.rs:226-268, src/response/tracking.rs:123-240,
+ * src/response/energy_cut.rs:1120-1849). */
+int tbg_hall_energy_cut(const tbg_model* m, const int64_t* kmesh,
+                        const double* dirs2, int64_t nmu, const double* mu,
+                        double T, double eta, int spin, double* sigma_out);
+
 /* Unnormalised Direct-integration sums over the k-points of the uniform mesh
  * kmesh[dim] with flat indices [k_begin, k_begin + k_count) in gen_kmesh order:
  *   sums_out[j] = sum_k sum_n Omega_n f(E_n, mu_j).

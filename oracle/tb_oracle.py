@@ -581,3 +581,431 @@ def wannier_centre(model, occ, k_start, dir_1, dir_2, nk1, nk2):
         loop = np.array([ks + d1 * float(i) / float(nk1 - 1) + d2 * float(j) / float(nk2 - 1) for j in range(nk2)])
         out[i] = wilson_loop(model, loop, occ)
     return out.T
+
+
+# --------------------------------------------------------------------------
+# Energy-cut Hall integration (src/response/linear/mod.rs:226-268,
+# primitives.rs:33-137, tracking.rs, energy_cut.rs, quadrature.rs)
+# --------------------------------------------------------------------------
+
+EC_EPS = 1e-12                                   # energy_cut.rs:47
+FERMI_X_CUT, FERMI_X_STEPS = 18.0, 72            # energy_cut.rs:48-49
+TRI_Q = [[2 / 3, 1 / 6, 1 / 6], [1 / 6, 2 / 3, 1 / 6], [1 / 6, 1 / 6, 2 / 3]]      # quadrature.rs:10-14
+TET_Q = [[0.5854101966249685, 0.1381966011250105, 0.1381966011250105, 0.1381966011250105],
+         [0.1381966011250105, 0.5854101966249685, 0.1381966011250105, 0.1381966011250105],
+         [0.1381966011250105, 0.1381966011250105, 0.5854101966249685, 0.1381966011250105],
+         [0.1381966011250105, 0.1381966011250105, 0.1381966011250105, 0.5854101966249685]]
+CUBE_TETS = [[0, 1, 2, 4], [3, 1, 2, 7], [5, 1, 4, 7], [6, 2, 4, 7], [1, 2, 4, 7]]  # tracking.rs:8-14
+TET_VOL_FACTOR = [1 / 6, 1 / 6, 1 / 6, 1 / 6, 1 / 3]
+
+
+def vertex_kernels(model, kmesh, directions, spin=-1):
+    """compute_velocity_kernel at every mesh point (primitives.rs:33-137):
+    energies E (nk, N), eigenvectors W (nk, N, N) in columns, and
+    K_nm = va_nm vb_mn (va spin-dressed)."""
+    k = gen_kmesh(kmesh)
+    nk, N = k.shape[0], model.nsta
+    E = np.empty((nk, N))
+    Wv = np.empty((nk, N, N), dtype=np.complex128)
+    K = np.empty((nk, N, N), dtype=np.complex128)
+    for i, kk in enumerate(k):
+        V, H = gen_v_projected(model, kk, 1, directions)
+        e, w = eigh(H)
+        J = V[0]
+        if model.spin and spin is not None and spin >= 0:
+            S = spin_matrix(model.norb, spin)
+            J = 0.5 * (S @ J + J @ S)
+        va = w.conj().T @ J @ w
+        vb = w.conj().T @ V[1] @ w
+        E[i], Wv[i], K[i] = e, w, va * vb.T
+    return E, Wv, K
+
+
+def neighbour_indices(i, kmesh):
+    """tracking.rs:177-240 (non-periodic, in the order +x, -x, +y, -y, +z, -z)."""
+    dim = len(kmesh)
+    out = []
+    if dim == 1:
+        for d in (1, -1):
+            j = i + d
+            if 0 <= j < kmesh[0]:
+                out.append(j)
+    elif dim == 2:
+        nx, ny = kmesh
+        ix, iy = divmod(i, ny)
+        for dx, dy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+            jx, jy = ix + dx, iy + dy
+            if 0 <= jx < nx and 0 <= jy < ny:
+                out.append(jx * ny + jy)
+    else:
+        nx, ny, nz = kmesh
+        ix, rem = divmod(i, ny * nz)
+        iy, iz = divmod(rem, nz)
+        for dx, dy, dz in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+            jx, jy, jz = ix + dx, iy + dy, iz + dz
+            if 0 <= jx < nx and 0 <= jy < ny and 0 <= jz < nz:
+                out.append(jx * ny * nz + jy * nz + jz)
+    return out
+
+
+def greedy_assign(ov):
+    """tracking.rs:43-68: rows by their best overlap (descending, stable), each
+    takes its best still-free column (the first on ties)."""
+    n = ov.shape[0]
+    rows = sorted(range(n), key=lambda i: -np.max(ov[i]))
+    taken = [False] * n
+    perm = [0] * n
+    for i in rows:
+        best_j, best = 0, -1.0
+        for j in range(n):
+            if not taken[j] and ov[i, j] > best:
+                best, best_j = ov[i, j], j
+        taken[best_j] = True
+        perm[i] = best_j
+    return perm
+
+
+def global_band_track(E, Wv, K, kmesh):
+    """tracking.rs:123-175: breadth-first from vertex 0; each new vertex is
+    permuted by the greedy assignment of its averaged overlaps with the
+    already-visited neighbours.  Returns the permutation of every vertex."""
+    nk = E.shape[0]
+    perms = [list(range(E.shape[1])) for _ in range(nk)]
+    if nk <= 1:
+        return perms
+    from collections import deque
+    visited = [False] * nk
+    visited[0] = True
+    q = deque([0])
+    while q:
+        cur = q.popleft()
+        for nb in neighbour_indices(cur, kmesh):
+            if visited[nb]:
+                continue
+            ov_sum, cnt = None, 0
+            for vn in neighbour_indices(nb, kmesh):
+                if not visited[vn]:
+                    continue
+                A = Wv[vn][:, perms[vn]]
+                ov = np.abs(A.conj().T @ Wv[nb]) ** 2
+                ov_sum = ov if ov_sum is None else ov_sum + ov
+                cnt += 1
+            if ov_sum is not None:
+                perms[nb] = greedy_assign(ov_sum / cnt)
+            visited[nb] = True
+            q.append(nb)
+    return perms
+
+
+def eval_berry_kernel(e, K, eta):
+    """kernel.rs:54-80 (Omega part): terms with denominator < 1e-30 skipped."""
+    N = len(e)
+    om = np.zeros(N)
+    eta2 = eta * eta
+    for n in range(N):
+        g = 0j
+        for m in range(N):
+            if m == n:
+                continue
+            de = e[n] - e[m]
+            den = de * de + eta2
+            if den < 1e-30:
+                continue
+            g += K[n, m] / den
+        om[n] = -2.0 * g.imag
+    return om
+
+
+def _eval_band_at_lam(n, bands, krows, lam, eta):
+    """eval_berry_band_at_lam_buf (kernel.rs:138-182): barycentric E_m and K_nm."""
+    N = len(bands[0])
+    e = np.zeros(N)
+    for v in range(len(bands)):
+        if lam[v] != 0.0:
+            e = e + bands[v] * lam[v]
+    kr = np.zeros(N, dtype=np.complex128)
+    for v in range(len(krows)):
+        if lam[v] != 0.0:
+            kr = kr + krows[v] * lam[v]
+    eta2 = eta * eta
+    g = 0j
+    for m in range(N):
+        if m == n:
+            continue
+        de = e[n] - e[m]
+        den = de * de + eta2
+        if den < 1e-30:
+            continue
+        g += kr[m] / den
+    return -2.0 * g.imag
+
+
+def _tri_area(c):
+    return 0.5 * abs((c[1][0] - c[0][0]) * (c[2][1] - c[0][1]) - (c[2][0] - c[0][0]) * (c[1][1] - c[0][1]))
+
+
+def _clip_triangle(ev, mu):
+    """energy_cut.rs:1120-1170."""
+    eps = 1e-12
+    if mu <= min(ev) + eps:
+        return []
+    if mu >= max(ev) - eps:
+        return [[[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]]]
+    a, b, c = sorted(range(3), key=lambda i: ev[i])
+
+    def unit(i):
+        l = [0.0, 0.0, 0.0]
+        l[i] = 1.0
+        return l
+
+    def cut(i, j):
+        de = ev[j] - ev[i]
+        t = 0.5 if abs(de) < eps else min(max((mu - ev[i]) / de, 0.0), 1.0)
+        l = [0.0, 0.0, 0.0]
+        l[i] = 1.0 - t
+        l[j] = t
+        return l
+
+    if mu <= ev[b] + eps:
+        return [[unit(a), cut(a, b), cut(a, c)]]
+    return [[unit(a), unit(b), cut(a, c)], [unit(b), cut(a, c), cut(b, c)]]
+
+
+def _tri_partial(coords, ev, bands, krows, mu, eta, n):
+    """triangle_occupied_hybrid's partial branch (energy_cut.rs:1205-1228)."""
+    total = 0.0
+    for sub in _clip_triangle(ev, mu):
+        pts = [[sum(l[i] * coords[i][0] for i in range(3)), sum(l[i] * coords[i][1] for i in range(3))] for l in sub]
+        p0 = [sub[0][0] * coords[0][0] + sub[0][1] * coords[1][0] + sub[0][2] * coords[2][0],
+              sub[0][0] * coords[0][1] + sub[0][1] * coords[1][1] + sub[0][2] * coords[2][1]]
+        p1 = [sub[1][0] * coords[0][0] + sub[1][1] * coords[1][0] + sub[1][2] * coords[2][0],
+              sub[1][0] * coords[0][1] + sub[1][1] * coords[1][1] + sub[1][2] * coords[2][1]]
+        p2 = [sub[2][0] * coords[0][0] + sub[2][1] * coords[1][0] + sub[2][2] * coords[2][0],
+              sub[2][0] * coords[0][1] + sub[2][1] * coords[1][1] + sub[2][2] * coords[2][1]]
+        del pts
+        sub_area = 0.5 * abs((p1[0] - p0[0]) * (p2[1] - p0[1]) - (p2[0] - p0[0]) * (p1[1] - p0[1]))
+        if sub_area < 1e-30:
+            continue
+        for q in range(3):
+            al = TRI_Q[q]
+            lam = [al[0] * sub[0][i] + al[1] * sub[1][i] + al[2] * sub[2][i] for i in range(3)]
+            total += sub_area * (1.0 / 3.0) * _eval_band_at_lam(n, bands, krows, lam, eta)
+    return total
+
+
+def _mu_ranges(mu, e_min, e_max):
+    i_partial = int(np.searchsorted(mu, e_min + EC_EPS, side="right"))   # partition_point(x <= e_min + eps)
+    i_full = int(np.searchsorted(mu, e_max - EC_EPS, side="left"))       # partition_point(x < e_max - eps)
+    return i_partial, i_full
+
+
+def integrate_fermi_cut_2d_t0(E, K, perms, kmesh, mu, eta):
+    """energy_cut.rs:1231-1352 with the diagonal-averaged triangles of
+    tracking.rs:278-341."""
+    nx, ny = kmesh
+    inx, iny = 1.0 / nx, 1.0 / ny
+    mu = np.asarray(mu, dtype=np.float64)
+    acc = np.zeros(len(mu))
+    N = E.shape[1]
+    Ep = [E[v][perms[v]] for v in range(E.shape[0])]
+    Kp = [K[v][np.ix_(perms[v], perms[v])] for v in range(E.shape[0])]
+    Om = [eval_berry_kernel(Ep[v], Kp[v], eta) for v in range(E.shape[0])]
+    for idx in range(nx * ny):
+        iy, ix = idx % ny, idx // ny
+        ixp, iyp = (ix + 1) % nx, (iy + 1) % ny
+        i00, i10, i11, i01 = ix * ny + iy, ixp * ny + iy, ixp * ny + iyp, ix * ny + iyp
+
+        def coord_of(i):
+            if i == i00:
+                return (ix * inx, iy * iny)
+            if i == i10:
+                return ((ix + 1) * inx, iy * iny)
+            if i == i11:
+                return ((ix + 1) * inx, (iy + 1) * iny)
+            return (ix * inx, (iy + 1) * iny)
+
+        for vs in ((i00, i10, i01), (i11, i10, i01), (i00, i10, i11), (i00, i11, i01)):
+            coords = [coord_of(v) for v in vs]
+            area = _tri_area(coords)
+            if area < EC_EPS:
+                continue
+            scale = (inx * iny / 4.0) / area
+            bands = [Ep[v] for v in vs]
+            for n in range(N):
+                ev = [Ep[v][n] for v in vs]
+                ov = [Om[v][n] for v in vs]
+                krows = [Kp[v][n] for v in vs]
+                full = area * (ov[0] + ov[1] + ov[2]) / 3.0
+                ip, iff = _mu_ranges(mu, min(ev), max(ev))
+                for im in range(ip, iff):
+                    if mu[im] <= min(ev) + EC_EPS:
+                        val = 0.0
+                    elif mu[im] >= max(ev) - EC_EPS:
+                        val = full
+                    else:
+                        val = _tri_partial(coords, ev, bands, krows, mu[im], eta, n)
+                    acc[im] += scale * val
+                if iff < len(mu):
+                    acc[iff:] += scale * full
+    return acc
+
+
+def _tet_vol(p0, p1, p2, p3):
+    """tet_vol_from_pts (energy_cut.rs:1449-1459)."""
+    x0, y0, z0 = p0
+    x1, y1, z1 = p1
+    x2, y2, z2 = p2
+    x3, y3, z3 = p3
+    det = ((x1 - x0) * ((y2 - y0) * (z3 - z0) - (z2 - z0) * (y3 - y0))
+           - (y1 - y0) * ((x2 - x0) * (z3 - z0) - (z2 - z0) * (x3 - x0))
+           + (z1 - z0) * ((x2 - x0) * (y3 - y0) - (y2 - y0) * (x3 - x0)))
+    return abs(det) / 6.0
+
+
+def _b2p3(coords, lam):
+    return [lam[0] * coords[0][d] + lam[1] * coords[1][d] + lam[2] * coords[2][d] + lam[3] * coords[3][d]
+            for d in range(3)]
+
+
+def _sub_tet(sub, coords, bands, krows, n, eta):
+    """sub_tet_k_quad (energy_cut.rs:1501-1527)."""
+    vol = _tet_vol(*[_b2p3(coords, l) for l in sub])
+    if vol < 1e-30:
+        return 0.0
+    total = 0.0
+    for q in range(4):
+        al = TET_Q[q]
+        lam = [0.0] * 4
+        for k in range(4):
+            for i in range(4):
+                lam[i] += al[k] * sub[k][i]
+        total += vol * 0.25 * _eval_band_at_lam(n, bands, krows, lam, eta)
+    return total
+
+
+def _tet_hybrid(coords, ev, ov, bands, krows, mu, eta, n):
+    """tetrahedron_occupied_hybrid (energy_cut.rs:1529-1648)."""
+    eps = EC_EPS
+    full_vol = _tet_vol(*coords)
+    if full_vol < eps:
+        return 0.0
+    if mu <= min(ev) + eps:
+        return 0.0
+    if mu >= max(ev) - eps:
+        return full_vol * (ov[0] + ov[1] + ov[2] + ov[3]) / 4.0
+    a, b, c, d = sorted(range(4), key=lambda i: ev[i])
+
+    def unit(i):
+        l = [0.0] * 4
+        l[i] = 1.0
+        return l
+
+    def cut(i, j):
+        de = ev[j] - ev[i]
+        t = 0.5 if abs(de) < eps else min(max((mu - ev[i]) / de, 0.0), 1.0)
+        l = [0.0] * 4
+        l[i] = 1.0 - t
+        l[j] = t
+        return l
+
+    args = (coords, bands, krows, n, eta)
+    if mu <= ev[b] + eps:
+        return _sub_tet([unit(a), cut(a, b), cut(a, c), cut(a, d)], *args)
+    if mu <= ev[c] + eps:
+        return (_sub_tet([unit(a), unit(b), cut(a, c), cut(b, d)], *args)
+                + _sub_tet([unit(a), cut(a, c), cut(a, d), cut(b, d)], *args)
+                + _sub_tet([unit(b), cut(b, c), cut(b, d), cut(a, c)], *args))
+    full_val = full_vol * (ov[0] + ov[1] + ov[2] + ov[3]) / 4.0
+    return full_val - _sub_tet([unit(d), cut(a, d), cut(b, d), cut(c, d)], *args)
+
+
+def integrate_fermi_cut_3d_t0(E, K, perms, kmesh, mu, eta):
+    """energy_cut.rs:1651-1795 with build_tetrahedra_3d (tracking.rs:343-405)."""
+    nx, ny, nz = kmesh
+    inx, iny, inz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    mu = np.asarray(mu, dtype=np.float64)
+    acc = np.zeros(len(mu))
+    N = E.shape[1]
+    Ep = [E[v][perms[v]] for v in range(E.shape[0])]
+    Kp = [K[v][np.ix_(perms[v], perms[v])] for v in range(E.shape[0])]
+    Om = [eval_berry_kernel(Ep[v], Kp[v], eta) for v in range(E.shape[0])]
+    cube_vol = inx * iny * inz
+    for idx in range(nx * ny * nz):
+        iz = idx % nz
+        iy = (idx // nz) % ny
+        ix = idx // (ny * nz)
+        ixp, iyp, izp = (ix + 1) % nx, (iy + 1) % ny, (iz + 1) % nz
+        i3 = lambda x, y, z: x * ny * nz + y * nz + z  # noqa: E731
+        c = [i3(ix, iy, iz), i3(ixp, iy, iz), i3(ix, iyp, iz), i3(ixp, iyp, iz),
+             i3(ix, iy, izp), i3(ixp, iy, izp), i3(ix, iyp, izp), i3(ixp, iyp, izp)]
+        f = lambda a, b, cc: (a * inx, b * iny, cc * inz)  # noqa: E731
+        corners = [f(ix, iy, iz), f(ix + 1, iy, iz), f(ix, iy + 1, iz), f(ix + 1, iy + 1, iz),
+                   f(ix, iy, iz + 1), f(ix + 1, iy, iz + 1), f(ix, iy + 1, iz + 1), f(ix + 1, iy + 1, iz + 1)]
+        for t, tet in enumerate(CUBE_TETS):
+            coords = [corners[l] for l in tet]
+            vs = [c[l] for l in tet]
+            vol = _tet_vol(*coords)
+            if vol < EC_EPS:
+                continue
+            scale = (cube_vol * TET_VOL_FACTOR[t]) / vol
+            bands = [Ep[v] for v in vs]
+            for n in range(N):
+                ev = [Ep[v][n] for v in vs]
+                ov = [Om[v][n] for v in vs]
+                krows = [Kp[v][n] for v in vs]
+                full = vol * (ov[0] + ov[1] + ov[2] + ov[3]) / 4.0
+                ip, iff = _mu_ranges(mu, min(ev), max(ev))
+                for im in range(ip, iff):
+                    acc[im] += scale * _tet_hybrid(coords, ev, ov, bands, krows, mu[im], eta, n)
+                if iff < len(mu):
+                    acc[iff:] += scale * full
+    return acc
+
+
+def _fermi_window_x(x):
+    if abs(x) > 50.0:
+        return 0.0
+    ex = np.exp(x)
+    return ex / ((1.0 + ex) * (1.0 + ex))
+
+
+def integrate_fermi_cut(E, K, perms, kmesh, mu, width, eta):
+    """integrate_fermi_cut_2d / _3d (energy_cut.rs:1355-1428, 1797-1849): the
+    T = 0 sweep, or its thermal convolution on an extended fine mu grid."""
+    t0 = integrate_fermi_cut_2d_t0 if len(kmesh) == 2 else integrate_fermi_cut_3d_t0
+    mu = np.asarray(mu, dtype=np.float64)
+    if width == 0.0:
+        return t0(E, K, perms, kmesh, mu, eta)
+    beta = 1.0 / width
+    x_max = 12.0
+    mu_lo = float(mu.min()) - x_max / beta
+    mu_hi = float(mu.max()) + x_max / beta
+    dmu = 0.1 / beta
+    n_ext = int(np.ceil((mu_hi - mu_lo) / dmu)) + 1
+    step = (mu_hi - mu_lo) / (n_ext - 1) if n_ext > 1 else 0.0
+    mu_ext = mu_lo + step * np.arange(n_ext, dtype=np.float64)
+    s0 = t0(E, K, perms, kmesh, mu_ext, eta)
+    dx = 2.0 * FERMI_X_CUT / FERMI_X_STEPS
+    out = np.empty(len(mu))
+    for j, m in enumerate(mu):
+        s = 0.0
+        for iq in range(FERMI_X_STEPS):
+            x = -FERMI_X_CUT + (iq + 0.5) * dx
+            w = _fermi_window_x(x)
+            i_f = (m + x / beta - mu_lo) / dmu
+            i_lo = max(int(np.floor(i_f)), 0)
+            i_hi = min(i_lo + 1, n_ext - 1)
+            if i_hi > i_lo:
+                t = i_f - i_lo
+                s += dx * w * (s0[i_lo] + t * (s0[i_hi] - s0[i_lo]))
+        out[j] = s
+    return out
+
+
+def hall_energy_cut(model, kmesh, directions, mu_list, T=0.0, eta=1e-3, spin=-1):
+    """``hall_conductivity`` with Integration::EnergyCut (linear/mod.rs:226-268)."""
+    E, Wv, K = vertex_kernels(model, kmesh, directions, spin)
+    perms = global_band_track(E, Wv, K, list(kmesh))
+    width = occupation_width(T)
+    s = integrate_fermi_cut(E, K, perms, list(kmesh), mu_list, width, eta)
+    return s / float(np.linalg.det(model.lat))

@@ -103,6 +103,8 @@ SIGNATURES = [
     ("tbg_bands_mesh", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p]),
     ("tbg_dos", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                ctypes.c_double, _c_double_p, _c_double_p]),
+    ("tbg_hall_energy_cut", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p, ctypes.c_int64, _c_double_p,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_int, _c_double_p]),
     ("tbg_wilson_loops", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, _c_double_p,
                                         ctypes.c_int64, _c_int64_p, ctypes.c_int, _c_double_p]),
     ("tbg_w90_read_hr", ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]),

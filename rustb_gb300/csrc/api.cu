@@ -1009,6 +1009,155 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
     return ctx.sync("tbg_wilson_loops");
 }
 
+int tbg_hall_energy_cut(const tbg_model* m, const int64_t* kmesh, const double* dirs2, int64_t nmu, const double* mu,
+                        double T, double eta, int spin, double* sigma_out) {
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    // validate_rank2 (config.rs:141-147), then the energy-cut checks (linear/mod.rs:177-185)
+    int64_t nk = 0;
+    if ((rc = check_kmesh(M, kmesh, &nk))) return rc;
+    if ((rc = check_dirs(dirs2, 2, M.dim, 2))) return rc;
+    if (nmu < 1 || !mu)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "chemical_potentials: must contain at least one value");
+    for (int64_t j = 0; j < nmu; ++j)
+        if (!std::isfinite(mu[j]))
+            return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "chemical_potentials: all values must be finite");
+    if ((rc = check_eta(eta))) return rc;
+    if (!std::isfinite(T) || T < 0.0)
+        return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "T: all values must be finite and non-negative");
+    if ((rc = check_spin(m, spin))) return rc;
+    for (int64_t j = 0; j + 1 < nmu; ++j)
+        if (mu[j] > mu[j + 1]) return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "mu: must be sorted in ascending order");
+    if (M.dim != 2 && M.dim != 3) return set_error(TBG_E_INVALID_DIMENSION, "energy-cut integration supports dim 2 and 3");
+    if (!sigma_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    const double det = lattice_det(M.lat, M.dim);
+    if (det == 0.0 || !std::isfinite(det)) return set_error(TBG_E_LINALG, "Linear algebra operation failed: singular lattice");
+    const int N = (int)M.nsta, dim = M.dim;
+    const int64_t NN = (int64_t)N * N;
+    Ctx ctx;
+    BerryJob J;
+    J.m = const_cast<ModelDev*>(&M);
+    J.spin = spin;
+    J.eta = eta;
+    J.precision = TBG_PREC_FP64;
+    J.want_metric = false;
+    J.chunk = choose_chunk(nk, sizeof(zc) * NN * 5 + 64 * N);
+    double* dirs_d = ctx.alloc<double>(2 * dim);
+    J.dirs_d = dirs_d;
+    double* E_all = ctx.alloc<double>(nk * N);
+    double* Om_all = ctx.alloc<double>(nk * N);
+    zc* U_all = ctx.alloc<zc>(nk * NN);
+    zc* K_all = ctx.alloc<zc>(nk * NN);
+    double* Rd = ctx.alloc<double>(J.chunk * NN);
+    int* perm_d = ctx.alloc<int>(nk * N);
+    if (ctx.rc) return ctx.rc;
+    if ((rc = alloc_berry(ctx, J))) return rc;
+    TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * dim, cudaMemcpyHostToDevice, ctx.st));
+    const int64_t n0 = kmesh[0], n1 = dim > 1 ? kmesh[1] : 1, n2 = dim > 2 ? kmesh[2] : 1;
+    // 1. vertex data of the whole mesh (compute_velocity_kernel, primitives.rs:33-137)
+    for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
+        const int64_t nkc = std::min(J.chunk, nk - c0);
+        kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(c0, nkc, dim, n0, n1, n2, J.k_d);
+        TBG_LAUNCHED("kmesh_kernel");
+        if ((rc = run_berry_chunk(ctx, J, nkc, nullptr))) return rc;
+        TBG_CUDA(cudaMemcpyAsync(E_all + c0 * N, J.E, sizeof(double) * nkc * N, cudaMemcpyDeviceToDevice, ctx.st));
+        TBG_CUDA(cudaMemcpyAsync(U_all + c0 * NN, J.U, sizeof(zc) * nkc * NN, cudaMemcpyDeviceToDevice, ctx.st));
+        if ((rc = ec_vertex_data(ctx.st, N, nkc, J.V, 2 * NN, J.E, eta, K_all + c0 * NN, Om_all + c0 * N))) return rc;
+    }
+    // 2. squared overlaps of the forward mesh edges, per dimension
+    const int64_t n3[3] = {n0, n1, n2};
+    const int64_t stride[3] = {n3[1] * n3[2], n3[2], 1};
+    std::vector<double> R_h((size_t)nk * dim * NN, 0.0);
+    for (int d = 0; d < dim; ++d) {
+        const int64_t sd = stride[d];
+        for (int64_t a0 = 0; a0 + sd < nk; a0 += J.chunk) {
+            const int64_t na = std::min(J.chunk, nk - sd - a0);
+            if ((rc = zgemm_batched(ctx.st, N, na, true, U_all + a0 * NN, NN, U_all + (a0 + sd) * NN, NN, J.scratch,
+                                    NN)))
+                return rc;
+            if ((rc = ec_abs2(ctx.st, na * NN, J.scratch, Rd))) return rc;
+            TBG_CUDA(cudaMemcpy2DAsync(R_h.data() + ((size_t)a0 * dim + d) * NN, sizeof(double) * dim * NN, Rd,
+                                       sizeof(double) * NN, sizeof(double) * NN, na, cudaMemcpyDeviceToHost, ctx.st));
+            if (ctx.sync("tbg_hall_energy_cut overlaps")) return ctx.rc;
+        }
+    }
+    if ((rc = check_status(J.status_d, ctx.st))) return rc;
+    // 3. band tracking on the host, permutations to the device
+    std::vector<int> perm_h((size_t)nk * N);
+    ec_track(dim, kmesh, N, R_h.data(), perm_h.data());
+    TBG_CUDA(cudaMemcpyAsync(perm_d, perm_h.data(), sizeof(int) * nk * N, cudaMemcpyHostToDevice, ctx.st));
+    // 4. the mu grid: the chemical potentials, or the extended fine grid of the thermal convolution
+    const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
+    std::vector<double> grid;
+    double mu_lo = 0.0, dmu = 0.0, beta = 0.0;
+    if (width == 0.0) {
+        grid.assign(mu, mu + nmu);
+    } else {
+        beta = 1.0 / width;
+        const double x_max = 12.0;
+        const double mmin = *std::min_element(mu, mu + nmu), mmax = *std::max_element(mu, mu + nmu);
+        mu_lo = mmin - x_max / beta;
+        const double mu_hi = mmax + x_max / beta;
+        dmu = 0.1 / beta;
+        const int64_t n_ext = (int64_t)std::ceil((mu_hi - mu_lo) / dmu) + 1;
+        if (n_ext > (int64_t)1 << 26) return set_error(TBG_E_UNSUPPORTED, "thermal grid too fine");
+        const double step = n_ext > 1 ? (mu_hi - mu_lo) / (double)(n_ext - 1) : 0.0;
+        grid.resize(n_ext);
+        for (int64_t i = 0; i < n_ext; ++i) grid[i] = mu_lo + step * (double)i;  // ndarray linspace
+    }
+    const int ng = (int)grid.size();
+    const int window = std::min(ng, kEcWindow);
+    const int S = dim == 2 ? 4 : 5;
+    const int64_t items = nk * S * N;
+    const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>((items + 127) / 128, 152 * 8));
+    double* grid_d = ctx.alloc<double>(ng);
+    double* part = ctx.alloc<double>((int64_t)nblocks * window);
+    double* fpart = ctx.alloc<double>((int64_t)nblocks * window);
+    double* acc_d = ctx.alloc<double>(ng);
+    double* full_d = ctx.alloc<double>(ng);
+    if (ctx.rc) return ctx.rc;
+    TBG_CUDA(cudaMemcpyAsync(grid_d, grid.data(), sizeof(double) * ng, cudaMemcpyHostToDevice, ctx.st));
+    // 5. occupancy cut of every simplex
+    if ((rc = ec_integrate(ctx.st, dim, kmesh, N, E_all, K_all, Om_all, perm_d, ng, grid_d, eta, part, fpart, nblocks,
+                           window, acc_d, full_d)))
+        return rc;
+    std::vector<double> acc_h(ng), full_h(ng);
+    TBG_CUDA(cudaMemcpyAsync(acc_h.data(), acc_d, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx.st));
+    TBG_CUDA(cudaMemcpyAsync(full_h.data(), full_d, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx.st));
+    if (ctx.sync("tbg_hall_energy_cut")) return ctx.rc;
+    std::vector<double> s0(ng);
+    for (int w0 = 0; w0 < ng; w0 += window) {  // the full-occupancy difference array restarts per window
+        double run = 0.0;
+        for (int i = w0; i < std::min(ng, w0 + window); ++i) {
+            run += full_h[i];
+            s0[i] = acc_h[i] + run;
+        }
+    }
+    // 6. thermal convolution (energy_cut.rs:1380-1427), then the Cartesian normalisation
+    if (width == 0.0) {
+        for (int64_t j = 0; j < nmu; ++j) sigma_out[j] = s0[j] / det;
+    } else {
+        const double dx = 2.0 * 18.0 / 72.0;
+        for (int64_t j = 0; j < nmu; ++j) {
+            double sum = 0.0;
+            for (int iq = 0; iq < 72; ++iq) {
+                const double x = -18.0 + ((double)iq + 0.5) * dx;
+                const double w = std::fabs(x) > 50.0 ? 0.0 : std::exp(x) / ((1.0 + std::exp(x)) * (1.0 + std::exp(x)));
+                const double i_f = (mu[j] + x / beta - mu_lo) / dmu;
+                const int64_t i_lo = std::max<int64_t>((int64_t)std::floor(i_f), 0);
+                const int64_t i_hi = std::min<int64_t>(i_lo + 1, ng - 1);
+                if (i_hi > i_lo) {
+                    const double t = i_f - (double)i_lo;
+                    sum += dx * w * (s0[i_lo] + t * (s0[i_hi] - s0[i_lo]));
+                }
+            }
+            sigma_out[j] = sum / det;
+        }
+    }
+    return TBG_OK;
+}
+
 int tbg_quantum_geometry(const tbg_model* m, int64_t nk, const double* k, const double* dirs2, double eta,
                          int precision, double* metric_out, double* berry_out, double* E_out) {
     if (nk > 0 && (!metric_out || !berry_out)) return set_error(TBG_E_INVALID_ARGUMENT, "null output");

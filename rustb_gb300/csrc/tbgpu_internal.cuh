@@ -229,6 +229,17 @@ constexpr int kSmallMaxN = 8;
 // Gaussian-smeared DOS: add the terms of count band energies ev (device) to
 // the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds
 // slices * E_n doubles; slices from dos_slices(E_n, chunk energies).
+// Energy-cut Hall integration (see ec.cu).
+constexpr int kEcWindow = 8192;  // mu points per integration launch
+void ec_track(int dim, const int64_t* kmesh, int N, const double* R, int* perm);
+size_t ec_smem_max();
+int ec_vertex_data(cudaStream_t st, int N, int64_t batch, const zc* V, int64_t ldV, const double* E, double eta,
+                   zc* K, double* Om);
+int ec_abs2(cudaStream_t st, int64_t n, const zc* C, double* R);
+int ec_integrate(cudaStream_t st, int dim, const int64_t* kmesh, int N, const double* E, const zc* K, const double* Om,
+                 const int* perm, int nmu, const double* mu_d, double eta, double* part, double* fpart, int nblocks,
+                 int window, double* acc_out, double* full_out);
+
 // Wilson loops from the eigenvectors at the loop points (see wilson.cu).
 constexpr int kWilsonMaxOcc = 64;
 size_t wilson_workspace_bytes(int N, int64_t n_loops, int n_k, int n_occ);

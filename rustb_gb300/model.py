@@ -350,21 +350,31 @@ class Model:
     # ------------------------------------------------------------------ Hall
     def hall_conductivity(self, params: Parameters, precision=Precision.FP64,
                           report: dict | None = None) -> HallConductivityResult:
-        """``hall_conductivity`` (src/response/linear/mod.rs:160-225), Direct
-        integration.  EnergyCut is outside this library's scope; Simplex is
-        rejected as in the reference (:166-176)."""
+        """``hall_conductivity`` (src/response/linear/mod.rs:160-268): Direct
+        integration, or EnergyCut (band tracking + simplex occupancy cut, FP64;
+        ``precision`` applies to Direct only); Simplex is rejected as in the
+        reference (:166-176)."""
         params.validate_rank2(self.dim)
         if not self.spin and params.spin is not None:
             raise errors.SpinNotAllowed(f"Spin direction '{params.spin!r}' is invalid for a model without spin.")
         if params.integration == Integration.Simplex:
             raise errors.InvalidResponseParameter(
                 "integration: hall_conductivity supports Integration::Direct or EnergyCut, not Simplex")
-        if params.integration == Integration.EnergyCut:
-            raise errors.TbPanic("Integration::EnergyCut is not provided by the GPU library")
         kmesh = np.ascontiguousarray(np.asarray(params.kmesh, dtype=np.int64))
         mu = _lib.as_f64(params.mu)
         d = _lib.as_f64(params.direction)
         sigma = np.empty(len(mu))
+        if params.integration == Integration.EnergyCut:
+            # linear/mod.rs:177-185: sorted mu, dimension 2 or 3; FP64 path
+            if np.any(np.diff(mu) < 0):
+                raise errors.InvalidResponseParameter("mu: must be sorted in ascending order")
+            if self.dim not in (2, 3):
+                raise errors.InvalidDimension(f"dimension {self.dim} is not supported; supported: [2, 3]")
+            lib = _lib.load()
+            _lib.check(lib.tbg_hall_energy_cut(self.device_handle(), _lib.iptr(kmesh), _lib.dptr(d), len(mu),
+                                               _lib.dptr(mu), float(params.T[0]), float(params.eta),
+                                               spin_code(params.spin), _lib.dptr(sigma)), lib)
+            return HallConductivityResult(chemical_potentials=params.mu.copy(), conductivity=sigma)
         rep = _lib.TbgReport()
         lib = _lib.load()
         _lib.check(lib.tbg_hall_conductivity(self.device_handle(), _lib.iptr(kmesh), _lib.dptr(d), len(mu),

@@ -107,3 +107,16 @@ def flat_bands(energies, dim=2) -> Model:
     m = Model.tb_model(np.eye(dim), np.zeros((n, dim)))
     m.set_onsite(list(energies))
     return m
+
+
+def haldane_2d(t2_imag: float) -> Model:
+    """build_haldane_2d (src/lib.rs:2356-2375): NNN amplitude t2_imag * i."""
+    m = Model.tb_model(HEX_LAT, HEX_ORB)
+    m.set_onsite([-0.7, 0.7])
+    for R in [(0, 0), (-1, 0), (0, -1)]:
+        m.add_hop(-1.0, 0, 1, R)
+    for R in [(1, 0), (-1, 1), (0, -1)]:
+        m.add_hop(t2_imag * 1j, 0, 0, R)
+    for R in [(-1, 0), (1, -1), (0, 1)]:
+        m.add_hop(t2_imag * 1j, 1, 1, R)
+    return m
