@@ -17,6 +17,10 @@
 * ``wilson``    -- hybrid Wannier centres (Berry::wannier_centre) of a random
                    spinful 2D model with 64 bands, 32 occupied, 64 loops of
                    64 points; a step is the whole set of loops.
+* ``ec``        -- Hall conductivity with Integration::EnergyCut on the
+                   reference's own ec_vs_reference case (Haldane t2 = -0.3,
+                   101 x 101 mesh, 201 chemical potentials, eta = 0.05); a step
+                   is the whole mesh.
 * ``w90``       -- Wannier90 loading: a 64-orbital, 125-R seedname_hr.dat
                    (512 000 lines, Wannier90's 5I5,2F12.6 format) read into a
                    device-resident model; a step is one load.
@@ -63,7 +67,7 @@ def run(args, rank, world, local):
     if rank != 0 and args.impl == "reference":
         return 0
     fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench,
-          "dos": dos_bench, "w90": w90_bench, "wilson": wilson_bench}[args.workload]
+          "dos": dos_bench, "w90": w90_bench, "wilson": wilson_bench, "ec": ec_bench}[args.workload]
     return fn(args, rank, world, local)
 
 
@@ -565,4 +569,90 @@ def wilson_bench(args, rank, world, local):
                             "sample": f"{sample} of the loops (numpy + LAPACK per loop, one thread)"},
            "e2e": {"value": e2e, "unit": "loops/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
                    "d2h_bytes_per_step": int(wcc.nbytes)}})
+    return 0
+
+
+# ---------------------------------------------------------------------- ec --
+EC_METRIC = "k-pts/s (hall_conductivity, Integration::EnergyCut)"
+
+
+def _haldane_2d(t2_imag: float):
+    from .model import Model
+
+    s3 = math.sqrt(3.0)
+    m = Model.tb_model([[1.0, 0.0], [0.5, s3 / 2.0]], [[1.0 / 3.0, 1.0 / 3.0], [2.0 / 3.0, 2.0 / 3.0]])
+    m.set_onsite([-0.7, 0.7])
+    for R in [(0, 0), (-1, 0), (0, -1)]:
+        m.add_hop(-1.0, 0, 1, R)
+    for R in [(1, 0), (-1, 1), (0, -1)]:
+        m.add_hop(t2_imag * 1j, 0, 0, R)
+    for R in [(-1, 0), (1, -1), (0, 1)]:
+        m.add_hop(t2_imag * 1j, 1, 1, R)
+    return m
+
+
+def ec_bench(args, rank, world, local):
+    from .params import Integration
+
+    model = _haldane_2d(-0.3)
+    mesh = (101, 101)
+    nk = mesh[0] * mesh[1]
+    mu = np.linspace(-3.0, 3.0, 201)
+    p = Parameters.rank2(mesh, [1.0, 0.0], [0.0, 1.0], list(mu))
+    p.eta = 0.05
+    p.integration = Integration.EnergyCut
+    cfg = {"workload": "Haldane (t2 = -0.3 i, onsite -/+0.7), 101x101 mesh, 201 mu in [-3, 3], eta = 0.05, T = 0, "
+                       "Integration::EnergyCut", "k_mesh": list(mesh), "n_mu": len(mu)}
+    sample = (21, 21)
+
+    def cpu_once():
+        from oracle import tb_oracle as O
+
+        t0 = time.perf_counter()
+        O.hall_energy_cut(model, list(sample), np.eye(2), mu, 0.0, 0.05)
+        return sample[0] * sample[1] / (time.perf_counter() - t0)
+
+    if args.impl == "reference":
+        val = cpu_once()
+        _line(args, world, EC_METRIC, val, "k-pts/s", nk / val * 1e3, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "k-pts/s", "cores": 1, "kind": "port",
+                                                     "sample": "the same model on a 21x21 mesh (numpy restatement)"},
+               "e2e": {"value": val, "unit": "k-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    lib.tbg_set_device(local)
+    for _ in range(args.warmup):
+        model.hall_conductivity(p)
+    lib.tbg_kernel_timing_enable(1)
+    _lib.kernel_timing(reset=True)
+    l0 = lib.tbg_kernel_launch_count(0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sig = model.hall_conductivity(p).conductivity
+    wall = time.perf_counter() - t0
+    launches = lib.tbg_kernel_launch_count(0) - l0
+    lib.tbg_kernel_timing_enable(0)
+    timing = _lib.kernel_timing(reset=True)
+    val = args.steps * nk * world / wall
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m2 = _haldane_2d(-0.3)
+        m2.hall_conductivity(p)
+        m2._invalidate()
+    e2e = args.steps * nk / (time.perf_counter() - t0)
+    dev_ms = sum(v[1] for v in timing.values()) / args.steps
+    name, (ln, ms, work) = max(timing.items(), key=lambda kv: kv[1][1])
+    cpu = cpu_once()
+    _line(args, world, EC_METRIC, val, "k-pts/s", wall / args.steps * 1e3, "f64", cfg,
+          {"roofline": {"bound": "fp64 / latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                        "traffic": None, "kernel": name, "share_of_device_time": ms / args.steps / max(dev_ms, 1e-9),
+                        "note": "host band tracking and launch latency dominate at this size; per-kernel times "
+                                "in kernel_times_ms"},
+           "gpu_launches": int(launches), "device_ms_per_step": dev_ms,
+           "chern_mu0": float(sig[100] * 2 * math.pi),
+           "kernel_times_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in timing.items()},
+           "cpu_baseline": {"value": cpu, "unit": "k-pts/s", "cores": 1, "kind": "port",
+                            "sample": "the same model on a 21x21 mesh (numpy restatement, one thread)"},
+           "e2e": {"value": e2e, "unit": "k-pts/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
+                   "d2h_bytes_per_step": int(sig.nbytes)}})
     return 0

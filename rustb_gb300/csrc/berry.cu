@@ -85,6 +85,31 @@ __global__ void __launch_bounds__(256) zgemm_batched_kernel(int N, const zc* __r
     }
 }
 
+// Small matrices (N <= 16): one thread per output element, 256 / N^2 matrices
+// per block, operands read through L1.  C[b] = op(A[b]) B[b].
+template <bool CONJ_A>
+__global__ void __launch_bounds__(256) zgemm_small_kernel(int N, int64_t batch, const zc* __restrict__ A, int64_t sA,
+                                                          const zc* __restrict__ B, int64_t sB, zc* __restrict__ C,
+                                                          int64_t sC) {
+    const int NN = N * N;
+    const int per = blockDim.x / NN;
+    const int local = threadIdx.x / NN, e = threadIdx.x % NN;
+    if (local >= per) return;
+    const int i = e / N, j = e % N;
+    for (int64_t b = (int64_t)blockIdx.x * per + local; b < batch; b += (int64_t)gridDim.x * per) {
+        const zc* Ab = A + b * sA;
+        const zc* Bb = B + b * sB;
+        zc acc = mk(0.0, 0.0);
+        for (int l = 0; l < N; ++l) {
+            if (CONJ_A)
+                fma_cjx(acc, Ab[(int64_t)l * N + i], Bb[(int64_t)l * N + j]);
+            else
+                fma_cx(acc, Ab[(int64_t)i * N + l], Bb[(int64_t)l * N + j]);
+        }
+        C[b * sC + e] = acc;
+    }
+}
+
 // Omega_n = sum_{m != n} -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2), one warp per row n.
 // With MET, also the quantum metric g_n = sum_{m != n} Re(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2)
 // (src/quantum_geometry.rs:160-187: the real part of the same tensor).
@@ -264,6 +289,16 @@ inline unsigned grid_for(int64_t total, int threads) {
 int zgemm_batched(cudaStream_t st, int N, int64_t batch, bool conj_a, const zc* A, int64_t sA, const zc* B,
                   int64_t sB, zc* C, int64_t sC) {
     KTimer kt(st, "zgemm_batched_kernel", 8.0 * (double)N * N * N * batch);
+    if (N <= 16) {
+        const int per = 256 / (N * N);
+        const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((batch + per - 1) / per, 152LL * 64));
+        if (conj_a)
+            zgemm_small_kernel<true><<<g, 256, 0, st>>>(N, batch, A, sA, B, sB, C, sC);
+        else
+            zgemm_small_kernel<false><<<g, 256, 0, st>>>(N, batch, A, sA, B, sB, C, sC);
+        TBG_LAUNCHED("zgemm_small_kernel");
+        return TBG_OK;
+    }
     for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
         const int64_t nb = std::min<int64_t>(65535, batch - b0);
         dim3 grid((N + 63) / 64, (N + 63) / 64, (unsigned)nb);
