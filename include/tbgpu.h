@@ -248,9 +248,11 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
  *         loops the caller builds, berry_flux / berry_phase / wannier_centre
  *         (geometry.rs:272-420).
  * mode 1: out (n_loops) = -arg det of the product of the raw overlaps;
- *         replaces Berry::berry_loop_det (geometry.rs:217-270). */
+ *         replaces Berry::berry_loop_det (geometry.rs:217-270).
+ * precision: FP64 eigenpairs at the loop points, or MIXED (FP32 eigenpairs
+ * refined with FP64-class tensor-core products, <= 256 bands). */
 int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const double* kvec,
-                     int64_t n_occ, const int64_t* occ, int mode, double* out);
+                     int64_t n_occ, const int64_t* occ, int mode, int precision, double* out);
 
 /* ------------------------------------------------------ Wannier90 input --- */
 

@@ -106,7 +106,7 @@ SIGNATURES = [
     ("tbg_hall_energy_cut", ctypes.c_int, [ctypes.c_void_p, _c_int64_p, _c_double_p, ctypes.c_int64, _c_double_p,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_int, _c_double_p]),
     ("tbg_wilson_loops", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, _c_double_p,
-                                        ctypes.c_int64, _c_int64_p, ctypes.c_int, _c_double_p]),
+                                        ctypes.c_int64, _c_int64_p, ctypes.c_int, ctypes.c_int, _c_double_p]),
     ("tbg_w90_read_hr", ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]),
     ("tbg_w90_read_r", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     ("tbg_w90_apply_wsvec", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]),

@@ -938,11 +938,13 @@ int tbg_bands_mesh(const tbg_model* m, const int64_t* kmesh, double* E_out) {
 }
 
 int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const double* kvec, int64_t n_occ,
-                     const int64_t* occ, int mode, double* out) {
+                     const int64_t* occ, int mode, int precision, double* out) {
     int rc = check_model(m);
     if (rc) return rc;
     const ModelDev& M = m->d;
     if (mode != 0 && mode != 1) return set_error(TBG_E_INVALID_ARGUMENT, "mode must be 0 (berry_loop) or 1 (det)");
+    if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
+        return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
     if (n_loops < 0 || n_k < 1 || n_occ < 0) return set_error(TBG_E_INVALID_ARGUMENT, "negative size or empty loop");
     if (n_loops == 0) return TBG_OK;
     if (!kvec || !out || (n_occ > 0 && !occ)) return set_error(TBG_E_INVALID_ARGUMENT, "null argument");
@@ -959,6 +961,8 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
         if (occ[i] < 0 || occ[i] >= N) return set_error(TBG_E_INVALID_ARGUMENT, "occupied band index out of bounds");
     if (n_occ > kWilsonMaxOcc) return set_error(TBG_E_UNSUPPORTED, "Wilson loops support at most 64 occupied bands");
     const int svd = mode == 0;
+    // mixed: FP32 eigenpairs refined on the tensor cores (9 .. 256 bands), else FP64
+    const bool mixed = effective_precision(M, precision) == TBG_PREC_MIXED && N > kSmallMaxN;
     if (n_occ == 0) {  // empty product: det 1 (phase 0); no eigenphases
         if (!svd)
             for (int64_t l = 0; l < n_loops; ++l) out[l] = 0.0;
@@ -967,8 +971,10 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
     const int T = (int)(n_k - 1);
     const int64_t NN = (int64_t)N * N;
     // loops per chunk: eigenpairs at T points per loop plus the loop workspace
-    const int64_t per_loop = (int64_t)std::max(T, 1) * (sizeof(zc) * NN * 2 + 8 * N + 8 * dim) +
-                             (int64_t)wilson_workspace_bytes(N, 1, (int)n_k, (int)n_occ) + 8 * n_k * dim;
+    const int64_t per_loop =
+        (int64_t)std::max(T, 1) * (sizeof(zc) * NN * 2 + 8 * N + 8 * dim +
+                                   (mixed ? (int64_t)(sizeof(float4) * NN + mixed_berry_workspace_bytes(N, 1)) : 0)) +
+        (int64_t)wilson_workspace_bytes(N, 1, (int)n_k, (int)n_occ) + 8 * n_k * dim;
     int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_loops, chunk_budget_bytes() / per_loop));
     chunk = std::min<int64_t>(chunk, std::max<int64_t>(1, 65535 / std::max(T, 1)));
     Ctx ctx;
@@ -982,6 +988,10 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
     void* work = ctx.alloc<unsigned char>(wb);
     double* out_d = ctx.alloc<double>(chunk * (svd ? n_occ : 1));
     int* status_d = ctx.alloc<int>(1);
+    const int64_t npmax = chunk * std::max(T, 1);
+    float4* Hp = mixed ? ctx.alloc<float4>(npmax * NN) : nullptr;
+    const size_t mwb = mixed ? mixed_berry_workspace_bytes(N, npmax) : 0;
+    void* mwork = mixed ? ctx.alloc<unsigned char>(mwb) : nullptr;
     if (ctx.rc) return ctx.rc;
     std::vector<int> occ32(occ, occ + n_occ);
     TBG_CUDA(cudaMemcpyAsync(occ_d, occ32.data(), sizeof(int) * n_occ, cudaMemcpyHostToDevice, ctx.st));
@@ -996,7 +1006,14 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
                                        sizeof(double) * T * dim, nl, cudaMemcpyDeviceToDevice, ctx.st));
             const int64_t np = nl * T;
             if ((rc = fourier_direct(M, ctx.st, np, kp_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0))) return rc;
-            if ((rc = eig_batched(ctx.st, N, np, H, E, U, nullptr, 0, status_d))) return rc;
+            if (mixed) {
+                if ((rc = z_to_pairs(ctx.st, np, NN, H, NN, Hp))) return rc;
+                if ((rc = mixed_berry(ctx.st, N, np, Hp, nullptr, nullptr, 0.0, E, nullptr, mwork, mwb, status_d,
+                                      nullptr, nullptr, U)))
+                    return rc;
+            } else if ((rc = eig_batched(ctx.st, N, np, H, E, U, nullptr, 0, status_d))) {
+                return rc;
+            }
         }
         if ((rc = wilson_from_vectors(ctx.st, M, nl, (int)n_k, kv_d, U, (int)n_occ, occ_d, svd, out_d, work, wb,
                                       status_d)))

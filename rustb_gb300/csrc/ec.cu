@@ -379,12 +379,17 @@ __global__ void __launch_bounds__(128) ec_integrate_kernel(int N, int nx, int ny
     }
 }
 
-// out[i] = sum over blocks (in block order) of p[b][i]
+// out[i] = sum over blocks of p[b][i]: one warp per column, lane-strided
+// partial sums combined by a fixed shuffle tree (the same order every run).
 __global__ void ec_colsum_kernel(int nblocks, int nmu, const double* __restrict__ p, double* __restrict__ out) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nmu; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nmu; i += nw) {
         double s = 0.0;
-        for (int b = 0; b < nblocks; ++b) s += p[(int64_t)b * nmu + i];
-        out[i] = s;
+        for (int b = lane; b < nblocks; b += 32) s += p[(int64_t)b * nmu + i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[i] = s;
     }
 }
 
@@ -535,9 +540,10 @@ int ec_integrate(cudaStream_t st, int dim, const int64_t* kmesh, int N, const do
             }
             TBG_LAUNCHED("ec_integrate_kernel");
         }
-        ec_colsum_kernel<<<(w + 255) / 256, 256, 0, st>>>(nblocks, w, part, acc_out + mu0);
+        const unsigned cg = (unsigned)std::min(152 * 16, (w * 32 + 255) / 256);
+        ec_colsum_kernel<<<cg, 256, 0, st>>>(nblocks, w, part, acc_out + mu0);
         TBG_LAUNCHED("ec_colsum_kernel");
-        ec_colsum_kernel<<<(w + 255) / 256, 256, 0, st>>>(nblocks, w, fpart, full_out + mu0);
+        ec_colsum_kernel<<<cg, 256, 0, st>>>(nblocks, w, fpart, full_out + mu0);
         TBG_LAUNCHED("ec_colsum_kernel");
     }
     return TBG_OK;

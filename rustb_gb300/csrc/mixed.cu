@@ -264,6 +264,33 @@ __global__ void xprime_kernel(int64_t n, const cc* __restrict__ X, const float4*
     }
 }
 
+// Eigenpairs out of the refinement: E ascending (rank by value, ties by index)
+// and the columns of X' = hi + lo (FP64) in the same order.  One block per matrix.
+__global__ void eigpairs_sorted_kernel(int N, int64_t batch, const float4* __restrict__ Xp, const double* Ein,
+                                       double* Eout, zc* __restrict__ U) {  // Ein may be Eout
+    extern __shared__ double es[];  // N values, N ranks (as double)
+    double* ev = es;
+    int* rk = reinterpret_cast<int*>(es + N);
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) ev[i] = Ein[b * N + i];
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            int r = 0;
+            for (int j = 0; j < N; ++j) r += (ev[j] < ev[i]) || (ev[j] == ev[i] && j < i);
+            rk[i] = r;
+            Eout[b * N + r] = ev[i];
+        }
+        __syncthreads();
+        for (int64_t e = threadIdx.x; e < NN; e += blockDim.x) {
+            const int row = (int)(e / N), col = (int)(e % N);
+            const float4 x = Xp[b * NN + e];
+            U[b * NN + (int64_t)row * N + rk[col]] = mk((double)x.x + (double)x.y, (double)x.z + (double)x.w);
+        }
+    }
+}
+
 __device__ __forceinline__ float2 df_warp_sum(float2 s) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -373,7 +400,7 @@ size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
 // not null, the quantum metric.
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met) {
+                int64_t* clusters_d, double* Met, zc* Uout) {
     if (batch <= 0) return TBG_OK;
     const int64_t NN = (int64_t)N * N;
     if (work_bytes < mixed_berry_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
@@ -436,6 +463,13 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         KTimer kt(st, "xprime_kernel");
         xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, X, bE, bA);
         TBG_LAUNCHED("xprime_kernel");
+    }
+    if (Uout) {  // eigenpairs only: refined E and X' in ascending order, no velocities
+        const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)N;
+        eigpairs_sorted_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, E, E,
+                                                                                             Uout);
+        TBG_LAUNCHED("eigpairs_sorted_kernel");
+        return TBG_OK;
     }
     // 5. band-basis velocities B = X'^H V X'
     if ((rc = exps(PAIR, true, bA, XPC)) || (rc = exps(PAIR, false, Vx, VXR)) || (rc = exps(PAIR, false, Vy, VYR)))

@@ -261,7 +261,9 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met = nullptr);
+                int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr);
+// With Uout, mixed_berry stops after the refinement: refined E ascending and the
+// refined eigenvectors (columns, FP64) in Uout; Vx, Vy are not read.
 // Spin-current dressing of float-pair velocities (V_0 blocks, batch stride ldV).
 int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
                      float4* scratch);

@@ -510,14 +510,15 @@ class Model:
         return len(getattr(self, "atoms", []) or [])
 
     # ----------------------------------------------------------- Wilson loops
-    def _wilson(self, kvec3: np.ndarray, occ, mode: int) -> np.ndarray:
+    def _wilson(self, kvec3: np.ndarray, occ, mode: int, precision=Precision.FP64) -> np.ndarray:
         kv = np.ascontiguousarray(np.asarray(kvec3, dtype=np.float64))
         n_loops, n_k = kv.shape[0], kv.shape[1]
         occ_a = np.ascontiguousarray(np.asarray(list(occ), dtype=np.int64).reshape(-1))
         out = np.empty((n_loops, occ_a.size) if mode == 0 else (n_loops,))
         lib = _lib.load()
         _lib.check(lib.tbg_wilson_loops(self.device_handle(), n_loops, n_k, _lib.dptr(kv), occ_a.size,
-                                        _lib.iptr(occ_a) if occ_a.size else None, int(mode), _lib.dptr(out)), lib)
+                                        _lib.iptr(occ_a) if occ_a.size else None, int(mode), int(precision),
+                                        _lib.dptr(out)), lib)
         return out
 
     def _check_loop(self, kvec):
@@ -526,20 +527,20 @@ class Model:
             raise errors.TbPanic(f"k-loop must have shape (n_k, {self.dim})")
         return k
 
-    def berry_loop(self, kvec, occ) -> np.ndarray:
+    def berry_loop(self, kvec, occ, precision=Precision.FP64) -> np.ndarray:
         """``Berry::berry_loop`` (src/geometry.rs:156-215): -arg of the eigenvalues
         of the product of the unitary parts of the overlap matrices along the
         closed loop ``kvec`` (n_k, dim); ascending (the reference's order is
         LAPACK zgeev's)."""
         k = self._check_loop(kvec)
-        return self._wilson(k[None], occ, 0)[0]
+        return self._wilson(k[None], occ, 0, precision)[0]
 
-    def berry_loop_det(self, kvec, occ) -> float:
+    def berry_loop_det(self, kvec, occ, precision=Precision.FP64) -> float:
         """``Berry::berry_loop_det`` (src/geometry.rs:217-270)."""
         k = self._check_loop(kvec)
-        return float(self._wilson(k[None], occ, 1)[0])
+        return float(self._wilson(k[None], occ, 1, precision)[0])
 
-    def berry_flux(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int) -> np.ndarray:
+    def berry_flux(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int, precision=Precision.FP64) -> np.ndarray:
         """``Berry::berry_flux`` (src/geometry.rs:272-339): Wilson loop around
         every plaquette of the (nk1, nk2) mesh spanned by dir_1, dir_2 from
         k_start; (nk1, nk2, n_occ), each plaquette's phases ascending."""
@@ -561,15 +562,15 @@ class Model:
         loops[:, :, 4] = ks + i0 * d1 + j0 * d2
         loops = loops.reshape(nk1 * nk2, 5, self.dim)
         occ = list(occ)
-        return self._wilson(loops, occ, 0).reshape(nk1, nk2, len(occ))
+        return self._wilson(loops, occ, 0, precision).reshape(nk1, nk2, len(occ))
 
-    def berry_phase(self, occ, kvec) -> np.ndarray:
+    def berry_phase(self, occ, kvec, precision=Precision.FP64) -> np.ndarray:
         """``Berry::berry_phase`` (src/geometry.rs:341-358): one loop per
         ``kvec[i]`` (nk1, nk2, dim); returns (n_occ, nk1), each column sorted."""
         kv = np.asarray(kvec, dtype=np.float64)
-        return self._wilson(kv, occ, 0).T.copy()
+        return self._wilson(kv, occ, 0, precision).T.copy()
 
-    def wannier_centre(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int) -> np.ndarray:
+    def wannier_centre(self, occ, k_start, dir_1, dir_2, nk1: int, nk2: int, precision=Precision.FP64) -> np.ndarray:
         """``Berry::wannier_centre`` (src/geometry.rs:360-420): loops along dir_2
         at nk1 positions along dir_1 (both ends included); (n_occ, nk1)."""
         ks, d1, d2 = (np.asarray(v, dtype=np.float64).reshape(-1) for v in (k_start, dir_1, dir_2))
@@ -583,4 +584,4 @@ class Model:
         fi = np.arange(nk1, dtype=np.float64)[:, None, None]
         fj = np.arange(nk2, dtype=np.float64)[None, :, None]
         kv = ks + d1 * fi / float(nk1 - 1) + d2 * fj / float(nk2 - 1)
-        return self._wilson(kv, occ, 0).T.copy()
+        return self._wilson(kv, occ, 0, precision).T.copy()

@@ -116,3 +116,20 @@ def test_wilson_errors():
     big = W.random_model(2, 70, False, 1, seed=404)
     with pytest.raises(errors.TbPanic):  # more than 64 occupied bands
         big.berry_loop(np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]]), list(range(66)))
+
+
+@pytest.mark.parametrize("norb,spin,occ", [(24, False, list(range(10))), (16, True, list(range(16)))])
+def test_berry_loop_mixed_precision(norb, spin, occ):
+    """Mixed eigenpairs (FP32 + tensor-core refinement) against the oracle, 1e-6 on the circle."""
+    from rustb_gb300.params import Precision
+
+    m = W.random_model(2, norb, spin, 1, seed=406 + norb)
+    for loop in _loops(m, 3, 33, seed=9):
+        ph = m.berry_loop(loop, occ, Precision.MIXED)
+        assert same_phases(ph, O.wilson_loop(m, loop, occ), tol=1e-6)
+        d = m.berry_loop_det(loop, occ, Precision.MIXED)
+        assert same_phases(d, O.wilson_loop_det(m, loop, occ), tol=1e-6)
+    wcc = m.wannier_centre(occ, [0.0, 0.0], [1.0, 0.0], [0.0, 1.0], 5, 21, Precision.MIXED)
+    ref = O.wannier_centre(m, occ, [0.0, 0.0], [1.0, 0.0], [0.0, 1.0], 5, 21)
+    for i in range(5):
+        assert same_phases(wcc[:, i], ref[:, i], tol=1e-6)
