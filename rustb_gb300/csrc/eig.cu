@@ -172,64 +172,72 @@ __device__ void tri_solve(int N, const T* __restrict__ d, const T* __restrict__ 
 // D+ and progressive (bottom-up) pivots D-, twist index r at the smallest
 // |gamma_k| = |D+_k + D-_k - (d_k - lam)|, then z_r = 1 and
 //   z_i = -e_i z_{i+1} / D+_i (i < r),   z_{i+1} = -e_i z_i / D-_{i+1} (i >= r).
-// Pivots smaller than pert are replaced by -pert.  Dp holds N values with
-// stride G, followed by the N values of D- (same stride).  Writes the
-// normalised (real) vector to u[i * ldu]; returns false if it is not finite.
+// Pivots smaller than pert are replaced by -pert.  X holds N values with
+// stride S: D+ first; once the twist index is known, D- is recomputed into
+// the slots above it (D+ is needed only below it), and the vector overwrites
+// both.  Writes the normalised (real) vector to u[i * ldu]; returns false if
+// it is not finite.
 template <typename T>
 __device__ bool twisted_vector(int N, const T* __restrict__ d, const T* __restrict__ e, const T* __restrict__ e2,
-                               T lam, T pert, T* __restrict__ Dp, int G, cx<T>* __restrict__ u, int ldu) {
-    T* Dm = Dp + (size_t)N * G;
+                               T lam, T pert, T* __restrict__ X, int S, cx<T>* __restrict__ u, int ldu) {
     T p = d[0] - lam;
     if (fabs(p) < pert) p = -pert;
-    Dp[0] = p;
+    X[0] = p;
     for (int i = 0; i < N - 1; ++i) {
         p = (d[i + 1] - lam) - Lim<T>::div(e2[i], p);
         if (fabs(p) < pert) p = -pert;
-        Dp[(size_t)(i + 1) * G] = p;
+        X[(size_t)(i + 1) * S] = p;
     }
     T q = d[N - 1] - lam;
     if (fabs(q) < pert) q = -pert;
-    Dm[(size_t)(N - 1) * G] = q;
+    const T q_last = q;
     int r = N - 1;
     T best = fabs(p + q - (d[N - 1] - lam));
     for (int i = N - 1; i >= 1; --i) {
         q = (d[i - 1] - lam) - Lim<T>::div(e2[i - 1], q);
         if (fabs(q) < pert) q = -pert;
-        Dm[(size_t)(i - 1) * G] = q;
-        const T g = fabs(Dp[(size_t)(i - 1) * G] + q - (d[i - 1] - lam));
+        const T g = fabs(X[(size_t)(i - 1) * S] + q - (d[i - 1] - lam));
         if (g < best) {
             best = g;
             r = i - 1;
         }
     }
+    // D-_i for i > r (the same operations as above, so the same values)
+    q = q_last;
+    if (r < N - 1) X[(size_t)(N - 1) * S] = q;
+    for (int i = N - 1; i >= r + 2; --i) {
+        q = (d[i - 1] - lam) - Lim<T>::div(e2[i - 1], q);
+        if (fabs(q) < pert) q = -pert;
+        X[(size_t)(i - 1) * S] = q;
+    }
     // the vector, in place: z_i (i < r) over D+, z_i (i > r) over D-
     T z = 1, amax = 1;
 #pragma unroll 4
     for (int i = r - 1; i >= 0; --i) {
-        const T ratio = Lim<T>::div(e[i], Dp[(size_t)i * G]);
+        const T ratio = Lim<T>::div(e[i], X[(size_t)i * S]);
         z = -ratio * z;
-        Dp[(size_t)i * G] = z;
+        X[(size_t)i * S] = z;
         amax = max(amax, fabs(z));
     }
     z = 1;
 #pragma unroll 4
     for (int i = r; i < N - 1; ++i) {
-        const T ratio = Lim<T>::div(e[i], Dm[(size_t)(i + 1) * G]);
+        const T ratio = Lim<T>::div(e[i], X[(size_t)(i + 1) * S]);
         z = -ratio * z;
-        Dm[(size_t)(i + 1) * G] = z;
+        X[(size_t)(i + 1) * S] = z;
         amax = max(amax, fabs(z));
     }
     if (!(amax < T(INFINITY))) return false;  // also NaN
     const T sc = T(1) / amax;
     T nrm = 0;
     for (int i = 0; i < N; ++i) {
-        const T v = (i < r ? Dp[(size_t)i * G] : (i == r ? T(1) : Dm[(size_t)i * G])) * sc;
+        const T v = (i == r ? T(1) : X[(size_t)i * S]) * sc;
         nrm += v * v;
     }
     if (!(nrm > T(0))) return false;
     const T inv = sc / sqrt(nrm);
     for (int i = 0; i < N; ++i) {
-        const T v = (i < r ? Dp[(size_t)i * G] : (i == r ? T(1) : Dm[(size_t)i * G])) * inv;
+        const T v = (i == r ? T(1) : X[(size_t)i * S]) * inv;
         u[(size_t)i * ldu] = mk<T>(v, T(0));
     }
     return true;
@@ -253,21 +261,41 @@ struct EigShared {
 
 constexpr int BT_NB = 16;  // reflectors per block of the blocked back-transformation
 
+// Offset of A(i, i) in the working matrix.  In shared memory the upper
+// triangle is packed row by row (row i holds columns i .. N-1, so two
+// matrices of 128 bands fit one SM); in global memory rows are LDA apart.
+// A(i, l) for l >= i is at diag_off(i) + (l - i).
+template <bool PACKED>
+__host__ __device__ __forceinline__ size_t diag_off(int N, int LDA, int i) {
+    return PACKED ? (size_t)i * N - ((size_t)i * (size_t)(i - 1)) / 2 : (size_t)i * LDA + i;
+}
+template <bool PACKED>
+__host__ __device__ inline size_t packed_elems(int N) {  // rounded to 16 bytes for the next buffers
+    return PACKED ? (((size_t)N * (N + 1) / 2 + 1) & ~(size_t)1) : (size_t)N * N;
+}
+
 template <typename T>
 __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB) {
     size_t b = 0;
-    if (a_smem) b += sizeof(cx<T>) * (size_t)N * (N + 4);  // rows padded to N + 4 (bank spread)
+    if (a_smem) b += sizeof(cx<T>) * packed_elems<true>(N);  // packed upper triangle
     b += sizeof(T) * 4 * (size_t)N;
     b += sizeof(cx<T>) * 4 * (size_t)N;  // tau, v, v2, w
     b += sizeof(T) * 64;
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-    // back-transform: blocked (matrix in shared memory): panel N x PB, Y (BT_NB x PB), Gram and T;
-    // otherwise a column-major panel with stride N + 4
-    size_t s2 = a_smem ? sizeof(cx<T>) * ((size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB)
-                       : sizeof(cx<T>) * (size_t)(N + 4) * PB;
+    // back-transform in the kernel (matrix in global memory): a column-major
+    // panel with stride N + 4; with the matrix in shared memory it is a pass
+    // of its own (heev_bt_kernel)
+    size_t s2 = a_smem ? 0 : sizeof(cx<T>) * (size_t)(N + 4) * PB;
     b += std::max(s1, s2);
     b += sizeof(int) * (4 + (size_t)N);  // flags + per-eigenvalue redo marks
     return b;
+}
+
+// Shared memory of the separate back-transformation pass: packed reflectors,
+// tau, panel N x PB, Y (BT_NB x PB), Gram and T.
+template <typename T>
+__host__ __device__ inline size_t bt_smem_bytes(int N, int PB) {
+    return sizeof(cx<T>) * (packed_elems<true>(N) + (size_t)N + (size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB);
 }
 
 // U <- H_0 H_1 ... H_{N-2} U with H_j = I - tau_j v_j v_j^H (v_j in row j of
@@ -278,12 +306,15 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 // last-first to panels of PB columns of U held row-major in shared memory:
 //   Y = V^H P;  Y <- T Y by back-substitution with T^{-1}, per column:
 //   y_i = tau_i (y_i - sum_{l>i} G_il y_l)  (tau_i = 0 gives y_i = 0);
-//   P <- P - V Y in 4 x 4 register tiles.
+//   P <- P - V Y in 4 x QN register tiles (QN = 2 for narrow panels keeps
+//   every thread busy).
 // work: P (N x PB), Y (BT_NB x PB), G (BT_NB x BT_NB).
-template <typename T>
-__device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__ A, const cx<T>* __restrict__ tau,
+template <typename T, int QN>
+__device__ void back_transform_blocked(int N, const cx<T>* __restrict__ A, const cx<T>* __restrict__ tau,
                                        cx<T>* __restrict__ U, cx<T>* __restrict__ work, int PB) {
     const int tid = threadIdx.x, nthr = blockDim.x;
+    // vrow(r)[c] = A(r, c) for c >= r (packed upper triangle)
+    auto vrow = [&](int r) { return A + diag_off<true>(N, 0, r) - r; };
     cx<T>* P = work;
     cx<T>* Y = P + (size_t)N * PB;
     cx<T>* G = Y + (size_t)BT_NB * PB;
@@ -304,8 +335,8 @@ __device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__
                 const int l = e / BT_NB, i = e - l * BT_NB;
                 cx<T> acc = mk<T>(0, 0);
                 if (l < i && i < nb) {
-                    const cx<T>* vl = A + (size_t)(j0 + l) * LDA;
-                    const cx<T>* vi = A + (size_t)(j0 + i) * LDA;
+                    const cx<T>* vl = vrow(j0 + l);
+                    const cx<T>* vi = vrow(j0 + i);
                     cx<T> q[4] = {mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0)};
                     for (int kk = j0 + i + 1; kk < N; kk += 4) {
 #pragma unroll
@@ -322,9 +353,9 @@ __device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__
                 const int i0 = ig, i1 = ig + 8;
                 cx<T> y0 = mk<T>(0, 0), y1 = mk<T>(0, 0);
                 if (i0 < nb) {
-                    const cx<T>* v0 = A + (size_t)(j0 + i0) * LDA;
+                    const cx<T>* v0 = vrow(j0 + i0);
                     const bool h1 = i1 < nb;
-                    const cx<T>* v1 = A + (size_t)(j0 + (h1 ? i1 : i0)) * LDA;
+                    const cx<T>* v1 = vrow(j0 + (h1 ? i1 : i0));
                     for (int k = k0; k < kf; ++k) {  // rows where part of the block is still zero
                         const cx<T> pk = P[(size_t)k * PB + c];
                         if (k > j0 + i0) fma_cjx(y0, v0[k], pk);
@@ -376,34 +407,35 @@ __device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__
                 for (int i = 0; i < BT_NB; ++i) Y[i * PB + c] = y[i];
             }
             __syncthreads();
-            // P <- P - V Y: item (rg, cg) updates rows k0 + 4 rg .. +3, columns cg + 16 q
+            // P <- P - V Y: item (rg, cg) updates rows k0 + 4 rg .. +3, columns cg + CS q
             const int nrg = (N - k0 + 3) / 4;
-            for (int it = tid; it < nrg * 16; it += nthr) {
-                const int rg = it >> 4, cg = it & 15;
+            const int CS = (PB + QN - 1) / QN;
+            for (int it = tid; it < nrg * CS; it += nthr) {
+                const int rg = it / CS, cg = it - rg * CS;
                 const int kb = k0 + 4 * rg;
-                cx<T> acc[4][4];
+                cx<T> acc[4][QN];
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[a][q] = mk<T>(0, 0);
+                    for (int q = 0; q < QN; ++q) acc[a][q] = mk<T>(0, 0);
                 for (int l = 0; l < nb; ++l) {
-                    const cx<T>* vl = A + (size_t)(j0 + l) * LDA;
-                    cx<T> v[4], y[4];
+                    const cx<T>* vl = vrow(j0 + l);
+                    cx<T> v[4], y[QN];
 #pragma unroll
                     for (int a = 0; a < 4; ++a) v[a] = (kb + a < N && kb + a > j0 + l) ? vl[kb + a] : mk<T>(0, 0);
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) y[q] = Y[l * PB + min(cg + 16 * q, PB - 1)];
+                    for (int q = 0; q < QN; ++q) y[q] = Y[l * PB + min(cg + CS * q, PB - 1)];
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) fma_cx(acc[a][q], v[a], y[q]);
+                        for (int q = 0; q < QN; ++q) fma_cx(acc[a][q], v[a], y[q]);
                 }
 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
                     if (kb + a >= N) continue;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int c = cg + 16 * q;
+                    for (int q = 0; q < QN; ++q) {
+                        const int c = cg + CS * q;
                         if (c < pw) P[(size_t)(kb + a) * PB + c] = P[(size_t)(kb + a) * PB + c] - acc[a][q];
                     }
                 }
@@ -421,7 +453,7 @@ __device__ void back_transform_blocked(int N, int LDA, const cx<T>* __restrict__
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
 template <typename T, bool A_SMEM>
-__global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
+__global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    const float4* __restrict__ Hpair, double* __restrict__ Eout,
                                                    cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
                                                    int* __restrict__ status, int G, int PB) {
@@ -431,7 +463,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         unsigned char* p = smem_raw;
         if (A_SMEM) {
             sh.A = reinterpret_cast<cx<T>*>(p);
-            p += sizeof(cx<T>) * (size_t)N * (N + 4);
+            p += sizeof(cx<T>) * packed_elems<true>(N);
         }
         sh.tau = reinterpret_cast<cx<T>*>(p);
         p += sizeof(cx<T>) * N;
@@ -452,17 +484,14 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         sh.red = reinterpret_cast<T*>(p);
         p += sizeof(T) * 64;
         sh.scratch = reinterpret_cast<T*>(p);
-        // same layout as eig_smem_bytes
-        const size_t s1 = sizeof(T) * 4 * (size_t)N * G;
-        const size_t s2 = A_SMEM ? sizeof(cx<T>) * ((size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB)
-                                 : sizeof(cx<T>) * (size_t)(N + 4) * PB;
-        p += std::max(s1, s2);
-        sh.flags = reinterpret_cast<int*>(p);
+        // flags close the layout that eig_smem_bytes sizes
+        sh.flags = reinterpret_cast<int*>(smem_raw + eig_smem_bytes<T>(N, A_SMEM, G, PB) - sizeof(int) * (4 + (size_t)N));
     }
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
     const size_t NN = (size_t)N * N;
-    const int LDA = A_SMEM ? N + 4 : N;  // row stride of the working matrix
+    const int LDA = N;  // row stride of the working matrix in global memory
+    auto doff = [&](int i) { return diag_off<A_SMEM>(N, LDA, i); };
 
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         cx<T>* A;
@@ -478,14 +507,18 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             // float-pair input {re_hi, re_lo, im_hi, im_lo} (FP32 solver only)
             const float4* src = Hpair + b * NN;
             for (size_t idx = tid; idx < NN; idx += nthr) {
+                const int r = (int)(idx / N), c = (int)(idx % N);
+                if (A_SMEM && c < r) continue;  // upper triangle only
                 const float4 h = src[idx];
-                A[(idx / N) * LDA + idx % N] = mk<T>((T)(h.x + h.y), (T)(h.z + h.w));
+                A[doff(r) + (c - r)] = mk<T>((T)(h.x + h.y), (T)(h.z + h.w));
             }
         } else if (A_SMEM || sizeof(T) != sizeof(double)) {
             const zc* src = Hin + b * NN;
             for (size_t idx = tid; idx < NN; idx += nthr) {
+                const int r = (int)(idx / N), c = (int)(idx % N);
+                if (A_SMEM && c < r) continue;
                 zc h = src[idx];
-                A[(idx / N) * LDA + idx % N] = mk<T>((T)h.re, (T)h.im);
+                A[doff(r) + (c - r)] = mk<T>((T)h.re, (T)h.im);
             }
         }
         if (tid == 0) sh.flags[0] = 0;
@@ -500,7 +533,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         // reflector by warp 0 from row jr: H^H [alpha; x] = [beta; 0]
         auto make_reflector = [&](int jr, cx<T>* vout) {
             const int mr = N - 1 - jr;
-            cx<T>* rowj = A + (size_t)jr * LDA + (jr + 1);  // row jr, columns jr+1.. = conj(column jr)
+            cx<T>* rowj = A + doff(jr) + 1;  // row jr, columns jr+1.. = conj(column jr)
             T part = 0;
             for (int i = 1 + lane; i < mr; i += 32) part += abs2(rowj[i]);
             const T xnorm2 = warp_sum(part);
@@ -527,7 +560,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             if (lane == 0) {
                 sh.tau[jr] = tau;
                 sh.e[jr] = beta;
-                sh.d[jr] = A[(size_t)jr * LDA + jr].re;
+                sh.d[jr] = A[doff(jr)].re;
             }
         };
         if (N > 1 && warp == 0) make_reflector(0, sh.v);
@@ -536,14 +569,15 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             const int m = N - 1 - j;
             const cx<T>* v = (j & 1) ? sh.v2 : sh.v;
             const cx<T> tau = sh.tau[j];
-            const size_t o22 = (size_t)(j + 1) * LDA + (j + 1);  // A22(0, 0)
+            // A22(i, l) = A(j+1+i, j+1+l); row22(i)[l] = A22(i, l) for l >= i
+            auto row22 = [&](int i) { return A + doff(j + 1 + i) - i; };
             // w = tau * A22 v: four threads per row, two-level butterfly; partial of w^H v
             cx<T> dpart = mk<T>(0, 0);
             {
                 const int q = tid & 3;
                 const unsigned gm = 0xFu << (lane & 28);
                 for (int i = tid >> 2; i < m; i += nthr >> 2) {
-                    const cx<T>* row = A + o22 + (size_t)i * LDA;  // row[l] = A22(i, l), l >= i
+                    const cx<T>* row = row22(i);
                     // two partial sums per part: independent load/FMA chains
                     cx<T> acc = mk<T>(0, 0), acc2 = mk<T>(0, 0);
                     int l = i + q;
@@ -552,12 +586,22 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                         fma_cx(acc2, row[l + 4], v[l + 4]);
                     }
                     if (l < m) fma_cx(acc, row[l], v[l]);
+                    // conj(A22(l, i)) from the column above the diagonal, l = q, q + 4, ...:
+                    // element offsets advance by doff(r + 4) - doff(r) - 4 per 4 rows
+                    // (4 LDA for full rows; 4 N - 4 r - 10 packed, r the global row)
                     l = q;
-                    for (; l + 4 < i; l += 8) {  // conj(A22(l, i)) from the column above the diagonal
-                        fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);
-                        fma_cjx(acc2, A[o22 + (size_t)(l + 4) * LDA + i], v[l + 4]);
+                    {
+                        int r = j + 1 + q;
+                        int a = (int)doff(r) + (j + 1 + i) - r;
+                        int s4 = A_SMEM ? 4 * N - 4 * r - 10 : 4 * LDA;
+                        for (; l + 4 < i; l += 8) {
+                            fma_cjx(acc, A[a], v[l]);
+                            fma_cjx(acc2, A[a + s4], v[l + 4]);
+                            a += A_SMEM ? 2 * s4 - 16 : 2 * s4;  // doff(r + 8) - doff(r) - 8
+                            if (A_SMEM) s4 -= 32;
+                        }
+                        if (l < i) fma_cjx(acc, A[a], v[l]);
                     }
-                    if (l < i) fma_cjx(acc, A[o22 + (size_t)l * LDA + i], v[l]);
                     acc = acc + acc2;
                     acc.re += __shfl_xor_sync(gm, acc.re, 1);
                     acc.im += __shfl_xor_sync(gm, acc.im, 1);
@@ -577,21 +621,22 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                 sh.red[32 + warp] = dpart.im;
             }
             __syncthreads();
-            cx<T> dp = mk<T>(0, 0);
-            for (int w2 = 0; w2 < nwarps; ++w2) {
-                dp.re += sh.red[w2];
-                dp.im += sh.red[32 + w2];
-            }
-            // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H (upper triangle)
+            // w^H v: lane k holds warp k's partial, then a fixed butterfly (same order everywhere)
+            cx<T> dp = (lane < nwarps) ? mk<T>(sh.red[lane], sh.red[32 + lane]) : mk<T>(0, 0);
+            dp.re = warp_sum(dp.re);
+            dp.im = warp_sum(dp.im);
+            // alpha2 = -1/2 tau (w^H v); w' = w + alpha2 v;  A22 -= v w'^H + w' v^H (upper triangle):
+            // A22(i, l) -= v_i conj(w_l) + c_i conj(v_l),  c_i = v_i conj(alpha2) + w'_i
             const cx<T> alpha2 = T(-0.5) * (tau * dp);
             auto update_row = [&](int i) {
-                cx<T>* row = A + o22 + (size_t)i * LDA;
+                cx<T>* row = row22(i);
                 const cx<T> vi = v[i];
-                const cx<T> wi = sh.w[i] + alpha2 * vi;
+                const cx<T> ci = mulc(vi, alpha2) + (sh.w[i] + alpha2 * vi);
                 for (int l = i + lane; l < m; l += 32) {
-                    const cx<T> vl = v[l];
-                    const cx<T> wl = sh.w[l] + alpha2 * vl;
-                    row[l] = row[l] - mulc(vi, wl) - mulc(wi, vl);
+                    cx<T> x = row[l];
+                    fms_mulc(x, vi, sh.w[l]);
+                    fms_mulc(x, ci, v[l]);
+                    row[l] = x;
                 }
             };
             if (warp == 0) {
@@ -607,7 +652,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
             __syncthreads();
         }
         if (tid == 0) {
-            sh.d[N - 1] = A[(size_t)(N - 1) * LDA + (N - 1)].re;
+            sh.d[N - 1] = A[doff(N - 1)].re;
             sh.e[N - 1] = 0;
         }
         __syncthreads();
@@ -724,14 +769,15 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
         const T ctol = T(1e-3) * max(tnorm, Lim<T>::tiny());
         const T pert = max(Lim<T>::eps() * tnorm, pivmin);
         int* redo = sh.flags + 4;
-        // (1) isolated eigenvalues: twisted factorisation, 2N scratch values
-        //     each, 2G at a time
-        for (int g0 = 0; g0 < N; g0 += 2 * G) {
-            if (tid < 2 * G && g0 + tid < N) {
+        // (1) isolated eigenvalues: twisted factorisation, N scratch values
+        //     each, 4G (at most one per thread) at a time
+        const int tw = min(4 * G, nthr);
+        for (int g0 = 0; g0 < N; g0 += tw) {
+            if (tid < tw && g0 + tid < N) {
                 const int i = g0 + tid;
                 const bool iso = (i == 0 || sh.lam[i] - sh.lam[i - 1] > ctol) &&
                                  (i == N - 1 || sh.lam[i + 1] - sh.lam[i] > ctol);
-                redo[i] = iso ? !twisted_vector<T>(N, sh.d, sh.e, sh.e2, sh.lam[i], pert, sh.scratch + tid, 2 * G,
+                redo[i] = iso ? !twisted_vector<T>(N, sh.d, sh.e, sh.e2, sh.lam[i], pert, sh.scratch + tid, tw,
                                                    U + i, N)
                               : 1;
             }
@@ -796,7 +842,11 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
 
         // ----------------------------------------------- back-transform --
         if constexpr (A_SMEM) {
-            back_transform_blocked<T>(N, LDA, A, sh.tau, U, reinterpret_cast<cx<T>*>(sh.scratch), PB);
+            // reflectors (packed rows) and tau to the back-transformation pass
+            const size_t pe = packed_elems<true>(N);
+            cx<T>* dst = Awork + (size_t)b * (pe + N);
+            for (size_t i = tid; i < pe; i += nthr) dst[i] = A[i];
+            for (int i = tid; i < N; i += nthr) dst[pe + i] = sh.tau[i];
             if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
             __syncthreads();
             continue;
@@ -822,7 +872,7 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
                     const cx<T> tau = sh.tau[j];
                     if (tau.re == T(0) && tau.im == T(0)) continue;
                     const int m = N - 1 - j;
-                    const cx<T>* vj = A + (size_t)j * LDA + (j + 1);
+                    const cx<T>* vj = A + doff(j) + 1;
                     cx<T> acc = mk<T>(0, 0);
                     for (int i = q8; i < m; i += 8) fma_cjx(acc, vj[i], pc[j + 1 + i]);
 #pragma unroll
@@ -847,18 +897,257 @@ __global__ void __launch_bounds__(512) heev_kernel(int N, int64_t batch, zc* __r
     }
 }
 
+// Back-transformation of the FP32 solver as a pass of its own, one CTA per
+// matrix: the reflectors (packed) and a panel of PB columns of U (all of U up
+// to about 150 bands) in shared memory, so each compact-WY block is applied
+// to the whole panel at once.  Vt: (batch, packed + N) = reflectors, tau.
+template <typename T>
+__global__ void __launch_bounds__(512) heev_bt_kernel(int N, int64_t batch, const cx<T>* __restrict__ Vt,
+                                                      cx<T>* __restrict__ Uout, int PB) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const size_t pe = packed_elems<true>(N);
+    cx<T>* V = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tau = V + pe;
+    cx<T>* work = tau + N;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const cx<T>* src = Vt + (size_t)b * (pe + N);
+        for (size_t i = threadIdx.x; i < pe + N; i += blockDim.x) V[i] = src[i];
+        __syncthreads();
+        if (PB <= 32)
+            back_transform_blocked<T, 2>(N, V, tau, Uout + (size_t)b * N * N, work, PB);
+        else
+            back_transform_blocked<T, 4>(N, V, tau, Uout + (size_t)b * N * N, work, PB);
+        __syncthreads();
+    }
+}
+
+// Back-transformation pass for up to kBtTiledMaxN bands (FP32): U (N4 x N4,
+// N4 = N rounded up to 4, zero padded) in shared memory, and each block of
+// BT_NB reflectors staged as a dense zero-masked BT_NB x N4 tile Vb
+// (Vb[i][k] = v_{j0+i}[k] for k > j0 + i, else 0), so no product needs masks:
+//   Gram G(l, i) = Vb[l]^H Vb[i] for l < i, four lanes per entry;
+//   Y = Vb^H P: a thread holds rows i and i + 8 by four adjacent columns over
+//       a quarter of the rows k (k = k0 + q (mod 4)); quarters are summed by
+//       shuffles between lanes 8 and 16 apart;
+//   Y <- T Y by back-substitution with T^{-1} = diag(1/tau) + striu(G);
+//   P <- P - Vb^T Y in 4 x 4 register tiles (rows k..k+3, columns 4c..4c+3).
+// The next block's tile is read from global memory into registers while this
+// block's products run and stored into the other of two tile buffers.
+constexpr int kBtTiledMaxN = 144;
+__host__ __device__ inline size_t bt_tiled_smem_bytes(int N) {
+    const size_t N4 = (size_t)((N + 3) & ~3);
+    return sizeof(cc) * (N4 * N4 + 3 * (size_t)BT_NB * N4 + (size_t)BT_NB * BT_NB + N4);
+}
+
+__device__ __forceinline__ cc bt_vb_elem(const cc* __restrict__ Vm, int N, int N4, int j0, int e) {
+    const int i = e / N4, k = e - i * N4, j = j0 + i;
+    if (j >= N - 1 || k <= j || k >= N) return mk<float>(0.f, 0.f);
+    return Vm[diag_off<true>(N, 0, j) + (size_t)(k - j)];
+}
+
+__global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t batch, const cc* __restrict__ Vt,
+                                                               cc* __restrict__ Uout) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N4 = (N + 3) & ~3, CG = N4 / 4, cgb = (CG + 7) / 8;
+    const size_t pe = packed_elems<true>(N);
+    cc* P = reinterpret_cast<cc*>(smem_raw);  // N4 x N4
+    cc* Vbuf = P + (size_t)N4 * N4;             // 2 x BT_NB x N4
+    cc* Y = Vbuf + 2 * (size_t)BT_NB * N4;      // BT_NB x N4
+    cc* G = Y + (size_t)BT_NB * N4;             // BT_NB x BT_NB
+    cc* tau = G + BT_NB * BT_NB;                // N4
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
+    constexpr int kPre = 8;  // tile elements per thread: BT_NB * N4 <= 8 * 512
+    if (N < 2) return;
+    const int jtop = ((N - 2) / BT_NB) * BT_NB;
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const cc* Vm = Vt + (size_t)b * (pe + N);
+        cc* U = Uout + (size_t)b * N * N;
+        for (int e = tid; e < N4 * N4; e += nthr) {
+            const int r = e / N4, c = e - r * N4;
+            P[e] = (r < N && c < N) ? U[(size_t)r * N + c] : mk<float>(0.f, 0.f);
+        }
+        for (int i = tid; i < N4; i += nthr) tau[i] = (i < N) ? Vm[pe + i] : mk<float>(0.f, 0.f);
+        for (int e = tid; e < BT_NB * N4; e += nthr) Vbuf[e] = bt_vb_elem(Vm, N, N4, jtop, e);
+        __syncthreads();
+        int buf = 0;
+        for (int j0 = jtop; j0 >= 0; j0 -= BT_NB) {
+            const cc* Vb = Vbuf + (size_t)buf * BT_NB * N4;
+            const int nb = min(BT_NB, N - 1 - j0);
+            const int k0 = j0 + 1;
+            cc pre[kPre];
+#pragma unroll
+            for (int u = 0; u < kPre; ++u) {
+                const int e = tid + u * nthr;
+                pre[u] = (j0 > 0 && e < BT_NB * N4) ? bt_vb_elem(Vm, N, N4, j0 - BT_NB, e) : mk<float>(0.f, 0.f);
+            }
+            // Gram: entry p = i (i - 1) / 2 + l, four lanes each
+            if (tid < 4 * (BT_NB * (BT_NB - 1) / 2)) {
+                const int p = tid >> 2, q = tid & 3;
+                int i = 1;
+                while ((i + 1) * i / 2 <= p) ++i;
+                const int l = p - i * (i - 1) / 2;
+                cc g = mk<float>(0.f, 0.f);
+                for (int k = k0 + q; k < N; k += 4) fma_cjx(g, Vb[l * N4 + k], Vb[i * N4 + k]);
+                g.re += __shfl_xor_sync(0xffffffffu, g.re, 1);
+                g.im += __shfl_xor_sync(0xffffffffu, g.im, 1);
+                g.re += __shfl_xor_sync(0xffffffffu, g.re, 2);
+                g.im += __shfl_xor_sync(0xffffffffu, g.im, 2);
+                if (q == 0) G[l * BT_NB + i] = g;
+            }
+            // Y = Vb^H P
+            for (int base = 0; base < 256 * cgb; base += nthr) {
+                const int it = base + tid, wt = it >> 5;
+                const int qk = lane >> 3, ig = wt / cgb, cg = (wt - ig * cgb) * 8 + (lane & 7);
+                const bool valid = it < 256 * cgb && cg < CG;
+                float y[2][4][2];
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) y[r][c][0] = y[r][c][1] = 0.f;
+                if (valid) {
+                    const cc* va = Vb + ig * N4;
+                    const cc* vc = Vb + (ig + 8) * N4;
+                    for (int k = k0 + qk; k < N; k += 4) {
+                        const cc a0 = va[k], a1 = vc[k];
+                        const float4 p01 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 4 * cg);
+                        const float4 p23 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 4 * cg + 2);
+                        const float pr[4] = {p01.x, p01.z, p23.x, p23.z}, pi[4] = {p01.y, p01.w, p23.y, p23.w};
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {  // y += conj(a) p
+                            y[0][c][0] = fmaf(a0.re, pr[c], y[0][c][0]);
+                            y[0][c][0] = fmaf(a0.im, pi[c], y[0][c][0]);
+                            y[0][c][1] = fmaf(a0.re, pi[c], y[0][c][1]);
+                            y[0][c][1] = fmaf(-a0.im, pr[c], y[0][c][1]);
+                            y[1][c][0] = fmaf(a1.re, pr[c], y[1][c][0]);
+                            y[1][c][0] = fmaf(a1.im, pi[c], y[1][c][0]);
+                            y[1][c][1] = fmaf(a1.re, pi[c], y[1][c][1]);
+                            y[1][c][1] = fmaf(-a1.im, pr[c], y[1][c][1]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            float v = y[r][c][h];
+                            v += __shfl_xor_sync(0xffffffffu, v, 8);
+                            v += __shfl_xor_sync(0xffffffffu, v, 16);
+                            y[r][c][h] = v;
+                        }
+                if (valid && qk == 0) {
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        cc* yr = Y + (ig + 8 * r) * N4 + 4 * cg;
+                        *reinterpret_cast<float4*>(yr) = make_float4(y[r][0][0], y[r][0][1], y[r][1][0], y[r][1][1]);
+                        *reinterpret_cast<float4*>(yr + 2) =
+                            make_float4(y[r][2][0], y[r][2][1], y[r][3][0], y[r][3][1]);
+                    }
+                }
+            }
+            __syncthreads();
+            // Y <- T Y, per column
+            for (int c = tid; c < N4; c += nthr) {
+                cc yv[BT_NB];
+#pragma unroll
+                for (int i = 0; i < BT_NB; ++i) yv[i] = Y[i * N4 + c];
+#pragma unroll
+                for (int i = BT_NB - 1; i >= 0; --i) {
+                    cc sv = yv[i];
+#pragma unroll
+                    for (int l = i + 1; l < BT_NB; ++l) sv = sv - G[i * BT_NB + l] * yv[l];
+                    yv[i] = (i < nb) ? tau[j0 + i] * sv : mk<float>(0.f, 0.f);
+                }
+#pragma unroll
+                for (int i = 0; i < BT_NB; ++i) Y[i * N4 + c] = yv[i];
+            }
+            __syncthreads();
+            // P <- P - Vb^T Y over row groups from k0 rounded down to 4 (rows
+            // above k0 get exact zeros)
+            {
+                const int ka = k0 & ~3, nrg = (N4 - ka) / 4;
+                for (int it = tid; it < nrg * CG; it += nthr) {
+                    const int rg = it / CG, cg = it - rg * CG, kb = ka + 4 * rg;
+                    float acc[4][4][2];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) acc[a][c][0] = acc[a][c][1] = 0.f;
+                    for (int i = 0; i < nb; ++i) {
+                        const float4 v01 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb);
+                        const float4 v23 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb + 2);
+                        const float4 y01 = *reinterpret_cast<const float4*>(Y + i * N4 + 4 * cg);
+                        const float4 y23 = *reinterpret_cast<const float4*>(Y + i * N4 + 4 * cg + 2);
+                        const float vr[4] = {v01.x, v01.z, v23.x, v23.z}, vi[4] = {v01.y, v01.w, v23.y, v23.w};
+                        const float yr[4] = {y01.x, y01.z, y23.x, y23.z}, yi[4] = {y01.y, y01.w, y23.y, y23.w};
+#pragma unroll
+                        for (int a = 0; a < 4; ++a)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                acc[a][c][0] = fmaf(vr[a], yr[c], acc[a][c][0]);
+                                acc[a][c][0] = fmaf(-vi[a], yi[c], acc[a][c][0]);
+                                acc[a][c][1] = fmaf(vr[a], yi[c], acc[a][c][1]);
+                                acc[a][c][1] = fmaf(vi[a], yr[c], acc[a][c][1]);
+                            }
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        float4* pr = reinterpret_cast<float4*>(P + (size_t)(kb + a) * N4 + 4 * cg);
+                        float4 p01 = pr[0], p23 = pr[1];
+                        p01.x -= acc[a][0][0];
+                        p01.y -= acc[a][0][1];
+                        p01.z -= acc[a][1][0];
+                        p01.w -= acc[a][1][1];
+                        p23.x -= acc[a][2][0];
+                        p23.y -= acc[a][2][1];
+                        p23.z -= acc[a][3][0];
+                        p23.w -= acc[a][3][1];
+                        pr[0] = p01;
+                        pr[1] = p23;
+                    }
+                }
+            }
+            // the next block's tile into the other buffer
+            if (j0 > 0) {
+                cc* nxt = Vbuf + (size_t)(buf ^ 1) * BT_NB * N4;
+#pragma unroll
+                for (int u = 0; u < kPre; ++u) {
+                    const int e = tid + u * nthr;
+                    if (e < BT_NB * N4) nxt[e] = pre[u];
+                }
+            }
+            buf ^= 1;
+            __syncthreads();
+        }
+        for (int e = tid; e < N * N; e += nthr) {
+            const int r = e / N, c = e - r * N;
+            U[e] = P[(size_t)r * N4 + c];
+        }
+        __syncthreads();
+    }
+}
+
+// Shared memory per CTA: one CTA per SM, or two sharing the SM's 228 KB
+// (1 KB of it reserved per CTA).
+constexpr size_t kEigSmemOne = 220 * 1024;
+constexpr size_t kEigSmemTwo = 113 * 1024;
+
 // Inverse-iteration group G and back-transform panel PB sized to the shared
 // memory left after the matrix (when resident) and the per-matrix vectors.
 template <typename T>
-inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB) {
-    const size_t budget = 220 * 1024;
+inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB, size_t budget = kEigSmemOne) {
     const size_t fixed = eig_smem_bytes<T>(N, a_smem, 0, 0);
     const size_t left = budget > fixed ? budget - fixed : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
     if (a_smem) {
-        const size_t fix2 = sizeof(cx<T>) * 2 * BT_NB * BT_NB;
-        const size_t l2 = left > fix2 ? left - fix2 : 0;
-        PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, l2 / (sizeof(cx<T>) * (size_t)(N + BT_NB))));
+        // the back-transformation is a pass of its own: its panel is as wide
+        // as its shared memory allows (up to all N columns)
+        const size_t base = bt_smem_bytes<T>(N, 0);
+        const size_t l2 = kEigSmemOne > base ? kEigSmemOne - base : 0;
+        PB = (int)std::min<size_t>((size_t)((N + 3) & ~3), l2 / (sizeof(cx<T>) * (size_t)(N + BT_NB)));
+        if (PB >= 8) PB &= ~3;  // whole 4-column groups in the V Y update
+        PB = std::max(PB, 1);
     } else {
         PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 4))));
     }
@@ -899,27 +1188,63 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
         if (cap < 1) return set_error(TBG_E_OOM, "eigensolver workspace too small");
         grid = std::min(grid, cap);
     }
+    if (A_SMEM && U && work_bytes < sizeof(cx<T>) * (packed_elems<true>(N) + N) * (size_t)batch)
+        return set_error(TBG_E_OOM, "eigensolver workspace too small for the reflectors");
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
-    KTimer kt(st, name, 14.0 * (double)N * N * N * batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work), status_d, G,
-                                                PB);
-    TBG_LAUNCHED(name);
+    {
+        // flops as LAPACK counts them: 16/3 N^3 (reduction) + 8 N^3 (back-transformation, a
+        // separate pass when the matrix is in shared memory) + O(N^2) per matrix
+        KTimer kt(st, name, (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N * batch);
+        kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work),
+                                                    status_d, G, PB);
+        TBG_LAUNCHED(name);
+    }
+    if constexpr (A_SMEM) {
+        if (!U) return TBG_OK;
+        if constexpr (sizeof(T) == sizeof(float)) {
+            if (N <= kBtTiledMaxN) {
+                const size_t bsm = bt_tiled_smem_bytes(N);
+                auto bk = heev_bt_tiled_kernel;
+                if (int rc = allow_max_smem(bk, bsm)) return rc;
+                KTimer kt(st, "heev_bt_kernel", 8.0 * (double)N * N * N * batch);
+                bk<<<(unsigned)std::min<int64_t>(nsm, batch), 512, bsm, st>>>(
+                    N, batch, reinterpret_cast<const cc*>(work), reinterpret_cast<cc*>(U));
+                TBG_LAUNCHED("heev_bt_kernel");
+                return TBG_OK;
+            }
+        }
+        const size_t bsm = bt_smem_bytes<T>(N, PB);
+        auto bk = heev_bt_kernel<T>;
+        if (int rc = allow_max_smem(bk, bsm)) return rc;
+        int64_t g2 = std::min<int64_t>(nsm, batch);
+        KTimer kt(st, "heev_bt_kernel", 8.0 * (double)N * N * N * batch);
+        bk<<<(unsigned)g2, 512, bsm, st>>>(N, batch, reinterpret_cast<const cx<T>*>(work), U, PB);
+        TBG_LAUNCHED("heev_bt_kernel");
+    }
     return TBG_OK;
 }
 
-// FP32 solver: matrix in shared memory when it fits.
+// FP32 solver: matrix in shared memory when it fits, two matrices per SM
+// when both fit (up to about 150 bands).
+inline bool f32_smem_fits(int N, size_t budget, int& G, int& PB) {
+    choose_g_pb<float>(N, true, 32, 64, G, PB, budget);
+    return eig_smem_bytes<float>(N, true, G, PB) <= budget && G >= 8 && PB >= std::min(16, (N + 3) & ~3) &&
+           bt_smem_bytes<float>(N, PB) <= kEigSmemOne;
+}
+inline bool f32_in_smem(int N, int& G, int& PB) {
+    return f32_smem_fits(N, kEigSmemTwo, G, PB) || f32_smem_fits(N, kEigSmemOne, G, PB);
+}
 inline bool f32_in_smem(int N) {
     int G, PB;
-    choose_g_pb<float>(N, true, 32, 64, G, PB);
-    return eig_smem_bytes<float>(N, true, G, PB) <= 220 * 1024 && G >= 8 && PB >= 16;
+    return f32_in_smem(N, G, PB);
 }
 
 }  // namespace
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (precision == 0) return 0;
-    if (f32_in_smem(N)) return 0;
+    if (f32_in_smem(N)) return sizeof(cc) * (packed_elems<true>(N) + N) * (size_t)std::max<int64_t>(batch, 1);
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
@@ -961,8 +1286,7 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
                     size_t work_bytes, int* status_d, const float4* Hpair) {
     if (batch <= 0) return TBG_OK;
     int G, PB;
-    if (f32_in_smem(N)) {
-        choose_g_pb<float>(N, true, 32, 64, G, PB);
+    if (f32_in_smem(N, G, PB)) {
         return launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
                                         G, PB, Hpair);
     }

@@ -12,8 +12,10 @@
 namespace tbg {
 
 // ----------------------------------------------------------------- complex --
+// Aligned to its full size, so a complex element moves as one vector load or
+// store (LDS.64 / LDG.128) rather than two scalar ones.
 template <typename T>
-struct cx {
+struct alignas(2 * sizeof(T)) cx {
     T re, im;
 };
 
@@ -55,6 +57,14 @@ __host__ __device__ __forceinline__ void fma_cx(cx<T>& acc, cx<T> a, cx<T> b) {
     acc.re = fma(-a.im, b.im, acc.re);
     acc.im = fma(a.re, b.im, acc.im);
     acc.im = fma(a.im, b.re, acc.im);
+}
+// acc -= a * conj(b)
+template <typename T>
+__host__ __device__ __forceinline__ void fms_mulc(cx<T>& acc, cx<T> a, cx<T> b) {
+    acc.re = fma(-a.re, b.re, acc.re);
+    acc.re = fma(-a.im, b.im, acc.re);
+    acc.im = fma(-a.im, b.re, acc.im);
+    acc.im = fma(a.re, b.im, acc.im);
 }
 // acc += conj(a) * b
 template <typename T>
