@@ -111,11 +111,28 @@ int64_t chunk_budget_bytes() {
     return 6LL << 30;
 }
 
+// k-points per chunk: as many as the memory budget allows, then balanced over
+// the chunks the call needs and rounded to whole waves of the batched
+// per-matrix kernels (two resident matrices per SM), so no chunk ends in a
+// nearly empty wave.
 int64_t choose_chunk(int64_t nk, int64_t per_k_bytes) {
     int64_t c = std::max<int64_t>(1, chunk_budget_bytes() / std::max<int64_t>(per_k_bytes, 1));
     c = std::min<int64_t>(c, 65535);
     const char* s = std::getenv("TBG_MAX_CHUNK");
     if (s && std::atoll(s) > 0) c = std::min<int64_t>(c, std::atoll(s));
+    if (nk > c) {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) nsm = 1;
+        const int64_t q = 2 * (int64_t)nsm;
+        const int64_t n = (nk + c - 1) / c;
+        const int64_t bal = (nk + n - 1) / n;
+        const int64_t up = (bal + q - 1) / q * q;
+        if (up <= c)
+            c = up;
+        else if (c >= q)
+            c = c / q * q;
+    }
     return std::max<int64_t>(1, std::min(c, nk));
 }
 

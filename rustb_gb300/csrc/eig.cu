@@ -665,6 +665,16 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
         }
         __syncthreads();
         for (int i = tid; i < N; i += nthr) sh.e2[i] = sh.e[i] * sh.e[i];
+        if constexpr (A_SMEM) {
+            // reflectors (packed rows) and tau to the back-transformation pass;
+            // the matrix's shared memory then serves the eigenvector scratch
+            if (Uout) {
+                const size_t pe = packed_elems<true>(N);
+                cx<T>* dst = Awork + (size_t)b * (pe + N);
+                for (size_t i = tid; i < pe; i += nthr) dst[i] = A[i];
+                for (int i = tid; i < N; i += nthr) dst[pe + i] = sh.tau[i];
+            }
+        }
         __syncthreads();
 
         // ------------------------------------------------------ bisection --
@@ -770,15 +780,16 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
         const T pert = max(Lim<T>::eps() * tnorm, pivmin);
         int* redo = sh.flags + 4;
         // (1) isolated eigenvalues: twisted factorisation, N scratch values
-        //     each, 4G (at most one per thread) at a time
-        const int tw = min(4 * G, nthr);
+        //     each, at most one per thread at a time: all N in the freed matrix
+        //     storage (N (N + 1) values) when it is in shared memory, else 4G
+        const int tw = A_SMEM ? min(N, nthr) : min(4 * G, nthr);
+        T* twx = A_SMEM ? reinterpret_cast<T*>(A) : sh.scratch;
         for (int g0 = 0; g0 < N; g0 += tw) {
             if (tid < tw && g0 + tid < N) {
                 const int i = g0 + tid;
                 const bool iso = (i == 0 || sh.lam[i] - sh.lam[i - 1] > ctol) &&
                                  (i == N - 1 || sh.lam[i + 1] - sh.lam[i] > ctol);
-                redo[i] = iso ? !twisted_vector<T>(N, sh.d, sh.e, sh.e2, sh.lam[i], pert, sh.scratch + tid, tw,
-                                                   U + i, N)
+                redo[i] = iso ? !twisted_vector<T>(N, sh.d, sh.e, sh.e2, sh.lam[i], pert, twx + tid, tw, U + i, N)
                               : 1;
             }
             __syncthreads();
@@ -842,11 +853,7 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
 
         // ----------------------------------------------- back-transform --
         if constexpr (A_SMEM) {
-            // reflectors (packed rows) and tau to the back-transformation pass
-            const size_t pe = packed_elems<true>(N);
-            cx<T>* dst = Awork + (size_t)b * (pe + N);
-            for (size_t i = tid; i < pe; i += nthr) dst[i] = A[i];
-            for (int i = tid; i < N; i += nthr) dst[pe + i] = sh.tau[i];
+            // the reflectors went out after the reduction
             if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
             __syncthreads();
             continue;
@@ -926,11 +933,13 @@ __global__ void __launch_bounds__(512) heev_bt_kernel(int N, int64_t batch, cons
 // BT_NB reflectors staged as a dense zero-masked BT_NB x N4 tile Vb
 // (Vb[i][k] = v_{j0+i}[k] for k > j0 + i, else 0), so no product needs masks:
 //   Gram G(l, i) = Vb[l]^H Vb[i] for l < i, four lanes per entry;
-//   Y = Vb^H P: a thread holds rows i and i + 8 by four adjacent columns over
-//       a quarter of the rows k (k = k0 + q (mod 4)); quarters are summed by
+//   Y = Vb^H P: a thread holds rows i and i + 8 by four columns over a
+//       quarter of the rows k (k = k0 + q (mod 4)); quarters are summed by
 //       shuffles between lanes 8 and 16 apart;
 //   Y <- T Y by back-substitution with T^{-1} = diag(1/tau) + striu(G);
-//   P <- P - Vb^T Y in 4 x 4 register tiles (rows k..k+3, columns 4c..4c+3).
+//   P <- P - Vb^T Y in 4 x 4 register tiles (rows k..k+3).
+// A thread's four columns are 2c, 2c + 1 and the same two N4 / 2 further on,
+// so consecutive lanes read consecutive 16-byte pairs (no bank conflicts).
 // The next block's tile is read from global memory into registers while this
 // block's products run and stored into the other of two tile buffers.
 constexpr int kBtTiledMaxN = 144;
@@ -948,7 +957,7 @@ __device__ __forceinline__ cc bt_vb_elem(const cc* __restrict__ Vm, int N, int N
 __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t batch, const cc* __restrict__ Vt,
                                                                cc* __restrict__ Uout) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N4 = (N + 3) & ~3, CG = N4 / 4, cgb = (CG + 7) / 8;
+    const int N4 = (N + 3) & ~3, CG = N4 / 4, cgb = (CG + 7) / 8, H = N4 / 2;
     const size_t pe = packed_elems<true>(N);
     cc* P = reinterpret_cast<cc*>(smem_raw);  // N4 x N4
     cc* Vbuf = P + (size_t)N4 * N4;             // 2 x BT_NB x N4
@@ -1009,8 +1018,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     const cc* vc = Vb + (ig + 8) * N4;
                     for (int k = k0 + qk; k < N; k += 4) {
                         const cc a0 = va[k], a1 = vc[k];
-                        const float4 p01 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 4 * cg);
-                        const float4 p23 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 4 * cg + 2);
+                        const float4 p01 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 2 * cg);
+                        const float4 p23 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 2 * cg + H);
                         const float pr[4] = {p01.x, p01.z, p23.x, p23.z}, pi[4] = {p01.y, p01.w, p23.y, p23.w};
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {  // y += conj(a) p
@@ -1039,9 +1048,9 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                 if (valid && qk == 0) {
 #pragma unroll
                     for (int r = 0; r < 2; ++r) {
-                        cc* yr = Y + (ig + 8 * r) * N4 + 4 * cg;
+                        cc* yr = Y + (ig + 8 * r) * N4 + 2 * cg;
                         *reinterpret_cast<float4*>(yr) = make_float4(y[r][0][0], y[r][0][1], y[r][1][0], y[r][1][1]);
-                        *reinterpret_cast<float4*>(yr + 2) =
+                        *reinterpret_cast<float4*>(yr + H) =
                             make_float4(y[r][2][0], y[r][2][1], y[r][3][0], y[r][3][1]);
                     }
                 }
@@ -1077,8 +1086,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     for (int i = 0; i < nb; ++i) {
                         const float4 v01 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb);
                         const float4 v23 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb + 2);
-                        const float4 y01 = *reinterpret_cast<const float4*>(Y + i * N4 + 4 * cg);
-                        const float4 y23 = *reinterpret_cast<const float4*>(Y + i * N4 + 4 * cg + 2);
+                        const float4 y01 = *reinterpret_cast<const float4*>(Y + i * N4 + 2 * cg);
+                        const float4 y23 = *reinterpret_cast<const float4*>(Y + i * N4 + 2 * cg + H);
                         const float vr[4] = {v01.x, v01.z, v23.x, v23.z}, vi[4] = {v01.y, v01.w, v23.y, v23.w};
                         const float yr[4] = {y01.x, y01.z, y23.x, y23.z}, yi[4] = {y01.y, y01.w, y23.y, y23.w};
 #pragma unroll
@@ -1093,8 +1102,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     }
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
-                        float4* pr = reinterpret_cast<float4*>(P + (size_t)(kb + a) * N4 + 4 * cg);
-                        float4 p01 = pr[0], p23 = pr[1];
+                        cc* prow = P + (size_t)(kb + a) * N4 + 2 * cg;
+                        float4 p01 = *reinterpret_cast<float4*>(prow), p23 = *reinterpret_cast<float4*>(prow + H);
                         p01.x -= acc[a][0][0];
                         p01.y -= acc[a][0][1];
                         p01.z -= acc[a][1][0];
@@ -1103,8 +1112,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                         p23.y -= acc[a][2][1];
                         p23.z -= acc[a][3][0];
                         p23.w -= acc[a][3][1];
-                        pr[0] = p01;
-                        pr[1] = p23;
+                        *reinterpret_cast<float4*>(prow) = p01;
+                        *reinterpret_cast<float4*>(prow + H) = p23;
                     }
                 }
             }
