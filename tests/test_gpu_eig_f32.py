@@ -39,7 +39,11 @@ def quality(H, E, U):
     return orth.max(), res.max(), eerr.max()
 
 
-@pytest.mark.parametrize("n", [128, 100, 40, 12])
+# Sizes cover each layout of the solver: two matrices per SM with the
+# register-tiled back-transformation (<= 144 bands, including N not a multiple
+# of 4), one matrix per SM with the panel back-transformation (150, 200), the
+# matrix in global memory (220), and the small-matrix thread counts (9, 12, 17).
+@pytest.mark.parametrize("n", [220, 200, 150, 144, 131, 128, 100, 64, 40, 17, 12, 9])
 def test_fp32_eigenpairs_random_hermitian(n):
     rng = np.random.default_rng(n)
     X = rng.standard_normal((16, n, n)) + 1j * rng.standard_normal((16, n, n))
@@ -57,4 +61,21 @@ def test_fp32_eigenpairs_benchmark_model():
     E, U = eig_f32(H)
     orth, res, eerr = quality(H, E, U)
     print(f"128-band model: orthogonality {orth:.2e}, residual {res:.2e}, eigenvalues {eerr:.2e}")
+    assert orth < 1e-3 and res < 1e-5 and eerr < 1e-6
+
+
+def test_fp32_eigenpairs_many_waves_and_clusters():
+    """More matrices than resident CTAs (the persistent loop), and spectra with
+    exact multiplicities (block-diagonal copies: the cluster path)."""
+    rng = np.random.default_rng(5)
+    n, nk = 64, 700
+    X = rng.standard_normal((nk, n, n)) + 1j * rng.standard_normal((nk, n, n))
+    H = 0.5 * (X + np.conj(np.transpose(X, (0, 2, 1))))
+    h = H[:64, :32, :32].copy()
+    H[:64] = 0
+    H[:64, :32, :32] = h
+    H[:64, 32:, 32:] = h  # every eigenvalue twice
+    E, U = eig_f32(H)
+    orth, res, eerr = quality(H, E, U)
+    print(f"n={n}, {nk} matrices: orthogonality {orth:.2e}, residual {res:.2e}, eigenvalues {eerr:.2e}")
     assert orth < 1e-3 and res < 1e-5 and eerr < 1e-6

@@ -247,6 +247,24 @@ def test_mixed_matches_plain_cfg2_model():
         assert np.max(np.abs(E[i] - Er)) <= 1e-9 * np.linalg.norm(Hs[i], 2)
 
 
+# band counts that reach each layout of the FP32 solver inside the mixed
+# chain: two matrices per SM with the tiled back-transformation (67; 134 with
+# padding to a multiple of 4), one per SM with the panel back-transformation
+# (150, 200)
+@pytest.mark.parametrize("norb,spin", [(67, False), (134, False), (75, True), (100, True)])
+def test_mixed_matches_plain_across_solver_layouts(norb, spin):
+    m = W.random_model(2, norb, spin, 1, seed=900 + norb)
+    p = Parameters.rank2((4, 4), [1.0, 0.0], [0.0, 1.0], [-0.1, 0.0, 0.2])
+    plain = m.hall_conductivity(p, Precision.FP64).conductivity
+    mixed = m.hall_conductivity(p, Precision.MIXED).conductivity
+    assert np.max(np.abs(mixed - plain)) <= 1e-6 * np.max(np.abs(plain))
+    k = O.gen_kmesh((4, 4))[:3]
+    _, E = m.berry_curvature_on(k, p, Precision.MIXED)
+    Hs = O.gen_ham_batch(m, k, 1)
+    for i in range(len(k)):
+        assert np.max(np.abs(E[i] - O.eigvalsh(Hs[i]))) <= 1e-9 * np.linalg.norm(Hs[i], 2)
+
+
 def test_mixed_handles_kramers_clusters():
     km = M.kane_mele()
     p = Parameters.rank2((12, 12), [1.0, 0.0], [0.0, 1.0], [-0.5, 0.0, 0.5]).with_spin(SpinDirection.Z)
