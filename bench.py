@@ -153,7 +153,11 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
 # heev_kernel<float,smem>: 169.3 MB for one launch over 512 matrices
 # (profiles/heev_f32_random3d_b512.md).  The traffic of a bench launch is this
 # figure times the matrices that launch processes.
-DRAM_BYTES_PER_MATRIX = {"heev_kernel<float,smem>": 169.3e6 / 512}
+# DRAM bytes (read + write) per k-point of each kernel family, from ncu captures over 512 k-points
+# of this workload: the FP32 solver's two passes, and the seven FP64-class tcgen05 products of one
+# k-point (refinement and rotation) together.
+DRAM_BYTES_PER_MATRIX = {"heev_kernel<float,smem>": 112.5e6 / 512, "heev_bt_kernel": 112.5e6 / 512,
+                         "ozaki_tc_kernel<high>": 2176.1e6 / 512}
 
 
 def kernel_roofline(timing: dict, peaks: dict, units: int = 0) -> dict | None:
