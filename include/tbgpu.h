@@ -134,6 +134,14 @@ int tbg_gen_v_projected(const tbg_model* m, int64_t nk, const double* k,
 int tbg_solve_band(const tbg_model* m, int64_t nk, const double* k,
                    double* E_out);
 
+/* The same with a precision choice: TBG_PREC_FP64 is tbg_solve_band;
+ * TBG_PREC_MIXED runs the FP32 eigensolve with the FP64-class refinement of
+ * the eigenvalues (<= 1e-9 ||H||; models of 9..256 bands, others FP64).  For
+ * callers that want band energies faster than the drop-in (the serving loop's
+ * bands requests); no counterpart in the reference. */
+int tbg_solve_band_prec(const tbg_model* m, int64_t nk, const double* k,
+                        int precision, double* E_out);
+
 /* Energies and eigenvectors -> E_out (nk, nsta), U_out (nk, nsta, nsta).
  * evec_rows != 0: U_out[k][n][:] is the n-th eigenvector (the layout of
  * Solve::solve_onek / solve_all_parallel, src/solve_ham.rs:110-184);

@@ -79,6 +79,7 @@ SIGNATURES = [
     ("tbg_gen_v_projected", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, ctypes.c_int,
                                            ctypes.c_int64, _c_double_p, _c_double_p, _c_double_p]),
     ("tbg_solve_band", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p]),
+    ("tbg_solve_band_prec", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, ctypes.c_int, _c_double_p]),
     ("tbg_solve", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p, _c_double_p,
                                  ctypes.c_int]),
     ("tbg_berry_curvature", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p,

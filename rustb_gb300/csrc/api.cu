@@ -659,6 +659,69 @@ int tbg_solve_band(const tbg_model* m, int64_t nk, const double* k, double* E_ou
     return solve_impl(m, nk, k, E_out, nullptr, 0);
 }
 
+// Band energies in mixed precision: H as float pairs (tensor-core Fourier sum,
+// or the FP64 sum converted when the contraction does not apply), FP32
+// eigensolve, FP64-class refinement of the eigenvalues; no eigenvectors out.
+static int solve_band_mixed(const tbg_model* m, int64_t nk, const double* k, double* E_out) {
+    const ModelDev& M = m->d;
+    const int N = (int)M.nsta;
+    const int64_t NN = (int64_t)N * N;
+    Ctx ctx;
+    const int64_t chunk = choose_chunk(nk, sizeof(zc) * NN * 15 + 64 * N + 48 * (int64_t)M.nR);
+    const bool tcf = M.n_rmat == 0 && fourier_mixed_ok(M);
+    double* k_d = ctx.alloc<double>(chunk * M.dim);
+    double* dirs_d = ctx.alloc<double>(2 * M.dim);
+    double* E = ctx.alloc<double>(chunk * N);
+    int* status_d = ctx.alloc<int>(1);
+    int64_t* clusters_d = ctx.alloc<int64_t>(1);
+    float4* P = ctx.alloc<float4>((tcf ? 3 : 1) * chunk * NN);
+    const size_t fwb = tcf ? fourier_mixed_scratch_bytes(M, chunk) : 0;
+    void* fwork = tcf ? static_cast<void*>(ctx.alloc<unsigned char>(fwb)) : nullptr;
+    zc* H = tcf ? nullptr : ctx.alloc<zc>(chunk * NN);
+    const size_t wb = mixed_berry_workspace_bytes(N, chunk);
+    void* work = ctx.alloc<unsigned char>(wb);
+    if (ctx.rc) return ctx.rc;
+    // velocity directions of the contraction (its V blocks are not used here)
+    std::vector<double> dirs(2 * M.dim, 0.0);
+    dirs[0] = 1.0;
+    dirs[M.dim + (M.dim > 1 ? 1 : 0)] = 1.0;
+    TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs.data(), sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
+    TBG_CUDA(cudaMemsetAsync(status_d, 0, sizeof(int), ctx.st));
+    TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
+    int rc;
+    for (int64_t c0 = 0; c0 < nk; c0 += chunk) {
+        const int64_t nkc = std::min(chunk, nk - c0);
+        TBG_CUDA(cudaMemcpyAsync(k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
+        if (tcf) {
+            rc = fourier_mixed_pairs(const_cast<ModelDev&>(M), ctx.st, nkc, k_d, dirs_d, P, fwork, fwb);
+        } else {
+            rc = fourier_direct(M, ctx.st, nkc, k_d, TBG_GAUGE_ATOM, 0, nullptr, H, nullptr, NN, 0);
+            if (!rc) rc = z_to_pairs(ctx.st, nkc, NN, H, NN, P);
+        }
+        if (rc) return rc;
+        if ((rc = mixed_berry(ctx.st, N, nkc, P, nullptr, nullptr, 0.0, E, nullptr, work, wb, status_d, clusters_d)))
+            return rc;
+        TBG_CUDA(cudaMemcpyAsync(E_out + c0 * N, E, sizeof(double) * nkc * N, cudaMemcpyDeviceToHost, ctx.st));
+    }
+    if (ctx.sync("tbg_solve_band_prec")) return ctx.rc;
+    if ((rc = check_status(status_d, ctx.st))) return rc;
+    return ctx.sync("tbg_solve_band_prec");
+}
+
+int tbg_solve_band_prec(const tbg_model* m, int64_t nk, const double* k, int precision, double* E_out) {
+    if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
+        return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
+    int rc = check_model(m);
+    if (rc) return rc;
+    const ModelDev& M = m->d;
+    if (effective_precision(M, precision) != TBG_PREC_MIXED || M.nsta <= kSmallMaxN)
+        return solve_impl(m, nk, k, E_out, nullptr, 0);
+    if ((rc = check_k(k, nk, M.dim))) return rc;
+    if (nk > 0 && !E_out) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
+    if (nk == 0) return TBG_OK;
+    return solve_band_mixed(m, nk, k, E_out);
+}
+
 int tbg_solve(const tbg_model* m, int64_t nk, const double* k, double* E_out, double* U_out, int evec_rows) {
     if (!U_out && nk > 0) return set_error(TBG_E_INVALID_ARGUMENT, "null eigenvector output");
     return solve_impl(m, nk, k, E_out, U_out, evec_rows);

@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, con
     }
 }
 
-// Keep E ascending (with Omega and, when given, the metric) after refinement;
+// Keep E ascending (with Omega and the metric when given) after refinement;
 // a no-op when already sorted.
 __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, double* __restrict__ Om,
                                  double* __restrict__ Met) {
@@ -363,7 +363,7 @@ __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, d
         __syncthreads();
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
             e[i] = E[b * N + i];
-            o[i] = Om[b * N + i];
+            if (Om) o[i] = Om[b * N + i];
             if (Met) g[i] = Met[b * N + i];
         }
         __syncthreads();
@@ -375,7 +375,7 @@ __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, d
                 int rank = 0;
                 for (int j = 0; j < N; ++j) rank += (e[j] < e[i]) || (e[j] == e[i] && j < i);
                 E[b * N + rank] = e[i];
-                Om[b * N + rank] = o[i];
+                if (Om) Om[b * N + rank] = o[i];
                 if (Met) Met[b * N + rank] = g[i];
             }
         }
@@ -453,6 +453,12 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, bC, E, F,
                                                                                         clusters_d);
         TBG_LAUNCHED("oa_kernel");
+    }
+    if (!Om && !Uout) {  // band energies only
+        sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 3 * sizeof(double) * N, st>>>(
+            N, batch, E, nullptr, nullptr);
+        TBG_LAUNCHED("sort_e_om_kernel");
+        return TBG_OK;
     }
     // 4. X' = X + X F  (float pair: hi = X, lo = X F)
     if ((rc = exps(F32, false, X, XR)) || (rc = exps(F32, true, F, FC))) return rc;

@@ -273,7 +273,9 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
                 int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr);
 // With Uout, mixed_berry stops after the refinement: refined E ascending and the
-// refined eigenvectors (columns, FP64) in Uout; Vx, Vy are not read.
+// refined eigenvectors (columns, FP64) in Uout; Vx, Vy are not read.  With
+// neither Om nor Uout it stops after the eigenvalue refinement (refined E
+// ascending only).
 // Spin-current dressing of float-pair velocities (V_0 blocks, batch stride ldV).
 int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
                      float4* scratch);

@@ -255,12 +255,18 @@ class Model:
         return V[0], H[0]
 
     # ---------------------------------------------------------------- Solve
-    def solve_band_all_parallel(self, kvec) -> np.ndarray:
-        """``solve_band_all_parallel`` (src/solve_ham.rs:94-107)."""
+    def solve_band_all_parallel(self, kvec, precision: Precision = Precision.FP64) -> np.ndarray:
+        """``solve_band_all_parallel`` (src/solve_ham.rs:94-107).  ``precision``
+        (not in the reference) selects the mixed-precision band energies
+        (FP32 eigensolve + FP64-class eigenvalue refinement, <= 1e-9 ||H||)."""
         k = self._klist(kvec)
         E = np.empty((k.shape[0], self.nsta))
         lib = _lib.load()
-        _lib.check(lib.tbg_solve_band(self.device_handle(), k.shape[0], _lib.dptr(k), _lib.dptr(E)), lib)
+        if int(precision) == int(Precision.FP64):
+            _lib.check(lib.tbg_solve_band(self.device_handle(), k.shape[0], _lib.dptr(k), _lib.dptr(E)), lib)
+        else:
+            _lib.check(lib.tbg_solve_band_prec(self.device_handle(), k.shape[0], _lib.dptr(k), int(precision),
+                                               _lib.dptr(E)), lib)
         return E
 
     solve_band_all = solve_band_all_parallel

@@ -135,7 +135,7 @@ def execute(m: Model, req: Request):
     alone-vs-in-the-mix check)."""
     k = np.ascontiguousarray(req.k, dtype=np.float64)
     if req.observable == "bands":
-        return m.solve_band_all_parallel(k)
+        return m.solve_band_all_parallel(k, req.precision)
     dirs = np.eye(m.dim)[:2] if m.dim > 1 else np.array([[1.0], [1.0]])
     p = Parameters(kmesh=(1,) * m.dim, direction=dirs, mu=[req.mu])
     p.eta = req.eta

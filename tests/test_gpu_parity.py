@@ -265,6 +265,23 @@ def test_mixed_matches_plain_across_solver_layouts(norb, spin):
         assert np.max(np.abs(E[i] - O.eigvalsh(Hs[i]))) <= 1e-9 * np.linalg.norm(Hs[i], 2)
 
 
+# mixed-precision band energies (tbg_solve_band_prec): the tensor-core
+# Fourier sum (nR <= 408) or the FP64 sum converted (3D, |R_i| <= 4: nR = 729),
+# solver layouts from 24 to 251 bands
+@pytest.mark.parametrize("dim,norb,spin,rmax", [(2, 24, False, 1), (3, 64, True, 1), (2, 134, False, 1),
+                                                (2, 251, False, 1), (3, 20, False, 4)])
+def test_mixed_band_energies(dim, norb, spin, rmax):
+    m = W.random_model(dim, norb, spin, rmax, seed=700 + norb)
+    k = np.random.default_rng(norb).uniform(0, 1, (40, dim))
+    E = m.solve_band_all_parallel(k, Precision.MIXED)
+    Hs = O.gen_ham_batch(m, k[:6], 1)
+    for i in range(6):
+        assert np.max(np.abs(E[i] - O.eigvalsh(Hs[i]))) <= 1e-9 * np.linalg.norm(Hs[i], 2)
+    E64 = m.solve_band_all_parallel(k)
+    assert np.max(np.abs(E - E64)) <= 1e-9 * np.max(np.abs(E64))
+    assert np.all(np.diff(E, axis=1) >= 0)
+
+
 def test_mixed_handles_kramers_clusters():
     km = M.kane_mele()
     p = Parameters.rank2((12, 12), [1.0, 0.0], [0.0, 1.0], [-0.5, 0.0, 0.5]).with_spin(SpinDirection.Z)
