@@ -62,8 +62,8 @@ enum tbg_gauge { TBG_GAUGE_LATTICE = 0, TBG_GAUGE_ATOM = 1 };
 enum tbg_spin { TBG_SPIN_NONE = -1, TBG_SPIN_X = 0, TBG_SPIN_Y = 1, TBG_SPIN_Z = 2 };
 
 /* Arithmetic of tbg_hall_conductivity / tbg_berry_curvature.  MIXED applies
- * to models with nsta <= 256; larger models run FP64 (tbg_report.precision
- * says which ran). */
+ * to models with 9 <= nsta <= 2048 (products longer than 256 run in exact
+ * chunks); other models run FP64 (tbg_report.precision says which ran). */
 enum tbg_precision {
     TBG_PREC_FP64 = 0,  /* plain: FP64 end to end (the drop-in) */
     TBG_PREC_MIXED = 1  /* FP32 eigensolve, refinement and rotation on the
@@ -136,7 +136,7 @@ int tbg_solve_band(const tbg_model* m, int64_t nk, const double* k,
 
 /* The same with a precision choice: TBG_PREC_FP64 is tbg_solve_band;
  * TBG_PREC_MIXED runs the FP32 eigensolve with the FP64-class refinement of
- * the eigenvalues (<= 1e-9 ||H||; models of 9..256 bands, others FP64).  For
+ * the eigenvalues (<= 1e-9 ||H||; models of 9..2048 bands, others FP64).  For
  * callers that want band energies faster than the drop-in (the serving loop's
  * bands requests); no counterpart in the reference. */
 int tbg_solve_band_prec(const tbg_model* m, int64_t nk, const double* k,
@@ -258,7 +258,7 @@ int tbg_dos(const tbg_model* m, const int64_t* kmesh, double E_min, double E_max
  * mode 1: out (n_loops) = -arg det of the product of the raw overlaps;
  *         replaces Berry::berry_loop_det (geometry.rs:217-270).
  * precision: FP64 eigenpairs at the loop points, or MIXED (FP32 eigenpairs
- * refined with FP64-class tensor-core products, <= 256 bands). */
+ * refined with FP64-class tensor-core products, <= 2048 bands). */
 int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const double* kvec,
                      int64_t n_occ, const int64_t* occ, int mode, int precision, double* out);
 

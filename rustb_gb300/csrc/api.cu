@@ -116,15 +116,25 @@ int64_t chunk_budget_bytes() {
 // per-matrix kernels (two resident matrices per SM), so no chunk ends in a
 // nearly empty wave.
 int64_t choose_chunk(int64_t nk, int64_t per_k_bytes) {
-    int64_t c = std::max<int64_t>(1, chunk_budget_bytes() / std::max<int64_t>(per_k_bytes, 1));
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) nsm = 1;
+    const int64_t q = 2 * (int64_t)nsm;
+    per_k_bytes = std::max<int64_t>(per_k_bytes, 1);
+    int64_t budget = chunk_budget_bytes();
+    if (!std::getenv("TBG_CHUNK_BYTES") && budget / per_k_bytes < std::min<int64_t>(nk, q)) {
+        // large matrices: room for one full wave of the per-matrix kernels
+        // (two per SM) when half of the free device memory allows it
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+            budget = std::max<int64_t>(budget, std::min<int64_t>(per_k_bytes * std::min<int64_t>(nk, q),
+                                                                 (int64_t)(free_b / 2)));
+    }
+    int64_t c = std::max<int64_t>(1, budget / per_k_bytes);
     c = std::min<int64_t>(c, 65535);
     const char* s = std::getenv("TBG_MAX_CHUNK");
     if (s && std::atoll(s) > 0) c = std::min<int64_t>(c, std::atoll(s));
     if (nk > c) {
-        int dev = 0, nsm = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) nsm = 1;
-        const int64_t q = 2 * (int64_t)nsm;
         const int64_t n = (nk + c - 1) / c;
         const int64_t bal = (nk + n - 1) / n;
         const int64_t up = (bal + q - 1) / q * q;
@@ -241,10 +251,13 @@ double lattice_det(const std::vector<double>& lat, int dim) {
            lat[2] * (lat[3] * lat[7] - lat[4] * lat[6]);
 }
 
-// The mixed path's exact-slice tensor-core GEMM contracts over the band index
-// with K <= 256; larger models run the FP64 path (reported in tbg_report).
+// Models of more than kMixedMaxN bands (or of more than 256 with the mma.sync
+// products) run the FP64 path (reported in tbg_report).
 int effective_precision(const ModelDev& M, int precision) {
-    if (precision == TBG_PREC_MIXED && M.nsta > 256) return TBG_PREC_FP64;
+    // the tcgen05 products run longer contractions in exact chunks of 256; the
+    // mma.sync form (selectable for comparison) stops at 256
+    if (precision == TBG_PREC_MIXED && (M.nsta > kMixedMaxN || (M.nsta > 256 && !ozaki_use_tc())))
+        return TBG_PREC_FP64;
     return precision;
 }
 
@@ -1041,7 +1054,7 @@ int tbg_wilson_loops(const tbg_model* m, int64_t n_loops, int64_t n_k, const dou
         if (occ[i] < 0 || occ[i] >= N) return set_error(TBG_E_INVALID_ARGUMENT, "occupied band index out of bounds");
     if (n_occ > kWilsonMaxOcc) return set_error(TBG_E_UNSUPPORTED, "Wilson loops support at most 64 occupied bands");
     const int svd = mode == 0;
-    // mixed: FP32 eigenpairs refined on the tensor cores (9 .. 256 bands), else FP64
+    // mixed: FP32 eigenpairs refined on the tensor cores (9 .. 2048 bands), else FP64
     const bool mixed = effective_precision(M, precision) == TBG_PREC_MIXED && N > kSmallMaxN;
     if (n_occ == 0) {  // empty product: det 1 (phase 0); no eigenphases
         if (!svd)

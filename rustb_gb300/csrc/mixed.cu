@@ -454,16 +454,25 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
                                                                                         clusters_d);
         TBG_LAUNCHED("oa_kernel");
     }
-    if (!Om && !Uout) {  // band energies only
+    auto energies_out = [&]() -> int {
         sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 3 * sizeof(double) * N, st>>>(
             N, batch, E, nullptr, nullptr);
         TBG_LAUNCHED("sort_e_om_kernel");
-        return TBG_OK;
-    }
-    // 4. X' = X + X F  (float pair: hi = X, lo = X F)
+        return (int)TBG_OK;
+    };
+    if (!Om && !Uout) return energies_out();  // band energies only
+    // 4. X' = X + X F  (float pair: hi = X, lo = X F).  F is small except for
+    // the rotations inside eigenvalue clusters, where the LOW class's 2^-21
+    // leaves errors that leak out of near-degenerate subspaces; above
+    // kHighCorrN bands (dense spectra, many clusters) X F is a HIGH product.
     if ((rc = exps(F32, false, X, XR)) || (rc = exps(F32, true, F, FC))) return rc;
-    rc = tc ? ozaki_zgemm_tc_low(st, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, slot(XR), slot(FC), status_d, true)
-            : ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB);
+    if (tc && N > kHighCorrN)
+        rc = ozaki_zgemm_tc(st, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, slot(XR), slot(FC),
+                            status_d, true);
+    else
+        rc = tc ? ozaki_zgemm_tc_low(st, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, slot(XR), slot(FC), status_d,
+                                     true)
+                : ozaki_zgemm(st, false, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, EA, EB);
     if (rc) return rc;
     {
         KTimer kt(st, "xprime_kernel");

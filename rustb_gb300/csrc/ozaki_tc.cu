@@ -58,6 +58,9 @@ constexpr int MMA_WARP = 12;
 constexpr int A_PRODUCERS = 256;
 constexpr int B_PRODUCERS = 128;
 constexpr int ZERO_EXP = -100000;
+// Longest contraction one launch keeps exact: 2K real terms of digit products
+// below 2^15 per level stay within FP32's 24-bit significand.
+constexpr int kTcMaxK = 256;
 
 enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2, FMT_PRESLICED = 3 };
 
@@ -263,6 +266,15 @@ __device__ __forceinline__ void elem_digits(const int4& r, int E, float s1, floa
         digits_fixed(F, P);
     }
 }
+// (ah + al) + (bh + bl) as a float pair: two-sum of the leading parts, the
+// trailing parts and the rounding error added, then renormalised.
+__device__ __forceinline__ float2 pair_add(float ah, float al, float bh, float bl) {
+    const float s = __fadd_rn(ah, bh);
+    const float v = __fsub_rn(s, ah);
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(ah, __fsub_rn(s, v)), __fsub_rn(bh, v)), __fadd_rn(al, bl));
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo_k, float hi_k) {
     __nv_bfloat162 h = __floats2bfloat162_rn(lo_k, hi_k);
     return *reinterpret_cast<uint32_t*>(&h);
@@ -298,7 +310,8 @@ template <bool CONJ_A, int FMTA, int FMTB, int S>
 __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
                  int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
-                 float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err) {
+                 float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err,
+                 int accumulate) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
     constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
     constexpr int HS = S * PLANE;             // planes of one operand in a stage
@@ -534,7 +547,14 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                             const float sc = pow2f(n);
                             out = make_float4(hl[0] * sc, hl[1] * sc, hl[2] * sc, hl[3] * sc);
                         }
-                        C[b * sC + (int64_t)r * ldc + j] = out;
+                        float4* cp = C + b * sC + (int64_t)r * ldc + j;
+                        if (accumulate) {  // a later K chunk: add to the stored pair
+                            const float4 prev = *cp;
+                            const float2 re = pair_add(prev.x, prev.y, out.x, out.y);
+                            const float2 im = pair_add(prev.z, prev.w, out.z, out.w);
+                            out = make_float4(re.x, re.y, im.x, im.y);
+                        }
+                        *cp = out;
                     }
                 }
             }
@@ -602,7 +622,7 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
 template <bool CJ, int FA, int FB, int S>
 static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                      const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
-                     int* err, const char* name, double work) {
+                     int* err, const char* name, double work, int accumulate = 0) {
     auto kern = oz_tc_kernel<CJ, FA, FB, S>;
     constexpr int smem = tc_smem_bytes(S);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -615,30 +635,56 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
         const size_t eb = FB == FMT_F32 ? 8 : 16;
         kern<<<grid, TC_THREADS, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
                                                 static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
-                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err);
+                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err, accumulate);
         TBG_LAUNCHED(name);
     }
     return TBG_OK;
 }
+
+static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
+                                int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
+                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate);
 
 // With exps_ready the caller has filled EA (rows of op(A)) and EB (columns of
 // B) already, e.g. once for an operand shared by several products.
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
                    int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready) {
-    if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: K > 256");
     if (!exps_ready) {
         int rc = ozaki_exp_launch(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
         if (rc) return rc;
     }
+    // Contractions longer than kTcMaxK run in chunks of kTcMaxK (each exact in
+    // its level accumulators); later chunks add their float pairs to C.  The
+    // exponents stay those of the whole rows and columns.
+    if (K > kTcMaxK) {
+        const size_t ea = fmt_a == FMT_F32 ? 8 : 16, eb = fmt_b == FMT_F32 ? 8 : 16;
+        for (int k0 = 0; k0 < K; k0 += kTcMaxK) {
+            const int kc = std::min(kTcMaxK, K - k0);
+            const char* Ak = static_cast<const char*>(A) + (conj_a ? (int64_t)k0 * lda : (int64_t)k0) * ea;
+            const char* Bk = static_cast<const char*>(B) + (int64_t)k0 * ldb * eb;
+            const int rc = ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, kc, Ak, lda, sA, Bk, ldb, sB, C,
+                                                ldc, sC, EA, EB, err, k0 > 0);
+            if (rc) return rc;
+        }
+        return TBG_OK;
+    }
+    return ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB,
+                                err, false);
+}
+
+static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
+                                int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
+                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate) {
     const double work = 8.0 * (double)M * Nc * K * batch;
 #define TC_CASE(CJ, FA, FB)                                                                                          \
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
         return launch_tc<CJ, FA, FB, TC_S>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,    \
-                                           "ozaki_tc_kernel<high>", work);
+                                           "ozaki_tc_kernel<high>", work, accumulate ? 1 : 0);
     TC_CASE(false, FMT_F64, FMT_F64)   // unit test
     TC_CASE(true, FMT_F64, FMT_F64)    // unit test
     TC_CASE(true, FMT_F32, FMT_F32)    // X^H X
+    TC_CASE(false, FMT_F32, FMT_F32)   // X F (HIGH above kHighCorrN bands)
     TC_CASE(false, FMT_PAIR, FMT_F32)  // H X
     TC_CASE(true, FMT_F32, FMT_PAIR)   // X^H (H X)
     TC_CASE(false, FMT_PAIR, FMT_PAIR) // V X'
@@ -652,13 +698,19 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                        int* err, bool exps_ready) {
-    if (K > 256) return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc_low: K > 256");
     if (!exps_ready) {
         int rc = ozaki_exp_launch(st, false, FMT_F32, FMT_F32, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
         if (rc) return rc;
     }
-    return launch_tc<false, FMT_F32, FMT_F32, 3>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,
-                                                 "ozaki_tc_kernel<low>", 8.0 * (double)M * Nc * K * batch);
+    for (int k0 = 0; k0 < K; k0 += kTcMaxK) {  // chunks of kTcMaxK, as in ozaki_zgemm_tc
+        const int kc = std::min(kTcMaxK, K - k0);
+        const int rc = launch_tc<false, FMT_F32, FMT_F32, 3>(
+            st, batch, M, Nc, kc, static_cast<const char*>(A) + (int64_t)k0 * 8, lda, sA,
+            static_cast<const char*>(B) + (int64_t)k0 * ldb * 8, ldb, sB, C, ldc, sC, EA, EB, err,
+            "ozaki_tc_kernel<low>", 8.0 * (double)M * Nc * kc * batch, k0 > 0);
+        if (rc) return rc;
+    }
+    return TBG_OK;
 }
 
 // Bytes of the hop-table stage images (K = nR rows of Nc = N^2 elements).
@@ -691,7 +743,7 @@ int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A,
         return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier_tc: grid too large");
     KTimer kt(st, "ozaki_tc_fourier_kernel", 8.0 * (double)M * Nc * K);
     dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
-    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err);
+    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0);
     TBG_LAUNCHED("ozaki_tc_fourier_kernel");
     return TBG_OK;
 }

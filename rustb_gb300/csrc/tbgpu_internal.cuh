@@ -235,6 +235,13 @@ int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* kl
                 const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
                 double width, double* Om, double* E, double* S, double* Met = nullptr, double* SM = nullptr);
 constexpr int kSmallMaxN = 8;
+// Largest model the mixed path takes (FP32 solver with the matrix in global
+// memory above 215 bands; tcgen05 products in chunks of 256 along K).
+constexpr int kMixedMaxN = 2048;
+// Above this many bands the refinement's correction X F is a HIGH product.
+constexpr int kHighCorrN = 256;
+// tcgen05 form of the exact-slice products (default) or the mma.sync form.
+bool ozaki_use_tc();
 
 // Gaussian-smeared DOS: add the terms of count band energies ev (device) to
 // the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds

@@ -70,3 +70,34 @@ def test_ozaki_low_precision_and_zeros(use_tc):
     scale = np.abs(A).max() * np.abs(B).max() * 64
     assert np.abs(C - ref).max() / scale < 1e-5
     assert np.all(C[0, 5, :] == 0.0)
+
+
+@pytest.mark.parametrize("conj_a", [False, True])
+@pytest.mark.parametrize("M,Nc,K", [(128, 64, 600), (70, 130, 257), (256, 128, 1024)])
+def test_ozaki_tc_long_contractions(conj_a, M, Nc, K):
+    """K > 256: exact chunks of 256 whose float pairs are added in the epilogue."""
+    lib = _lib.load()
+    rng = np.random.default_rng(M + Nc + K + 1)
+    batch = 2
+    shapeA = (batch, K, M) if conj_a else (batch, M, K)
+    A = rng.standard_normal(shapeA) + 1j * rng.standard_normal(shapeA)
+    B = rng.standard_normal((batch, K, Nc)) + 1j * rng.standard_normal((batch, K, Nc))
+    if conj_a:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, 1, M))
+    else:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, M, 1))
+    B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
+    opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
+    ref = opA @ B
+    C = ozaki(lib, A, B, conj_a, True, 1)
+    scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
+    assert (np.abs(C - ref) / scale).max() < 1e-12
+
+
+def test_ozaki_tc_low_long_contraction():
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal((2, 64, 700)) + 1j * rng.standard_normal((2, 64, 700))
+    B = rng.standard_normal((2, 700, 48)) + 1j * rng.standard_normal((2, 700, 48))
+    C = ozaki(lib, A, B, False, False, 1)
+    assert np.abs(C - A @ B).max() / (np.abs(A).max() * np.abs(B).max() * 700) < 1e-5

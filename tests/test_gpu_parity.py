@@ -282,6 +282,30 @@ def test_mixed_band_energies(dim, norb, spin, rmax):
     assert np.all(np.diff(E, axis=1) >= 0)
 
 
+def test_mixed_beyond_256_bands():
+    """300 bands: the FP32 solver with the matrix in global memory and the
+    tensor-core products in chunks of 256 along K."""
+    m = W.random_model(2, 300, False, 1, seed=1300)
+    p = Parameters.rank2((3, 3), [1.0, 0.0], [0.0, 1.0], [-0.1, 0.0, 0.2])
+    plain = m.hall_conductivity(p, Precision.FP64).conductivity
+    mixed = m.hall_conductivity(p, Precision.MIXED).conductivity
+    assert np.max(np.abs(mixed - plain)) <= 1e-6 * np.max(np.abs(plain))
+    k = O.gen_kmesh((3, 3))[:2]
+    E = m.solve_band_all_parallel(k, Precision.MIXED)
+    Hs = O.gen_ham_batch(m, k, 1)
+    for i in range(len(k)):
+        assert np.max(np.abs(E[i] - O.eigvalsh(Hs[i]))) <= 1e-9 * np.linalg.norm(Hs[i], 2)
+
+
+def test_mixed_supercell_1024_bands():
+    """The 1024-orbital supercell workload: dense spectrum, two refinement sweeps."""
+    m = W.supercell_2d()
+    p = Parameters.rank2((2, 2), [1.0, 0.0], [0.0, 1.0], [0.0])
+    plain = m.hall_conductivity(p, Precision.FP64).conductivity
+    mixed = m.hall_conductivity(p, Precision.MIXED).conductivity
+    assert abs(mixed[0] - plain[0]) <= 1e-6 * abs(plain[0])
+
+
 def test_mixed_handles_kramers_clusters():
     km = M.kane_mele()
     p = Parameters.rank2((12, 12), [1.0, 0.0], [0.0, 1.0], [-0.5, 0.0, 0.5]).with_spin(SpinDirection.Z)
