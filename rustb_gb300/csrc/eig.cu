@@ -1261,6 +1261,7 @@ size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
 int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
                 size_t work_bytes, int* status_d) {
     if (batch <= 0) return TBG_OK;
+    if (N <= kSmallMaxN) return eig_small(st, N, batch, A, E, U, status_d);  // one thread per matrix
     int G, PB;
     choose_g_pb<double>(N, false, 16, 16, G, PB);
     return launch_heev<double, false>(st, N, batch, A, E, U, work, work_bytes, status_d, "heev_kernel<double>", G,

@@ -282,6 +282,47 @@ __global__ void __launch_bounds__(128) small_fused_kernel(
     }
 }
 
+// Eigenpairs of batched N x N (N <= 8) Hermitian matrices, one thread per
+// matrix: cyclic Jacobi in registers, E ascending, U with the eigenvectors in
+// columns (row-major, the layout of the batched solver); U may be null.
+// Non-finite input sets bit 0 of *status, as the batched solver does.
+template <int NM>
+__global__ void __launch_bounds__(128) small_eig_kernel(int N, int64_t batch, const zc* __restrict__ H,
+                                                       double* __restrict__ E_out, zc* __restrict__ U_out,
+                                                       int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= batch) return;
+    const int64_t NN = (int64_t)N * N;
+    zc A[NM][NM], W[NM][NM];
+    for (int i = 0; i < NM; ++i)
+        for (int j = 0; j < NM; ++j) A[i][j] = (i < N && j < N) ? H[t * NN + i * N + j] : mk(0.0, 0.0);
+    jacobi<NM, true>(N, A, W);
+    double E[NM];
+    int ord[NM];
+    for (int i = 0; i < N; ++i) {
+        E[i] = A[i][i].re;
+        ord[i] = i;
+    }
+    for (int i = 1; i < N; ++i) {  // ascending (insertion sort of the index)
+        const int oi = ord[i];
+        int j = i - 1;
+        while (j >= 0 && E[ord[j]] > E[oi]) {
+            ord[j + 1] = ord[j];
+            --j;
+        }
+        ord[j + 1] = oi;
+    }
+    bool bad = false;
+    for (int i = 0; i < N; ++i) {
+        E_out[t * N + i] = E[ord[i]];
+        bad = bad || !isfinite(E[i]);
+    }
+    if (bad && status) atomicOr(status, 1);
+    if (U_out)
+        for (int r = 0; r < N; ++r)
+            for (int c = 0; c < N; ++c) U_out[t * NN + r * N + c] = W[r][ord[c]];
+}
+
 }  // namespace
 
 int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* klist_d, int64_t k0,
@@ -320,4 +361,19 @@ int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* kl
     return TBG_OK;
 }
 
+}  // namespace tbg
+
+namespace tbg {
+int eig_small(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status) {
+    if (batch <= 0) return TBG_OK;
+    const unsigned blocks = (unsigned)((batch + 127) / 128);
+    if (N <= 2)
+        small_eig_kernel<2><<<blocks, 128, 0, st>>>(N, batch, H, E, U, status);
+    else if (N <= 4)
+        small_eig_kernel<4><<<blocks, 128, 0, st>>>(N, batch, H, E, U, status);
+    else
+        small_eig_kernel<8><<<blocks, 128, 0, st>>>(N, batch, H, E, U, status);
+    TBG_LAUNCHED("small_eig_kernel");
+    return TBG_OK;
+}
 }  // namespace tbg

@@ -235,6 +235,9 @@ int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* kl
                 const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
                 double width, double* Om, double* E, double* S, double* Met = nullptr, double* SM = nullptr);
 constexpr int kSmallMaxN = 8;
+// Eigenpairs of N <= kSmallMaxN matrices by per-thread Jacobi (E ascending,
+// U columns; U may be null; non-finite input sets bit 0 of *status).
+int eig_small(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status);
 // Largest model the mixed path takes (FP32 solver with the matrix in global
 // memory above 215 bands; tcgen05 products in chunks of 256 along K).
 constexpr int kMixedMaxN = 2048;
