@@ -220,6 +220,36 @@ __device__ __forceinline__ void digits_float(float u, float* P) {
     r = __fsub_rn(r, P[4]);
     P[5] = round_to_pow2<-35>(r);
 }
+// Six pre-scaled digits of u = (hi + lo) 2^(7 - E) in (-128, 128] for a
+// float pair, in FP32 arithmetic only.  The pair is first renormalised by an
+// error-free two-sum (the producers' pairs need not have |lo| <= ulp(hi) / 2);
+// digits 0..2 then come from the leading part, whose remainder r (|r| <=
+// 2^-15, a subset of its bits) is exact; t = r + lo then needs the bits from
+// 2^-15 down to the grid 2^-35 (21 bits), so its rounding stays below the
+// grid, and digits 3..5 come from t.  The sum of the digits is u on the grid
+// 2^-35 up to half a grid step plus t's rounding (the integer form truncates
+// each part: up to two grid steps).  |q_0| <= 128, |q_1|, |q_2|, |q_4|,
+// |q_5| <= 64, |q_3| <= 72.
+__device__ __forceinline__ void digits_pair(float uh, float ul, float* P) {
+    {
+        const float sm = __fadd_rn(uh, ul);
+        const float v = __fsub_rn(sm, uh);
+        ul = __fadd_rn(__fsub_rn(uh, __fsub_rn(sm, v)), __fsub_rn(ul, v));
+        uh = sm;
+    }
+    P[0] = round_to_pow2<0>(uh);
+    float r = __fsub_rn(uh, P[0]);
+    P[1] = round_to_pow2<-7>(r);
+    r = __fsub_rn(r, P[1]);
+    P[2] = round_to_pow2<-14>(r);
+    r = __fsub_rn(r, P[2]);
+    float t = __fadd_rn(r, ul);
+    P[3] = round_to_pow2<-21>(t);
+    t = __fsub_rn(t, P[3]);
+    P[4] = round_to_pow2<-28>(t);
+    t = __fsub_rn(t, P[4]);
+    P[5] = round_to_pow2<-35>(t);
+}
 __device__ __forceinline__ float pow2f(int n) { return __int_as_float((127 + n) << 23); }  // n in [-126, 127]
 // 2^(7 - E) as s1 * s2 (each a normal float) for FP32 operands; 0 for a zero line.
 __device__ __forceinline__ void f32_scales(int E, float& s1, float& s2) {
@@ -254,6 +284,9 @@ __device__ __forceinline__ void elem_digits(const int4& r, int E, float s1, floa
     if (FMT == FMT_F32) {
         const float x = __int_as_float(PART ? r.y : r.x);
         digits_float((x * s1) * s2, P);
+    } else if (FMT == FMT_PAIR) {
+        const float hi = __int_as_float(PART ? r.z : r.x), lo = __int_as_float(PART ? r.w : r.y);
+        digits_pair(__fmul_rn(__fmul_rn(hi, s1), s2), __fmul_rn(__fmul_rn(lo, s1), s2), P);
     } else {
         long long F = 0;
         if (E != ZERO_EXP) {
