@@ -531,6 +531,12 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     }
 
     // ---------------------------------------------------------- epilogue
+    // With room in the (now idle) stage buffers the 128 x 64 tile of float
+    // pairs is staged in shared memory (rows padded to 65 entries: no bank
+    // conflicts either way) and written out row by row, coalesced.
+    constexpr int TROW = TC_TN + 1;
+    constexpr bool STAGE = 2 * SB >= TC_TM * TROW * 16;
+    float4* tile = reinterpret_cast<float4*>(base);
     if (warp < 8) {
         bool ok = mbar_wait(&bar_done, 0, &abort_sh) && !abort_sh;
         ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld is warp-collective
@@ -549,11 +555,11 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     tmem_ld8(lane_addr + (uint32_t)(L * 128 + TC_TN + c0), v[2 * L + 1]);
                 }
                 tmem_wait_ld();
-                if (r < M) {
+                if (STAGE || r < M) {
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
                         const int j = col0 + c0 + c;
-                        if (j >= Nc) continue;
+                        if (!STAGE && j >= Nc) continue;
                         float hl[4];
 #pragma unroll
                         for (int part = 0; part < 2; ++part) {
@@ -573,14 +579,42 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                             hl[2 * part] = hi;
                             hl[2 * part + 1] = (e1 + e2) + a3;
                         }
-                        const int eb = EB[b * Nc + j];
+                        const int eb = (j < Nc) ? EB[b * Nc + j] : ZERO_EXP;
                         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
                         if (ea != ZERO_EXP && eb != ZERO_EXP) {
                             const int n = max(-126, min(127, ea + eb - 14));
                             const float sc = pow2f(n);
                             out = make_float4(hl[0] * sc, hl[1] * sc, hl[2] * sc, hl[3] * sc);
                         }
+                        if (STAGE) {
+                            tile[(32 * q + lane) * TROW + c0 + c] = out;
+                            continue;
+                        }
                         float4* cp = C + b * sC + (int64_t)r * ldc + j;
+                        if (accumulate) {  // a later K chunk: add to the stored pair
+                            const float4 prev = *cp;
+                            const float2 re = pair_add(prev.x, prev.y, out.x, out.y);
+                            const float2 im = pair_add(prev.z, prev.w, out.z, out.w);
+                            out = make_float4(re.x, re.y, im.x, im.y);
+                        }
+                        *cp = out;
+                    }
+                }
+            }
+        }
+        if (STAGE) {
+            asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
+            if (ok) {
+                // warp w writes rows w, w + 8, ...; lanes over the 64 columns
+                for (int rl = warp; rl < TC_TM; rl += 8) {
+                    const int rr = row0 + rl;
+                    if (rr >= M) break;
+#pragma unroll
+                    for (int half = 0; half < 2; ++half) {
+                        const int jl = lane + 32 * half, j = col0 + jl;
+                        if (j >= Nc) continue;
+                        float4 out = tile[rl * TROW + jl];
+                        float4* cp = C + b * sC + (int64_t)rr * ldc + j;
                         if (accumulate) {  // a later K chunk: add to the stored pair
                             const float4 prev = *cp;
                             const float2 re = pair_add(prev.x, prev.y, out.x, out.y);
