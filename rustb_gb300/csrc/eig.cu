@@ -284,171 +284,13 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     size_t s1 = sizeof(T) * 4 * (size_t)N * G;
     // back-transform in the kernel (matrix in global memory): a column-major
     // panel with stride N + 4; with the matrix in shared memory it is a pass
-    // of its own (heev_bt_kernel)
+    // of its own (heev_bt_tiled_kernel)
     size_t s2 = a_smem ? 0 : sizeof(cx<T>) * (size_t)(N + 4) * PB;
     b += std::max(s1, s2);
     b += sizeof(int) * (4 + (size_t)N);  // flags + per-eigenvalue redo marks
     return b;
 }
 
-// Shared memory of the separate back-transformation pass: packed reflectors,
-// tau, panel N x PB, Y (BT_NB x PB), Gram and T.
-template <typename T>
-__host__ __device__ inline size_t bt_smem_bytes(int N, int PB) {
-    return sizeof(cx<T>) * (packed_elems<true>(N) + (size_t)N + (size_t)(N + BT_NB) * PB + 2 * BT_NB * BT_NB);
-}
-
-// U <- H_0 H_1 ... H_{N-2} U with H_j = I - tau_j v_j v_j^H (v_j in row j of
-// A from column j+1, v_j[j+1] = 1), in compact-WY blocks of BT_NB reflectors:
-// H_{j0} ... H_{j1-1} = I - V T V^H with T^{-1} = diag(1/tau) + striu(V^H V)
-// (Joffrain, Low, Quintana-Orti, van de Geijn, Van Zee, "Accumulating
-// Householder transformations, revisited", 2006).  Blocks are applied
-// last-first to panels of PB columns of U held row-major in shared memory:
-//   Y = V^H P;  Y <- T Y by back-substitution with T^{-1}, per column:
-//   y_i = tau_i (y_i - sum_{l>i} G_il y_l)  (tau_i = 0 gives y_i = 0);
-//   P <- P - V Y in 4 x QN register tiles (QN = 2 for narrow panels keeps
-//   every thread busy).
-// work: P (N x PB), Y (BT_NB x PB), G (BT_NB x BT_NB).
-template <typename T, int QN>
-__device__ void back_transform_blocked(int N, const cx<T>* __restrict__ A, const cx<T>* __restrict__ tau,
-                                       cx<T>* __restrict__ U, cx<T>* __restrict__ work, int PB) {
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    // vrow(r)[c] = A(r, c) for c >= r (packed upper triangle)
-    auto vrow = [&](int r) { return A + diag_off<true>(N, 0, r) - r; };
-    cx<T>* P = work;
-    cx<T>* Y = P + (size_t)N * PB;
-    cx<T>* G = Y + (size_t)BT_NB * PB;
-    if (N < 2) return;
-    for (int c0 = 0; c0 < N; c0 += PB) {
-        const int pw = min(PB, N - c0);
-        for (int idx = tid; idx < N * pw; idx += nthr) {
-            const int r = idx / pw, c = idx - r * pw;
-            P[(size_t)r * PB + c] = U[(size_t)r * N + c0 + c];
-        }
-        __syncthreads();
-        for (int j0 = ((N - 2) / BT_NB) * BT_NB; j0 >= 0; j0 -= BT_NB) {
-            const int nb = min(BT_NB, N - 1 - j0);
-            const int k0 = j0 + 1;        // first row touched by the block
-            const int kf = min(N, j0 + BT_NB + 1);  // from here on every v_i of the block is unmasked
-            // Gram G(l, i) = v_l^H v_i for l < i < nb (zero elsewhere)
-            for (int e = tid; e < BT_NB * BT_NB; e += nthr) {
-                const int l = e / BT_NB, i = e - l * BT_NB;
-                cx<T> acc = mk<T>(0, 0);
-                if (l < i && i < nb) {
-                    const cx<T>* vl = vrow(j0 + l);
-                    const cx<T>* vi = vrow(j0 + i);
-                    cx<T> q[4] = {mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0)};
-                    for (int kk = j0 + i + 1; kk < N; kk += 4) {
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            if (kk + u < N) fma_cjx(q[u], vl[kk + u], vi[kk + u]);
-                    }
-                    acc = (q[0] + q[1]) + (q[2] + q[3]);
-                }
-                G[e] = acc;
-            }
-            // Y = V^H P: item (ig, c) computes rows ig and ig + 8
-            for (int it = tid; it < 8 * pw; it += nthr) {
-                const int ig = it / pw, c = it - ig * pw;
-                const int i0 = ig, i1 = ig + 8;
-                cx<T> y0 = mk<T>(0, 0), y1 = mk<T>(0, 0);
-                if (i0 < nb) {
-                    const cx<T>* v0 = vrow(j0 + i0);
-                    const bool h1 = i1 < nb;
-                    const cx<T>* v1 = vrow(j0 + (h1 ? i1 : i0));
-                    for (int k = k0; k < kf; ++k) {  // rows where part of the block is still zero
-                        const cx<T> pk = P[(size_t)k * PB + c];
-                        if (k > j0 + i0) fma_cjx(y0, v0[k], pk);
-                        if (h1 && k > j0 + i1) fma_cjx(y1, v1[k], pk);
-                    }
-                    // eight interleaved partial sums: shorter FP32 accumulation chains
-                    // (error and latency) than one running sum over the column
-                    cx<T> p0[8], p1[8];
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) p0[u] = p1[u] = mk<T>(0, 0);
-                    for (int kk = kf; kk < N; kk += 8) {
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const int k = kk + u;
-                            if (k < N) {
-                                const cx<T> pk = P[(size_t)k * PB + c];
-                                fma_cjx(p0[u], v0[k], pk);
-                                if (h1) fma_cjx(p1[u], v1[k], pk);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int w = 4; w > 0; w >>= 1)
-#pragma unroll
-                        for (int u = 0; u < w; ++u) {
-                            p0[u] = p0[u] + p0[u + w];
-                            p1[u] = p1[u] + p1[u + w];
-                        }
-                    y0 = y0 + p0[0];
-                    y1 = y1 + p1[0];
-                }
-                Y[i0 * PB + c] = y0;
-                Y[i1 * PB + c] = y1;
-            }
-            __syncthreads();
-            // Y <- T Y: back-substitution with T^{-1} = diag(1/tau) + striu(G), per column
-            for (int c = tid; c < pw; c += nthr) {
-                cx<T> y[BT_NB];
-#pragma unroll
-                for (int i = 0; i < BT_NB; ++i) y[i] = Y[i * PB + c];
-#pragma unroll
-                for (int i = BT_NB - 1; i >= 0; --i) {
-                    cx<T> s = y[i];
-#pragma unroll
-                    for (int l = i + 1; l < BT_NB; ++l) s = s - G[i * BT_NB + l] * y[l];
-                    y[i] = (i < nb) ? tau[j0 + i] * s : mk<T>(0, 0);
-                }
-#pragma unroll
-                for (int i = 0; i < BT_NB; ++i) Y[i * PB + c] = y[i];
-            }
-            __syncthreads();
-            // P <- P - V Y: item (rg, cg) updates rows k0 + 4 rg .. +3, columns cg + CS q
-            const int nrg = (N - k0 + 3) / 4;
-            const int CS = (PB + QN - 1) / QN;
-            for (int it = tid; it < nrg * CS; it += nthr) {
-                const int rg = it / CS, cg = it - rg * CS;
-                const int kb = k0 + 4 * rg;
-                cx<T> acc[4][QN];
-#pragma unroll
-                for (int a = 0; a < 4; ++a)
-#pragma unroll
-                    for (int q = 0; q < QN; ++q) acc[a][q] = mk<T>(0, 0);
-                for (int l = 0; l < nb; ++l) {
-                    const cx<T>* vl = vrow(j0 + l);
-                    cx<T> v[4], y[QN];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) v[a] = (kb + a < N && kb + a > j0 + l) ? vl[kb + a] : mk<T>(0, 0);
-#pragma unroll
-                    for (int q = 0; q < QN; ++q) y[q] = Y[l * PB + min(cg + CS * q, PB - 1)];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a)
-#pragma unroll
-                        for (int q = 0; q < QN; ++q) fma_cx(acc[a][q], v[a], y[q]);
-                }
-#pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    if (kb + a >= N) continue;
-#pragma unroll
-                    for (int q = 0; q < QN; ++q) {
-                        const int c = cg + CS * q;
-                        if (c < pw) P[(size_t)(kb + a) * PB + c] = P[(size_t)(kb + a) * PB + c] - acc[a][q];
-                    }
-                }
-            }
-            __syncthreads();
-        }
-        for (int idx = tid; idx < N * pw; idx += nthr) {
-            const int r = idx / pw, c = idx - r * pw;
-            U[(size_t)r * N + c0 + c] = P[(size_t)r * PB + c];
-        }
-        __syncthreads();
-    }
-}
 
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
@@ -904,48 +746,38 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
     }
 }
 
-// Back-transformation of the FP32 solver as a pass of its own, one CTA per
-// matrix: the reflectors (packed) and a panel of PB columns of U (all of U up
-// to about 150 bands) in shared memory, so each compact-WY block is applied
-// to the whole panel at once.  Vt: (batch, packed + N) = reflectors, tau.
-template <typename T>
-__global__ void __launch_bounds__(512) heev_bt_kernel(int N, int64_t batch, const cx<T>* __restrict__ Vt,
-                                                      cx<T>* __restrict__ Uout, int PB) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const size_t pe = packed_elems<true>(N);
-    cx<T>* V = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* tau = V + pe;
-    cx<T>* work = tau + N;
-    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
-        const cx<T>* src = Vt + (size_t)b * (pe + N);
-        for (size_t i = threadIdx.x; i < pe + N; i += blockDim.x) V[i] = src[i];
-        __syncthreads();
-        if (PB <= 32)
-            back_transform_blocked<T, 2>(N, V, tau, Uout + (size_t)b * N * N, work, PB);
-        else
-            back_transform_blocked<T, 4>(N, V, tau, Uout + (size_t)b * N * N, work, PB);
-        __syncthreads();
-    }
-}
-
-// Back-transformation pass for up to kBtTiledMaxN bands (FP32): U (N4 x N4,
-// N4 = N rounded up to 4, zero padded) in shared memory, and each block of
-// BT_NB reflectors staged as a dense zero-masked BT_NB x N4 tile Vb
-// (Vb[i][k] = v_{j0+i}[k] for k > j0 + i, else 0), so no product needs masks:
+// Back-transformation pass of the FP32 solver (matrix in shared memory during
+// the reduction): U <- H_0 H_1 ... H_{N-2} U with H_j = I - tau_j v_j v_j^H,
+// in compact-WY blocks of BT_NB reflectors, H_{j0} ... H_{j1-1} = I - V T V^H
+// with T^{-1} = diag(1/tau) + striu(V^H V) (Joffrain, Low, Quintana-Orti,
+// van de Geijn, Van Zee, "Accumulating Householder transformations,
+// revisited", 2006), applied last-first.  One CTA per matrix; U in column
+// panels of PB (a multiple of 4; all of U up to 144 bands) held in shared
+// memory with N4 = N rounded up to 4 rows (zero padded), and each block of
+// reflectors staged as a dense zero-masked BT_NB x N4 tile Vb (Vb[i][k] =
+// v_{j0+i}[k] for k > j0 + i, else 0), so no product needs masks:
 //   Gram G(l, i) = Vb[l]^H Vb[i] for l < i, four lanes per entry;
 //   Y = Vb^H P: a thread holds rows i and i + 8 by four columns over a
 //       quarter of the rows k (k = k0 + q (mod 4)); quarters are summed by
 //       shuffles between lanes 8 and 16 apart;
-//   Y <- T Y by back-substitution with T^{-1} = diag(1/tau) + striu(G);
+//   Y <- T Y by back-substitution, per column: y_i = tau_i (y_i - sum_{l>i} G_il y_l);
 //   P <- P - Vb^T Y in 4 x 4 register tiles (rows k..k+3).
-// A thread's four columns are 2c, 2c + 1 and the same two N4 / 2 further on,
-// so consecutive lanes read consecutive 16-byte pairs (no bank conflicts).
-// The next block's tile is read from global memory into registers while this
-// block's products run and stored into the other of two tile buffers.
-constexpr int kBtTiledMaxN = 144;
-__host__ __device__ inline size_t bt_tiled_smem_bytes(int N) {
+// A thread's four columns are 2c, 2c + 1 and the same two W / 2 further on (W
+// the panel width), so consecutive lanes read consecutive 16-byte pairs (no
+// bank conflicts).  The next block's tile is read from global memory into
+// registers while this block's products run and stored into the other of two
+// tile buffers.  Vt: (batch, packed + N) = reflectors (packed rows), tau.
+__host__ __device__ inline size_t bt_tiled_smem_bytes(int N, int PB) {
     const size_t N4 = (size_t)((N + 3) & ~3);
-    return sizeof(cc) * (N4 * N4 + 3 * (size_t)BT_NB * N4 + (size_t)BT_NB * BT_NB + N4);
+    return sizeof(cc) * (N4 * PB + 2 * (size_t)BT_NB * N4 + (size_t)BT_NB * PB + (size_t)BT_NB * BT_NB + N4);
+}
+// Widest panel (a multiple of 4, at most N rounded up to 4) that fits `budget`.
+inline int bt_tiled_panel(int N, size_t budget) {
+    const int N4 = (N + 3) & ~3;
+    const size_t base = bt_tiled_smem_bytes(N, 0);
+    if (budget <= base) return 0;
+    const size_t pb = (budget - base) / (sizeof(cc) * (size_t)(N4 + BT_NB));
+    return (int)std::min<size_t>((size_t)N4, pb & ~(size_t)3);
 }
 
 __device__ __forceinline__ cc bt_vb_elem(const cc* __restrict__ Vm, int N, int N4, int j0, int e) {
@@ -954,15 +786,16 @@ __device__ __forceinline__ cc bt_vb_elem(const cc* __restrict__ Vm, int N, int N
     return Vm[diag_off<true>(N, 0, j) + (size_t)(k - j)];
 }
 
+template <bool PANELS>
 __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t batch, const cc* __restrict__ Vt,
-                                                               cc* __restrict__ Uout) {
+                                                               cc* __restrict__ Uout, int PB) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N4 = (N + 3) & ~3, CG = N4 / 4, cgb = (CG + 7) / 8, H = N4 / 2;
+    const int N4 = (N + 3) & ~3;
     const size_t pe = packed_elems<true>(N);
-    cc* P = reinterpret_cast<cc*>(smem_raw);  // N4 x N4
-    cc* Vbuf = P + (size_t)N4 * N4;             // 2 x BT_NB x N4
-    cc* Y = Vbuf + 2 * (size_t)BT_NB * N4;      // BT_NB x N4
-    cc* G = Y + (size_t)BT_NB * N4;             // BT_NB x BT_NB
+    cc* P = reinterpret_cast<cc*>(smem_raw);  // N4 x W (W <= PB)
+    cc* Vbuf = P + (size_t)N4 * PB;             // 2 x BT_NB x N4
+    cc* Y = Vbuf + 2 * (size_t)BT_NB * N4;      // BT_NB x W
+    cc* G = Y + (size_t)BT_NB * PB;             // BT_NB x BT_NB
     cc* tau = G + BT_NB * BT_NB;                // N4
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     constexpr int kPre = 8;  // tile elements per thread: BT_NB * N4 <= 8 * 512
@@ -971,9 +804,11 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         const cc* Vm = Vt + (size_t)b * (pe + N);
         cc* U = Uout + (size_t)b * N * N;
-        for (int e = tid; e < N4 * N4; e += nthr) {
-            const int r = e / N4, c = e - r * N4;
-            P[e] = (r < N && c < N) ? U[(size_t)r * N + c] : mk<float>(0.f, 0.f);
+      auto panel = [&](const int c0, const int W) {
+        const int CG = W / 4, cgb = (CG + 7) / 8, H = W / 2;
+        for (int e = tid; e < N4 * W; e += nthr) {
+            const int r = e / W, c = e - r * W;
+            P[e] = (r < N && c0 + c < N) ? U[(size_t)r * N + c0 + c] : mk<float>(0.f, 0.f);
         }
         for (int i = tid; i < N4; i += nthr) tau[i] = (i < N) ? Vm[pe + i] : mk<float>(0.f, 0.f);
         for (int e = tid; e < BT_NB * N4; e += nthr) Vbuf[e] = bt_vb_elem(Vm, N, N4, jtop, e);
@@ -1018,8 +853,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     const cc* vc = Vb + (ig + 8) * N4;
                     for (int k = k0 + qk; k < N; k += 4) {
                         const cc a0 = va[k], a1 = vc[k];
-                        const float4 p01 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 2 * cg);
-                        const float4 p23 = *reinterpret_cast<const float4*>(P + (size_t)k * N4 + 2 * cg + H);
+                        const float4 p01 = *reinterpret_cast<const float4*>(P + (size_t)k * W + 2 * cg);
+                        const float4 p23 = *reinterpret_cast<const float4*>(P + (size_t)k * W + 2 * cg + H);
                         const float pr[4] = {p01.x, p01.z, p23.x, p23.z}, pi[4] = {p01.y, p01.w, p23.y, p23.w};
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {  // y += conj(a) p
@@ -1048,7 +883,7 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                 if (valid && qk == 0) {
 #pragma unroll
                     for (int r = 0; r < 2; ++r) {
-                        cc* yr = Y + (ig + 8 * r) * N4 + 2 * cg;
+                        cc* yr = Y + (ig + 8 * r) * W + 2 * cg;
                         *reinterpret_cast<float4*>(yr) = make_float4(y[r][0][0], y[r][0][1], y[r][1][0], y[r][1][1]);
                         *reinterpret_cast<float4*>(yr + H) =
                             make_float4(y[r][2][0], y[r][2][1], y[r][3][0], y[r][3][1]);
@@ -1057,10 +892,10 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
             }
             __syncthreads();
             // Y <- T Y, per column
-            for (int c = tid; c < N4; c += nthr) {
+            for (int c = tid; c < W; c += nthr) {
                 cc yv[BT_NB];
 #pragma unroll
-                for (int i = 0; i < BT_NB; ++i) yv[i] = Y[i * N4 + c];
+                for (int i = 0; i < BT_NB; ++i) yv[i] = Y[i * W + c];
 #pragma unroll
                 for (int i = BT_NB - 1; i >= 0; --i) {
                     cc sv = yv[i];
@@ -1069,7 +904,7 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     yv[i] = (i < nb) ? tau[j0 + i] * sv : mk<float>(0.f, 0.f);
                 }
 #pragma unroll
-                for (int i = 0; i < BT_NB; ++i) Y[i * N4 + c] = yv[i];
+                for (int i = 0; i < BT_NB; ++i) Y[i * W + c] = yv[i];
             }
             __syncthreads();
             // P <- P - Vb^T Y over row groups from k0 rounded down to 4 (rows
@@ -1086,8 +921,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     for (int i = 0; i < nb; ++i) {
                         const float4 v01 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb);
                         const float4 v23 = *reinterpret_cast<const float4*>(Vb + i * N4 + kb + 2);
-                        const float4 y01 = *reinterpret_cast<const float4*>(Y + i * N4 + 2 * cg);
-                        const float4 y23 = *reinterpret_cast<const float4*>(Y + i * N4 + 2 * cg + H);
+                        const float4 y01 = *reinterpret_cast<const float4*>(Y + i * W + 2 * cg);
+                        const float4 y23 = *reinterpret_cast<const float4*>(Y + i * W + 2 * cg + H);
                         const float vr[4] = {v01.x, v01.z, v23.x, v23.z}, vi[4] = {v01.y, v01.w, v23.y, v23.w};
                         const float yr[4] = {y01.x, y01.z, y23.x, y23.z}, yi[4] = {y01.y, y01.w, y23.y, y23.w};
 #pragma unroll
@@ -1102,7 +937,7 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     }
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
-                        cc* prow = P + (size_t)(kb + a) * N4 + 2 * cg;
+                        cc* prow = P + (size_t)(kb + a) * W + 2 * cg;
                         float4 p01 = *reinterpret_cast<float4*>(prow), p23 = *reinterpret_cast<float4*>(prow + H);
                         p01.x -= acc[a][0][0];
                         p01.y -= acc[a][0][1];
@@ -1129,11 +964,17 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
             buf ^= 1;
             __syncthreads();
         }
-        for (int e = tid; e < N * N; e += nthr) {
-            const int r = e / N, c = e - r * N;
-            U[e] = P[(size_t)r * N4 + c];
+        for (int e = tid; e < N * W; e += nthr) {
+            const int r = e / W, c = e - r * W;
+            if (c0 + c < N) U[(size_t)r * N + c0 + c] = P[e];
         }
         __syncthreads();
+      };
+        if constexpr (PANELS) {
+            for (int c0 = 0; c0 < N; c0 += PB) panel(c0, min(PB, N4 - c0));
+        } else {
+            panel(0, N4);  // all of U in one pass
+        }
     }
 }
 
@@ -1150,13 +991,9 @@ inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB
     const size_t left = budget > fixed ? budget - fixed : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
     if (a_smem) {
-        // the back-transformation is a pass of its own: its panel is as wide
-        // as its shared memory allows (up to all N columns)
-        const size_t base = bt_smem_bytes<T>(N, 0);
-        const size_t l2 = kEigSmemOne > base ? kEigSmemOne - base : 0;
-        PB = (int)std::min<size_t>((size_t)((N + 3) & ~3), l2 / (sizeof(cx<T>) * (size_t)(N + BT_NB)));
-        if (PB >= 8) PB &= ~3;  // whole 4-column groups in the V Y update
-        PB = std::max(PB, 1);
+        // the back-transformation is a pass of its own (heev_bt_tiled_kernel):
+        // its panel is as wide as its shared memory allows (up to all columns)
+        PB = bt_tiled_panel(N, kEigSmemOne);
     } else {
         PB = (int)std::max<size_t>(1, std::min<size_t>(pbmax, left / (sizeof(cx<T>) * (size_t)(N + 4))));
     }
@@ -1211,24 +1048,13 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     }
     if constexpr (A_SMEM) {
         if (!U) return TBG_OK;
-        if constexpr (sizeof(T) == sizeof(float)) {
-            if (N <= kBtTiledMaxN) {
-                const size_t bsm = bt_tiled_smem_bytes(N);
-                auto bk = heev_bt_tiled_kernel;
-                if (int rc = allow_max_smem(bk, bsm)) return rc;
-                KTimer kt(st, "heev_bt_kernel", 8.0 * (double)N * N * N * batch);
-                bk<<<(unsigned)std::min<int64_t>(nsm, batch), 512, bsm, st>>>(
-                    N, batch, reinterpret_cast<const cc*>(work), reinterpret_cast<cc*>(U));
-                TBG_LAUNCHED("heev_bt_kernel");
-                return TBG_OK;
-            }
-        }
-        const size_t bsm = bt_smem_bytes<T>(N, PB);
-        auto bk = heev_bt_kernel<T>;
+        static_assert(sizeof(T) == sizeof(float), "the shared-memory solver is the FP32 one");
+        const size_t bsm = bt_tiled_smem_bytes(N, PB);
+        auto bk = PB >= ((N + 3) & ~3) ? heev_bt_tiled_kernel<false> : heev_bt_tiled_kernel<true>;
         if (int rc = allow_max_smem(bk, bsm)) return rc;
-        int64_t g2 = std::min<int64_t>(nsm, batch);
         KTimer kt(st, "heev_bt_kernel", 8.0 * (double)N * N * N * batch);
-        bk<<<(unsigned)g2, 512, bsm, st>>>(N, batch, reinterpret_cast<const cx<T>*>(work), U, PB);
+        bk<<<(unsigned)std::min<int64_t>(nsm, batch), 512, bsm, st>>>(N, batch, reinterpret_cast<const cc*>(work),
+                                                                      reinterpret_cast<cc*>(U), PB);
         TBG_LAUNCHED("heev_bt_kernel");
     }
     return TBG_OK;
@@ -1239,7 +1065,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
 inline bool f32_smem_fits(int N, size_t budget, int& G, int& PB) {
     choose_g_pb<float>(N, true, 32, 64, G, PB, budget);
     return eig_smem_bytes<float>(N, true, G, PB) <= budget && G >= 8 && PB >= std::min(16, (N + 3) & ~3) &&
-           bt_smem_bytes<float>(N, PB) <= kEigSmemOne;
+           bt_tiled_smem_bytes(N, PB) <= kEigSmemOne;
 }
 inline bool f32_in_smem(int N, int& G, int& PB) {
     return f32_smem_fits(N, kEigSmemTwo, G, PB) || f32_smem_fits(N, kEigSmemOne, G, PB);
