@@ -4,7 +4,8 @@
 // ndarray-linalg Eigh; src/ndarray_lapack.rs:412-448).  Algorithm per matrix:
 //
 //   1. Householder reduction to real symmetric tridiagonal form T = Q^H A Q
-//      (unblocked, full storage).  The reflector H_j = I - tau_j v_j v_j^H is
+//      (unblocked, on the upper triangle: packed rows in shared memory, full
+//      rows in global memory).  The reflector H_j = I - tau_j v_j v_j^H is
 //      chosen so that H_j^H [alpha; x] = [beta; 0] with real beta of sign
 //      opposite to Re(alpha) (no cancellation).  v_j is kept in row j of A.
 //   2. Eigenvalues of T by Sturm-count multisection, a few threads per
@@ -16,11 +17,14 @@
 //      are computed by one thread by inverse iteration (tridiagonal LU with
 //      partial pivoting) with modified Gram-Schmidt against the earlier
 //      members.
-//   4. Back-transformation U = H_0 H_1 ... H_{N-2} Z in column panels.
+//   4. Back-transformation U = H_0 H_1 ... H_{N-2} Z: in compact-WY blocks by
+//      a pass of its own (heev_bt_tiled_kernel) when the matrix was in shared
+//      memory, else reflector by reflector on column panels in the kernel.
 //
 // Output: E ascending (double), U with eigenvectors in columns (row-major).
 // Precision T = double (plain path; A stays in global memory, L2-resident)
-// or float (mixed path; A in shared memory when it fits).
+// or float (mixed path; A in shared memory when it fits: two matrices per SM
+// up to 148 bands, one up to 215).
 
 #include <cuda_runtime.h>
 
