@@ -422,7 +422,6 @@ int ozaki_fourier_max_k();
 size_t ozaki_hop_slices_bytes(int K, int64_t Nc);
 int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
                            int64_t ncols);
-bool ozaki_use_tc();
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
                   const void* Bs, float4* C, int* err);
 

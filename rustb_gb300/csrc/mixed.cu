@@ -40,7 +40,6 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                        int* err, bool exps_ready = false);
-bool ozaki_use_tc();
 size_t ozaki_exp_bytes(int64_t batch, int M, int Nc);
 int ozaki_line_exps(cudaStream_t st, int fmt, bool cols, int64_t batch, int lines, int K, const void* X, int64_t ld,
                     int64_t sX, int* E);
