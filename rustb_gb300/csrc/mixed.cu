@@ -36,7 +36,8 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
                 int64_t sC, int* EA, int* EB);
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false);
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false,
+                   int* Ecol = nullptr);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                        int* err, bool exps_ready = false);
@@ -436,14 +437,23 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
                                   slot(sb), status_d, true);
         return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB);
     };
+    // the same with the column exponents of the output into slot sc: fused into
+    // the product's epilogue when one tile holds every row (N <= 128)
+    auto hpe = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb,
+                   int sc) -> int {
+        if (tc && N <= 128)
+            return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, slot(sa),
+                                  slot(sb), status_d, true, slot(sc));
+        const int r = hp(conj_a, fa, fb, A, B, C, sa, sb);
+        return r ? r : exps(PAIR, true, C, sc);
+    };
     int rc;
     // 1. FP32 eigenpairs of H
     if ((rc = eig_batched_f32(st, N, batch, nullptr, E, X, eigw, eigw_bytes, status_d, H))) return rc;
     // 2. X^H X and S = X^H (H X)   (FP64-class, tensor cores)
     if ((rc = exps(F32, true, X, XC)) || (rc = exps(PAIR, false, H, HR))) return rc;
     if ((rc = hp(true, F32, F32, X, X, bA, XC, XC))) return rc;
-    if ((rc = hp(false, PAIR, F32, H, X, bB, HR, XC))) return rc;
-    if ((rc = exps(PAIR, true, bB, HXC))) return rc;
+    if ((rc = hpe(false, PAIR, F32, H, X, bB, HR, XC, HXC))) return rc;
     if ((rc = hp(true, F32, PAIR, X, bB, bC, XC, HXC))) return rc;
     // 3. Ogita-Aishima update F and refined eigenvalues
     {
@@ -488,9 +498,8 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     // 5. band-basis velocities B = X'^H V X'
     if ((rc = exps(PAIR, true, bA, XPC)) || (rc = exps(PAIR, false, Vx, VXR)) || (rc = exps(PAIR, false, Vy, VYR)))
         return rc;
-    if ((rc = hp(false, PAIR, PAIR, Vx, bA, bB, VXR, XPC))) return rc;
-    if ((rc = hp(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC))) return rc;
-    if ((rc = exps(PAIR, true, bB, BXC)) || (rc = exps(PAIR, true, bC, BYC))) return rc;
+    if ((rc = hpe(false, PAIR, PAIR, Vx, bA, bB, VXR, XPC, BXC))) return rc;
+    if ((rc = hpe(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC, BYC))) return rc;
     if ((rc = hp(true, PAIR, PAIR, bA, bB, bD, XPC, BXC))) return rc;
     if ((rc = hp(true, PAIR, PAIR, bA, bC, bE, XPC, BYC))) return rc;
     // 6. Omega

@@ -432,7 +432,8 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
 
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false);
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false,
+                   int* Ecol = nullptr);
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
                      const void* Bs, float4* C, int* err);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,

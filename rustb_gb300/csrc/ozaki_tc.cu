@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
                  int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
                  float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err,
-                 int accumulate) {
+                 int accumulate, int* __restrict__ Ecol) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
     constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
     constexpr int HS = S * PLANE;             // planes of one operand in a stage
@@ -604,6 +604,20 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
         }
         if (STAGE) {
             asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
+            if (ok && Ecol) {
+                // exponents of the output's columns, as the line scan would take
+                // them (one row tile holds all rows): warp w, columns w, w + 8, ...
+                for (int cl = warp; cl < TC_TN; cl += 8) {
+                    float m = 0.f;
+                    for (int rl = lane; rl < TC_TM; rl += 32) {
+                        const float4 v = tile[rl * TROW + cl];
+                        m = fmaxf(m, fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w)));
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                    if (lane == 0 && col0 + cl < Nc) Ecol[b * Nc + col0 + cl] = (m > 0.f) ? ilogbf(m) + 1 : ZERO_EXP;
+                }
+            }
             if (ok) {
                 // warp w writes rows w, w + 8, ...; lanes over the 64 columns
                 for (int rl = warp; rl < TC_TM; rl += 8) {
@@ -689,7 +703,7 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
 template <bool CJ, int FA, int FB, int S>
 static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                      const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
-                     int* err, const char* name, double work, int accumulate = 0) {
+                     int* err, const char* name, double work, int accumulate = 0, int* Ecol = nullptr) {
     auto kern = oz_tc_kernel<CJ, FA, FB, S>;
     constexpr int smem = tc_smem_bytes(S);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -702,7 +716,8 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
         const size_t eb = FB == FMT_F32 ? 8 : 16;
         kern<<<grid, TC_THREADS, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
                                                 static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
-                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err, accumulate);
+                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err, accumulate,
+                                                Ecol ? Ecol + b0 * Nc : nullptr);
         TBG_LAUNCHED(name);
     }
     return TBG_OK;
@@ -710,13 +725,18 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
 
 static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
                                 int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
-                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate);
+                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate,
+                                int* Ecol);
 
 // With exps_ready the caller has filled EA (rows of op(A)) and EB (columns of
-// B) already, e.g. once for an operand shared by several products.
+// B) already, e.g. once for an operand shared by several products.  With
+// Ecol (only for M <= 128 and K <= 256: one row tile, one launch) the
+// epilogue also writes the exponents of C's columns.
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready) {
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready, int* Ecol) {
+    if (Ecol && (M > TC_TM || K > kTcMaxK))
+        return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: fused column exponents need M <= 128 and K <= 256");
     if (!exps_ready) {
         int rc = ozaki_exp_launch(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB);
         if (rc) return rc;
@@ -731,23 +751,24 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
             const char* Ak = static_cast<const char*>(A) + (conj_a ? (int64_t)k0 * lda : (int64_t)k0) * ea;
             const char* Bk = static_cast<const char*>(B) + (int64_t)k0 * ldb * eb;
             const int rc = ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, kc, Ak, lda, sA, Bk, ldb, sB, C,
-                                                ldc, sC, EA, EB, err, k0 > 0);
+                                                ldc, sC, EA, EB, err, k0 > 0, nullptr);
             if (rc) return rc;
         }
         return TBG_OK;
     }
     return ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB,
-                                err, false);
+                                err, false, Ecol);
 }
 
 static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
                                 int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
-                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate) {
+                                float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate,
+                                int* Ecol) {
     const double work = 8.0 * (double)M * Nc * K * batch;
 #define TC_CASE(CJ, FA, FB)                                                                                          \
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
         return launch_tc<CJ, FA, FB, TC_S>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,    \
-                                           "ozaki_tc_kernel<high>", work, accumulate ? 1 : 0);
+                                           "ozaki_tc_kernel<high>", work, accumulate ? 1 : 0, Ecol);
     TC_CASE(false, FMT_F64, FMT_F64)   // unit test
     TC_CASE(true, FMT_F64, FMT_F64)    // unit test
     TC_CASE(true, FMT_F32, FMT_F32)    // X^H X
@@ -810,7 +831,8 @@ int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A,
         return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier_tc: grid too large");
     KTimer kt(st, "ozaki_tc_fourier_kernel", 8.0 * (double)M * Nc * K);
     dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
-    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0);
+    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0,
+                                            nullptr);
     TBG_LAUNCHED("ozaki_tc_fourier_kernel");
     return TBG_OK;
 }
