@@ -559,6 +559,7 @@ int tbg_model_destroy(tbg_model* m) {
     cudaFree(M.box);
     cudaFree(M.hop_slices);
     cudaFree(M.hop_EB);
+    cudaFree(M.hop_pair_d);
     M.ham = nullptr;
     delete m;
     return TBG_OK;

@@ -420,6 +420,8 @@ std::mutex g_hop_mu;
 
 int ozaki_fourier_max_k();
 size_t ozaki_hop_slices_bytes(int K, int64_t Nc);
+int ozaki_build_hop_slices_real(cudaStream_t st, int Kc, int64_t Nc, const zc* T, int* EB, void* Bs,
+                                const int* colmap, int64_t ncols);
 int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
                            int64_t ncols);
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
@@ -430,7 +432,8 @@ bool fourier_mixed_ok(const ModelDev& m) { return m.nR <= ozaki_fourier_max_k();
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
     const size_t N = (size_t)m.nsta, nR = (size_t)m.nR;
     // phases, orbital phases, exponents; the packed (upper-triangle) contraction output
-    return (size_t)nk * (3 * nR * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) + 3 * (N * (N + 1) / 2) * sizeof(float4)) +
+    return (size_t)nk * (3 * (nR + 1) * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) +
+                         3 * (N * (N + 1) / 2) * sizeof(float4)) +
            2 * nR * sizeof(double) + 2 * N * sizeof(double) + 2 * N * sizeof(float2) + 10 * 256;
 }
 
@@ -448,16 +451,119 @@ __global__ void gather_exps_kernel(int64_t n, const int* __restrict__ idx, const
         dst[i] = src[idx[i]];
 }
 
+// The table paired over +-R for real coefficients: with theta = 2 pi k . R,
+//   t(R) e^{i theta} + t(-R) e^{-i theta} = A cos(theta) + B sin(theta),
+//   A = t(R) + t(-R),  B = i (t(R) - t(-R))
+// (an R without its -R partner takes t(-R) = 0).  Rows: 0 = t(0), 1 = 0,
+// 2 + 2p = A_p, 3 + 2p = B_p.  pi[p] is the pair's R, pj[p] its -R or -1.
+__global__ void pair_table_kernel(int np, const int* __restrict__ pi, const int* __restrict__ pj, int z, int64_t NN,
+                                  const zc* __restrict__ ham, zc* __restrict__ T) {
+    const int64_t total = (int64_t)(np + 1) * NN;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = idx / NN - 1, e = idx % NN;
+        if (p < 0) {
+            T[e] = (z >= 0) ? ham[(int64_t)z * NN + e] : mk(0.0, 0.0);
+            T[NN + e] = mk(0.0, 0.0);
+        } else {
+            const zc a = ham[(int64_t)pi[p] * NN + e];
+            const zc b = (pj[p] >= 0) ? ham[(int64_t)pj[p] * NN + e] : mk(0.0, 0.0);
+            T[(2 + 2 * p) * NN + e] = mk(a.re + b.re, a.im + b.im);
+            T[(3 + 2 * p) * NN + e] = mk(-(a.im - b.im), a.re - b.re);
+        }
+    }
+}
+
+// Real coefficients of the paired table, as complex numbers whose real and
+// imaginary parts are consecutive rows (Phi (3, nk, Kc), Kc = 1 + np): H row
+// (1, 0 | cos, sin ...), V_p rows (0, 0 | -c_p(R) sin, c_p(R) cos ...), from
+//   i c_p(R) (t(R) e^{i theta} - t(-R) e^{-i theta}) = c_p(R) (B cos - A sin).
+__global__ void phases_real_kernel(int64_t nk, int dim, const double* __restrict__ k, int np,
+                                   const int* __restrict__ pair, const int* __restrict__ hamR, int nR,
+                                   const double* __restrict__ coef, zc* __restrict__ Phi) {
+    const int Kc = np + 1;
+    const int64_t total = nk * (int64_t)Kc;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / Kc;
+        const int c = (int)(idx % Kc);
+        zc h = mk(1.0, 0.0), vx = mk(0.0, 0.0), vy = mk(0.0, 0.0);
+        if (c > 0) {
+            const int j = pair[c - 1];
+            const int* r = hamR + 3 * j;
+            const double* kv = k + kk * dim;
+            // same operation order as the reference: r0*k0 + r1*k1 + r2*k2
+            double s = (double)r[0] * kv[0];
+            if (dim > 1) s += (double)r[1] * kv[1];
+            if (dim > 2) s += (double)r[2] * kv[2];
+            double sn, cs;
+            sincos(kTwoPi * s, &sn, &cs);
+            const double c0 = coef[j], c1 = coef[nR + j];
+            h = mk(cs, sn);
+            vx = mk(-c0 * sn, c0 * cs);
+            vy = mk(-c1 * sn, c1 * cs);
+        }
+        Phi[idx] = h;
+        Phi[total + idx] = vx;
+        Phi[2 * total + idx] = vy;
+    }
+}
+
 int build_hop_table(ModelDev& m, cudaStream_t st) {
     const int N = (int)m.nsta, nR = (int)m.nR;
     const int64_t NN = (int64_t)N * N, NP = (int64_t)N * (N + 1) / 2;
     const bool packed = ozaki_use_tc();
     const int64_t ncols = packed ? NP : NN;
+    // +-R pairs (tcgen05 form)
+    int z = -1;
+    std::vector<int> pi, pj;
+    if (packed) {
+        std::vector<char> used((size_t)nR, 0);
+        auto rvec = [&](int i, int d) { return d < m.dim ? m.hamR[(size_t)i * m.dim + d] : 0; };
+        for (int i = 0; i < nR; ++i) {
+            if (used[i]) continue;
+            used[i] = 1;
+            if (rvec(i, 0) == 0 && rvec(i, 1) == 0 && rvec(i, 2) == 0) {
+                z = i;
+                continue;
+            }
+            int partner = -1;
+            for (int j = i + 1; j < nR && partner < 0; ++j)
+                if (!used[j] && rvec(j, 0) == -rvec(i, 0) && rvec(j, 1) == -rvec(i, 1) && rvec(j, 2) == -rvec(i, 2))
+                    partner = j;
+            if (partner >= 0) used[partner] = 1;
+            pi.push_back(i);
+            pj.push_back(partner);
+        }
+    }
+    const int np = (int)pi.size(), Kc = packed ? np + 1 : nR;
     void* bs = nullptr;
-    int *eb_full = nullptr, *eb = nullptr, *colmap = nullptr;
+    int *eb_full = nullptr, *eb = nullptr, *colmap = nullptr, *pair_d = nullptr, *pj_d = nullptr;
+    zc* T = nullptr;
     int rc = TBG_OK;
-    if (cudaMalloc(&bs, ozaki_hop_slices_bytes(nR, ncols)) != cudaSuccess ||
-        cudaMalloc(&eb_full, sizeof(int) * NN) != cudaSuccess ||
+    if (packed && (cudaMalloc(&T, sizeof(zc) * 2 * (size_t)Kc * NN) != cudaSuccess ||
+                   cudaMalloc(&pair_d, sizeof(int) * std::max(np, 1)) != cudaSuccess ||
+                   cudaMalloc(&pj_d, sizeof(int) * std::max(np, 1)) != cudaSuccess))
+        rc = set_error(TBG_E_OOM, "paired hop table");
+    if (!rc && packed && np > 0 &&
+        (cudaMemcpy(pair_d, pi.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy(pj_d, pj.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess))
+        rc = set_error(TBG_E_CUDA, "paired hop table indices");
+    if (!rc && packed) {
+        pair_table_kernel<<<(unsigned)std::min<int64_t>(((int64_t)Kc * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
+            np, pair_d, pj_d, z, NN, m.ham, T);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_error(e, "paired hop table");
+    }
+    if (!rc && cudaMalloc(&bs, ozaki_hop_slices_bytes(Kc, ncols)) != cudaSuccess) rc = set_error(TBG_E_OOM, "hop table digit planes");
+    if (rc) {
+        cudaFree(T);
+        cudaFree(pair_d);
+        cudaFree(pj_d);
+        return rc;
+    }
+    if (cudaMalloc(&eb_full, sizeof(int) * NN) != cudaSuccess ||
         (packed && (cudaMalloc(&eb, sizeof(int) * NP) != cudaSuccess ||
                     cudaMalloc(&colmap, sizeof(int) * NP) != cudaSuccess)))
         rc = set_error(TBG_E_OOM, "hop table digit planes");
@@ -468,7 +574,9 @@ int build_hop_table(ModelDev& m, cudaStream_t st) {
         if (cudaMemcpy(colmap, cm.data(), sizeof(int) * NP, cudaMemcpyHostToDevice) != cudaSuccess)
             rc = set_error(TBG_E_CUDA, "hop table column map");
     }
-    if (!rc) rc = ozaki_build_hop_slices(st, nR, NN, m.ham, eb_full, bs, packed ? colmap : nullptr, ncols);
+    if (!rc)
+        rc = packed ? ozaki_build_hop_slices_real(st, Kc, NN, T, eb_full, bs, colmap, ncols)
+                    : ozaki_build_hop_slices(st, nR, NN, m.ham, eb_full, bs, nullptr, ncols);
     if (!rc && packed) {
         gather_exps_kernel<<<(unsigned)std::min<int64_t>((NP + 255) / 256, 1024), 256, 0, st>>>(NP, colmap, eb_full,
                                                                                                   eb);
@@ -480,16 +588,23 @@ int build_hop_table(ModelDev& m, cudaStream_t st) {
         if (e != cudaSuccess) rc = cuda_error(e, "hop table digit planes");
     }
     cudaFree(colmap);
+    cudaFree(T);
+    cudaFree(pj_d);
     if (rc) {
         cudaFree(bs);
         cudaFree(eb_full);
         cudaFree(eb);
+        cudaFree(pair_d);
         return rc;
     }
     if (packed) cudaFree(eb_full);
     m.hop_slices = bs;
     m.hop_EB = packed ? eb : eb_full;
     m.hop_packed = packed;
+    m.hop_K = Kc;
+    m.hop_np = np;
+    m.hop_pair_d = packed ? pair_d : nullptr;
+    if (!packed) cudaFree(pair_d);
     return TBG_OK;
 }
 
@@ -510,7 +625,7 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
         p += (bytes + 255) & ~size_t(255);
         return q;
     };
-    zc* ph3 = static_cast<zc*>(take(sizeof(zc) * 3 * nk * nR));
+    zc* ph3 = static_cast<zc*>(take(sizeof(zc) * 3 * nk * (nR + 1)));  // Phi (3 nk x hop_K <= nR + 1) when packed
     zc* orbph = static_cast<zc*>(take(sizeof(zc) * nk * N));
     double* coef = static_cast<double*>(take(sizeof(double) * 2 * nR));
     double* taup = static_cast<double*>(take(sizeof(double) * 2 * N));
@@ -524,12 +639,22 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
         const int total = 2 * (nR + N);
         proj_coef_kernel<<<(total + 255) / 256, 256, 0, st>>>(2, m.dim, dirs_d, nR, m.Rcart_d, N, m.taucart_d, coef,
                                                               taup);
-        const int64_t t1 = nk * (int64_t)(nR + N);
-        phases_kernel<<<(unsigned)std::min<int64_t>((t1 + 255) / 256, 65535 * 8), 256, 0, st>>>(
-            nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph3, orbph);  // ph3[0 .. nk*nR) reused below
-        const int64_t t2 = nk * (int64_t)nR;
-        phases3_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
-            nk, m.dim, k_d, nR, m.hamR_d, coef, ph3);
+        if (m.hop_packed) {
+            // orbital phases only, then the real coefficients of the paired table
+            const int64_t t1 = nk * (int64_t)N;
+            phases_kernel<<<(unsigned)std::min<int64_t>((t1 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+                nk, m.dim, k_d, 0, m.hamR_d, N, m.tau_d, ph3, orbph);
+            const int64_t t2 = nk * (int64_t)m.hop_K;
+            phases_real_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+                nk, m.dim, k_d, m.hop_np, m.hop_pair_d, m.hamR_d, nR, coef, ph3);
+        } else {
+            const int64_t t1 = nk * (int64_t)(nR + N);
+            phases_kernel<<<(unsigned)std::min<int64_t>((t1 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+                nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph3, orbph);  // ph3[0 .. nk*nR) reused below
+            const int64_t t2 = nk * (int64_t)nR;
+            phases3_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+                nk, m.dim, k_d, nR, m.hamR_d, coef, ph3);
+        }
         tau_split_kernel<<<(2 * N + 255) / 256, 256, 0, st>>>(2 * N, taup, tau2);
         count_launch(4);
         cudaError_t e = cudaGetLastError();
@@ -537,7 +662,8 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     }
     int rc = cudaMemsetAsync(err, 0, sizeof(int), st) == cudaSuccess ? TBG_OK : set_error(TBG_E_CUDA, "memset");
     if (rc) return rc;
-    rc = ozaki_fourier(st, 3 * nk, m.hop_packed ? NP : NN, nR, ph3, EA, m.hop_EB, m.hop_slices, Cg, err);
+    rc = ozaki_fourier(st, 3 * nk, m.hop_packed ? NP : NN, m.hop_packed ? m.hop_K : nR, ph3, EA, m.hop_EB,
+                       m.hop_slices, Cg, err);
     if (rc) return rc;
     *Cg_out = Cg;
     *orbph_out = orbph;

@@ -537,6 +537,19 @@ int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, in
     return TBG_OK;
 }
 
+int ozaki_hop_image_real_launch(cudaStream_t st, int Kc, int64_t Nc, const zc* T, const int* EB, void* img,
+                                const int* colmap, int64_t ldh);
+// Stage images of a table T with 2 Kc rows contracted against real
+// coefficients (tcgen05 form only); EB over all 2 Kc rows of each element.
+int ozaki_build_hop_slices_real(cudaStream_t st, int Kc, int64_t Nc, const zc* T, int* EB, void* Bs,
+                                const int* colmap, int64_t ncols) {
+    if (!ozaki_use_tc()) return set_error(TBG_E_UNSUPPORTED, "real-coefficient hop images need the tcgen05 kernels");
+    KTimer kt(st, "hop_slice_kernel");
+    hop_exp_kernel<<<(unsigned)std::min<int64_t>((Nc * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(2 * Kc, Nc, T, EB);
+    TBG_LAUNCHED("hop_exp_kernel");
+    return ozaki_hop_image_real_launch(st, Kc, colmap ? ncols : Nc, T, EB, Bs, colmap, Nc);
+}
+
 // C (M x Nc, float pairs) = A (M x K, complex double) . hop (digit planes).
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
                   const void* Bs, float4* C, int* err) {

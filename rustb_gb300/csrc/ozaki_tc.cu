@@ -694,6 +694,52 @@ __global__ void hop_image_kernel(int K, int64_t Nc, const zc* __restrict__ ham, 
     }
 }
 
+// Stage images for a contraction with real coefficients: A' = Phi as complex
+// numbers whose real and imaginary parts are consecutive coefficients
+// (A'_kappa = Phi_{2 kappa} + i Phi_{2 kappa + 1}), B = table T with 2 Kc rows.
+// With B rows j = [Re T_{2 kappa} | Re T_{2 kappa + 1}] and 64 + j =
+// [Im T_{2 kappa} | Im T_{2 kappa + 1}] over the stage's 16 + 16 k slots, the
+// unchanged kernel yields column j = Re(sum_k Phi_k T_k), 64 + j = its
+// imaginary part: half the stages of the complex-coefficient form.
+__global__ void hop_image_real_kernel(int Kc, int64_t Nc, const zc* __restrict__ T, const int* __restrict__ EB,
+                                      unsigned char* __restrict__ img, const int* __restrict__ colmap, int64_t ldh) {
+    const int nst = (Kc + TC_TK - 1) / TC_TK;
+    const int64_t nct = (Nc + TC_TN - 1) / TC_TN;
+    const int64_t total = nct * nst * B_PRODUCERS;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(idx % B_PRODUCERS);
+        const int64_t blk = idx / B_PRODUCERS;  // ct * nst + it
+        const int it = (int)(blk % nst);
+        const int64_t ct = blk / nst;
+        const int j = q & 63, g = q >> 6;
+        const int64_t gj = ct * TC_TN + j;
+        const bool cv = gj < Nc;
+        const int64_t el = cv ? (colmap ? (int64_t)colmap[gj] : gj) : 0;
+        const int E = cv ? EB[el] : ZERO_EXP;
+        const int kf = it * TC_TK + 8 * g;  // first kappa of this thread
+        const int nv = cv ? n_valid(Kc, kf) : 0;
+        int4 re[8], ro[8];                   // rows 2 kappa and 2 kappa + 1
+        load8<FMT_F64>(T, (int64_t)(2 * kf) * ldh + el, 2 * ldh, nv, re);
+        load8<FMT_F64>(T, (int64_t)(2 * kf + 1) * ldh + el, 2 * ldh, nv, ro);
+        unsigned char* dst = img + blk * HALF_STAGE;
+        uint4 d[TC_S];
+        item_planes<FMT_F64, 0, TC_S>(re, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(j, 8 * g)) = d[s];
+        item_planes<FMT_F64, 0, TC_S>(ro, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(j, 16 + 8 * g)) = d[s];
+        item_planes<FMT_F64, 1, TC_S>(re, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s) *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 8 * g)) = d[s];
+        item_planes<FMT_F64, 1, TC_S>(ro, E, 0.f, 0.f, d);
+#pragma unroll
+        for (int s = 0; s < TC_S; ++s)
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(64 + j, 16 + 8 * g)) = d[s];
+    }
+}
+
 }  // namespace
 
 int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
@@ -816,6 +862,17 @@ int ozaki_hop_image_launch(cudaStream_t st, int K, int64_t Nc, const zc* ham, co
     hop_image_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
         K, Nc, ham, EB, static_cast<unsigned char*>(img), colmap, ldh);
     TBG_LAUNCHED("hop_image_kernel");
+    return TBG_OK;
+}
+
+// Stage images of a real-coefficient table (2 Kc rows; hop_image_real_kernel).
+int ozaki_hop_image_real_launch(cudaStream_t st, int Kc, int64_t Nc, const zc* T, const int* EB, void* img,
+                                const int* colmap, int64_t ldh) {
+    const int64_t nst = (Kc + TC_TK - 1) / TC_TK, nct = (Nc + TC_TN - 1) / TC_TN;
+    const int64_t total = nct * nst * B_PRODUCERS;
+    hop_image_real_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(
+        Kc, Nc, T, EB, static_cast<unsigned char*>(img), colmap, ldh);
+    TBG_LAUNCHED("hop_image_real_kernel");
     return TBG_OK;
 }
 

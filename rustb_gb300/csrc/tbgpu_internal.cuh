@@ -135,6 +135,11 @@ struct ModelDev {
     void* hop_slices = nullptr;
     int* hop_EB = nullptr;         // per contraction column
     bool hop_packed = false;       // columns = upper-triangle elements (m <= n) only
+    // tcgen05 form: the table is paired over +-R and contracted against real
+    // coefficients (cos, sin): hop_K = 1 + hop_np complex contraction steps,
+    // hop_pair_d (hop_np) = the index of each pair's R in hamR
+    int hop_K = 0, hop_np = 0;
+    int* hop_pair_d = nullptr;
 };
 
 // ------------------------------------------------------------------ errors --
