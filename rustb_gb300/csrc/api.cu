@@ -560,6 +560,7 @@ int tbg_model_destroy(tbg_model* m) {
     cudaFree(M.hop_slices);
     cudaFree(M.hop_EB);
     cudaFree(M.hop_pair_d);
+    cudaFree(M.pair_T);
     M.ham = nullptr;
     delete m;
     return TBG_OK;

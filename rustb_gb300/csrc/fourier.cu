@@ -219,6 +219,177 @@ int dispatch_gemm(cudaStream_t st, int np, int64_t nk, int nR, int ldph, int N, 
     }
 }
 
+// Fourier sums from the +-R paired table (FP64; rows 2q, 2q + 1 of T are A_q,
+// B_q, pair 0 is R = 0 with A_0 = t(0), B_0 = 0): with (c, s) = (cos, sin) of
+// 2 pi k . R_q,
+//   H += c A_q + s B_q,   V_p += c_p(R_q) (c B_q - s A_q)   (c_p(R_0) = 0),
+// 8 + 2 NP FMAs per pair and element for two R (10 + 2 NP per R unpaired).
+// Same tiling and epilogue as fourier_gemm_kernel; the velocity accumulators
+// already hold V_p (no factor i).
+template <int NP>
+__global__ void __launch_bounds__(256) fourier_pair_kernel(
+    int64_t nk, int Kc, int N, const zc* __restrict__ cs, const zc* __restrict__ T, const int* __restrict__ pair,
+    int nR, const double* __restrict__ coef, const zc* __restrict__ orbph, const double* __restrict__ taup,
+    int gauge, zc* __restrict__ H, int64_t ldH, zc* __restrict__ V, int64_t ldV) {
+    __shared__ zc s_A[RC][TE], s_B[RC][TE];
+    __shared__ zc s_cs[RC][TK];
+    __shared__ double s_coef[NP > 0 ? NP : 1][RC];
+    const int tid = threadIdx.x;
+    const int te = tid & 15;  // element lane: e = te + 16 j
+    const int tk = tid >> 4;  // k lane: k = tk + 16 i
+    const int64_t NN = (int64_t)N * N;
+    const int64_t e0 = (int64_t)blockIdx.x * TE;
+    const int64_t k0 = (int64_t)blockIdx.y * TK;
+
+    zc accH[2][4];
+    zc accV[NP > 0 ? NP : 1][2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            accH[i][j] = mk(0.0, 0.0);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) accV[p][i][j] = mk(0.0, 0.0);
+        }
+
+    for (int q0 = 0; q0 < Kc; q0 += RC) {
+        for (int idx = tid; idx < RC * TE; idx += 256) {
+            const int r = idx / TE, e = idx % TE;
+            zc a = mk(0.0, 0.0), b = mk(0.0, 0.0);
+            if (q0 + r < Kc && e0 + e < NN) {
+                a = T[(int64_t)(2 * (q0 + r)) * NN + e0 + e];
+                b = T[(int64_t)(2 * (q0 + r) + 1) * NN + e0 + e];
+            }
+            s_A[r][e] = a;
+            s_B[r][e] = b;
+        }
+        {
+            const int r = tid / TK, kk = tid % TK;  // 256 == RC*TK
+            zc u = mk(0.0, 0.0);
+            if (q0 + r < Kc && k0 + kk < nk) u = cs[(k0 + kk) * Kc + q0 + r];
+            s_cs[r][kk] = u;
+        }
+        if (NP > 0 && tid < NP * RC) {
+            const int p = tid / RC, r = tid % RC, q = q0 + r;
+            s_coef[p][r] = (q > 0 && q < Kc) ? coef[(int64_t)p * nR + pair[q - 1]] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {
+            zc a[4], b[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                a[j] = s_A[r][te + 16 * j];
+                b[j] = s_B[r][te + 16 * j];
+            }
+            double cp[NP > 0 ? NP : 1];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) cp[p] = s_coef[p][r];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const zc u = s_cs[r][tk + 16 * i];  // (cos, sin)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    accH[i][j].re = fma(u.re, a[j].re, accH[i][j].re);
+                    accH[i][j].re = fma(u.im, b[j].re, accH[i][j].re);
+                    accH[i][j].im = fma(u.re, a[j].im, accH[i][j].im);
+                    accH[i][j].im = fma(u.im, b[j].im, accH[i][j].im);
+                    if (NP > 0) {
+                        const double wr = fma(u.re, b[j].re, -u.im * a[j].re);
+                        const double wi = fma(u.re, b[j].im, -u.im * a[j].im);
+#pragma unroll
+                        for (int p = 0; p < NP; ++p) {
+                            accV[p][i][j].re = fma(cp[p], wr, accV[p][i][j].re);
+                            accV[p][i][j].im = fma(cp[p], wi, accV[p][i][j].im);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int64_t kk = k0 + tk + 16 * i;
+        if (kk >= nk) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t e = e0 + te + 16 * j;
+            if (e >= NN) continue;
+            const int mrow = (int)(e / N), ncol = (int)(e % N);
+            const zc hl = accH[i][j];
+            zc g = mk(1.0, 0.0);
+            if (gauge == TBG_GAUGE_ATOM) g = cmul(orbph[kk * N + mrow], orbph[kk * N + ncol]);
+            if (H) H[kk * ldH + e] = hl * g;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                zc v = accV[p][i][j];
+                if (gauge == TBG_GAUGE_ATOM) {
+                    const double diff = taup[p * N + ncol] - taup[p * N + mrow];
+                    v.re -= diff * hl.im;
+                    v.im += diff * hl.re;
+                    v = v * g;
+                }
+                V[kk * ldV + p * NN + e] = v;
+            }
+        }
+    }
+}
+
+// (cos, sin) of 2 pi k . R_q per k-point and pair (pair 0: R = 0), from the
+// same operation order as phases_kernel.
+__global__ void phases_pair_kernel(int64_t nk, int dim, const double* __restrict__ k, int np,
+                                   const int* __restrict__ pair, const int* __restrict__ hamR, zc* __restrict__ cs) {
+    const int Kc = np + 1;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < nk * Kc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kk = idx / Kc;
+        const int q = (int)(idx % Kc);
+        if (q == 0) {
+            cs[idx] = mk(1.0, 0.0);
+            continue;
+        }
+        const int* r = hamR + 3 * pair[q - 1];
+        const double* kv = k + kk * dim;
+        double s = (double)r[0] * kv[0];
+        if (dim > 1) s += (double)r[1] * kv[1];
+        if (dim > 2) s += (double)r[2] * kv[2];
+        double sn, c;
+        sincos(kTwoPi * s, &sn, &c);
+        cs[idx] = mk(c, sn);
+    }
+}
+
+template <int NP>
+int launch_pair(cudaStream_t st, int64_t nk, int Kc, int N, const zc* cs, const zc* T, const int* pair, int nR,
+                const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH, zc* V,
+                int64_t ldV) {
+    const int64_t NN = (int64_t)N * N;
+    // algorithmic work as for the unpaired sum (8 nR N^2 per output matrix)
+    KTimer kt(st, "fourier_gemm_kernel", 8.0 * nR * (double)NN * nk * ((H ? 1 : 0) + NP));
+    for (int64_t kb = 0; kb < nk; kb += (int64_t)TK * 65535) {
+        const int64_t nkb = std::min<int64_t>(nk - kb, (int64_t)TK * 65535);
+        dim3 grid((unsigned)((NN + TE - 1) / TE), (unsigned)((nkb + TK - 1) / TK));
+        fourier_pair_kernel<NP><<<grid, 256, 0, st>>>(nkb, Kc, N, cs + kb * Kc, T, pair, nR, coef, orbph + kb * N,
+                                                        taup, gauge, H ? H + kb * ldH : nullptr, ldH,
+                                                        V ? V + kb * ldV : nullptr, ldV);
+        TBG_LAUNCHED("fourier_pair_kernel");
+    }
+    return TBG_OK;
+}
+
+int dispatch_pair(cudaStream_t st, int np, int64_t nk, int Kc, int N, const zc* cs, const zc* T, const int* pair,
+                  int nR, const double* coef, const zc* orbph, const double* taup, int gauge, zc* H, int64_t ldH,
+                  zc* V, int64_t ldV) {
+    switch (np) {
+        case 0: return launch_pair<0>(st, nk, Kc, N, cs, T, pair, nR, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        case 1: return launch_pair<1>(st, nk, Kc, N, cs, T, pair, nR, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        case 2: return launch_pair<2>(st, nk, Kc, N, cs, T, pair, nR, coef, orbph, taup, gauge, H, ldH, V, ldV);
+        default: return launch_pair<3>(st, nk, Kc, N, cs, T, pair, nR, coef, orbph, taup, gauge, H, ldH, V, ldV);
+    }
+}
+
 // Gauge transform + zeroed diagonal of the rmatrix Fourier sum (Atom gauge),
 // velocity.rs:646-656.
 __global__ void rmat_gauge_kernel(int64_t nk, int N, const zc* __restrict__ orbph, zc* __restrict__ A) {
@@ -509,60 +680,78 @@ __global__ void phases_real_kernel(int64_t nk, int dim, const double* __restrict
     }
 }
 
+// The +-R paired table (pair_table_kernel) and the index of each pair's R,
+// built once per model for both Fourier forms; the caller holds g_hop_mu.
+int ensure_pair_table(ModelDev& m, cudaStream_t st) {
+    if (m.pair_T) return TBG_OK;
+    const int nR = (int)m.nR;
+    const int64_t NN = (int64_t)m.nsta * m.nsta;
+    int z = -1;
+    std::vector<int> pi, pj;
+    std::vector<char> used((size_t)nR, 0);
+    auto rvec = [&](int i, int d) { return d < m.dim ? m.hamR[(size_t)i * m.dim + d] : (int64_t)0; };
+    for (int i = 0; i < nR; ++i) {
+        if (used[i]) continue;
+        used[i] = 1;
+        if (rvec(i, 0) == 0 && rvec(i, 1) == 0 && rvec(i, 2) == 0) {
+            z = i;
+            continue;
+        }
+        int partner = -1;
+        for (int j = i + 1; j < nR && partner < 0; ++j)
+            if (!used[j] && rvec(j, 0) == -rvec(i, 0) && rvec(j, 1) == -rvec(i, 1) && rvec(j, 2) == -rvec(i, 2))
+                partner = j;
+        if (partner >= 0) used[partner] = 1;
+        pi.push_back(i);
+        pj.push_back(partner);
+    }
+    const int np = (int)pi.size(), Kc = np + 1;
+    int *pair_d = nullptr, *pj_d = nullptr;
+    zc* T = nullptr;
+    int rc = TBG_OK;
+    if (cudaMalloc(&T, sizeof(zc) * 2 * (size_t)Kc * NN) != cudaSuccess ||
+        cudaMalloc(&pair_d, sizeof(int) * std::max(np, 1)) != cudaSuccess ||
+        cudaMalloc(&pj_d, sizeof(int) * std::max(np, 1)) != cudaSuccess)
+        rc = set_error(TBG_E_OOM, "paired hop table");
+    if (!rc && np > 0 &&
+        (cudaMemcpy(pair_d, pi.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy(pj_d, pj.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess))
+        rc = set_error(TBG_E_CUDA, "paired hop table indices");
+    if (!rc) {
+        pair_table_kernel<<<(unsigned)std::min<int64_t>(((int64_t)Kc * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
+            np, pair_d, pj_d, z, NN, m.ham, T);
+        count_launch();
+        cudaError_t e = cudaStreamSynchronize(st);  // other streams use the table next
+        if (e != cudaSuccess) rc = cuda_error(e, "paired hop table");
+    }
+    cudaFree(pj_d);
+    if (rc) {
+        cudaFree(T);
+        cudaFree(pair_d);
+        return rc;
+    }
+    m.pair_T = T;
+    m.hop_pair_d = pair_d;
+    m.hop_np = np;
+    m.hop_K = Kc;
+    return TBG_OK;
+}
+
 int build_hop_table(ModelDev& m, cudaStream_t st) {
     const int N = (int)m.nsta, nR = (int)m.nR;
     const int64_t NN = (int64_t)N * N, NP = (int64_t)N * (N + 1) / 2;
     const bool packed = ozaki_use_tc();
     const int64_t ncols = packed ? NP : NN;
-    // +-R pairs (tcgen05 form)
-    int z = -1;
-    std::vector<int> pi, pj;
     if (packed) {
-        std::vector<char> used((size_t)nR, 0);
-        auto rvec = [&](int i, int d) { return d < m.dim ? m.hamR[(size_t)i * m.dim + d] : 0; };
-        for (int i = 0; i < nR; ++i) {
-            if (used[i]) continue;
-            used[i] = 1;
-            if (rvec(i, 0) == 0 && rvec(i, 1) == 0 && rvec(i, 2) == 0) {
-                z = i;
-                continue;
-            }
-            int partner = -1;
-            for (int j = i + 1; j < nR && partner < 0; ++j)
-                if (!used[j] && rvec(j, 0) == -rvec(i, 0) && rvec(j, 1) == -rvec(i, 1) && rvec(j, 2) == -rvec(i, 2))
-                    partner = j;
-            if (partner >= 0) used[partner] = 1;
-            pi.push_back(i);
-            pj.push_back(partner);
-        }
+        int rc = ensure_pair_table(m, st);
+        if (rc) return rc;
     }
-    const int np = (int)pi.size(), Kc = packed ? np + 1 : nR;
+    const int Kc = packed ? m.hop_K : nR;
+    const zc* T = m.pair_T;
     void* bs = nullptr;
-    int *eb_full = nullptr, *eb = nullptr, *colmap = nullptr, *pair_d = nullptr, *pj_d = nullptr;
-    zc* T = nullptr;
+    int *eb_full = nullptr, *eb = nullptr, *colmap = nullptr;
     int rc = TBG_OK;
-    if (packed && (cudaMalloc(&T, sizeof(zc) * 2 * (size_t)Kc * NN) != cudaSuccess ||
-                   cudaMalloc(&pair_d, sizeof(int) * std::max(np, 1)) != cudaSuccess ||
-                   cudaMalloc(&pj_d, sizeof(int) * std::max(np, 1)) != cudaSuccess))
-        rc = set_error(TBG_E_OOM, "paired hop table");
-    if (!rc && packed && np > 0 &&
-        (cudaMemcpy(pair_d, pi.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess ||
-         cudaMemcpy(pj_d, pj.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess))
-        rc = set_error(TBG_E_CUDA, "paired hop table indices");
-    if (!rc && packed) {
-        pair_table_kernel<<<(unsigned)std::min<int64_t>(((int64_t)Kc * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
-            np, pair_d, pj_d, z, NN, m.ham, T);
-        count_launch();
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) rc = cuda_error(e, "paired hop table");
-    }
-    if (!rc && cudaMalloc(&bs, ozaki_hop_slices_bytes(Kc, ncols)) != cudaSuccess) rc = set_error(TBG_E_OOM, "hop table digit planes");
-    if (rc) {
-        cudaFree(T);
-        cudaFree(pair_d);
-        cudaFree(pj_d);
-        return rc;
-    }
+    if (cudaMalloc(&bs, ozaki_hop_slices_bytes(Kc, ncols)) != cudaSuccess) return set_error(TBG_E_OOM, "hop table digit planes");
     if (cudaMalloc(&eb_full, sizeof(int) * NN) != cudaSuccess ||
         (packed && (cudaMalloc(&eb, sizeof(int) * NP) != cudaSuccess ||
                     cudaMalloc(&colmap, sizeof(int) * NP) != cudaSuccess)))
@@ -588,23 +777,16 @@ int build_hop_table(ModelDev& m, cudaStream_t st) {
         if (e != cudaSuccess) rc = cuda_error(e, "hop table digit planes");
     }
     cudaFree(colmap);
-    cudaFree(T);
-    cudaFree(pj_d);
     if (rc) {
         cudaFree(bs);
         cudaFree(eb_full);
         cudaFree(eb);
-        cudaFree(pair_d);
         return rc;
     }
     if (packed) cudaFree(eb_full);
     m.hop_slices = bs;
     m.hop_EB = packed ? eb : eb_full;
     m.hop_packed = packed;
-    m.hop_K = Kc;
-    m.hop_np = np;
-    m.hop_pair_d = packed ? pair_d : nullptr;
-    if (!packed) cudaFree(pair_d);
     return TBG_OK;
 }
 
@@ -723,9 +905,16 @@ int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double*
                    const double* dirs_d, zc* H, zc* V, int64_t ldH, int64_t ldV) {
     if (nk <= 0) return TBG_OK;
     const int N = (int)m.nsta, nR = (int)m.nR;
-    zc *ph = nullptr, *orbph = nullptr;
+    {
+        // the +-R paired table, built once per model (a cache: logically const)
+        std::lock_guard<std::mutex> lk(g_hop_mu);
+        int rc = ensure_pair_table(const_cast<ModelDev&>(m), st);
+        if (rc) return rc;
+    }
+    const int Kc = m.hop_K;
+    zc *cs = nullptr, *orbph = nullptr;
     double *coef = nullptr, *taup = nullptr;
-    TBG_CUDA(cudaMallocAsync(&ph, sizeof(zc) * nk * nR, st));
+    TBG_CUDA(cudaMallocAsync(&cs, sizeof(zc) * nk * Kc, st));
     TBG_CUDA(cudaMallocAsync(&orbph, sizeof(zc) * nk * N, st));
     const int npc = std::max(nproj, 1);
     TBG_CUDA(cudaMallocAsync(&coef, sizeof(double) * npc * nR, st));
@@ -733,10 +922,13 @@ int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double*
     int rc = TBG_OK;
     {
         KTimer kt(st, "phases_kernel");
-        const int64_t total = nk * (int64_t)(nR + N);
-        const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 65535 * 8);
-        phases_kernel<<<blocks, 256, 0, st>>>(nk, m.dim, k_d, nR, m.hamR_d, N, m.tau_d, ph, orbph);
-        count_launch();
+        const int64_t t1 = nk * (int64_t)N;  // orbital phases only
+        phases_kernel<<<(unsigned)std::min<int64_t>((t1 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+            nk, m.dim, k_d, 0, m.hamR_d, N, m.tau_d, cs, orbph);
+        const int64_t t2 = nk * (int64_t)Kc;
+        phases_pair_kernel<<<(unsigned)std::min<int64_t>((t2 + 255) / 256, 65535 * 8), 256, 0, st>>>(
+            nk, m.dim, k_d, m.hop_np, m.hop_pair_d, m.hamR_d, cs);
+        count_launch(2);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = cuda_error(e, "phases_kernel");
     }
@@ -753,11 +945,11 @@ int fourier_direct(const ModelDev& m, cudaStream_t st, int64_t nk, const double*
         const int np = std::min(3, std::max(0, nproj - p0));
         zc* Hout = (p0 == 0) ? H : nullptr;
         if (!Hout && np == 0) break;
-        rc = dispatch_gemm(st, np, nk, nR, nR, N, ph, m.ham, coef + (int64_t)p0 * nR, orbph,
+        rc = dispatch_pair(st, np, nk, Kc, N, cs, m.pair_T, m.hop_pair_d, nR, coef + (int64_t)p0 * nR, orbph,
                            taup + (int64_t)p0 * N, gauge, Hout, ldH, V ? V + (int64_t)p0 * N * N : nullptr, ldV);
         if (nproj == 0) break;
     }
-    cudaFreeAsync(ph, st);
+    cudaFreeAsync(cs, st);
     cudaFreeAsync(orbph, st);
     cudaFreeAsync(coef, st);
     cudaFreeAsync(taup, st);

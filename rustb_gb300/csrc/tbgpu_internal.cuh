@@ -140,6 +140,7 @@ struct ModelDev {
     // hop_pair_d (hop_np) = the index of each pair's R in hamR
     int hop_K = 0, hop_np = 0;
     int* hop_pair_d = nullptr;
+    zc* pair_T = nullptr;          // the paired table (2 hop_K rows, nsta^2 columns)
 };
 
 // ------------------------------------------------------------------ errors --
