@@ -693,8 +693,8 @@ int ensure_pair_table(ModelDev& m, cudaStream_t st) {
     for (int i = 0; i < nR; ++i) {
         if (used[i]) continue;
         used[i] = 1;
-        if (rvec(i, 0) == 0 && rvec(i, 1) == 0 && rvec(i, 2) == 0) {
-            z = i;
+        if (rvec(i, 0) == 0 && rvec(i, 1) == 0 && rvec(i, 2) == 0 && z < 0) {
+            z = i;  // a repeated R = 0 entry is paired below as a singleton (theta = 0)
             continue;
         }
         int partner = -1;
