@@ -72,6 +72,46 @@ def test_gen_v_cfg2_size_matches_oracle():
     assert rel(H, Hr) < 1e-12 and rel(V, Vr) < 1e-12
 
 
+def test_fourier_sums_with_repeated_and_unpaired_R():
+    """The +-R paired table: a repeated R = 0 block and a repeated R give the same
+    sums as the oracle; an R whose -R is missing is refused when the model is
+    uploaded, as the reference's hopping check refuses it."""
+    m = W.random_model(2, 6, False, 1, seed=77)
+    ham, hamR = m.ham.copy(), m.hamR.copy()
+    i0 = int(np.flatnonzero(np.all(hamR == 0, axis=1))[0])
+    i1 = int(np.flatnonzero(np.any(hamR != 0, axis=1))[0])
+    ham2 = np.concatenate([ham, 0.5 * ham[[i0]], 0.25 * ham[[i1]]])
+    ham2[i0] *= 0.5
+    ham2[i1] *= 0.75
+    hamR2 = np.concatenate([hamR, hamR[[i0]], hamR[[i1]]])
+    same = Model(m.lat, m.orb, False, ham=ham2, hamR=hamR2)
+    k = np.random.default_rng(3).uniform(0, 1, (9, 2))
+    ref = O.gen_ham_batch(m, k, 1)
+    assert rel(same.gen_ham_batch(k), ref) < 1e-12
+    V, H = same.gen_v_projected_batch(k, Gauge.Atom, np.eye(2))
+    Vr, Hr = O.gen_v_projected_batch(m, k, 1, np.eye(2))
+    assert rel(V, Vr) < 1e-12
+    E = same.solve_band_all_parallel(k, Precision.MIXED)
+    assert np.max(np.abs(E - np.linalg.eigvalsh(ref))) <= 1e-9 * np.max(np.abs(np.linalg.eigvalsh(ref)))
+    lone = Model(m.lat, m.orb, False, ham=np.concatenate([ham, ham[[i1]] * 0.3j]),
+                 hamR=np.concatenate([hamR, hamR[[i1]] * 3]))
+    with pytest.raises(errors.InvalidModel):
+        lone.gen_ham_batch(k)
+    # 40 bands: the same duplicates through the tensor-core Fourier table
+    b = W.random_model(3, 40, False, 1, seed=78)
+    j0 = int(np.flatnonzero(np.all(b.hamR == 0, axis=1))[0])
+    j1 = int(np.flatnonzero(np.any(b.hamR != 0, axis=1))[0])
+    hb = np.concatenate([b.ham, 0.5 * b.ham[[j0]], 0.25 * b.ham[[j1]]])
+    hb[j0] *= 0.5
+    hb[j1] *= 0.75
+    big = Model(b.lat, b.orb, False, ham=hb, hamR=np.concatenate([b.hamR, b.hamR[[j0]], b.hamR[[j1]]]))
+    kb = np.random.default_rng(4).uniform(0, 1, (24, 3))
+    Eb = big.solve_band_all_parallel(kb, Precision.MIXED)
+    Hb = O.gen_ham_batch(b, kb, 1)
+    for i in range(24):
+        assert np.max(np.abs(Eb[i] - O.eigvalsh(Hb[i]))) <= 1e-9 * np.linalg.norm(Hb[i], 2)
+
+
 def test_rmatrix_commutator_term():
     m = W.random_model(2, 3, False, 1, seed=21)
     rng = np.random.default_rng(4)
