@@ -253,7 +253,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0, help="k-points for the CPU baseline (0 = auto)")
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["random3d", "haldane", "batched", "supercell", "serve", "dos", "w90", "wilson", "ec"],
+    ap.add_argument("--workload", choices=["random3d", "haldane", "batched", "supercell", "serve", "dos", "w90", "wilson", "ec", "eig-small"],
                     default="random3d")
     ap.add_argument("--models", type=int, default=64, help="batched: models taken from the 512-model set")
     ap.add_argument("--serve-seconds", type=float, default=8.0)

@@ -21,6 +21,10 @@
                    reference's own ec_vs_reference case (Haldane t2 = -0.3,
                    101 x 101 mesh, 201 chemical potentials, eta = 0.05); a step
                    is the whole mesh.
+* ``eig-small`` -- the FP64 eigensolvers for 9-32 bands: the Householder
+                   solver (one warp per matrix up to 16 bands) and the
+                   warp-per-matrix cyclic Jacobi solver on 9728 random
+                   Hermitian matrices per size; a step is one solve of the set.
 * ``w90``       -- Wannier90 loading: a 64-orbital, 125-R seedname_hr.dat
                    (512 000 lines, Wannier90's 5I5,2F12.6 format) read into a
                    device-resident model; a step is one load.
@@ -67,7 +71,8 @@ def run(args, rank, world, local):
     if rank != 0 and args.impl == "reference":
         return 0
     fn = {"haldane": haldane, "supercell": supercell, "batched": batched, "serve": serve_bench,
-          "dos": dos_bench, "w90": w90_bench, "wilson": wilson_bench, "ec": ec_bench}[args.workload]
+          "dos": dos_bench, "w90": w90_bench, "wilson": wilson_bench, "ec": ec_bench,
+          "eig-small": eig_small_bench}[args.workload]
     return fn(args, rank, world, local)
 
 
@@ -689,3 +694,63 @@ def ec_bench(args, rank, world, local):
            "e2e": {"value": e2e, "unit": "k-pts/s", "h2d_bytes_per_step": int(model.ham.nbytes + model.hamR.nbytes),
                    "d2h_bytes_per_step": int(sig.nbytes)}})
     return 0
+
+
+# --------------------------------------------------------------- eig-small --
+def eig_small_bench(args, rank, world, local):
+    """Matrices/s of the two FP64 solvers for 9-32 bands (CUDA events around
+    the solver launch on a device copy; the headline is 32 bands through the
+    solver the driver picks).  The reference arm times numpy's LAPACK eigh."""
+    import ctypes
+
+    sizes = [9, 12, 16, 20, 24, 32]
+    nk = 152 * 64
+    cfg = {"workload": f"random Hermitian complex matrices, {nk} per size, 9-32 bands", "sizes": sizes,
+           "l2": "inputs copied to a fresh device buffer before each timed solve"}
+    if args.impl == "reference":
+        rng = np.random.default_rng(32)
+        X = rng.standard_normal((512, 32, 32)) + 1j * rng.standard_normal((512, 32, 32))
+        H = 0.5 * (X + np.conj(np.transpose(X, (0, 2, 1))))
+        np.linalg.eigh(H[:8])
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            np.linalg.eigh(H)
+        val = 512 * args.steps / (time.perf_counter() - t0)
+        thr = os.cpu_count() or 1
+        _line(args, world, "matrices/s (FP64 eigenpairs, 32 bands)", val, "matrices/s", 512 / val * 1e3, "f64", cfg,
+              {"impl": "reference", "cpu_baseline": {"value": val, "unit": "matrices/s", "cores": thr, "kind": "port",
+                                                      "sample": "512 random 32-band matrices, numpy LAPACK eigh"},
+               "e2e": {"value": val, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return 0
+    lib = _lib.load()
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn = lib.tbg_internal_eig_f64
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_int64, dp, dp, dp, ctypes.c_int, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_float)]
+    by_n = {}
+    for n in sizes:
+        rng = np.random.default_rng(n)
+        X = rng.standard_normal((nk, n, n)) + 1j * rng.standard_normal((nk, n, n))
+        H = np.ascontiguousarray(0.5 * (X + np.conj(np.transpose(X, (0, 2, 1)))))
+        E = np.zeros((nk, n))
+        U = np.zeros((nk, n, n), dtype=np.complex128)
+        row = {}
+        for method, name in ((0, "householder"), (1, "jacobi")):
+            ms = ctypes.c_float(0.0)
+            for reps in (max(args.warmup, 1), max(args.steps, 1)):
+                _lib.check(fn(n, nk, H.view(np.float64).ctypes.data_as(dp), E.ctypes.data_as(dp),
+                              U.view(np.float64).ctypes.data_as(dp), method, reps, ctypes.byref(ms)), lib)
+            row[name] = {"ms": ms.value, "matrices_per_s": nk / ms.value * 1e3}
+        by_n[str(n)] = row
+    top = by_n[str(sizes[-1])]
+    ms = top["householder"]["ms"] if lib_jacobi_max_n() < sizes[-1] else top["jacobi"]["ms"]
+    _line(args, world, "matrices/s (FP64 eigenpairs, 32 bands)", nk / ms * 1e3, "matrices/s", ms, "f64", cfg,
+          {"by_n": by_n, "jacobi_max_n": lib_jacobi_max_n(), "gpu_launches": 2 * len(sizes) * max(args.steps, 1)})
+    return 0
+
+
+def lib_jacobi_max_n() -> int:
+    """The largest band count the FP64 driver gives to the Jacobi solver."""
+    v = os.environ.get("TBG_JACOBI_MAX_N")
+    return max(0, min(int(v), 32)) if v else 8

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "tbgpu_internal.cuh"
@@ -1087,11 +1088,20 @@ size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
+int jacobi_max_n() {
+    static const int v = [] {
+        const char* s = std::getenv("TBG_JACOBI_MAX_N");
+        return s ? std::max(0, std::min(std::atoi(s), kJacobiMaxN)) : kSmallMaxN;
+    }();
+    return v;
+}
+
 // FP64 driver (plain path): A destroyed, U complex<double>.
 int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
                 size_t work_bytes, int* status_d) {
     if (batch <= 0) return TBG_OK;
     if (N <= kSmallMaxN) return eig_small(st, N, batch, A, E, U, status_d);  // one thread per matrix
+    if (N <= jacobi_max_n()) return eig_jacobi(st, N, batch, A, E, U, status_d);  // one warp per matrix
     int G, PB;
     choose_g_pb<double>(N, false, 16, 16, G, PB);
     return launch_heev<double, false>(st, N, batch, A, E, U, work, work_bytes, status_d, "heev_kernel<double>", G,
@@ -1136,6 +1146,69 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 }
 
 }  // namespace tbg
+
+// Internal test hook (not part of the public header): FP64 eigenpairs of nk
+// host complex-double matrices by the Householder solver (method 0) or the
+// warp-per-matrix Jacobi solver (method 1), run `reps` times on a device copy;
+// *ms gets the mean device time of one run (CUDA events around the solver).
+extern "C" int tbg_internal_eig_f64(int n, int64_t nk, const double* H, double* E, double* U, int method, int reps,
+                                    float* ms) {
+    using namespace tbg;
+    const size_t NN = (size_t)n * n;
+    void *dH = nullptr, *dA = nullptr, *dE = nullptr, *dU = nullptr, *dS = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = TBG_OK;
+    if (n < 1 || nk < 1 || reps < 1 || (method == 1 && (n < 2 || n > kJacobiMaxN)))
+        return set_error(TBG_E_INVALID_ARGUMENT, "eig test: bad size or method");
+    if (cudaMalloc(&dH, 16 * NN * nk) || cudaMalloc(&dA, 16 * NN * nk) || cudaMalloc(&dE, 8 * n * nk) ||
+        cudaMalloc(&dU, 16 * NN * nk) || cudaMalloc(&dS, sizeof(int)) || cudaEventCreate(&e0) ||
+        cudaEventCreate(&e1))
+        rc = set_error(TBG_E_OOM, "eig test alloc");
+    float total = 0.0f;
+    if (!rc) {
+        cudaMemcpy(dH, H, 16 * NN * nk, cudaMemcpyHostToDevice);
+        cudaMemset(dS, 0, sizeof(int));
+        for (int it = 0; it < reps && !rc; ++it) {
+            cudaMemcpyAsync(dA, dH, 16 * NN * nk, cudaMemcpyDeviceToDevice, 0);
+            cudaEventRecord(e0, 0);
+            if (method == 1)
+                rc = eig_jacobi(0, n, nk, static_cast<zc*>(dA), static_cast<double*>(dE), static_cast<zc*>(dU),
+                                static_cast<int*>(dS));
+            else if (n <= kSmallMaxN)
+                rc = eig_small(0, n, nk, static_cast<zc*>(dA), static_cast<double*>(dE), static_cast<zc*>(dU),
+                               static_cast<int*>(dS));
+            else {
+                int G, PB;
+                choose_g_pb<double>(n, false, 16, 16, G, PB);
+                rc = launch_heev<double, false>(0, n, nk, static_cast<zc*>(dA), static_cast<double*>(dE),
+                                                static_cast<zc*>(dU), nullptr, 0, static_cast<int*>(dS),
+                                                "heev_kernel<double>", G, PB);
+            }
+            cudaEventRecord(e1, 0);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (!rc && e != cudaSuccess) rc = cuda_error(e, "eig test");
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, e0, e1);
+            total += t;
+        }
+        int st = 0;
+        cudaMemcpy(&st, dS, sizeof(int), cudaMemcpyDeviceToHost);
+        if (!rc && st) rc = set_error(TBG_E_NOCONV, "eig test: non-finite eigenvalues");
+    }
+    if (!rc) {
+        if (ms) *ms = total / reps;
+        cudaMemcpy(E, dE, 8 * n * nk, cudaMemcpyDeviceToHost);
+        cudaMemcpy(U, dU, 16 * NN * nk, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dH);
+    cudaFree(dA);
+    cudaFree(dE);
+    cudaFree(dU);
+    cudaFree(dS);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return rc;
+}
 
 // Internal test hook (not part of the public header): FP32 eigenpairs of nk
 // host complex-double matrices (n x n) -> E (nk, n) and U (nk, n, n) complex

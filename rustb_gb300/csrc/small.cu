@@ -377,3 +377,171 @@ int eig_small(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc*
     return TBG_OK;
 }
 }  // namespace tbg
+
+namespace tbg {
+namespace {
+
+// Warp-per-matrix cyclic complex Jacobi (FP64) for kSmallMaxN < N <= 32.  The
+// matrix (upper triangle read, as by the Householder solver) and the
+// eigenvector accumulator sit in shared memory; the N(N-1)/2 rotations of a
+// sweep run as N-1 rounds of N/2 disjoint pairs (circle-method round robin:
+// the last index fixed, the others turning), and in each round every 2x2 block
+// (rows of pair I, columns of pair J) becomes G_I^H B G_J, one block per lane,
+// with the rotation of the one-thread solver above:
+//   G = [[c, -s], [s e^{-i phi}, c e^{-i phi}]],  e^{i phi} = a_pq / |a_pq|,
+//   tan 2 theta = 2 |a_pq| / (a_pp - a_qq), |theta| <= pi/4
+// (the small angle: with every pair of a round rotated at once, the near-swaps
+// that the angle up to pi/2 allows make the rounds cycle without converging).
+// Sweeps stop when the off-diagonal norm is 1e-15 of the diagonal's: blocks
+// off the diagonal only reach rounding level, never exact zeros (at most 40).
+template <int NP>
+struct JacobiWarp {
+    zc A[NP * NP];
+    zc V[NP * NP];
+    zc em[NP / 2];
+    double c[NP / 2], s[NP / 2];
+    int p[NP / 2], q[NP / 2], rank[NP];
+};
+
+template <int NP>
+__global__ void __launch_bounds__(64) jacobi_warp_kernel(int N, int64_t batch, const zc* __restrict__ H,
+                                                         double* __restrict__ E_out, zc* __restrict__ U_out,
+                                                         int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char jacobi_smem[];
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    JacobiWarp<NP>& w = reinterpret_cast<JacobiWarp<NP>*>(jacobi_smem)[threadIdx.x >> 5];
+    const int n2 = (N + 1) & ~1, nh = n2 / 2, NN = N * N;
+    for (int64_t m = blockIdx.x * (int64_t)nw + (threadIdx.x >> 5); m < batch; m += (int64_t)gridDim.x * nw) {
+        const zc* h = H + m * NN;
+        for (int e = lane; e < n2 * n2; e += 32) {
+            const int i = e / n2, j = e - i * n2;
+            zc a = mk(0.0, 0.0);
+            if (i < N && j < N) a = j >= i ? h[i * N + j] : conj(h[j * N + i]);
+            if (i == j) a.im = 0.0;
+            w.A[i * NP + j] = a;
+            w.V[i * NP + j] = mk(i == j ? 1.0 : 0.0, 0.0);
+        }
+        __syncwarp();
+        for (int sweep = 0; sweep < 40; ++sweep) {
+            double off = 0.0, dia = 0.0;
+            for (int e = lane; e < n2 * n2; e += 32) {
+                const int i = e / n2, j = e - i * n2;
+                const double v = abs2(w.A[i * NP + j]);
+                if (i == j)
+                    dia += v;
+                else
+                    off += v;
+            }
+            for (int o = 16; o; o >>= 1) {
+                off += __shfl_xor_sync(0xffffffffu, off, o);
+                dia += __shfl_xor_sync(0xffffffffu, dia, o);
+            }
+            if (off <= 1e-30 * dia || off == 0.0) break;  // warp-uniform
+            for (int r = 0; r < n2 - 1; ++r) {
+                if (lane < nh) {
+                    const int p = lane == 0 ? r : (r + lane) % (n2 - 1);
+                    const int q = lane == 0 ? n2 - 1 : (r - lane + n2 - 1) % (n2 - 1);
+                    const zc apq = w.A[p * NP + q];
+                    const double mag = sqrt(abs2(apq));
+                    double sn = 0.0, cs = 1.0;
+                    zc em = mk(1.0, 0.0);
+                    if (mag > 0.0) {
+                        em = mk(apq.re / mag, -apq.im / mag);
+                        const double dl = w.A[p * NP + p].re - w.A[q * NP + q].re;
+                        sincos(0.5 * atan2(copysign(2.0 * mag, dl), fabs(dl)), &sn, &cs);
+                    }
+                    w.p[lane] = p;
+                    w.q[lane] = q;
+                    w.c[lane] = cs;
+                    w.s[lane] = sn;
+                    w.em[lane] = em;
+                }
+                __syncwarp();
+                for (int b = lane; b < nh * nh; b += 32) {
+                    const int I = b / nh, J = b - I * nh;
+                    const int pi = w.p[I], qi = w.q[I], pj = w.p[J], qj = w.q[J];
+                    const double ci = w.c[I], si = w.s[I], cj = w.c[J], sj = w.s[J];
+                    const zc ei = conj(w.em[I]), ej = w.em[J];
+                    const zc b00 = w.A[pi * NP + pj], b01 = w.A[pi * NP + qj];
+                    const zc b10 = w.A[qi * NP + pj], b11 = w.A[qi * NP + qj];
+                    // columns: B G_J
+                    const zc t01 = ej * b01, t11 = ej * b11;
+                    const zc r00 = cj * b00 + sj * t01, r01 = cj * t01 - sj * b00;
+                    const zc r10 = cj * b10 + sj * t11, r11 = cj * t11 - sj * b10;
+                    // rows: G_I^H (B G_J)
+                    const zc u10 = ei * r10, u11 = ei * r11;
+                    zc a00 = ci * r00 + si * u10, a01 = ci * r01 + si * u11;
+                    zc a10 = ci * u10 - si * r00, a11 = ci * u11 - si * r01;
+                    if (I == J) {
+                        a00.im = 0.0;
+                        a11.im = 0.0;
+                        a01 = mk(0.0, 0.0);
+                        a10 = mk(0.0, 0.0);
+                    }
+                    w.A[pi * NP + pj] = a00;
+                    w.A[pi * NP + qj] = a01;
+                    w.A[qi * NP + pj] = a10;
+                    w.A[qi * NP + qj] = a11;
+                }
+                for (int e = lane; e < n2 * nh; e += 32) {
+                    const int row = e / nh, J = e - row * nh;
+                    const int pj = w.p[J], qj = w.q[J];
+                    const double cj = w.c[J], sj = w.s[J];
+                    const zc v0 = w.V[row * NP + pj], v1 = w.em[J] * w.V[row * NP + qj];
+                    w.V[row * NP + pj] = cj * v0 + sj * v1;
+                    w.V[row * NP + qj] = cj * v1 - sj * v0;
+                }
+                __syncwarp();
+            }
+        }
+        // ascending order: rank of each diagonal entry, ties by index
+        for (int i = lane; i < N; i += 32) {
+            const double di = w.A[i * NP + i].re;
+            int rk = 0;
+            for (int j = 0; j < N; ++j) {
+                const double dj = w.A[j * NP + j].re;
+                rk += (dj < di) || (dj == di && j < i);
+            }
+            w.rank[i] = rk;
+            E_out[m * N + rk] = di;
+            if (!isfinite(di) && status) atomicOr(status, 1);
+        }
+        __syncwarp();
+        if (U_out)
+            for (int e = lane; e < NN; e += 32) {
+                const int r = e / N, c = e - r * N;
+                U_out[m * NN + r * N + w.rank[c]] = w.V[r * NP + c];
+            }
+        __syncwarp();
+    }
+}
+
+template <int NP>
+int launch_jacobi(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status) {
+    constexpr int kWarps = 2;
+    const size_t smem = kWarps * sizeof(JacobiWarp<NP>);
+    auto kern = jacobi_warp_kernel<NP>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_error(e, "jacobi_warp_kernel smem");
+    int dev = 0, nsm = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 32 * kWarps, smem);
+    if (e != cudaSuccess || perSM < 1) perSM = 1;
+    const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, (batch + kWarps - 1) / kWarps);
+    KTimer kt(st, "jacobi_warp_kernel");
+    kern<<<(unsigned)grid, 32 * kWarps, smem, st>>>(N, batch, H, E, U, status);
+    TBG_LAUNCHED("jacobi_warp_kernel");
+    return TBG_OK;
+}
+
+}  // namespace
+
+int eig_jacobi(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status) {
+    if (batch <= 0) return TBG_OK;
+    if (N < 2 || N > kJacobiMaxN) return set_error(TBG_E_UNSUPPORTED, "eig_jacobi: N outside [2, 32]");
+    return N <= 16 ? launch_jacobi<16>(st, N, batch, H, E, U, status)
+                   : launch_jacobi<32>(st, N, batch, H, E, U, status);
+}
+
+}  // namespace tbg

@@ -244,6 +244,12 @@ constexpr int kSmallMaxN = 8;
 // Eigenpairs of N <= kSmallMaxN matrices by per-thread Jacobi (E ascending,
 // U columns; U may be null; non-finite input sets bit 0 of *status).
 int eig_small(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status);
+// Eigenpairs of kSmallMaxN < N <= kJacobiMaxN matrices by warp-per-matrix
+// cyclic Jacobi (FP64; same outputs as eig_small; H is not modified).
+constexpr int kJacobiMaxN = 32;
+int eig_jacobi(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status);
+// Largest N the FP64 driver gives to eig_jacobi (TBG_JACOBI_MAX_N overrides).
+int jacobi_max_n();
 // Largest model the mixed path takes (FP32 solver with the matrix in global
 // memory above 215 bands; tcgen05 products in chunks of 256 along K).
 constexpr int kMixedMaxN = 2048;
