@@ -388,6 +388,12 @@ int tbg_kernel_timing_enable(int enable);
 int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms,
                            double* total_flops, int max_entries, int reset);
 
+/* Bytes of device scratch one call sizes its k-point chunks to at this
+ * moment: TBG_CHUNK_BYTES when set, else an eighth of the free device memory
+ * between 6 and 24 GB (no reference counterpart; for callers that admit
+ * concurrent calls by device footprint). */
+int64_t tbg_chunk_budget_bytes(void);
+
 /* Library version string, e.g. "tbgpu 0.1.0 sm_103a". */
 const char* tbg_version(void);
 

@@ -118,6 +118,7 @@ SIGNATURES = [
     ("tbg_measure_fma_peaks", ctypes.c_int, [_c_double_p, _c_double_p]),
     ("tbg_set_device", ctypes.c_int, [ctypes.c_int]),
     ("tbg_kernel_timing_enable", ctypes.c_int, [ctypes.c_int]),
+    ("tbg_chunk_budget_bytes", ctypes.c_int64, []),
     ("tbg_kernel_timing_read", ctypes.c_int, [ctypes.c_char_p, _c_int64_p, _c_double_p, _c_double_p,
                                               ctypes.c_int, ctypes.c_int]),
     ("tbg_eigvalsh_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,

@@ -30,6 +30,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib
 from .model import Model
 from .params import Parameters, Precision
 
@@ -54,7 +55,7 @@ def footprint_bytes(model: Model, nk: int, observable: str, precision: int) -> i
     """Device bytes a request holds while running (chunked as the library does)."""
     N = model.nsta
     per_k = 16 * N * N * (2 if observable == "bands" else (15 if precision == int(Precision.MIXED) else 5))
-    chunk = max(1, min(nk, (6 << 30) // max(per_k, 1), 65535))
+    chunk = max(1, min(nk, int(_lib.load().tbg_chunk_budget_bytes()) // max(per_k, 1), 65535))
     return chunk * per_k + 16 * model.nR * N * N
 
 
