@@ -148,11 +148,6 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
     return 24.0 * nR * N * N + 46.0 * N ** 3
 
 
-# DRAM bytes per unit of work of a kernel family, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum) of the bench's 128-band model:
-# heev_kernel<float,smem>: 169.3 MB for one launch over 512 matrices
-# (profiles/heev_f32_random3d_b512.md).  The traffic of a bench launch is this
-# figure times the matrices that launch processes.
 # DRAM bytes (read + write) per k-point of each kernel family, from ncu captures over 512 k-points
 # of this workload: the FP32 solver's two passes, and the seven FP64-class tcgen05 products of one
 # k-point (refinement and rotation) together.
@@ -249,7 +244,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--batch", type=int, default=8192, help="k-points per rank per step")
-    ap.add_argument("--fp64-sample", type=int, default=2048)
+    ap.add_argument("--fp64-sample", type=int, default=0, help="k-points of the plain FP64 run (0 = --batch)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="k-points for the CPU baseline (0 = auto)")
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -260,7 +255,7 @@ def main():
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.workload != "random3d":
-        from rustb_gb300 import bench_workloads
+        import bench_workloads
 
         return bench_workloads.run(args, rank, world, local)
     if args.impl == "reference":
@@ -327,7 +322,7 @@ def main():
     orb = np.ascontiguousarray(model.orb)
     lat = np.ascontiguousarray(model.lat)
     h2d = ham_pin.numel() * 8 + hamR.nbytes + orb.nbytes + lat.nbytes + DIRS.nbytes + MU.nbytes + km.nbytes
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = args.steps
     dist.barrier()
     t0 = time.perf_counter()
     for s in range(e2e_steps):
@@ -344,14 +339,13 @@ def main():
     out = None
     if rank == 0:
         # ---------------------------------------------- plain FP64 beside it --
-        fs = args.fp64_sample
-        t_fp64 = 0.0
+        # plain FP64 path on a batch of the same size (flat indices [0, fs))
+        fs = args.fp64_sample or B
         step(0, Precision.FP64, fs)
-        t_fp64 = rep.device_ms / 1e3
+        fp64_val = fs / (rep.device_ms / 1e3)
         plain_sum = sums.copy()
         step(0, Precision.MIXED, fs)
         mixed_sum = sums.copy()
-        fp64_val = fs / t_fp64
         acc = {"ahc_partial_rel_err_mixed_vs_fp64": float(abs(mixed_sum[0] - plain_sum[0]) / abs(plain_sum[0])),
                "sample": f"flat k indices [0, {fs}) of the 64^3 mesh"}
         roof_line = kernel_roofline(timing, peaks, units=done)
@@ -364,10 +358,17 @@ def main():
             build_port.load()
             build_port.hall_sums(model, DIRS, MU, 0.0, ETA, -1, kmesh=KMESH, k0=0, nk=threads, threads=threads)
             t0 = time.perf_counter()
-            build_port.hall_sums(model, DIRS, MU, 0.0, ETA, -1, kmesh=KMESH, k0=0, nk=cs, threads=threads)
+            port_S = build_port.hall_sums(model, DIRS, MU, 0.0, ETA, -1, kmesh=KMESH, k0=0, nk=cs, threads=threads)
             cdt = time.perf_counter() - t0
             cpu = {"value": cs / cdt, "unit": "k-pts/s", "cores": threads, "kind": "port",
                    "sample": f"{cs} k-points of the 64^3 mesh (flat indices [0, {cs}))"}
+            # the GPU's FP64 and MIXED sums over the port's k-points, against the port
+            port_sum = float(math.fsum(port_S[:, 0]))
+            step(0, Precision.FP64, cs)
+            acc["fp64_vs_port_rel"] = float(abs(sums[0] - port_sum) / abs(port_sum))
+            step(0, Precision.MIXED, cs)
+            acc["mixed_vs_port_rel"] = float(abs(sums[0] - port_sum) / abs(port_sum))
+            acc["port_sample"] = f"flat k indices [0, {cs}) of the 64^3 mesh (C port, OpenBLAS zheev)"
         flops_k = algorithmic_flops_per_k(N, nR)
         out = {
             "metric": METRIC, "value": value, "unit": "k-pts/s", "n_gpus": world, "steps": args.steps,

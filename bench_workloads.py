@@ -42,8 +42,8 @@ import time
 
 import numpy as np
 
-from . import _lib, batch, serve, workloads as W
-from .params import Parameters, Precision
+from rustb_gb300 import _lib, batch, serve, workloads as W
+from rustb_gb300.params import Parameters, Precision
 
 METRIC_K = "k-pts/s (H+eig+Berry, norb=128) mixed vs FP64 GPU @AHC err≤1e-6; serve p99"
 
@@ -174,6 +174,23 @@ def supercell(args, rank, world, local):
         p64 = sums[int(Precision.FP64)]
         acc = {"ahc_partial_rel_err_mixed_vs_fp64": abs(sums[int(Precision.MIXED)] - p64) / abs(p64),
                "sample": "flat k indices [0, 16) of the 64x64 mesh"}
+        from oracle import build_port
+        from oracle import tb_oracle as O
+
+        port = float(np.sum(build_port.hall_sums(model, dirs, mu, 0.0, 1e-3, -1, kmesh=mesh, k0=0, nk=16)))
+        acc["fp64_vs_port_rel"] = abs(p64 - port) / abs(port)
+        acc["mixed_vs_port_rel"] = abs(sums[int(Precision.MIXED)] - port) / abs(port)
+        # the configuration's stated output: Omega of the 20 bands nearest E = 0
+        # (berry_curvature_at) at one mesh point, MIXED, against the numpy oracle
+        kq = O.gen_kmesh(mesh)[1000:1001]
+        pq = Parameters.rank2((1, 1), [1.0, 0.0], [0.0, 1.0], [0.0])
+        Om, E = model.berry_curvature_on(kq, pq, Precision.MIXED)
+        Omr, Er = O.berry_on(model, kq, dirs)
+        sel = np.sort(np.argsort(np.abs(E[0]), kind="stable")[:20])
+        acc["bands_near_zero"] = {
+            "k": kq[0].tolist(), "bands": sel.tolist(), "E": E[0][sel].tolist(), "Omega": Om[0][sel].tolist(),
+            "omega_rel_err_vs_oracle": float(np.max(np.abs(Om[0][sel] - Omr[0][sel])) / np.max(np.abs(Omr[0][sel]))),
+            "E_err_over_normH": float(np.max(np.abs(E[0] - Er[0])) / np.linalg.norm(O.gen_ham(model, kq[0]), 2))}
     dtype = "f32 eigensolve + f64-class refinement (tcgen05, K in chunks of 256)" if prec_ran == int(Precision.MIXED) \
         else "f64"
     _line(args, world, METRIC_K, val, "k-pts/s", t / args.steps * 1e3, dtype, cfg,
@@ -313,8 +330,8 @@ def _cpu_dos(model, mesh, E_min, E_max, E_n, sigma, nk, threads=None):
     return nk / (time.perf_counter() - t0), threads
 
 
-# ncu: DRAM bytes of one dos_kernel launch over the whole 1000 x 1000 mesh
-# (one chunk; profiles/dos_kernel_honeycomb_1000x1000.md)
+# ncu: DRAM bytes (read + write) of one dos_kernel launch over the whole
+# 1000 x 1000 mesh (one chunk)
 DOS_KERNEL_DRAM_BYTES = 16.02e6
 
 
@@ -443,7 +460,7 @@ def w90_bench(args, rank, world, local):
     import shutil
     import tempfile
 
-    from .model import Model
+    from rustb_gb300.model import Model
 
     src = W.random_model(3, 64, False, 2, seed=20260107)
     cfg = {"workload": "Wannier90 seedname_hr.dat of a random 64-orbital model, R in {-2..2}^3 (125 R, "
@@ -615,7 +632,7 @@ EC_METRIC = "k-pts/s (hall_conductivity, Integration::EnergyCut)"
 
 
 def _haldane_2d(t2_imag: float):
-    from .model import Model
+    from rustb_gb300.model import Model
 
     s3 = math.sqrt(3.0)
     m = Model.tb_model([[1.0, 0.0], [0.5, s3 / 2.0]], [[1.0 / 3.0, 1.0 / 3.0], [2.0 / 3.0, 2.0 / 3.0]])
@@ -630,7 +647,7 @@ def _haldane_2d(t2_imag: float):
 
 
 def ec_bench(args, rank, world, local):
-    from .params import Integration
+    from rustb_gb300.params import Integration
 
     model = _haldane_2d(-0.3)
     mesh = (101, 101)

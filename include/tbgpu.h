@@ -339,8 +339,10 @@ int tbg_batch_set_workers(int n);
 
 /* ------------------------------------------------ no-allocation variant --- */
 
-/* Size of the fixed device scratch array used by tbg_eigvalsh_noalloc. */
+/* Size of the fixed device scratch array used by tbg_eigvalsh_noalloc, and
+ * the largest matrix order it admits (one 1448 x 1448 complex FP64 matrix). */
 #define TBG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define TBG_NOALLOC_MAX_N 1448
 
 /* Band energies (ascending, FP64) of nk device-resident Hermitian matrices,
  * without allocating any device memory.  No counterpart in the reference: it
@@ -353,8 +355,12 @@ int tbg_batch_set_workers(int n);
  * fixed static device array of TBG_NOALLOC_SCRATCH_BYTES that every GPU that
  * loads this library holds until the process exits; a call needs
  * nk * n * n * 16 bytes of it and is rejected with TBG_E_UNSUPPORTED beyond
- * that.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * that (so n <= TBG_NOALLOC_MAX_N).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and keeps it; make that first
+ * call before any stream capture, and do not use the entry point on a device
+ * after cudaDeviceReset.  Non-finite input is not reported: there is no status
+ * word to read back without synchronising, and such a matrix yields NaN
+ * energies (check E_d, or use tbg_solve_band, which returns TBG_E_NOCONV).
  * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream) and
  * the call returns without waiting.  All calls share the one array: calls
  * whose work overlaps on the GPU (different streams, no ordering between them)

@@ -247,8 +247,9 @@ int check_status(int* status_d, cudaStream_t st) {
     cudaError_t e = cudaMemcpyAsync(&h, status_d, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "status readback");
-    if (h & 1) return set_error(TBG_E_NOCONV, "eigensolver input contains NaN or Inf");
+    // a time-out first: the kernels after it read what the aborted one left
     if (h & 2) return set_error(TBG_E_TIMEOUT, "a bounded device wait ran out in a tensor-core kernel");
+    if (h & 1) return set_error(TBG_E_NOCONV, "eigensolver input contains NaN or Inf");
     if (h & 4)
         return set_error(TBG_E_NOCONV,
                          "Wilson loop: an overlap matrix is singular (the occupied bands touch others on the loop)");

@@ -528,12 +528,15 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
         T lo_g, hi_g, tnorm, pivmin;
         {
             T lo = INFINITY, hi = -INFINITY, em = 0;
+            bool bad = false;  // min/max skip NaN, so non-finite entries are looked for as such
             for (int i = tid; i < N; i += nthr) {
                 const T r = ((i > 0) ? fabs(sh.e[i - 1]) : T(0)) + ((i < N - 1) ? fabs(sh.e[i]) : T(0));
                 lo = min(lo, sh.d[i] - r);
                 hi = max(hi, sh.d[i] + r);
                 em = max(em, sh.e2[i]);
+                bad = bad || !isfinite(sh.d[i]) || !isfinite(sh.e[i]);
             }
+            if (__any_sync(0xffffffffu, bad) && lane == 0) sh.flags[0] = 1;  // NaN/Inf input
             lo = -warp_max(-lo);
             hi = warp_max(hi);
             em = warp_max(em);
@@ -613,6 +616,9 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
             }
         }
         __syncthreads();
+        // non-finite input (found while bounding the spectrum) is reported for
+        // eigenvalue-only calls as well as for eigenpairs
+        if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
         if (Eout) {
             for (int i = tid; i < N; i += nthr) Eout[b * N + i] = (double)sh.lam[i];
         }
@@ -701,7 +707,6 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
         // ----------------------------------------------- back-transform --
         if constexpr (A_SMEM) {
             // the reflectors went out after the reduction
-            if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
             __syncthreads();
             continue;
         }
@@ -746,7 +751,6 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
             }
             __syncthreads();
         }
-        if (tid == 0 && sh.flags[0] && status) atomicOr(status, 1);
         __syncthreads();
     }
 }

@@ -627,21 +627,28 @@ __global__ void gather_exps_kernel(int64_t n, const int* __restrict__ idx, const
 //   A = t(R) + t(-R),  B = i (t(R) - t(-R))
 // (an R without its -R partner takes t(-R) = 0).  Rows: 0 = t(0), 1 = 0,
 // 2 + 2p = A_p, 3 + 2p = B_p.  pi[p] is the pair's R, pj[p] its -R or -1.
+// A non-finite entry sets *nonfinite (the exact-slice digits of the
+// tensor-core form cannot carry NaN or Inf, so the mixed path refuses such a
+// table up front).
 __global__ void pair_table_kernel(int np, const int* __restrict__ pi, const int* __restrict__ pj, int z, int64_t NN,
-                                  const zc* __restrict__ ham, zc* __restrict__ T) {
+                                  const zc* __restrict__ ham, zc* __restrict__ T, int* __restrict__ nonfinite) {
     const int64_t total = (int64_t)(np + 1) * NN;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t p = idx / NN - 1, e = idx % NN;
+        zc a, b;
         if (p < 0) {
-            T[e] = (z >= 0) ? ham[(int64_t)z * NN + e] : mk(0.0, 0.0);
-            T[NN + e] = mk(0.0, 0.0);
+            a = (z >= 0) ? ham[(int64_t)z * NN + e] : mk(0.0, 0.0);
+            b = mk(0.0, 0.0);
+            T[e] = a;
+            T[NN + e] = b;
         } else {
-            const zc a = ham[(int64_t)pi[p] * NN + e];
-            const zc b = (pj[p] >= 0) ? ham[(int64_t)pj[p] * NN + e] : mk(0.0, 0.0);
+            a = ham[(int64_t)pi[p] * NN + e];
+            b = (pj[p] >= 0) ? ham[(int64_t)pj[p] * NN + e] : mk(0.0, 0.0);
             T[(2 + 2 * p) * NN + e] = mk(a.re + b.re, a.im + b.im);
             T[(3 + 2 * p) * NN + e] = mk(-(a.im - b.im), a.re - b.re);
         }
+        if (!(isfinite(a.re) && isfinite(a.im) && isfinite(b.re) && isfinite(b.im))) atomicOr(nonfinite, 1);
     }
 }
 
@@ -711,18 +718,24 @@ int ensure_pair_table(ModelDev& m, cudaStream_t st) {
     int rc = TBG_OK;
     if (cudaMalloc(&T, sizeof(zc) * 2 * (size_t)Kc * NN) != cudaSuccess ||
         cudaMalloc(&pair_d, sizeof(int) * std::max(np, 1)) != cudaSuccess ||
-        cudaMalloc(&pj_d, sizeof(int) * std::max(np, 1)) != cudaSuccess)
+        cudaMalloc(&pj_d, sizeof(int) * (std::max(np, 1) + 1)) != cudaSuccess)
         rc = set_error(TBG_E_OOM, "paired hop table");
+    int* nonfinite_d = pj_d + std::max(np, 1);
+    if (!rc && cudaMemsetAsync(nonfinite_d, 0, sizeof(int), st) != cudaSuccess)
+        rc = set_error(TBG_E_CUDA, "paired hop table flag");
     if (!rc && np > 0 &&
         (cudaMemcpy(pair_d, pi.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess ||
          cudaMemcpy(pj_d, pj.data(), sizeof(int) * np, cudaMemcpyHostToDevice) != cudaSuccess))
         rc = set_error(TBG_E_CUDA, "paired hop table indices");
     if (!rc) {
         pair_table_kernel<<<(unsigned)std::min<int64_t>(((int64_t)Kc * NN + 255) / 256, 152 * 64), 256, 0, st>>>(
-            np, pair_d, pj_d, z, NN, m.ham, T);
+            np, pair_d, pj_d, z, NN, m.ham, T, nonfinite_d);
         count_launch();
-        cudaError_t e = cudaStreamSynchronize(st);  // other streams use the table next
+        int nf = 0;
+        cudaError_t e = cudaMemcpyAsync(&nf, nonfinite_d, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // other streams use the table next
         if (e != cudaSuccess) rc = cuda_error(e, "paired hop table");
+        m.nonfinite = nf != 0;
     }
     cudaFree(pj_d);
     if (rc) {
@@ -801,6 +814,7 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
             if (rc) return rc;
         }
     }
+    if (m.nonfinite) return set_error(TBG_E_NOCONV, "the hopping table contains NaN or Inf");
     unsigned char* p = static_cast<unsigned char*>(scratch);
     auto take = [&](size_t bytes) {
         void* q = p;

@@ -118,10 +118,18 @@ __device__ __forceinline__ zc pair_z(float4 v) { return mk((double)v.x + (double
 __device__ __forceinline__ zc widen(cc v) { return mk((double)v.re, (double)v.im); }
 
 // One CTA per matrix.  XX = X^H X and S = X^H H X as float pairs -> refined
-// eigenvalues E (FP64) and the update F (FP32 complex).
+// eigenvalues E (FP64) and the update F (FP32 complex).  The Rayleigh-Ritz
+// rotations of clusters (entries of order one) are not left in F: a product
+// X F whose operand columns hold them would be sliced on those columns'
+// exponents and lose the small first-order entries beside them.  They go to
+// Fcl in FP64 instead (row i + p, column q of the N x kMaxCluster block of the
+// matrix for member p of the cluster starting at i), with cinfo[j] =
+// (start << 4) | size for every member column j and -1 elsewhere, and their
+// block of F is zero.
 __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, const float4* __restrict__ XX,
                                                        const float4* __restrict__ S, double* __restrict__ E,
-                                                       cc* __restrict__ F, int64_t* __restrict__ clusters) {
+                                                       cc* __restrict__ F, int64_t* __restrict__ clusters,
+                                                       int* __restrict__ cinfo, zc* __restrict__ Fcl) {
     extern __shared__ double smem[];
     double* lam = smem;                                   // N
     float* lamf = reinterpret_cast<float*>(lam + N);      // N
@@ -193,6 +201,7 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
             }
             Fb[idx] = mk(fr, fi);
         }
+        for (int i = threadIdx.x; i < N; i += blockDim.x) cinfo[b * N + i] = -1;
         __syncthreads();
         // Rayleigh-Ritz on clusters (one thread per cluster, FP64)
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -233,7 +242,11 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
                     Fn[p * c + q] = acc;
                 }
             for (int p = 0; p < c; ++p) {
-                for (int q = 0; q < c; ++q) Fb[(i + p) * N + (i + q)] = mk((float)Fn[p * c + q].re, (float)Fn[p * c + q].im);
+                for (int q = 0; q < c; ++q) {
+                    Fb[(i + p) * N + (i + q)] = mk(0.f, 0.f);
+                    Fcl[(b * N + i + p) * kMaxCluster + q] = Fn[p * c + q];
+                }
+                cinfo[b * N + i + p] = (i << 4) | c;
                 lam[i + p] = w[p];
             }
             // rows outside the cluster: F_{t,c} <- F_{t,c} W
@@ -254,13 +267,37 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
     }
 }
 
-// X' = X + X F as a float pair: hi = X (exact FP32 eigenvectors), lo = X F.
-__global__ void xprime_kernel(int64_t n, const cc* __restrict__ X, const float4* __restrict__ XF,
-                              float4* __restrict__ Xp) {
+// X' = X + X F + X_c F_c as a float pair: hi = X (exact FP32 eigenvectors),
+// lo = X F (the product of the first-order part of the update).  A column j
+// of a cluster also gets the cluster's rotation, sum_p X[r, s + p] Fcl[s + p,
+// j - s] in FP64 (cinfo as oa_pairs_kernel writes it), and the pair is formed
+// from the FP64 sum.
+__global__ void xprime_kernel(int64_t n, int N, const cc* __restrict__ X, const float4* __restrict__ XF,
+                              const int* __restrict__ cinfo, const zc* __restrict__ Fcl, float4* __restrict__ Xp) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const cc x = X[i];
         const float4 f = XF[i];
-        Xp[i] = make_float4(x.re, f.x + f.y, x.im, f.z + f.w);
+        const int64_t b = i / ((int64_t)N * N);
+        const int j = (int)(i % N);
+        const int ci = cinfo[b * N + j];
+        if (ci < 0) {
+            Xp[i] = make_float4(x.re, f.x + f.y, x.im, f.z + f.w);
+            continue;
+        }
+        const int st = ci >> 4, c = ci & 15;
+        const cc* xr = X + (i - j);  // row r of this matrix
+        const zc* fc = Fcl + (b * N + st) * kMaxCluster + (j - st);
+        double re = ((double)f.x + (double)f.y), im = ((double)f.z + (double)f.w);
+        for (int p = 0; p < c; ++p) {
+            const cc a = xr[st + p];
+            const zc w = fc[p * kMaxCluster];
+            re += (double)a.re * w.re - (double)a.im * w.im;
+            im += (double)a.re * w.im + (double)a.im * w.re;
+        }
+        re += (double)x.re;
+        im += (double)x.im;
+        const float rh = (float)re, ih = (float)im;
+        Xp[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
     }
 }
 
@@ -393,7 +430,8 @@ size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     const size_t NN = (size_t)N * N;
     // X and F (cc) + 5 pair buffers + line exponents (10 operand sides) + FP32 solver workspace
     return (size_t)batch * NN * (2 * sizeof(cc) + 5 * sizeof(float4)) + sizeof(int) * 10 * (size_t)batch * N +
-           ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) + 4096;
+           ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) +
+           (size_t)batch * N * (sizeof(int) + kMaxCluster * sizeof(zc)) + 4096 + 512;
 }
 
 // H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega and, when Met is
@@ -422,6 +460,8 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     // tcgen05 form: the exponents of each operand side are scanned once and
     // shared by the products that use it
     int* ex = static_cast<int*>(take(sizeof(int) * 10 * (size_t)batch * N));
+    int* cinfo = static_cast<int*>(take(sizeof(int) * (size_t)batch * N));
+    zc* Fcl = static_cast<zc*>(take(sizeof(zc) * kMaxCluster * (size_t)batch * N));
     auto slot = [&](int i) { return ex + (size_t)i * batch * N; };
     enum { XC, HR, HXC, XR, FC, XPC, VXR, VYR, BXC, BYC };
     const bool tc = ozaki_use_tc();
@@ -460,7 +500,7 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         KTimer kt(st, "oa_kernel");
         const size_t smem = sizeof(double) * N + sizeof(float) * N + sizeof(int) * N;
         oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, bC, E, F,
-                                                                                        clusters_d);
+                                                                                        clusters_d, cinfo, Fcl);
         TBG_LAUNCHED("oa_kernel");
     }
     auto energies_out = [&]() -> int {
@@ -470,10 +510,11 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         return (int)TBG_OK;
     };
     if (!Om && !Uout) return energies_out();  // band energies only
-    // 4. X' = X + X F  (float pair: hi = X, lo = X F).  F is small except for
-    // the rotations inside eigenvalue clusters, where the LOW class's 2^-21
-    // leaves errors that leak out of near-degenerate subspaces; above
-    // kHighCorrN bands (dense spectra, many clusters) X F is a HIGH product.
+    // 4. X' = X + X F + X_c F_c  (float pair: hi = X, lo = the rest).  F holds
+    // only first-order entries (the cluster rotations F_c are applied in FP64
+    // by xprime_kernel), so the LOW class's 2^-21 of each column's largest
+    // entry stays far below the refinement's accuracy; above kHighCorrN bands
+    // X F is a HIGH product.
     if ((rc = exps(F32, false, X, XR)) || (rc = exps(F32, true, F, FC))) return rc;
     if (tc && N > kHighCorrN)
         rc = ozaki_zgemm_tc(st, false, F32, F32, batch, N, N, N, X, N, NN, F, N, NN, bE, N, NN, slot(XR), slot(FC),
@@ -485,7 +526,7 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     if (rc) return rc;
     {
         KTimer kt(st, "xprime_kernel");
-        xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, X, bE, bA);
+        xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, N, X, bE, cinfo, Fcl, bA);
         TBG_LAUNCHED("xprime_kernel");
     }
     if (Uout) {  // eigenpairs only: refined E and X' in ascending order, no velocities

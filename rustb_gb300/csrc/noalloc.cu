@@ -22,11 +22,19 @@ namespace {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[TBG_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
+// Largest n with one n x n complex FP64 matrix in the array: floor(sqrt(bytes / 16)).
+constexpr int64_t kMaxNoallocN = 1448;
+static_assert(16ULL * kMaxNoallocN * kMaxNoallocN <= TBG_NOALLOC_SCRATCH_BYTES &&
+                  16ULL * (kMaxNoallocN + 1) * (kMaxNoallocN + 1) > TBG_NOALLOC_SCRATCH_BYTES,
+              "kMaxNoallocN follows the array size");
 std::mutex g_setup_mu;
 void* g_scratch_addr[kMaxDevices] = {nullptr};
 
 // Set-up, once per device, with that device current: the host-side name of the
-// array is not a device address, so look the address up and keep it.
+// array is not a device address, so look the address up and keep it.  The
+// address belongs to the device's primary context as it is when looked up; a
+// cudaDeviceReset (which reloads the module) invalidates it, so the entry point
+// is not for processes that reset a device they use it on.
 int scratch_address(int dev, void** out) {
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_scratch_addr[dev]) {
@@ -44,7 +52,12 @@ int scratch_address(int dev, void** out) {
 
 extern "C" int tbg_eigvalsh_noalloc(int64_t n, int64_t nk, const double* H_d, double* E_d, void* stream) {
     using namespace tbg;
-    if (n < 1 || n > 4096) return set_error(TBG_E_UNSUPPORTED, "tbg_eigvalsh_noalloc: n must be in [1, 4096]");
+    // one matrix must fit the array: 16 n^2 <= TBG_NOALLOC_SCRATCH_BYTES, n <= 1448
+    if (n < 1 || 16ULL * (unsigned long long)n * (unsigned long long)n > TBG_NOALLOC_SCRATCH_BYTES)
+        return set_error(TBG_E_UNSUPPORTED, "tbg_eigvalsh_noalloc: n must be in [1, " +
+                                                std::to_string(kMaxNoallocN) + "] (one matrix of " +
+                                                std::to_string((unsigned long long)TBG_NOALLOC_SCRATCH_BYTES) +
+                                                " bytes of scratch at most)");
     if (nk < 0) return set_error(TBG_E_INVALID_ARGUMENT, "tbg_eigvalsh_noalloc: negative nk");
     if (nk == 0) return TBG_OK;
     if (!H_d || !E_d) return set_error(TBG_E_INVALID_ARGUMENT, "tbg_eigvalsh_noalloc: null device pointer");

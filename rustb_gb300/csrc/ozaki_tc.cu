@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "tbgpu_internal.cuh"
@@ -89,15 +90,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Polls of a stage hand-off wait before the CTA gives up (a few milliseconds
+// at the default).  The drains before TMEM is freed keep their own bound.
+constexpr int kTcWaitPolls = 1 << 20;
+std::atomic<int> g_tc_wait_limit{kTcWaitPolls};
+inline int tc_wait_limit() { return g_tc_wait_limit.load(std::memory_order_relaxed); }
+
 // Bounded wait without abort check (used to drain committed MMAs and copies).
 __device__ __forceinline__ bool mbar_wait_plain(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 20); ++it)
+    for (int it = 0; it < kTcWaitPolls; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
-// Bounded wait: false on time-out or when another warp has flagged an abort.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-    for (int it = 0; it < (1 << 20); ++it) {
+// Bounded wait (at most `limit` polls): false on time-out or when another warp
+// has flagged an abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int limit) {
+    for (int it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
     }
@@ -344,7 +352,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
                  int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
                  float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err,
-                 int accumulate, int* __restrict__ Ecol) {
+                 int accumulate, int* __restrict__ Ecol, int wait_limit) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
     constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
     constexpr int HS = S * PLANE;             // planes of one operand in a stage
@@ -392,7 +400,8 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
             for (int it = 0; it < nstages; ++it) {
                 const int bi = it & 1;
                 const uint32_t ph = (it >> 1) & 1;
-                if (!mbar_wait(&bar_full[bi], ph, &abort_sh) || (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh))) {
+                if (!mbar_wait(&bar_full[bi], ph, &abort_sh, wait_limit) ||
+                    (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh, wait_limit))) {
                     abort_sh = 1;
                     break;
                 }
@@ -443,7 +452,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                 const int kf = (it + 1) * TC_TK + 8 * g;
                 load8<FMTA>(A, idx0 + (int64_t)kf * kstride, kstride, rv ? n_valid(K, kf) : 0, nxt);
             }
-            if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
+            if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
                 abort_sh = 1;
                 break;
             }
@@ -468,7 +477,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                 int last[2] = {-1, -1};
                 for (int it = 0; it < nstages; ++it) {
                     const int bi = it & 1;
-                    if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
+                    if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
                         abort_sh = 1;
                         break;
                     }
@@ -505,7 +514,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     const int kf = (it + 1) * TC_TK + 8 * g;
                     load8<FB>(B, idx0 + (int64_t)kf * ldb, ldb, cv ? n_valid(K, kf) : 0, nxt);
                 }
-                if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh)) {
+                if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
                     abort_sh = 1;
                     break;
                 }
@@ -538,8 +547,12 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     constexpr bool STAGE = 2 * SB >= TC_TM * TROW * 16;
     float4* tile = reinterpret_cast<float4*>(base);
     if (warp < 8) {
-        bool ok = mbar_wait(&bar_done, 0, &abort_sh) && !abort_sh;
-        ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld is warp-collective
+        // A time-out here is an abort too; after the named barrier every
+        // epilogue warp sees the same flag (nothing sets it once every MMA has
+        // completed), so either the whole tile is written or none of it.
+        if (!mbar_wait(&bar_done, 0, &abort_sh, wait_limit)) abort_sh = 1;
+        asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
+        const bool ok = !abort_sh;
         tc_fence_after();
         const int q = warp & 3, h = warp >> 2;  // TMEM lanes 32q .. 32q+31; complex columns 32h .. 32h+31
         const int r = row0 + 32 * q + lane;
@@ -763,7 +776,7 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
         kern<<<grid, TC_THREADS, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
                                                 static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
                                                 EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err, accumulate,
-                                                Ecol ? Ecol + b0 * Nc : nullptr);
+                                                Ecol ? Ecol + b0 * Nc : nullptr, tc_wait_limit());
         TBG_LAUNCHED(name);
     }
     return TBG_OK;
@@ -889,9 +902,19 @@ int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A,
     KTimer kt(st, "ozaki_tc_fourier_kernel", 8.0 * (double)M * Nc * K);
     dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
     kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0,
-                                            nullptr);
+                                            nullptr, tc_wait_limit());
     TBG_LAUNCHED("ozaki_tc_fourier_kernel");
     return TBG_OK;
 }
 
 }  // namespace tbg
+
+// Internal test hook (not part of the public header): the number of polls a
+// tcgen05 stage hand-off wait makes before its CTA gives up and the call
+// reports TBG_E_TIMEOUT; polls <= 0 restores the default.  Returns the previous
+// value.  Lets a test run the time-out path (drain, TMEM release, status)
+// without a fault: the waits that drain in-flight copies and MMAs keep their
+// full bound.
+extern "C" int tbg_internal_tc_wait_limit(int polls) {
+    return tbg::g_tc_wait_limit.exchange(polls > 0 ? polls : tbg::kTcWaitPolls);
+}

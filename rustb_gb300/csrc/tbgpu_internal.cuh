@@ -141,6 +141,7 @@ struct ModelDev {
     int hop_K = 0, hop_np = 0;
     int* hop_pair_d = nullptr;
     zc* pair_T = nullptr;          // the paired table (2 hop_K rows, nsta^2 columns)
+    bool nonfinite = false;        // the table holds NaN or Inf (found when it is paired)
 };
 
 // ------------------------------------------------------------------ errors --

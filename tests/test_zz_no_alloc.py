@@ -53,6 +53,25 @@ def test_noalloc_matches_solve_band_twice(norb, spin, nk):
     assert np.max(np.abs(E[0] - Ez)) <= 1e-10 * nrm
 
 
+def _random_hermitian(rng, nk, n):
+    a = rng.standard_normal((nk, n, n)) + 1j * rng.standard_normal((nk, n, n))
+    return 0.5 * (a + np.conj(np.swapaxes(a, 1, 2)))
+
+
+@pytest.mark.parametrize("n,nk", [(1, 7), (2, 33), (128, SCRATCH_BYTES // (16 * 128 * 128))])
+def test_noalloc_edges_and_exact_capacity(n, nk):
+    """The smallest orders, and a call that fills the array exactly
+    (nk * 16 n^2 == 32 MiB), against LAPACK."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    H = _random_hermitian(np.random.default_rng(n), nk, n)
+    for _ in range(2):
+        E, _ = _noalloc_bands(lib, torch, H)
+        for i in range(0, nk, max(1, nk // 16)):
+            nrm = max(np.linalg.norm(H[i], 2), 1e-300)
+            assert np.max(np.abs(E[i] - O.eigvalsh(H[i]))) <= 1e-10 * nrm
+
+
 def test_noalloc_rejects_oversized_request():
     torch = pytest.importorskip("torch")
     lib = _lib.load()
@@ -64,3 +83,7 @@ def test_noalloc_rejects_oversized_request():
                                   None)
     assert st == errors.TBG_E_UNSUPPORTED
     assert "scratch" in _lib.last_error(lib)
+    # one matrix beyond the array's largest order
+    st = lib.tbg_eigvalsh_noalloc(1449, 1, ctypes.c_void_p(Hd.data_ptr()), ctypes.c_void_p(Ed.data_ptr()), None)
+    assert st == errors.TBG_E_UNSUPPORTED
+    assert "1448" in _lib.last_error(lib)
