@@ -286,7 +286,9 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
     b += sizeof(T) * 4 * (size_t)N;
     b += sizeof(cx<T>) * 4 * (size_t)N;  // tau, v, v2, w
     b += sizeof(T) * 64;
-    size_t s1 = sizeof(T) * 4 * (size_t)N * G;
+    // inverse-iteration scratch; with the matrix in shared memory it lives in
+    // the matrix's storage, free once the reflectors have gone out
+    size_t s1 = a_smem ? 0 : sizeof(T) * 4 * (size_t)N * G;
     // back-transform in the kernel (matrix in global memory): a column-major
     // panel with stride N + 4; with the matrix in shared memory it is a pass
     // of its own (heev_bt_tiled_kernel)
@@ -299,8 +301,10 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 
 // Main kernel.  Hin: (batch, N, N) FP64.  For T = double and !A_SMEM the
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
-template <typename T, bool A_SMEM>
-__global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
+// MINB = CTAs per SM the launch bounds are set for: 3 (320 threads) for the
+// packed matrices of up to about 130 bands, else 2 or 1 (512 threads).
+template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
+__global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    const float4* __restrict__ Hpair, double* __restrict__ Eout,
                                                    cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
                                                    int* __restrict__ status, int G, int PB) {
@@ -330,7 +334,7 @@ __global__ void __launch_bounds__(512, A_SMEM ? 2 : 1) heev_kernel(int N, int64_
         p += sizeof(T) * N;
         sh.red = reinterpret_cast<T*>(p);
         p += sizeof(T) * 64;
-        sh.scratch = reinterpret_cast<T*>(p);
+        sh.scratch = A_SMEM ? reinterpret_cast<T*>(sh.A) : reinterpret_cast<T*>(p);
         // flags close the layout that eig_smem_bytes sizes
         sh.flags = reinterpret_cast<int*>(smem_raw + eig_smem_bytes<T>(N, A_SMEM, G, PB) - sizeof(int) * (4 + (size_t)N));
     }
@@ -987,17 +991,28 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
     }
 }
 
-// Shared memory per CTA: one CTA per SM, or two sharing the SM's 228 KB
-// (1 KB of it reserved per CTA).
+// Shared memory per CTA: one CTA per SM, or two or three sharing the SM's
+// 228 KB (1 KB of it reserved per CTA).
 constexpr size_t kEigSmemOne = 220 * 1024;
 constexpr size_t kEigSmemTwo = 113 * 1024;
+constexpr size_t kEigSmemThree = 75 * 1024;
+
+// Threads of the solver's CTA (one matrix per CTA); FP32 with three CTAs per SM: 320.
+template <typename T>
+inline int eig_threads(int N, int ctas_per_sm = 2) {
+    if (N <= 16) return 32;
+    if (N <= 48) return 128;
+    if (sizeof(T) == sizeof(float)) return ctas_per_sm == 3 ? 320 : 512;
+    return 256;
+}
 
 // Inverse-iteration group G and back-transform panel PB sized to the shared
 // memory left after the matrix (when resident) and the per-matrix vectors.
 template <typename T>
 inline void choose_g_pb(int N, bool a_smem, int gmax, int pbmax, int& G, int& PB, size_t budget = kEigSmemOne) {
     const size_t fixed = eig_smem_bytes<T>(N, a_smem, 0, 0);
-    const size_t left = budget > fixed ? budget - fixed : 0;
+    // with the matrix in shared memory the scratch is the matrix's storage
+    const size_t left = a_smem ? sizeof(cx<T>) * packed_elems<true>(N) : (budget > fixed ? budget - fixed : 0);
     G = (int)std::max<size_t>(1, std::min<size_t>(gmax, left / (sizeof(T) * 4 * (size_t)N)));
     if (a_smem) {
         // the back-transformation is a pass of its own (heev_bt_tiled_kernel):
@@ -1022,17 +1037,17 @@ int allow_max_smem(K kern, size_t need) {
     return TBG_OK;
 }
 
-template <typename T, bool A_SMEM>
+template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
                 size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
-    auto kern = heev_kernel<T, A_SMEM>;
+    auto kern = heev_kernel<T, A_SMEM, MINB>;
     if (int rc = allow_max_smem(kern, smem)) return rc;
     cudaError_t e;
     int dev = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = (N <= 16) ? 32 : (N <= 48 ? 128 : (sizeof(T) == sizeof(float) ? 512 : 256));
+    const int threads = eig_threads<T>(N, MINB);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     int64_t grid = (int64_t)nsm * perSM;
@@ -1073,12 +1088,19 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
 // when both fit (up to about 150 bands).
 inline bool f32_smem_fits(int N, size_t budget, int& G, int& PB) {
     choose_g_pb<float>(N, true, 32, 64, G, PB, budget);
-    return eig_smem_bytes<float>(N, true, G, PB) <= budget && G >= 8 && PB >= std::min(16, (N + 3) & ~3) &&
+    return eig_smem_bytes<float>(N, true, G, PB) <= budget && PB >= std::min(16, (N + 3) & ~3) &&
            bt_tiled_smem_bytes(N, PB) <= kEigSmemOne;
 }
-inline bool f32_in_smem(int N, int& G, int& PB) {
-    return f32_smem_fits(N, kEigSmemTwo, G, PB) || f32_smem_fits(N, kEigSmemOne, G, PB);
+// CTAs per SM of the shared-memory FP32 solver (3, 2 or 1), 0 when the matrix
+// does not fit.  Three (320 threads each) from 49 bands while they fit: the
+// reduction is latency-bound, and a third matrix on the SM hides more of it.
+inline int f32_smem_ctas(int N, int& G, int& PB) {
+    if (N > 48 && f32_smem_fits(N, kEigSmemThree, G, PB)) return 3;
+    if (f32_smem_fits(N, kEigSmemTwo, G, PB)) return 2;
+    if (f32_smem_fits(N, kEigSmemOne, G, PB)) return 1;
+    return 0;
 }
+inline bool f32_in_smem(int N, int& G, int& PB) { return f32_smem_ctas(N, G, PB) > 0; }
 inline bool f32_in_smem(int N) {
     int G, PB;
     return f32_in_smem(N, G, PB);
@@ -1140,7 +1162,11 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
                     size_t work_bytes, int* status_d, const float4* Hpair) {
     if (batch <= 0) return TBG_OK;
     int G, PB;
-    if (f32_in_smem(N, G, PB)) {
+    const int ctas = f32_smem_ctas(N, G, PB);
+    if (ctas == 3)
+        return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                           "heev_kernel<float,smem>", G, PB, Hpair);
+    if (ctas > 0) {
         return launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
                                         G, PB, Hpair);
     }
