@@ -294,6 +294,7 @@ struct BerryJob {
     float4* pairs;  // mixed: H, V_0, V_1 as float pairs (3 chunk N^2)
     bool want_metric;
     double* Met;  // quantum metric (chunk, N) when want_metric
+    const OccSums* occ = nullptr;  // mixed hall path: fused Omega + occupation k-sum
 };
 
 int alloc_berry(Ctx& ctx, BerryJob& J) {
@@ -359,6 +360,9 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
                                   reinterpret_cast<float4*>(J.scratch));
             if (rc) return rc;
         }
+        if (J.occ)
+            return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, nullptr, J.work,
+                               J.work_bytes, J.status_d, clusters_d, nullptr, nullptr, J.occ);
         return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
                            J.status_d, clusters_d, J.Met);
     }
@@ -914,6 +918,19 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
     const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
     const bool small = N <= kSmallMaxN && M.n_rmat == 0;
+    // mixed path without the metric: Omega, occupation and the compensated
+    // k-sum in one kernel (per-CTA partials, added up in block order)
+    OccSums occ;
+    const bool fused = !small && !met && precision == TBG_PREC_MIXED && nmu <= (1 << 20) && occ_fused_ok(N, (int)nmu);
+    if (fused) {
+        occ.nmu = (int)nmu;
+        occ.mu = mu_d;
+        occ.width = width;
+        occ.blocks = occ_sums_blocks(J.chunk);
+        occ.part = ctx.alloc<double>((int64_t)occ.blocks * nmu * 2);
+        if (ctx.rc) return ctx.rc;
+        J.occ = &occ;
+    }
     for (int64_t c0 = 0; c0 < k_count; c0 += J.chunk) {
         const int64_t nkc = std::min(J.chunk, k_count - c0);
         if (small) {
@@ -923,7 +940,12 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
         } else {
             kmesh_kernel<<<blocks_for(nkc), 256, 0, ctx.st>>>(k_begin + c0, nkc, M.dim, n0, n1, n2, J.k_d);
             TBG_LAUNCHED("kmesh_kernel");
+            if (fused) occ.blocks = occ_sums_blocks(nkc);
             if ((rc = run_berry_chunk(ctx, J, nkc, clusters_d))) return rc;
+            if (fused) {
+                if ((rc = occ_partials_add(ctx.st, occ, acc))) return rc;
+                continue;
+            }
             if ((rc = occupation_sums(ctx.st, N, nkc, J.Om, J.E, (int)nmu, mu_d, width, S))) return rc;
             if (met && (rc = occupation_sums(ctx.st, N, nkc, J.Met, J.E, (int)nmu, mu_d, width, SG))) return rc;
         }

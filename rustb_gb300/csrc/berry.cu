@@ -229,13 +229,7 @@ __global__ void z_to_pairs_kernel(int64_t nb, int64_t N2, const zc* __restrict__
     }
 }
 
-__device__ __forceinline__ double fermi(double e, double mu, double width) {
-    if (width == 0.0) return (e < mu) ? 1.0 : ((e > mu) ? 0.0 : 0.5);
-    const double x = (e - mu) / width;
-    if (x > 50.0) return 0.0;
-    if (x < -50.0) return 1.0;
-    return 1.0 / (1.0 + exp(x));
-}
+__device__ __forceinline__ double fermi(double e, double mu, double width) { return occupation_f(e, mu, width); }
 
 __global__ void occupation_kernel(int N, int64_t batch, const double* __restrict__ Om, const double* __restrict__ E,
                                   int nmu, const double* __restrict__ mu, double width, double* __restrict__ S) {
@@ -250,15 +244,11 @@ __global__ void occupation_kernel(int N, int64_t batch, const double* __restrict
     }
 }
 
-__device__ __forceinline__ void kahan_add(double& sum, double& c, double x) {
-    const double y = x - c;
-    const double t = sum + y;
-    c = (t - sum) - y;
-    sum = t;
-}
+__device__ __forceinline__ void kahan_add(double& sum, double& c, double x) { kahan_step(sum, c, x); }
 
-// One block per mu: each thread Kahan-sums a contiguous k segment, then
-// thread 0 combines the partials in order (deterministic).
+// One block per mu: each thread Kahan-sums a contiguous k segment, then the
+// segments are combined along a fixed tree of double-double sums
+// (deterministic).
 __global__ void kahan_kernel(int64_t nk, int nmu, const double* __restrict__ S, double* __restrict__ acc) {
     __shared__ double ps[256], pc[256];
     const int j = blockIdx.x;
@@ -266,15 +256,13 @@ __global__ void kahan_kernel(int64_t nk, int nmu, const double* __restrict__ S, 
     const int64_t b0 = threadIdx.x * seg, b1 = std::min<int64_t>(nk, b0 + seg);
     double s = 0.0, c = 0.0;
     for (int64_t b = b0; b < b1; ++b) kahan_add(s, c, S[b * nmu + j]);
-    ps[threadIdx.x] = s;
-    pc[threadIdx.x] = c;
-    __syncthreads();
+    ps[threadIdx.x] = s;  // the value is s - c
+    pc[threadIdx.x] = -c;
+    dd_block_sum(ps, pc);
     if (threadIdx.x == 0) {
         double tot = acc[2 * j], comp = acc[2 * j + 1];
-        for (int t = 0; t < (int)blockDim.x; ++t) {
-            kahan_add(tot, comp, ps[t]);
-            kahan_add(tot, comp, -pc[t]);
-        }
+        kahan_add(tot, comp, ps[0]);
+        kahan_add(tot, comp, pc[0]);
         acc[2 * j] = tot;
         acc[2 * j + 1] = comp;
     }

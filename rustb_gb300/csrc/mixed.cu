@@ -386,6 +386,136 @@ __global__ void __launch_bounds__(256) berry_df_kernel(int N, int64_t batch, con
     }
 }
 
+// The Berry stage of the hall path in one pass (src/response/traits.rs:181-195
+// and src/response/linear/mod.rs:204-223).  With Bx, By Hermitian the term of
+// the pair (n, m),
+//   T_nm = -2 Im(Bx[n,m] By[m,n]) / ((E_n - E_m)^2 + eta^2) = -2 Im(Bx[n,m] conj(By[n,m])) / (...),
+// enters Omega_n as +T_nm and Omega_m as -T_nm, so only the upper triangles
+// are read: Omega_n = R_n - C_n with the row sums R_n = sum_{m>n} T_nm and
+// the column sums C_m = sum_{n<m} T_nm.  Per k-point, warps take rows n and
+// N-1-n together (equal work), lanes the columns m = n+1+lane, n+33+lane, ...
+// (consecutive addresses); T in float-pair arithmetic as berry_df_kernel;
+// R_n by a warp butterfly, C_m in the lane's registers over the warp's rows and
+// then summed over the warps in a fixed order.  Then S_k(mu_j) = sum_n Omega_n
+// f(E_n, mu_j) (lanes over n, a fixed butterfly) is Kahan-added into this
+// CTA's running sum for mu_j, and the CTA's compensated partials go to part at
+// the end.  No per-band Omega is stored and E need not be sorted.  HBM traffic
+// per k-point: the upper triangles of the two float-pair band-basis velocity
+// matrices (2 x 16 N(N-1)/2 bytes) and E (8 N bytes).  N <= kOccMaxN.
+constexpr int kOccMaxN = 256;
+constexpr int kOccSlots = kOccMaxN / 32;
+__global__ void __launch_bounds__(256) berry_occ_df_kernel(int N, int64_t batch, const float4* __restrict__ Bx,
+                                                           const float4* __restrict__ By, const double* __restrict__ E,
+                                                           float2 eta2, int nmu, const double* __restrict__ mu,
+                                                           double width, double* __restrict__ part) {
+    extern __shared__ double occ_sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double* ed = occ_sm;                                 // N
+    double* om = ed + N;                                 // N: R_n, then Omega_n
+    double* colp = om + N;                               // nw x N column sums
+    double* rs = colp + (size_t)nw * N;                  // nmu running sums
+    double* rc = rs + nmu;                               // nmu compensations
+    float2* e2s = reinterpret_cast<float2*>(rc + nmu);   // N
+    const int64_t NN = (int64_t)N * N;
+    for (int j = threadIdx.x; j < nmu; j += blockDim.x) {
+        rs[j] = 0.0;
+        rc[j] = 0.0;
+    }
+    const int npair = (N + 1) >> 1;  // rows n and N-1-n
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const double e = E[b * N + i];
+            ed[i] = e;
+            e2s[i] = df_of(e);
+        }
+        __syncthreads();
+        float2 cs[kOccSlots];  // column sums of m = 32 q + lane over this warp's rows
+#pragma unroll
+        for (int q = 0; q < kOccSlots; ++q) cs[q] = make_float2(0.f, 0.f);
+        for (int p = warp; p < npair; p += nw) {
+            for (int half = 0; half < 2; ++half) {
+                const int n = half ? N - 1 - p : p;
+                if (half && n == p) break;  // the middle row of an odd N
+                const float4* bx = Bx + b * NN + (int64_t)n * N;
+                const float4* by = By + b * NN + (int64_t)n * N;
+                const float2 en = e2s[n];
+                float2 racc = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < kOccSlots; ++q) {
+                    const int m = 32 * q + lane;
+                    if (m > n && m < N) {
+                        const float4 x = bx[m];
+                        const float4 y = by[m];
+                        // Im(x conj(y)) = x_im y_re - x_re y_im
+                        const float2 t1 = df_mul(make_float2(x.z, x.w), make_float2(y.x, y.y));
+                        const float2 t2 = df_mul(make_float2(x.x, x.y), make_float2(y.z, y.w));
+                        const float2 num = df_add(t1, df_neg(t2));
+                        const float2 de = df_add(en, df_neg(e2s[m]));
+                        const float2 den = df_add(df_mul(de, de), eta2);
+                        const float2 qv = df_div(num, den);
+                        const float2 t = make_float2(-2.f * qv.x, -2.f * qv.y);
+                        racc = df_add(racc, t);
+                        cs[q] = df_add(cs[q], t);
+                    }
+                }
+                racc = df_warp_sum(racc);
+                if (lane == 0) om[n] = df_to_double(racc);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kOccSlots; ++q) {
+            const int m = 32 * q + lane;
+            if (m < N) colp[(size_t)warp * N + m] = df_to_double(cs[q]);
+        }
+        __syncthreads();
+        for (int n = threadIdx.x; n < N; n += blockDim.x) {
+            double c = 0.0;
+            for (int w = 0; w < nw; ++w) c += colp[(size_t)w * N + n];
+            om[n] -= c;
+        }
+        __syncthreads();
+        for (int j = warp; j < nmu; j += nw) {
+            const double mj = mu[j];
+            double t = 0.0;
+            for (int n = lane; n < N; n += 32) t += om[n] * occupation_f(ed[n], mj, width);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) kahan_step(rs[j], rc[j], t);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nmu; j += blockDim.x) {
+        part[((int64_t)blockIdx.x * nmu + j) * 2] = rs[j];
+        part[((int64_t)blockIdx.x * nmu + j) * 2 + 1] = rc[j];
+    }
+}
+
+// acc[2 j], acc[2 j + 1] += the partials of every block: one CTA per mu, each
+// thread Kahan-sums a contiguous range of blocks, and the ranges are combined
+// along a fixed tree (deterministic).
+__global__ void occ_partials_kernel(int blocks, int nmu, const double* __restrict__ part, double* __restrict__ acc) {
+    __shared__ double ps[256], pc[256];
+    const int j = blockIdx.x;
+    const int seg = (blocks + blockDim.x - 1) / blockDim.x;
+    const int t0 = threadIdx.x * seg, t1 = min(blocks, t0 + seg);
+    double sm = 0.0, c = 0.0;
+    for (int t = t0; t < t1; ++t) {
+        kahan_step(sm, c, part[((int64_t)t * nmu + j) * 2]);
+        kahan_step(sm, c, -part[((int64_t)t * nmu + j) * 2 + 1]);
+    }
+    ps[threadIdx.x] = sm;  // the value is sm - c
+    pc[threadIdx.x] = -c;
+    dd_block_sum(ps, pc);
+    if (threadIdx.x == 0) {
+        double tot = acc[2 * j], comp = acc[2 * j + 1];
+        kahan_step(tot, comp, ps[0]);
+        kahan_step(tot, comp, pc[0]);
+        acc[2 * j] = tot;
+        acc[2 * j + 1] = comp;
+    }
+}
+
 // Keep E ascending (with Omega and the metric when given) after refinement;
 // a no-op when already sorted.
 __global__ void sort_e_om_kernel(int N, int64_t batch, double* __restrict__ E, double* __restrict__ Om,
@@ -426,6 +556,21 @@ inline unsigned nblk(int64_t total) {
 
 }  // namespace
 
+int occ_sums_blocks(int64_t batch) { return (int)std::max<int64_t>(1, std::min<int64_t>(batch, 152 * 8)); }
+
+// Dynamic shared memory of berry_occ_df_kernel (256 threads).
+size_t occ_smem_bytes(int N, int nmu) {
+    return (2 + 8) * sizeof(double) * (size_t)N + 2 * sizeof(double) * (size_t)nmu + sizeof(float2) * (size_t)N;
+}
+bool occ_fused_ok(int N, int nmu) { return N <= kOccMaxN && occ_smem_bytes(N, nmu) <= 48 * 1024; }
+
+int occ_partials_add(cudaStream_t st, const OccSums& o, double* acc) {
+    KTimer kt(st, "occ_partials_kernel");
+    occ_partials_kernel<<<o.nmu, 256, 0, st>>>(o.blocks, o.nmu, o.part, acc);
+    TBG_LAUNCHED("occ_partials_kernel");
+    return TBG_OK;
+}
+
 size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     const size_t NN = (size_t)N * N;
     // X and F (cc) + 5 pair buffers + line exponents (10 operand sides) + FP32 solver workspace
@@ -438,7 +583,7 @@ size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
 // not null, the quantum metric.
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met, zc* Uout) {
+                int64_t* clusters_d, double* Met, zc* Uout, const OccSums* occ) {
     if (batch <= 0) return TBG_OK;
     const int64_t NN = (int64_t)N * N;
     if (work_bytes < mixed_berry_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
@@ -509,7 +654,7 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         TBG_LAUNCHED("sort_e_om_kernel");
         return (int)TBG_OK;
     };
-    if (!Om && !Uout) return energies_out();  // band energies only
+    if (!Om && !Uout && !occ) return energies_out();  // band energies only
     // 4. X' = X + X F + X_c F_c  (float pair: hi = X, lo = the rest).  F holds
     // only first-order entries (the cluster rotations F_c are applied in FP64
     // by xprime_kernel), so the LOW class's 2^-21 of each column's largest
@@ -543,7 +688,22 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     if ((rc = hpe(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC, BYC))) return rc;
     if ((rc = hp(true, PAIR, PAIR, bA, bB, bD, XPC, BXC))) return rc;
     if ((rc = hp(true, PAIR, PAIR, bA, bC, bE, XPC, BYC))) return rc;
-    // 6. Omega
+    // 6. Omega (with the occupation k-sum when the caller wants only sums)
+    if (occ) {
+        if (Om || Met || occ->blocks != occ_sums_blocks(batch))
+            return set_error(TBG_E_INVALID_ARGUMENT, "mixed_berry: fused sums take no per-band outputs");
+        KTimer kt(st, "berry_occ_kernel");
+        const double e2 = eta * eta;
+        const float hi = (float)e2;
+        const float2 eta2 = make_float2(hi, (float)(e2 - (double)hi));
+        const size_t smem = occ_smem_bytes(N, occ->nmu);
+        if (N > kOccMaxN || smem > 48 * 1024)
+            return set_error(TBG_E_UNSUPPORTED, "mixed_berry: fused sums beyond 256 bands or too many potentials");
+        berry_occ_df_kernel<<<(unsigned)occ->blocks, 256, smem, st>>>(N, batch, bD, bE, E, eta2, occ->nmu, occ->mu,
+                                                                     occ->width, occ->part);
+        TBG_LAUNCHED("berry_occ_df_kernel");
+        return TBG_OK;
+    }
     {
         KTimer kt(st, "berry_kernel");
         const double e2 = eta * eta;

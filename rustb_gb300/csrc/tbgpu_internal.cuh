@@ -112,6 +112,49 @@ __device__ __forceinline__ float2 df_of(double x) {
 }
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
+// Occupation (src/thermodynamics.rs:100-118): T = 0 step with 1/2 at E == mu,
+// else the Fermi function with its +-50 clamp; width = k_B T.
+__device__ __forceinline__ double occupation_f(double e, double mu, double width) {
+    if (width == 0.0) return (e < mu) ? 1.0 : ((e > mu) ? 0.0 : 0.5);
+    const double x = (e - mu) / width;
+    if (x > 50.0) return 0.0;
+    if (x < -50.0) return 1.0;
+    return 1.0 / (1.0 + exp(x));
+}
+__device__ __forceinline__ void kahan_step(double& sum, double& c, double x) {
+    const double y = x - c;
+    const double t = sum + y;
+    c = (t - sum) - y;
+    sum = t;
+}
+// Double-double sum (hi, lo) + (bh, bl): two-sum of the leading parts, the
+// trailing parts added to the error, renormalised.
+__device__ __forceinline__ void dd_add(double& hi, double& lo, double bh, double bl) {
+    const double s = hi + bh;
+    const double v = s - hi;
+    double e = (hi - (s - v)) + (bh - v);
+    e += lo + bl;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+// Block-wide sum of per-thread double-doubles (ph[t], pl[t]) in shared memory
+// (blockDim.x a power of two, <= 1024) along a fixed binary tree, so the
+// result does not depend on timing; thread 0 gets it in (ph[0], pl[0]).  A
+// tree keeps the dependent FP64 chain at log2(threads) steps (FP64 latency is
+// long on this part).  Ends with a barrier.
+__device__ __forceinline__ void dd_block_sum(double* ph, double* pl) {
+    __syncthreads();
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            double a = ph[threadIdx.x], b = pl[threadIdx.x];
+            dd_add(a, b, ph[threadIdx.x + h], pl[threadIdx.x + h]);
+            ph[threadIdx.x] = a;
+            pl[threadIdx.x] = b;
+        }
+        __syncthreads();
+    }
+}
+
 // -------------------------------------------------------------- model data --
 struct ModelDev {
     int dim = 0, spin = 0;
@@ -292,9 +335,25 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
 // FP32 eigensolve, refinement and rotation on the tensor cores: H, Vx, Vy as
 // float pairs (batch stride N*N) -> refined E (ascending) and Omega.
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);
+// Occupation-weighted k-sum fused with Omega (hall path): per CTA, the
+// compensated partial sums of sum_k sum_n Omega_n f(E_n, mu_j), part[(block
+// nmu + j) 2 + {0: sum, 1: compensation}] for `blocks` CTAs.
+struct OccSums {
+    int nmu = 0;
+    const double* mu = nullptr;  // device
+    double width = 0.0;          // k_B T (0: step function)
+    double* part = nullptr;      // device (blocks, nmu, 2)
+    int blocks = 0;
+};
+int occ_sums_blocks(int64_t batch);
+bool occ_fused_ok(int N, int nmu);  // the fused kernel's band and shared-memory limits
+// acc[2 j] (sum) and acc[2 j + 1] (compensation) += the blocks' partials, in block order.
+int occ_partials_add(cudaStream_t st, const OccSums& o, double* acc);
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr);
+                int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr, const OccSums* occ = nullptr);
+// With occ (and Om, Met null) the Berry stage is the fused Omega + occupation +
+// compensated k-sum kernel: per-band Omega is not stored and E is not sorted.
 // With Uout, mixed_berry stops after the refinement: refined E ascending and the
 // refined eigenvectors (columns, FP64) in Uout; Vx, Vy are not read.  With
 // neither Om nor Uout it stops after the eigenvalue refinement (refined E

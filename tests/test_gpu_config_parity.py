@@ -181,3 +181,18 @@ def test_serving_observables_vs_oracle():
             occ = O.occupied_berry_curvature_on(m, r.k, dirs, r.mu)
             ref = math.fsum(occ) / len(r.k) / float(np.linalg.det(m.lat))
             assert abs(got - ref) <= 1e-6 * abs(ref)
+
+
+# ------------------------------------------ fused Berry + occupation sums --
+@pytest.mark.parametrize("T", [0.0, 300.0])
+def test_mixed_hall_fused_sums_many_mu(T):
+    """The mixed hall path sums Omega_n f(E_n, mu_j) in the fused kernel (upper
+    triangles of the band-basis velocities, per-CTA compensated partials):
+    against the oracle's Direct sums for 40 chemical potentials, T = 0 and
+    300 K, within 1e-6 of the largest |sigma|."""
+    m = W.random_model(3, 24, True, 1, seed=4100)  # 48 bands
+    mus = np.linspace(-1.0, 1.0, 40)
+    p = Parameters.rank2((3, 3, 2), XY3[0], XY3[1], mus).with_temperature(T)
+    s = m.hall_conductivity(p, Precision.MIXED).conductivity
+    ref = O.hall_conductivity(m, (3, 3, 2), XY3, mus, T)
+    assert np.max(np.abs(s - ref)) <= 1e-6 * np.max(np.abs(ref))
