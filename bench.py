@@ -251,6 +251,7 @@ def main():
     ap.add_argument("--workload", choices=["random3d", "haldane", "batched", "supercell", "serve", "dos", "w90", "wilson", "ec", "eig-small"],
                     default="random3d")
     ap.add_argument("--models", type=int, default=64, help="batched: models taken from the 512-model set")
+    ap.add_argument("--kcap", type=int, default=0, help="batched: first k-points of each mesh (0 = whole meshes)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     args = ap.parse_args()
     rank, world, local = dist_env()

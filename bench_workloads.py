@@ -216,15 +216,17 @@ def batched(args, rank, world, local):
     n = args.models
     specs_all = W.batched_uneven_specs(512)
     idx = list(range(n // 2)) + list(range(256, 256 + n - n // 2))
+    kcap = args.kcap if args.kcap > 0 else None
     jobs = []
     for i in idx:
         dim, norb, mesh, seed = specs_all[i]
         m = W.random_model(dim, norb, False, 3, seed=seed)
-        jobs.append(batch.Job(m, Parameters(kmesh=mesh, direction=np.eye(dim)[:2], mu=[0.0])))
-    nk = sum(int(np.prod(j.params.kmesh)) for j in jobs)
-    flops = sum(int(np.prod(j.params.kmesh)) * batch._work_per_k(j.model) for j in jobs)
+        jobs.append(batch.Job(m, Parameters(kmesh=mesh, direction=np.eye(dim)[:2], mu=[0.0]), k_limit=kcap))
+    nk = sum(j.k_count() for j in jobs)
+    flops = sum(j.k_count() * batch._work_per_k(j.model) for j in jobs)
     cfg = {"workload": f"batched uneven: {len(jobs)} of the 512 seeded models (norb log-uniform [4,256], half 2D "
-                       "R|<=3 (49 R), half 3D (343 R), meshes 32^2-128^2 / 16^3-48^3), sigma_xy mu=0",
+                       "R|<=3 (49 R), half 3D (343 R), meshes 32^2-128^2 / 16^3-48^3), sigma_xy mu=0"
+                       + (f", the first {kcap} points of each mesh" if kcap else ", whole meshes"),
            "models": len(jobs), "k_points": nk}
     if args.impl == "reference":
         j = max(jobs, key=lambda j: j.model.nsta)
@@ -245,10 +247,19 @@ def batched(args, rank, world, local):
     for _ in range(args.steps):
         runner.hall_many(jobs)
     dt = (time.perf_counter() - t0) / args.steps
+    # per-bucket breakdown: the same jobs, one bucket at a time
+    per_bucket = {}
+    for b in sorted({batch.bucket_of(j.model.nsta) for j in jobs}):
+        sub = [j for j in jobs if batch.bucket_of(j.model.nsta) == b]
+        t1 = time.perf_counter()
+        runner.hall_many(sub)
+        tb = time.perf_counter() - t1
+        fb = sum(j.k_count() * batch._work_per_k(j.model) for j in sub)
+        per_bucket[str(b)] = {"models": len(sub), "seconds": tb, "tflops": fb / tb / 1e12}
     _line(args, world, "algorithmic GFLOP/s (batched uneven models)", flops / dt / 1e9, "GFLOP/s", dt * 1e3,
           "f32 eigensolve + exact-slice tensor products", cfg,
           {"k_pts_per_s": nk / dt, "plan": runner.stats["plan"], "items": runner.stats["items"],
-           "workers": runner.stats["workers"]})
+           "workers": runner.stats["workers"], "per_bucket": per_bucket})
     return 0
 
 

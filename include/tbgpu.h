@@ -400,6 +400,13 @@ int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms,
  * concurrent calls by device footprint). */
 int64_t tbg_chunk_budget_bytes(void);
 
+/* Crossover of the FP64 eigensolvers: matrices of 9 .. n bands go to the
+ * warp-per-matrix cyclic Jacobi solver, larger ones to the Householder
+ * solver (n is clamped to [8, 32]; 8 = Householder from 9 bands on, the
+ * default).  Process-wide; returns the previous value.  A tuning knob for the
+ * batch autotuner (no reference counterpart). */
+int tbg_set_jacobi_max_n(int n);
+
 /* Library version string, e.g. "tbgpu 0.1.0 sm_103a". */
 const char* tbg_version(void);
 

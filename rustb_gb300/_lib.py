@@ -128,6 +128,7 @@ SIGNATURES = [
     ("tbg_batch_wait", ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     ("tbg_batch_set_workers", ctypes.c_int, [ctypes.c_int]),
     ("tbg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    ("tbg_set_jacobi_max_n", ctypes.c_int, [ctypes.c_int]),
     ("tbg_version", ctypes.c_char_p, []),
     ("tbg_kernel_launch_count", ctypes.c_int64, [ctypes.c_int]),
 ]

@@ -46,10 +46,19 @@ def bucket_of(nsta: int) -> int:
 class Job:
     model: Model
     params: Parameters
+    # only the first k_limit points of the mesh (flat gen_kmesh order): the
+    # result is then that partial sum / (nk det), as tbg_hall_sums_range gives it
+    k_limit: int | None = None
+
+    def k_count(self) -> int:
+        nk = int(np.prod(self.params.kmesh))
+        return nk if self.k_limit is None else min(nk, int(self.k_limit))
 
 
 class Autotuner:
-    """Chooses (chunk k-points, concurrent items) per (bucket, precision)."""
+    """Chooses (chunk k-points, concurrent items) per (bucket, precision), and
+    for the FP64 path the band count up to which the warp-per-matrix Jacobi
+    solver replaces the Householder one (timed on the 16- and 32-band buckets)."""
 
     CHUNKS = (256, 1024, 4096, 16384)
     WORKERS = (1, 2, 4)
@@ -71,10 +80,47 @@ class Autotuner:
     def get(self, bucket: int, precision: int):
         return self.table.get(self.key(bucket, precision))
 
+    def crossover(self, jobs: list, buckets: dict, lib) -> int:
+        """Jacobi/Householder crossover for the FP64 solver: for each of the
+        16- and 32-band buckets present, time one job's first k-points with the
+        Householder solver alone (crossover 8) and with Jacobi up to the bucket
+        size; the crossover is the largest bucket where Jacobi was faster."""
+        key = f"{self.gpu}|crossover"
+        with self.lock:
+            if key in self.table:
+                return int(self.table[key])
+        best = 8
+        for b in (16, 32):
+            if b not in buckets:
+                continue
+            j = jobs[max(buckets[b], key=lambda i: jobs[i].model.nsta)]
+            nk = min(4096, int(np.prod(j.params.kmesh)))
+            times = {}
+            for cross in (8, b):
+                lib.tbg_set_jacobi_max_n(cross)
+                _run_range(lib, j.model, j.params, int(Precision.FP64), 0, min(nk, 64))
+                t0 = time.perf_counter()
+                _run_range(lib, j.model, j.params, int(Precision.FP64), 0, nk)
+                times[cross] = time.perf_counter() - t0
+            if times[b] < times[8]:
+                best = b
+        lib.tbg_set_jacobi_max_n(best)
+        with self.lock:
+            self.table[key] = best
+            self._save()
+        return best
+
+    def _save(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            json.dump(self.table, open(self.path, "w"), indent=1)
+        except OSError:
+            pass
+
     def tune(self, bucket: int, precision: int, job: Job, lib) -> dict:
         """Time each candidate on a slice of this job's mesh."""
         m, p = job.model, job.params
-        nk = int(np.prod(p.kmesh))
+        nk = job.k_count()
         best = None
         for chunk in self.CHUNKS:
             if chunk > max(256, nk):
@@ -91,11 +137,7 @@ class Autotuner:
                     best = {"chunk": chunk, "workers": workers, "rate": rate}
         with self.lock:
             self.table[self.key(bucket, precision)] = best
-            try:
-                os.makedirs(os.path.dirname(self.path), exist_ok=True)
-                json.dump(self.table, open(self.path, "w"), indent=1)
-            except OSError:
-                pass
+            self._save()
         return best
 
 
@@ -128,17 +170,20 @@ class BatchRunner:
         for idx, j in enumerate(jobs):
             buckets.setdefault(bucket_of(j.model.nsta), []).append(idx)
         plan = {}
+        if self.precision == int(Precision.FP64):
+            # the crossover is process-wide; without tuning the library's setting stands
+            self.crossover = self.tuner.crossover(jobs, buckets, self.lib) if self.autotune else None
         for b, idxs in buckets.items():
             cfg = self.tuner.get(b, self.precision)
             if cfg is None and self.autotune:
-                probe = max(idxs, key=lambda i: np.prod(jobs[i].params.kmesh))
+                probe = max(idxs, key=lambda i: jobs[i].k_count())
                 cfg = self.tuner.tune(b, self.precision, jobs[probe], self.lib)
             plan[b] = cfg or {"chunk": 4096, "workers": 2}
         items = []
         for b, idxs in buckets.items():
             chunk = plan[b]["chunk"]
             for i in idxs:
-                nk = int(np.prod(jobs[i].params.kmesh))
+                nk = jobs[i].k_count()
                 for k0 in range(0, nk, chunk):
                     cost = min(chunk, nk - k0) * _work_per_k(jobs[i].model)
                     items.append((cost, i, k0, min(chunk, nk - k0)))
@@ -165,7 +210,8 @@ class BatchRunner:
             sig = np.array([math.fsum(arr[:, c]) for c in range(arr.shape[1])]) / nk / det
             out.append(HallConductivityResult(chemical_potentials=j.params.mu.copy(), conductivity=sig))
         self.stats = {"seconds": dt, "items": len(items), "workers": workers, "plan": plan,
-                      "k_points": sum(int(np.prod(j.params.kmesh)) for j in jobs)}
+                      "jacobi_crossover": getattr(self, "crossover", None),
+                      "k_points": sum(j.k_count() for j in jobs)}
         return out
 
 

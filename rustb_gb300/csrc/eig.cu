@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
@@ -1114,13 +1115,17 @@ size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
-int jacobi_max_n() {
-    static const int v = [] {
+// Largest band count the FP64 driver sends to the warp-per-matrix Jacobi
+// solver: TBG_JACOBI_MAX_N at load, then whatever tbg_set_jacobi_max_n sets
+// (the batch autotuner times both solvers per band-count bucket).
+std::atomic<int>& jacobi_max_n_ref() {
+    static std::atomic<int> v{[] {
         const char* s = std::getenv("TBG_JACOBI_MAX_N");
         return s ? std::max(0, std::min(std::atoi(s), kJacobiMaxN)) : kSmallMaxN;
-    }();
+    }()};
     return v;
 }
+int jacobi_max_n() { return jacobi_max_n_ref().load(std::memory_order_relaxed); }
 
 // FP64 driver (plain path): A destroyed, U complex<double>.
 int eig_batched(cudaStream_t st, int N, int64_t batch, zc* A, double* E, zc* U, void* work,
@@ -1275,4 +1280,10 @@ extern "C" int tbg_internal_eig_f32(int n, int64_t nk, const double* H, double* 
     cudaFree(dS);
     cudaFree(dW);
     return rc;
+}
+
+// Crossover between the FP64 solvers (see include/tbgpu.h); returns the previous value.
+extern "C" int tbg_set_jacobi_max_n(int n) {
+    using namespace tbg;
+    return jacobi_max_n_ref().exchange(std::max(kSmallMaxN, std::min(n, kJacobiMaxN)));
 }

@@ -19,15 +19,20 @@ def test_batch_runner_matches_single_calls(tmp_path):
         m = W.random_model(dim, norb, spin, 1, seed=300 + i)
         dirs = np.eye(dim)[:2]
         jobs.append(batch.Job(m, Parameters(kmesh=mesh, direction=dirs, mu=[-0.2, 0.0, 0.3])))
+    lib = batch._lib.load()
+    prev = lib.tbg_set_jacobi_max_n(8)
     for prec in (Precision.FP64, Precision.MIXED):
         runner = batch.BatchRunner(prec, autotune=True, cache_path=str(tmp_path / "tune.json"), max_workers=3)
         res = runner.hall_many(jobs)
         assert runner.stats["items"] >= len(jobs)
+        if prec == Precision.FP64:  # the 9-band model puts the 16-band bucket up for the Jacobi crossover
+            assert runner.stats["jacobi_crossover"] in (8, 16)
         for j, r in zip(jobs, res):
             single = j.model.hall_conductivity(j.params, prec).conductivity
             assert np.max(np.abs(r.conductivity - single)) <= 1e-12 * max(np.max(np.abs(single)), 1e-12)
     ref = O.hall_conductivity(jobs[0].model, (9, 9), np.eye(2), [-0.2, 0.0, 0.3])
     assert np.max(np.abs(res[0].conductivity - ref)) <= 1e-8 * np.max(np.abs(ref))
+    lib.tbg_set_jacobi_max_n(prev)
 
 
 def test_server_results_equal_alone_and_in_the_mix():
