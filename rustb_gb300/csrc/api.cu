@@ -267,11 +267,26 @@ double lattice_det(const std::vector<double>& lat, int dim) {
 // products) run the FP64 path (reported in tbg_report).
 int effective_precision(const ModelDev& M, int precision) {
     // the tcgen05 products run longer contractions in exact chunks of 256; the
-    // mma.sync form (selectable for comparison) stops at 256
-    if (precision == TBG_PREC_MIXED && (M.nsta > kMixedMaxN || (M.nsta > 256 && !ozaki_use_tc())))
+    // mma.sync form (selectable for comparison) stops at 256.  Models of at
+    // most kSmallMaxN states run FP64 (the small-model kernel, or the batched
+    // FP64 pipeline, which at these sizes is faster than 128-row tensor tiles).
+    if (precision == TBG_PREC_MIXED &&
+        (M.nsta > kMixedMaxN || (M.nsta > 256 && !ozaki_use_tc()) || M.nsta <= kSmallMaxN))
         return TBG_PREC_FP64;
     return precision;
 }
+
+}  // namespace
+
+int small_max_nr() {
+    static const int v = [] {
+        const char* s = std::getenv("TBG_SMALL_MAX_NR");
+        return s ? std::max(0, std::atoi(s)) : 32;
+    }();
+    return v;
+}
+
+namespace {
 
 // Shared per-chunk response pipeline: (k on device) -> Omega, E.
 struct BerryJob {
@@ -401,7 +416,7 @@ struct MeshEnergies {
         kmesh = km;
         const int N = (int)m.nsta;
         const int64_t NN = (int64_t)N * N;
-        small = N <= kSmallMaxN;
+        small = use_small_fused(m);
         // the fused small-model kernel has no batch limit: one chunk of up to 2^21 k-points
         chunk = small ? std::max<int64_t>(1, std::min<int64_t>({nk, int64_t(1) << 21,
                                                                 chunk_budget_bytes() / (16 * N + 64 + extra_per_k)}))
@@ -792,7 +807,7 @@ static int berry_common(const tbg_model* m, int64_t nk, const double* k, const d
     TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * M.dim, cudaMemcpyHostToDevice, ctx.st));
     if (nmu > 0) TBG_CUDA(cudaMemcpyAsync(mu_d, mu, sizeof(double) * nmu, cudaMemcpyHostToDevice, ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
-    const bool small = N <= kSmallMaxN && M.n_rmat == 0;
+    const bool small = use_small_fused(M);
     for (int64_t c0 = 0; c0 < nk; c0 += J.chunk) {
         const int64_t nkc = std::min(J.chunk, nk - c0);
         TBG_CUDA(cudaMemcpyAsync(J.k_d, k + c0 * M.dim, sizeof(double) * nkc * M.dim, cudaMemcpyHostToDevice, ctx.st));
@@ -917,7 +932,7 @@ static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, 
     TBG_CUDA(cudaMemsetAsync(clusters_d, 0, sizeof(int64_t), ctx.st));
     const double width = (T <= 0.0) ? 0.0 : T * 8.617333262145e-5;
     const int64_t n0 = kmesh[0], n1 = M.dim > 1 ? kmesh[1] : 1, n2 = M.dim > 2 ? kmesh[2] : 1;
-    const bool small = N <= kSmallMaxN && M.n_rmat == 0;
+    const bool small = use_small_fused(M);
     // mixed path without the metric: Omega, occupation and the compensated
     // k-sum in one kernel (per-CTA partials, added up in block order)
     OccSums occ;

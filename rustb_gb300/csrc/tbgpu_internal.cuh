@@ -285,6 +285,14 @@ int small_fused(const ModelDev& m, cudaStream_t st, int64_t nk, const double* kl
                 const int64_t* kmesh, const double* dirs_d, int spin, double eta, int nmu, const double* mu_d,
                 double width, double* Om, double* E, double* S, double* Met = nullptr, double* SM = nullptr);
 constexpr int kSmallMaxN = 8;
+// The one-thread-per-k small-model kernel serves models of up to kSmallMaxN
+// states whose hop table has at most small_max_nr() vectors (TBG_SMALL_MAX_NR
+// overrides the default); larger tables go through the batched FP64 pipeline,
+// whose Fourier sum spreads each k-point's R sum over many threads.
+int small_max_nr();
+inline bool use_small_fused(const ModelDev& m) {
+    return m.nsta <= kSmallMaxN && m.n_rmat == 0 && m.nR <= small_max_nr();
+}
 // Eigenpairs of N <= kSmallMaxN matrices by per-thread Jacobi (E ascending,
 // U columns; U may be null; non-finite input sets bit 0 of *status).
 int eig_small(cudaStream_t st, int N, int64_t batch, const zc* H, double* E, zc* U, int* status);

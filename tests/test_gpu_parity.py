@@ -435,3 +435,26 @@ def test_large_models_eigenvalues_and_berry(norb, spin):
         assert np.max(np.abs(Em - Er)) <= 1e-9 * np.linalg.norm(Hs[0], 2)
         occ = Er[0] < 0
         assert abs((Omm[0] * occ).sum() - (Omr[0] * occ).sum()) <= 1e-6 * np.abs(Omr[0]).sum()
+
+
+@pytest.mark.parametrize("norb,spin", [(6, False), (4, True)])
+def test_small_models_with_large_tables_take_the_batched_path(norb, spin):
+    """Models of at most 8 states with more than 32 R vectors (3D, |R_i| <= 3:
+    343 R) run the batched FP64 pipeline instead of the one-thread-per-k
+    kernel; MIXED requests on them run FP64.  Against the oracle."""
+    m = W.random_model(3, norb, spin, 3, seed=910 + norb)
+    assert m.nR == 343
+    k = np.random.default_rng(norb).uniform(0, 1, (23, 3))
+    p = Parameters.rank2((1, 1, 1), XY3[0], XY3[1], [0.0])
+    Omr, Er = O.berry_on(m, k, XY3)
+    for prec in (Precision.FP64, Precision.MIXED):
+        Om, E = m.berry_curvature_on(k, p, prec)
+        assert np.max(np.abs(E - Er)) <= 1e-10 * np.max(np.abs(Er))
+        assert rel(Om, Omr) < 1e-8
+        assert np.max(np.abs(m.solve_band_all_parallel(k, prec) - Er)) <= 1e-10 * np.max(np.abs(Er))
+    mus = np.array([-0.3, 0.0, 0.4])
+    ph = Parameters.rank2((3, 3, 2), XY3[0], XY3[1], mus)
+    ref = O.hall_conductivity(m, (3, 3, 2), XY3, mus)
+    for prec in (Precision.FP64, Precision.MIXED):
+        s = m.hall_conductivity(ph, prec).conductivity
+        assert np.max(np.abs(s - ref)) <= 1e-8 * np.max(np.abs(ref))
