@@ -101,3 +101,21 @@ def test_ozaki_tc_low_long_contraction():
     B = rng.standard_normal((2, 700, 48)) + 1j * rng.standard_normal((2, 700, 48))
     C = ozaki(lib, A, B, False, False, 1)
     assert np.abs(C - A @ B).max() / (np.abs(A).max() * np.abs(B).max() * 700) < 1e-5
+
+
+@pytest.mark.parametrize("conj_a", [False, True])
+def test_ozaki_tc_many_tiles_per_cta(conj_a):
+    """More tiles than SMs: every persistent CTA runs several tiles back to
+    back (ragged edges in rows, columns and k), HIGH class within 1e-12."""
+    lib = _lib.load()
+    rng = np.random.default_rng(77 + conj_a)
+    batch, M, Nc, K = 200, 200, 130, 100
+    shapeA = (batch, K, M) if conj_a else (batch, M, K)
+    A = rng.standard_normal(shapeA) + 1j * rng.standard_normal(shapeA)
+    B = rng.standard_normal((batch, K, Nc)) + 1j * rng.standard_normal((batch, K, Nc))
+    B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
+    opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
+    ref = opA @ B
+    C = ozaki(lib, A, B, conj_a, True, 1)
+    scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
+    assert (np.abs(C - ref) / scale).max() < 1e-12
