@@ -308,7 +308,8 @@ template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
 __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    const float4* __restrict__ Hpair, double* __restrict__ Eout,
                                                    cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
-                                                   int* __restrict__ status, int G, int PB) {
+                                                   int* __restrict__ status, int G, int PB,
+                                                   const float* __restrict__ tri_de) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     EigShared<T> sh;
     {
@@ -354,6 +355,16 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
         } else {
             A = Awork + (size_t)blockIdx.x * NN;
         }
+        if (tri_de) {
+            // tridiagonal form given (TMEM-resident reduction): d then e
+            const float* src = tri_de + (size_t)b * 2 * N;
+            for (int i = tid; i < N; i += nthr) {
+                sh.d[i] = (T)src[i];
+                sh.e[i] = (T)src[N + i];
+            }
+            if (tid == 0) sh.flags[0] = 0;
+            __syncthreads();
+        } else {
         // ---------------------------------------------------------- load --
         if (Hpair) {
             // float-pair input {re_hi, re_lo, im_hi, im_lo} (FP32 solver only)
@@ -508,6 +519,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
             sh.e[N - 1] = 0;
         }
         __syncthreads();
+        }  // reduction
         // deflation: off-diagonals below eps (|d_i| + |d_i+1|) are set to zero,
         // as QR-type solvers do, so decoupled 1x1 blocks give d_i exactly
         for (int i = tid; i < N; i += nthr) {
@@ -520,7 +532,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
         if constexpr (A_SMEM) {
             // reflectors (packed rows) and tau to the back-transformation pass;
             // the matrix's shared memory then serves the eigenvector scratch
-            if (Uout) {
+            if (Uout && !tri_de) {
                 const size_t pe = packed_elems<true>(N);
                 cx<T>* dst = Awork + (size_t)b * (pe + N);
                 for (size_t i = tid; i < pe; i += nthr) dst[i] = A[i];
@@ -1040,7 +1052,8 @@ int allow_max_smem(K kern, size_t need) {
 
 template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
-                size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr) {
+                size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr,
+                const float* tri_de = nullptr) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
     auto kern = heev_kernel<T, A_SMEM, MINB>;
     if (int rc = allow_max_smem(kern, smem)) return rc;
@@ -1066,9 +1079,10 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
     {
         // flops as LAPACK counts them: 16/3 N^3 (reduction) + 8 N^3 (back-transformation, a
         // separate pass when the matrix is in shared memory) + O(N^2) per matrix
-        KTimer kt(st, name, (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N * batch);
+        // (the tridiagonal stage alone, O(N^2) per matrix, is counted as no flops)
+        KTimer kt(st, name, tri_de ? 0.0 : (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N * batch);
         kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work),
-                                                    status_d, G, PB);
+                                                    status_d, G, PB, tri_de);
         TBG_LAUNCHED(name);
     }
     if constexpr (A_SMEM) {
@@ -1111,7 +1125,10 @@ inline bool f32_in_smem(int N) {
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (precision == 0) return 0;
-    if (f32_in_smem(N)) return sizeof(cc) * (packed_elems<true>(N) + N) * (size_t)std::max<int64_t>(batch, 1);
+    // reflectors (packed rows) and tau, then the tridiagonal forms of the TMEM-resident reduction
+    if (f32_in_smem(N))
+        return (sizeof(cc) * (packed_elems<true>(N) + N) + sizeof(float) * 2 * (size_t)N) *
+               (size_t)std::max<int64_t>(batch, 1);
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
@@ -1157,7 +1174,7 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB, nullptr);
     TBG_LAUNCHED("heev_kernel<double> (static scratch)");
     return TBG_OK;
 }
@@ -1168,6 +1185,17 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
     if (batch <= 0) return TBG_OK;
     int G, PB;
     const int ctas = f32_smem_ctas(N, G, PB);
+    if (ctas == 3 && N > 64 && hetrd_tc_fits(N) && eig_tc_enabled()) {
+        // reduction with the matrix in TMEM (tcgen05 rank-2 updates), then the
+        // tridiagonal stage and the back-transformation pass
+        const size_t vt = sizeof(cc) * (packed_elems<true>(N) + N) * (size_t)batch;
+        if (work_bytes < vt + hetrd_tc_de_bytes(N, batch))
+            return set_error(TBG_E_OOM, "eigensolver workspace too small for the reduction's output");
+        float* de = reinterpret_cast<float*>(static_cast<unsigned char*>(work) + vt);
+        if (int rc = hetrd_tc(st, N, batch, Hpair, H, static_cast<cc*>(work), de, status_d)) return rc;
+        return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                           "heev_tri_kernel<float>", G, PB, Hpair, de);
+    }
     if (ctas == 3)
         return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
                                            "heev_kernel<float,smem>", G, PB, Hpair);

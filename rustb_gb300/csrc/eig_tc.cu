@@ -1,0 +1,426 @@
+// Householder tridiagonalisation of batched Hermitian matrices of up to 128
+// bands with the matrix resident in tensor memory and its rank-2 updates on
+// the tensor cores: the reduction stage of the FP32 eigensolver of the mixed
+// path (LAPACK zhetrd's role inside Rustb's eigh, src/response/traits.rs:168
+// and src/ndarray_lapack.rs:412-448).
+//
+// One CTA (8 warps) per matrix, two CTAs per SM.  The whole matrix A (not
+// only a triangle) lives in TMEM as FP32: lane i = row i, column 2 l =
+// Re A(i, l), column 2 l + 1 = Im A(i, l); rows and columns past N are zero
+// and stay zero.  Step j (trailing block rows/columns j+1 .. N-1):
+//
+//   1. column j of the current matrix: read from TMEM during step j-1's
+//      matrix-vector product (before step j-1's update reached TMEM) and
+//      corrected here by that update, a_i -= v_i conj(w_j) + w_i conj(v_j);
+//      reflector H_j = I - tau v v^H with H_j^H [alpha; x] = [beta; 0]
+//      (beta real, sign opposite to Re alpha), v_{j+1} = 1;
+//   2. p = A22 v: the trailing columns in chunks of 8 complex, alternate
+//      chunks to the two warps of a lane quarter; each thread reads its row's
+//      chunks from TMEM (tcgen05.ld) and multiplies with v in FP32; the two
+//      shares meet in shared memory; y = tau p;
+//   3. w = y - 1/2 tau (y^H v) v;
+//   4. A -= v w^H + w v^H as one tcgen05.mma.kind::tf32 pair accumulating
+//      into the TMEM-resident matrix (M = 128 rows, N = the real columns from
+//      the first 8-column group the update touches, K = 8): the rank-2
+//      complex update in the real embedding is
+//        Re dA = [Re v, Im v, Re w, Im w] . [Re w, Im w, Re v, Im v]^T,
+//        Im dA = [Re v, Im v, Re w, Im w] . [-Im w, Re w, -Im v, Re v]^T,
+//      with each operand split into TF32 hi + lo (3xTF32: hi.hi + lo.hi in
+//      one MMA of K = 8 against [b_hi | b_hi], hi.lo in a second against
+//      [b_lo | 0]), about FP32 accuracy; the A operand is stored negated.
+//      The MMA runs while the next step forms its reflector; the next
+//      matrix-vector product waits for it on an mbarrier.
+//
+// Output, per matrix: the tridiagonal (d, e) for the solver's multisection /
+// twisted-factorisation stage, and the reflectors (packed rows) with tau in
+// the layout the blocked back-transformation pass reads.  The reflectors and
+// tau are the ones the shared-memory reduction forms (the same algorithm; the
+// products are rounded differently).
+//
+// Every wait is bounded; on a time-out the CTA records status bit 2, waits
+// (bounded) for its committed MMAs, frees TMEM and stops.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdlib>
+
+#include "tbgpu_internal.cuh"
+#include "tc_ptx.cuh"
+
+namespace tbg {
+namespace {
+
+using namespace tc;
+
+constexpr int HT_THREADS = 256;  // warp w: TMEM lanes 32 (w % 4) .. +31 (rows), column half w / 4
+constexpr int HT_NC = 128;       // complex columns held per row
+constexpr int HT_MAXN = 128;
+constexpr uint32_t HT_TMEM_COLS = 2 * HT_NC;
+// Dynamic shared memory: operand tiles A (4 KB), B1, B2 (8 KB each), then the
+// per-matrix vectors.  80 KB keeps at most two CTAs (512 TMEM columns) per SM.
+constexpr size_t HT_SMEM = 80 * 1024;
+constexpr int OPA_BYTES = 128 * 32, OPB_BYTES = 2 * HT_NC * 32;
+
+// instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major, M = 128; N (bits 17..22, N / 8) per call
+constexpr uint32_t IDESC_TF32_M128 = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 4) << 24);
+__device__ __forceinline__ uint32_t idesc_tf32(uint32_t n) { return IDESC_TF32_M128 | ((n >> 3) << 17); }
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc)
+        : "memory");
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Byte offset of row r, K group kc (4 tf32 values) in an operand tile: K-major
+// core matrices of 8 rows x 16 bytes; K-adjacent ones 128 bytes apart
+// (descriptor LBO), 8-row groups 256 bytes apart (SBO).
+__device__ __forceinline__ uint32_t op_off(int r, int kc) {
+    return (uint32_t)((r >> 3) * 256 + kc * 128 + (r & 7) * 16);
+}
+
+__device__ __forceinline__ float ht_warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void split4(float a, float b, float c, float d, uint4& hi, uint4& lo) {
+    const float h0 = tf32_rna(a), h1 = tf32_rna(b), h2 = tf32_rna(c), h3 = tf32_rna(d);
+    hi = make_uint4(__float_as_uint(h0), __float_as_uint(h1), __float_as_uint(h2), __float_as_uint(h3));
+    lo = make_uint4(__float_as_uint(tf32_rna(a - h0)), __float_as_uint(tf32_rna(b - h1)),
+                    __float_as_uint(tf32_rna(c - h2)), __float_as_uint(tf32_rna(d - h3)));
+}
+
+__host__ __device__ __forceinline__ size_t ht_diag_off(int N, int i) {
+    return (size_t)i * N - ((size_t)i * (size_t)(i - 1)) / 2;
+}
+__host__ __device__ __forceinline__ size_t ht_packed_elems(int N) { return ((size_t)N * (N + 1) / 2 + 1) & ~(size_t)1; }
+
+// Hpair: float pairs {re_hi, re_lo, im_hi, im_lo} (batch, N, N), or Hz:
+// complex FP64.  Vt: (batch, packed + N) reflectors (packed rows) and tau;
+// de: (batch, 2 N) d then e.
+__global__ void __launch_bounds__(HT_THREADS, 2)
+    hetrd_tc_kernel(int N, int64_t batch, const float4* __restrict__ Hpair, const zc* __restrict__ Hz,
+                    cc* __restrict__ Vt, float* __restrict__ de, int* __restrict__ status, int wait_limit) {
+    extern __shared__ __align__(1024) unsigned char ht_smem[];
+    __shared__ __align__(8) uint64_t bar_mma, bar_ops;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ volatile int abort_sh;
+    __shared__ cc alpha_sh;
+    __shared__ float red[20];
+    unsigned char* opA = reinterpret_cast<unsigned char*>(((uintptr_t)ht_smem + 127) & ~(uintptr_t)127);
+    unsigned char* opB1 = opA + OPA_BYTES;
+    unsigned char* opB2 = opB1 + OPB_BYTES;
+    cc* vbuf = reinterpret_cast<cc*>(opB2 + OPB_BYTES);
+    cc* wbuf = vbuf + HT_MAXN;
+    cc* colbuf = wbuf + HT_MAXN;
+    cc* pbuf = colbuf + HT_MAXN;   // half 1's share of p
+    cc* p0buf = pbuf + HT_MAXN;    // half 0's share of p
+    float* dsm = reinterpret_cast<float*>(p0buf + HT_MAXN);
+    float* esm = dsm + HT_MAXN;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int q = warp & 3, h = warp >> 2;
+    const int i = 32 * q + lane;  // this thread's row (TMEM lane)
+    const size_t NN = (size_t)N * N, pe = ht_packed_elems(N);
+    const uint32_t sA = su32(opA), sB1 = su32(opB1), sB2 = su32(opB2);
+
+    if (tid == 0) {
+        mbar_init(&bar_mma, 1);
+        mbar_init(&bar_ops, 128);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base_sh)),
+                     "r"(HT_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+    const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16);
+    // MMA bookkeeping: one operand hand-off (bar_ops, the 128 threads of half 0
+    // arrive) and one commit (bar_mma) per issued update, numbered from 0
+    // across the CTA's matrices; thread 128 issues, thread 0 waits for them.
+    uint32_t base = 0;     // updates issued for earlier matrices
+    uint32_t issued = 0;   // updates issued so far (thread 128)
+
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        // ------------------------------------------------ matrix -> TMEM --
+        for (int cb = 64 * h; cb < 64 * h + 64; cb += 8) {
+            uint32_t r[16];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int col = cb + c;
+                float xr = 0.f, xi = 0.f;
+                if (i < N && col < N) {
+                    if (Hpair) {
+                        const float4 p = Hpair[b * NN + (size_t)i * N + col];
+                        xr = p.x + p.y;
+                        xi = p.z + p.w;
+                    } else {
+                        const zc z = Hz[b * NN + (size_t)i * N + col];
+                        xr = (float)z.re;
+                        xi = (float)z.im;
+                    }
+                }
+                if (col == 0) colbuf[i] = mk<float>(xr, xi);
+                r[2 * c] = __float_as_uint(xr);
+                r[2 * c + 1] = __float_as_uint(xi);
+            }
+            tmem_st16(trow + (uint32_t)(2 * cb), r);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+
+        bool aborted = false;
+        cc* Vm = Vt + (size_t)b * (pe + N);
+        cc wnext = mk<float>(0.f, 0.f);  // w of the previous step at the current column (row j)
+        size_t dj = 0;                   // packed offset of row j's diagonal
+        for (int j = 0; j < N - 1; dj += (size_t)(N - j), ++j) {
+            const int jn = j + 1;
+            // ------------------------------------- column j, reflector --
+            cc a = mk<float>(0.f, 0.f);
+            if (h == 0) {
+                a = colbuf[i];
+                if (j > 0) {  // step j-1's update of this column (not in the value read from TMEM)
+                    fms_mulc(a, vbuf[i], wnext);
+                    fms_mulc(a, wbuf[i], vbuf[j]);
+                }
+                if (i == j) dsm[j] = a.re;
+                if (i == jn) alpha_sh = a;
+                float x2 = (i > jn && i < N) ? abs2(a) : 0.f;
+                x2 = ht_warp_sum(x2);
+                if (lane == 0) red[q] = x2;
+            }
+            __syncthreads();
+            // the reflector's scalars (half 0 only: the other half needs none of them)
+            cc tau = mk<float>(0.f, 0.f), scal = mk<float>(0.f, 0.f);
+            float beta = 0.f;
+            const float xnorm2 = (red[0] + red[1]) + (red[2] + red[3]);
+            const cc alpha = alpha_sh;
+            if (h == 1) {
+            } else if (xnorm2 == 0.f && alpha.im == 0.f) {
+                tau = mk<float>(0.f, 0.f);
+                scal = mk<float>(0.f, 0.f);
+                beta = alpha.re;
+            } else {
+                const float nrm = sqrtf(alpha.re * alpha.re + alpha.im * alpha.im + xnorm2);
+                beta = (alpha.re >= 0.f) ? -nrm : nrm;
+                const float rb = __frcp_rn(beta);
+                tau = mk<float>((beta - alpha.re) * rb, -alpha.im * rb);
+                const cc den = mk<float>(alpha.re - beta, alpha.im);
+                const float rd = __frcp_rn(den.re * den.re + den.im * den.im);
+                scal = mk<float>(den.re * rd, -den.im * rd);
+            }
+            if (h == 0) {
+                const cc v = (i == jn) ? mk<float>(1.f, 0.f) : ((i > jn && i < N) ? a * scal : mk<float>(0.f, 0.f));
+                vbuf[i] = v;
+                if (i >= jn && i < N) Vm[dj + (size_t)(i - j)] = v;
+            }
+            if (tid == 0) {
+                esm[j] = beta;
+                Vm[pe + j] = tau;
+                // step j-1's update must be in TMEM before the product below reads it
+                if (j > 0 && !mbar_wait(&bar_mma, (base + j - 1) & 1u, &abort_sh, wait_limit)) abort_sh = 1;
+            }
+            __syncthreads();
+            tc_fence_after();
+            if (abort_sh) {
+                aborted = true;
+                break;
+            }
+            // --------------------------- p = A22 v (TMEM), partial v^H p --
+            cc acc[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) acc[g] = mk<float>(0.f, 0.f);
+            uint32_t sre = 0u, sim = 0u;  // column j+1 of this row, for the next step (half 0)
+            if (32 * q + 31 >= jn && 32 * q < N) {  // warp-uniform: some row of this warp is trailing
+                if (h == 0) {
+                    sre = tmem_ld1(trow + (uint32_t)(2 * jn));
+                    sim = tmem_ld1(trow + (uint32_t)(2 * jn + 1));
+                }
+                // chunks of 8 complex columns cf .. cl; this half takes every other one,
+                // up to four per wait (one accumulator each)
+                const int cf = jn >> 3, cl = (N - 1) >> 3;
+                for (int c = cf + ((cf & 1) != h); c <= cl; c += 8) {
+                    uint32_t r[4][16];
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                        if (c + 2 * g <= cl) tmem_ld16(trow + (uint32_t)(16 * (c + 2 * g)), r[g]);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        if (c + 2 * g > cl) break;
+                        const float4* vp = reinterpret_cast<const float4*>(vbuf + 8 * (c + 2 * g));
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float4 v2 = vp[u];  // v at two consecutive columns
+                            const float ar = __uint_as_float(r[g][4 * u]), ai = __uint_as_float(r[g][4 * u + 1]);
+                            const float br = __uint_as_float(r[g][4 * u + 2]), bi = __uint_as_float(r[g][4 * u + 3]);
+                            acc[g].re = fmaf(ar, v2.x, acc[g].re);
+                            acc[g].re = fmaf(-ai, v2.y, acc[g].re);
+                            acc[g].re = fmaf(br, v2.z, acc[g].re);
+                            acc[g].re = fmaf(-bi, v2.w, acc[g].re);
+                            acc[g].im = fmaf(ar, v2.y, acc[g].im);
+                            acc[g].im = fmaf(ai, v2.x, acc[g].im);
+                            acc[g].im = fmaf(br, v2.w, acc[g].im);
+                            acc[g].im = fmaf(bi, v2.z, acc[g].im);
+                        }
+                    }
+                }
+                tmem_wait_ld();  // the column j+1 loads, when this half had no chunk to wait for
+            }
+            if (h == 0) colbuf[i] = mk<float>(__uint_as_float(sre), __uint_as_float(sim));
+            const cc accs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+            (h ? pbuf : p0buf)[i] = accs;
+            {
+                // this half's share of p^H v (v is zero outside the trailing rows)
+                const cc vi = vbuf[i];
+                float dr = accs.re * vi.re + accs.im * vi.im;
+                float di = accs.re * vi.im - accs.im * vi.re;
+                dr = ht_warp_sum(dr);
+                di = ht_warp_sum(di);
+                if (lane == 0) {
+                    red[4 + warp] = dr;
+                    red[12 + warp] = di;
+                }
+            }
+            tc_fence_before();
+            __syncthreads();
+            // ------------------ y = tau p, w = y - 1/2 tau (y^H v) v, operands --
+            const bool more = jn < N - 1;  // a later product reads this update from TMEM
+            if (h == 0) {
+                const cc p = accs + pbuf[i];
+                const cc y = (i >= jn && i < N) ? tau * p : mk<float>(0.f, 0.f);
+                cc s = mk<float>(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s = s + mk<float>(red[4 + k], red[12 + k]);
+                const cc dp = conj(tau) * s;  // y^H v = conj(tau) p^H v
+                const cc alpha2 = -0.5f * (tau * dp);
+                const cc vi = vbuf[i];
+                const cc w = y + alpha2 * vi;
+                wbuf[i] = w;
+                // the same value at row j+1 (another thread's row), for the next step's column
+                if (jn < N) wnext = tau * (p0buf[jn] + pbuf[jn]) + alpha2 * vbuf[jn];
+                if (more) {
+                    uint4 ahi, alo, rhi, rlo, ihi, ilo;
+                    split4(-vi.re, -vi.im, -w.re, -w.im, ahi, alo);
+                    split4(w.re, w.im, vi.re, vi.im, rhi, rlo);
+                    split4(-w.im, w.re, -vi.im, vi.re, ihi, ilo);
+                    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+                    st_shared_v4(sA + op_off(i, 0), ahi);
+                    st_shared_v4(sA + op_off(i, 1), alo);
+                    st_shared_v4(sB1 + op_off(2 * i, 0), rhi);
+                    st_shared_v4(sB1 + op_off(2 * i, 1), rhi);
+                    st_shared_v4(sB1 + op_off(2 * i + 1, 0), ihi);
+                    st_shared_v4(sB1 + op_off(2 * i + 1, 1), ihi);
+                    st_shared_v4(sB2 + op_off(2 * i, 0), rlo);
+                    st_shared_v4(sB2 + op_off(2 * i, 1), z);
+                    st_shared_v4(sB2 + op_off(2 * i + 1, 0), ilo);
+                    st_shared_v4(sB2 + op_off(2 * i + 1, 1), z);
+                    fence_async_smem();
+                    mbar_arrive(&bar_ops);
+                }
+            } else if (tid == 128 && more) {
+                // issue the update once half 0 has written its operands
+                if (!mbar_wait(&bar_ops, (base + j) & 1u, &abort_sh, wait_limit)) {
+                    abort_sh = 1;
+                } else {
+                    tc_fence_after();
+                    // columns below the 8-column group of j+1 are untouched: D and B start there
+                    const int c0 = jn & ~7;
+                    const uint32_t id = idesc_tf32((uint32_t)(2 * (HT_NC - c0)));
+                    const uint64_t ad = smem_desc(sA, 128, 256);
+                    umma_tf32(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB1 + 64u * (uint32_t)c0, 128, 256), id);
+                    umma_tf32(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB2 + 64u * (uint32_t)c0, 128, 256), id);
+                    umma_commit(&bar_mma);
+                    ++issued;
+                }
+            }
+        }
+        base += (uint32_t)max(N - 2, 0);
+        if (aborted) break;
+        // last diagonal entry: the stashed column N-1 with the last step's update
+        if (h == 0 && i == N - 1) {
+            cc a = colbuf[i];
+            if (N > 1) {
+                fms_mulc(a, vbuf[i], wbuf[i]);
+                fms_mulc(a, wbuf[i], vbuf[i]);
+            }
+            dsm[N - 1] = a.re;
+            esm[N - 1] = 0.f;
+        }
+        __syncthreads();
+        float* dout = de + (size_t)b * 2 * N;
+        for (int k = tid; k < N; k += HT_THREADS) {
+            dout[k] = dsm[k];
+            dout[N + k] = esm[k];
+        }
+        if (tid == 0) Vt[(size_t)b * (pe + N) + pe + (N - 1)] = mk<float>(0.f, 0.f);
+        __syncthreads();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (abort_sh) {
+        if (tid == 0) atomicOr(status, 2);  // bit 1: a bounded wait ran out
+        if (tid == 128 && issued > 0) mbar_wait_plain(&bar_mma, (issued - 1) & 1u);  // the last update issued
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(HT_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+}  // namespace
+
+bool eig_tc_enabled() {
+    static const bool on = [] {
+        const char* s = std::getenv("TBG_EIG_TC");
+        return !(s && s[0] == '0');
+    }();
+    return on;
+}
+
+bool hetrd_tc_fits(int N) { return N >= 2 && N <= HT_MAXN; }
+
+size_t hetrd_tc_de_bytes(int N, int64_t batch) { return sizeof(float) * 2 * (size_t)N * (size_t)batch; }
+
+int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
+             int* status_d) {
+    if (batch <= 0) return TBG_OK;
+    if (!hetrd_tc_fits(N)) return set_error(TBG_E_UNSUPPORTED, "hetrd_tc: matrix order beyond 128");
+    static std::atomic<bool> attr_set{false};
+    if (!attr_set.load()) {
+        cudaError_t e = cudaFuncSetAttribute(hetrd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HT_SMEM);
+        if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(hetrd_tc)");
+        attr_set.store(true);
+    }
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>((int64_t)nsm * 2, batch);
+    KTimer kt(st, "hetrd_tc_kernel", 16.0 / 3.0 * (double)N * N * N * batch);
+    hetrd_tc_kernel<<<(unsigned)grid, HT_THREADS, HT_SMEM, st>>>(N, batch, Hpair, H, Vt, de, status_d, tc_wait_limit());
+    TBG_LAUNCHED("hetrd_tc_kernel");
+    return TBG_OK;
+}
+
+}  // namespace tbg

@@ -34,6 +34,7 @@
 #include <cstdint>
 
 #include "tbgpu_internal.cuh"
+#include "tc_ptx.cuh"
 
 namespace tbg {
 
@@ -68,73 +69,15 @@ enum { FMT_F64 = 0, FMT_F32 = 1, FMT_PAIR = 2, FMT_PRESLICED = 3 };
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, K-major, N = 128, M = 128
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+using namespace tc;
 
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(su32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(su32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Polls of a stage hand-off wait before the CTA gives up (a few milliseconds
-// at the default).  The drains before TMEM is freed keep their own bound.
-constexpr int kTcWaitPolls = 1 << 20;
 std::atomic<int> g_tc_wait_limit{kTcWaitPolls};
-inline int tc_wait_limit() { return g_tc_wait_limit.load(std::memory_order_relaxed); }
-
-// Bounded wait without abort check (used to drain committed MMAs and copies).
-__device__ __forceinline__ bool mbar_wait_plain(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < kTcWaitPolls; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-// Bounded wait (at most `limit` polls): false on time-out or when another warp
-// has flagged an abort.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int limit) {
-    for (int it = 0; it < limit; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (*abort_flag) return false;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // 1-D bulk copy global -> shared, completion counted in bytes on `bar`.
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                  "l"(src), "r"(bytes), "r"(su32(bar))
                  : "memory");
-}
-
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
-                 : "memory");
-}
-
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version for sm_100-class tensor cores; no swizzle
-    return d;
 }
 
 __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
@@ -144,19 +87,6 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t b
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
         : "memory");
 }
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
-                 : "memory");
-}
-
-// 8 consecutive TMEM columns of this warp's 32 lanes (no wait).
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
 // ---- digit extraction ----
 // Fixed-point value trunc(x * 2^(42 - E)) of a double with |x| < 2^E.
 __device__ __forceinline__ long long fx64(double x, int E) {
@@ -755,6 +685,8 @@ __global__ void hop_image_real_kernel(int Kc, int64_t Nc, const zc* __restrict__
 
 }  // namespace
 
+int tc_wait_limit() { return g_tc_wait_limit.load(std::memory_order_relaxed); }
+
 int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                      const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, int* EA, int* EB);
 
@@ -916,5 +848,5 @@ int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A,
 // without a fault: the waits that drain in-flight copies and MMAs keep their
 // full bound.
 extern "C" int tbg_internal_tc_wait_limit(int polls) {
-    return tbg::g_tc_wait_limit.exchange(polls > 0 ? polls : tbg::kTcWaitPolls);
+    return tbg::g_tc_wait_limit.exchange(polls > 0 ? polls : tbg::tc::kTcWaitPolls);
 }

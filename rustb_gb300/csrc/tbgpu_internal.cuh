@@ -340,6 +340,15 @@ int dos_accumulate(cudaStream_t st, int64_t count, const double* ev, int64_t E_n
 // {re_hi, re_lo, im_hi, im_lo} (batch stride N*N); U32 eigenvectors in columns.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
                     size_t work_bytes, int* status_d, const float4* Hpair = nullptr);
+// Householder reduction of up to 128-band matrices with the matrix resident
+// in TMEM and tcgen05 rank-2 updates (eig_tc.cu): Vt (batch, packed + N)
+// reflectors and tau, de (batch, 2 N) the tridiagonal d then e.  Used by
+// eig_batched_f32 unless TBG_EIG_TC=0.
+bool eig_tc_enabled();
+bool hetrd_tc_fits(int N);
+size_t hetrd_tc_de_bytes(int N, int64_t batch);
+int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
+             int* status_d);
 // FP32 eigensolve, refinement and rotation on the tensor cores: H, Vx, Vy as
 // float pairs (batch stride N*N) -> refined E (ascending) and Omega.
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);

@@ -3,8 +3,17 @@ orthogonality and residual of the eigenpairs before refinement (GPU).
 
 Measured on GB300 (128 bands): orthogonality ~1.5e-4 (eigenvalue pairs just
 outside the 1e-3 ||T|| cluster threshold, error ~ eps ||T|| / gap), residual
-~8e-7 ||H||, eigenvalues ~2.6e-7 ||H||; the Ogita-Aishima sweep that follows
-takes these to ~1e-12.  The bounds leave margin and catch a broken stage."""
+~8e-7 ||H||, eigenvalues ~2.6e-7 ||H|| with the reduction on the CUDA cores;
+from 65 to 128 bands the reduction's rank-2 updates accumulate into the
+TMEM-resident matrix on the tensor cores, whose FP32 accumulation rounds
+less well (eigenvalues ~3.5e-6 ||H||, residual and orthogonality unchanged).
+The Ogita-Aishima sweep that follows takes these to ~1e-12.  The bounds leave
+margin and catch a broken stage."""
+
+
+def eig_bound(n):
+    """Eigenvalue bound (relative to ||H||) of the FP32 stage at order n."""
+    return 2e-5 if 64 < n <= 128 else 1e-6
 
 import ctypes
 
@@ -52,7 +61,7 @@ def test_fp32_eigenpairs_random_hermitian(n):
     E, U = eig_f32(H)
     orth, res, eerr = quality(H, E, U)
     print(f"n={n}: orthogonality {orth:.2e}, residual {res:.2e}, eigenvalues {eerr:.2e}")
-    assert orth < 1e-3 and res < 1e-5 and eerr < 1e-6
+    assert orth < 1e-3 and res < 1e-5 and eerr < eig_bound(n)
 
 
 def test_fp32_eigenpairs_benchmark_model():
@@ -62,21 +71,23 @@ def test_fp32_eigenpairs_benchmark_model():
     E, U = eig_f32(H)
     orth, res, eerr = quality(H, E, U)
     print(f"128-band model: orthogonality {orth:.2e}, residual {res:.2e}, eigenvalues {eerr:.2e}")
-    assert orth < 1e-3 and res < 1e-5 and eerr < 1e-6
+    assert orth < 1e-3 and res < 1e-5 and eerr < eig_bound(128)
 
 
-def test_fp32_eigenpairs_many_waves_and_clusters():
-    """More matrices than resident CTAs (the persistent loop), and spectra with
-    exact multiplicities (block-diagonal copies: the cluster path)."""
-    rng = np.random.default_rng(5)
-    n, nk = 64, 700
+@pytest.mark.parametrize("n", [64, 128, 100])
+def test_fp32_eigenpairs_many_waves_and_clusters(n):
+    """More matrices than resident CTAs (the persistent loop: the tensor-core
+    reduction's mbarrier phases run on across a CTA's matrices), and spectra
+    with exact multiplicities (block-diagonal copies: the cluster path)."""
+    rng = np.random.default_rng(5 + n)
+    nk, hn = 700, n // 2
     X = rng.standard_normal((nk, n, n)) + 1j * rng.standard_normal((nk, n, n))
     H = 0.5 * (X + np.conj(np.transpose(X, (0, 2, 1))))
-    h = H[:64, :32, :32].copy()
+    h = H[:64, :hn, :hn].copy()
     H[:64] = 0
-    H[:64, :32, :32] = h
-    H[:64, 32:, 32:] = h  # every eigenvalue twice
+    H[:64, :hn, :hn] = h
+    H[:64, hn:2 * hn, hn:2 * hn] = h  # every eigenvalue twice (plus a zero when n is odd)
     E, U = eig_f32(H)
     orth, res, eerr = quality(H, E, U)
     print(f"n={n}, {nk} matrices: orthogonality {orth:.2e}, residual {res:.2e}, eigenvalues {eerr:.2e}")
-    assert orth < 1e-3 and res < 1e-5 and eerr < 1e-6
+    assert orth < 1e-3 and res < 1e-5 and eerr < eig_bound(n)
