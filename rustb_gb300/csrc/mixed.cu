@@ -27,6 +27,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cstdlib>
+
 #include "tbgpu_internal.cuh"
 
 namespace tbg {
@@ -34,10 +36,6 @@ namespace tbg {
 int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                 const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc,
                 int64_t sC, int* EA, int* EB);
-int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
-                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false,
-                   int* Ecol = nullptr);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                        int* err, bool exps_ready = false);
@@ -571,6 +569,15 @@ int occ_partials_add(cudaStream_t st, const OccSums& o, double* acc) {
     return TBG_OK;
 }
 
+// Class of the rotation products B = X'^H V X': MID unless TBG_ROTATION_HIGH=1.
+bool rotation_mid() {
+    static const bool mid = [] {
+        const char* e = std::getenv("TBG_ROTATION_HIGH");
+        return !(e && e[0] == '1');
+    }();
+    return mid;
+}
+
 size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     const size_t NN = (size_t)N * N;
     // X and F (cc) + 5 pair buffers + line exponents (10 operand sides) + FP32 solver workspace
@@ -616,20 +623,22 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
     void* eigw = take(eigw_bytes);
     // FP64-class products: tcgen05 form unless the mma.sync form is selected
-    auto hp = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb) -> int {
+    // (mid: the MID class, for the rotation into the eigenbasis)
+    auto hp = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb,
+                  bool mid = false) -> int {
         if (tc)
             return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, slot(sa),
-                                  slot(sb), status_d, true);
+                                  slot(sb), status_d, true, nullptr, mid);
         return ozaki_zgemm(st, true, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, EA, EB);
     };
     // the same with the column exponents of the output into slot sc: fused into
     // the product's epilogue when one tile holds every row (N <= 128)
-    auto hpe = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb,
-                   int sc) -> int {
+    auto hpe = [&](bool conj_a, int fa, int fb, const void* A, const void* B, float4* C, int sa, int sb, int sc,
+                   bool mid = false) -> int {
         if (tc && N <= 128)
             return ozaki_zgemm_tc(st, conj_a, fa, fb, batch, N, N, N, A, N, NN, B, N, NN, C, N, NN, slot(sa),
-                                  slot(sb), status_d, true, slot(sc));
-        const int r = hp(conj_a, fa, fb, A, B, C, sa, sb);
+                                  slot(sb), status_d, true, slot(sc), mid);
+        const int r = hp(conj_a, fa, fb, A, B, C, sa, sb, mid);
         return r ? r : exps(PAIR, true, C, sc);
     };
     int rc;
@@ -684,10 +693,13 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     // 5. band-basis velocities B = X'^H V X'
     if ((rc = exps(PAIR, true, bA, XPC)) || (rc = exps(PAIR, false, Vx, VXR)) || (rc = exps(PAIR, false, Vy, VYR)))
         return rc;
-    if ((rc = hpe(false, PAIR, PAIR, Vx, bA, bB, VXR, XPC, BXC))) return rc;
-    if ((rc = hpe(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC, BYC))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, bB, bD, XPC, BXC))) return rc;
-    if ((rc = hp(true, PAIR, PAIR, bA, bC, bE, XPC, BYC))) return rc;
+    //    in the MID class (about 2^-35 of each product's scale): Omega and its
+    //    k-sum need about 1e-9, where the refinement above needs FP64 class
+    const bool rmid = rotation_mid();
+    if ((rc = hpe(false, PAIR, PAIR, Vx, bA, bB, VXR, XPC, BXC, rmid))) return rc;
+    if ((rc = hpe(false, PAIR, PAIR, Vy, bA, bC, VYR, XPC, BYC, rmid))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bB, bD, XPC, BXC, rmid))) return rc;
+    if ((rc = hp(true, PAIR, PAIR, bA, bC, bE, XPC, BYC, rmid))) return rc;
     // 6. Omega (with the occupation k-sum when the caller wants only sums)
     if (occ) {
         if (Om || Met || occ->blocks != occ_sums_blocks(batch))

@@ -430,10 +430,6 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
     return exps_of(st, fmt_b, true, batch, Nc, K, B, ldb, sB, EB);
 }
 
-int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
-                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false,
-                   int* Ecol = nullptr);
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
                      const void* Bs, float4* C, int* err);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
@@ -602,7 +598,8 @@ int ozaki_zgemm(cudaStream_t st, bool high, bool conj_a, int fmt_a, int fmt_b, i
 }  // namespace tbg
 
 // Internal test hook (not part of the public header): C = op(A) B for host
-// complex-double inputs, result as complex double (hi + lo).
+// complex-double inputs, result as complex double (hi + lo).  high: 1 HIGH
+// class, 0 LOW, 2 MID (tcgen05 only).
 extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int M, int Nc, int K, const double* A,
                                         const double* B, double* C, int use_tc) {
     using namespace tbg;
@@ -632,9 +629,10 @@ extern "C" int tbg_internal_ozaki_zgemm(int high, int conj_a, int64_t batch, int
             cudaMemcpy(dB, b32.data(), sizeof(float) * b32.size(), cudaMemcpyHostToDevice);
             rc = ozaki_zgemm_tc_low(st, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
                                     static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr);
-        } else if (use_tc && high)
+        } else if (use_tc && high)  // high = 2: the MID class
             rc = ozaki_zgemm_tc(st, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc, (int64_t)K * Nc,
-                                static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr);
+                                static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M, derr, false,
+                                nullptr, high == 2);
         else
             rc = ozaki_zgemm(st, high != 0, conj_a != 0, 0, 0, batch, M, Nc, K, dA, ac, ar * ac, dB, Nc,
                              (int64_t)K * Nc, static_cast<float4*>(dC), Nc, (int64_t)M * Nc, EA, EA + batch * M);

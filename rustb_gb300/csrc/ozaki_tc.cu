@@ -52,6 +52,8 @@ constexpr int HALF_STAGE = TC_S * PLANE;        // the six planes of one operand
 //   LOW : S = 3, LMAX = 2, NLEV = 1  (about 2^-21; for small corrections)
 template <int S> struct Class;
 template <> struct Class<6> { static constexpr int LMAX = 5, NLEV = 4, MIN_CTAS = 1; };
+//   MID : S = 5, LMAX = 4, NLEV = 4  (about 2^-35; the rotation into the eigenbasis)
+template <> struct Class<5> { static constexpr int LMAX = 4, NLEV = 4, MIN_CTAS = 1; };
 template <> struct Class<3> { static constexpr int LMAX = 2, NLEV = 1, MIN_CTAS = 2; };
 constexpr int tc_smem_bytes(int S) { return 2 * 2 * S * PLANE + 1024; }  // two stages of A and B planes + slack
 constexpr int TC_SMEM = tc_smem_bytes(TC_S);
@@ -717,7 +719,7 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
 static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
                                 int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
                                 float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate,
-                                int* Ecol);
+                                int* Ecol, bool mid);
 
 // With exps_ready the caller has filled EA (rows of op(A)) and EB (columns of
 // B) already, e.g. once for an operand shared by several products.  With
@@ -725,7 +727,7 @@ static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt
 // epilogue also writes the exponents of C's columns.
 int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                    const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
-                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready, int* Ecol) {
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready, int* Ecol, bool mid) {
     if (Ecol && (M > TC_TM || K > kTcMaxK))
         return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: fused column exponents need M <= 128 and K <= 256");
     if (!exps_ready) {
@@ -742,32 +744,39 @@ int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t b
             const char* Ak = static_cast<const char*>(A) + (conj_a ? (int64_t)k0 * lda : (int64_t)k0) * ea;
             const char* Bk = static_cast<const char*>(B) + (int64_t)k0 * ldb * eb;
             const int rc = ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, kc, Ak, lda, sA, Bk, ldb, sB, C,
-                                                ldc, sC, EA, EB, err, k0 > 0, nullptr);
+                                                ldc, sC, EA, EB, err, k0 > 0, nullptr, mid);
             if (rc) return rc;
         }
         return TBG_OK;
     }
     return ozaki_zgemm_tc_chunk(st, conj_a, fmt_a, fmt_b, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB,
-                                err, false, Ecol);
+                                err, false, Ecol, mid);
 }
 
 static int ozaki_zgemm_tc_chunk(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc,
                                 int K, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB,
                                 float4* C, int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool accumulate,
-                                int* Ecol) {
+                                int* Ecol, bool mid) {
     const double work = 8.0 * (double)M * Nc * K * batch;
-#define TC_CASE(CJ, FA, FB)                                                                                          \
+#define TC_CASE(CJ, FA, FB, S, NAME)                                                                                 \
     if (conj_a == CJ && fmt_a == FA && fmt_b == FB)                                                                  \
-        return launch_tc<CJ, FA, FB, TC_S>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err,    \
-                                           "ozaki_tc_kernel<high>", work, accumulate ? 1 : 0, Ecol);
-    TC_CASE(false, FMT_F64, FMT_F64)   // unit test
-    TC_CASE(true, FMT_F64, FMT_F64)    // unit test
-    TC_CASE(true, FMT_F32, FMT_F32)    // X^H X
-    TC_CASE(false, FMT_F32, FMT_F32)   // X F (HIGH above kHighCorrN bands)
-    TC_CASE(false, FMT_PAIR, FMT_F32)  // H X
-    TC_CASE(true, FMT_F32, FMT_PAIR)   // X^H (H X)
-    TC_CASE(false, FMT_PAIR, FMT_PAIR) // V X'
-    TC_CASE(true, FMT_PAIR, FMT_PAIR)  // X'^H (V X')
+        return launch_tc<CJ, FA, FB, S>(st, batch, M, Nc, K, A, lda, sA, B, ldb, sB, C, ldc, sC, EA, EB, err, NAME,  \
+                                        work, accumulate ? 1 : 0, Ecol);
+    if (mid) {
+        TC_CASE(false, FMT_F64, FMT_F64, 5, "ozaki_tc_kernel<mid>")   // unit test
+        TC_CASE(true, FMT_F64, FMT_F64, 5, "ozaki_tc_kernel<mid>")    // unit test
+        TC_CASE(false, FMT_PAIR, FMT_PAIR, 5, "ozaki_tc_kernel<mid>") // V X'
+        TC_CASE(true, FMT_PAIR, FMT_PAIR, 5, "ozaki_tc_kernel<mid>")  // X'^H (V X')
+        return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: operand format combination not instantiated (MID)");
+    }
+    TC_CASE(false, FMT_F64, FMT_F64, TC_S, "ozaki_tc_kernel<high>")   // unit test
+    TC_CASE(true, FMT_F64, FMT_F64, TC_S, "ozaki_tc_kernel<high>")    // unit test
+    TC_CASE(true, FMT_F32, FMT_F32, TC_S, "ozaki_tc_kernel<high>")    // X^H X
+    TC_CASE(false, FMT_F32, FMT_F32, TC_S, "ozaki_tc_kernel<high>")   // X F (HIGH above kHighCorrN bands)
+    TC_CASE(false, FMT_PAIR, FMT_F32, TC_S, "ozaki_tc_kernel<high>")  // H X
+    TC_CASE(true, FMT_F32, FMT_PAIR, TC_S, "ozaki_tc_kernel<high>")   // X^H (H X)
+    TC_CASE(false, FMT_PAIR, FMT_PAIR, TC_S, "ozaki_tc_kernel<high>") // V X'
+    TC_CASE(true, FMT_PAIR, FMT_PAIR, TC_S, "ozaki_tc_kernel<high>")  // X'^H (V X')
 #undef TC_CASE
     return set_error(TBG_E_UNSUPPORTED, "ozaki_zgemm_tc: operand format combination not instantiated");
 }

@@ -309,6 +309,13 @@ constexpr int kMixedMaxN = 2048;
 constexpr int kHighCorrN = 256;
 // tcgen05 form of the exact-slice products (default) or the mma.sync form.
 bool ozaki_use_tc();
+// Exact-slice complex GEMM on tcgen05 (ozaki_tc.cu): C = op(A) B as float
+// pairs.  HIGH class (six BF16 digits per value, about 2^-43 of the product
+// scale), or with `mid` the MID class (five digits, about 2^-35).
+int ozaki_zgemm_tc(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
+                   const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, float4* C,
+                   int64_t ldc, int64_t sC, int* EA, int* EB, int* err, bool exps_ready = false,
+                   int* Ecol = nullptr, bool mid = false);
 
 // Gaussian-smeared DOS: add the terms of count band energies ev (device) to
 // the compensated per-bin totals acc (2 E_n: sum, compensation).  part holds

@@ -1,7 +1,8 @@
 """Exact-slice BF16 tensor-core complex GEMM against numpy FP64 (GPU).
 
 The HIGH class must reach 1e-12 of the natural product scale
-(max|row of op(A)| * max|column of B| * K); the LOW class 1e-5."""
+(max|row of op(A)| * max|column of B| * K); the MID class (five digits,
+used for the rotation into the eigenbasis) 1e-10; the LOW class 1e-5."""
 
 import ctypes
 
@@ -119,3 +120,29 @@ def test_ozaki_tc_many_tiles_per_cta(conj_a):
     C = ozaki(lib, A, B, conj_a, True, 1)
     scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
     assert (np.abs(C - ref) / scale).max() < 1e-12
+
+
+@pytest.mark.parametrize("conj_a", [False, True])
+@pytest.mark.parametrize("M,Nc,K", [(128, 128, 128), (70, 40, 100), (200, 130, 300)])
+def test_ozaki_tc_mid_precision(conj_a, M, Nc, K):
+    """MID class on tcgen05: about 2^-35 of the natural scale (bound 1e-10),
+    with rows and columns of very different magnitude and a contraction
+    longer than one exact chunk (K = 300)."""
+    lib = _lib.load()
+    rng = np.random.default_rng(7 * M + Nc + K)
+    batch = 3
+    shapeA = (batch, K, M) if conj_a else (batch, M, K)
+    A = rng.standard_normal(shapeA) + 1j * rng.standard_normal(shapeA)
+    B = rng.standard_normal((batch, K, Nc)) + 1j * rng.standard_normal((batch, K, Nc))
+    if conj_a:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, 1, M))
+    else:
+        A *= 10.0 ** rng.uniform(-3, 3, (batch, M, 1))
+    B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
+    opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
+    ref = opA @ B
+    C = ozaki(lib, A, B, conj_a, 2, 1)
+    scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
+    err = (np.abs(C - ref) / scale).max()
+    print(f"MID class {M}x{Nc}x{K}: {err:.2e}")
+    assert err < 1e-10, err
