@@ -1053,7 +1053,7 @@ int allow_max_smem(K kern, size_t need) {
 template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
                 size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr,
-                const float* tri_de = nullptr) {
+                const float* tri_de = nullptr, bool skip_bt = false) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
     auto kern = heev_kernel<T, A_SMEM, MINB>;
     if (int rc = allow_max_smem(kern, smem)) return rc;
@@ -1086,7 +1086,7 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
         TBG_LAUNCHED(name);
     }
     if constexpr (A_SMEM) {
-        if (!U) return TBG_OK;
+        if (!U || skip_bt) return TBG_OK;
         static_assert(sizeof(T) == sizeof(float), "the shared-memory solver is the FP32 one");
         const size_t bsm = bt_tiled_smem_bytes(N, PB);
         auto bk = PB >= ((N + 3) & ~3) ? heev_bt_tiled_kernel<false> : heev_bt_tiled_kernel<true>;
@@ -1193,8 +1193,10 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
             return set_error(TBG_E_OOM, "eigensolver workspace too small for the reduction's output");
         float* de = reinterpret_cast<float*>(static_cast<unsigned char*>(work) + vt);
         if (int rc = hetrd_tc(st, N, batch, Hpair, H, static_cast<cc*>(work), de, status_d)) return rc;
-        return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
-                                           "heev_tri_kernel<float>", G, PB, Hpair, de);
+        if (int rc = launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                 "heev_tri_kernel<float>", G, PB, Hpair, de, bt_tc_enabled()))
+            return rc;
+        return (U && bt_tc_enabled()) ? bt_tc(st, N, batch, static_cast<const cc*>(work), U, status_d) : TBG_OK;
     }
     if (ctas == 3)
         return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,

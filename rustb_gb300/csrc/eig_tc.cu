@@ -389,6 +389,302 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
     }
 }
 
+
+// ------------------------------------------------------------------------
+// Back-transformation U <- H_0 H_1 ... H_{N-2} U of the FP32 solver for up to
+// 128 bands with U resident in tensor memory, transposed: lane c = column c
+// of U, columns 2 i / 2 i + 1 = Re / Im U(i, c).  The reflectors are applied
+// in blocks of BT8 = 8, last block first: for the block H_j0 ... H_j0+7 =
+// I - V T V^H (V: the 8 reflectors as dense zero-masked columns),
+//   z = V^H U(:, c)      each thread its column c, from TMEM rows, in FP32
+//                        (the two warps of a lane quarter take 4 reflectors
+//                        each);
+//   y = T z              back-substitution y_l = tau_l (z_l - sum_{m>l}
+//                        (v_l^H v_m) y_m) with the block's Gram matrix;
+//   U -= V Y             tcgen05.mma.kind::tf32 accumulating into TMEM:
+//                        row c of the A operand is -[Re y | Im y] (K = 16),
+//                        rows 2 i, 2 i + 1 of B are [Re V(i,:), -Im V(i,:)]
+//                        and [Im V(i,:), Re V(i,:)]; 3xTF32 (A_hi B_hi,
+//                        A_lo B_hi, A_hi B_lo), N = the rows from j0 on.
+// The next block's reflectors are read from global memory while the MMAs of
+// this one run.  Rows and columns past N are zero.
+constexpr int BT8 = 8;
+// Dynamic shared memory: tiles and scratch (61 KB); 80 KB keeps at most two CTAs (512 TMEM columns) per SM.
+constexpr size_t BT_SMEM = 80 * 1024;
+constexpr int BT_B_BYTES = 256 * 16 * 4, BT_A_BYTES = 128 * 16 * 4;
+
+// operand tiles of K = 16: row r, K group kc (4 values): K-adjacent core matrices 128 bytes apart, 8-row groups 512
+__device__ __forceinline__ uint32_t bt_off(int r, int kc) {
+    return (uint32_t)((r >> 3) * 512 + kc * 128 + (r & 7) * 16);
+}
+
+__global__ void __launch_bounds__(HT_THREADS, 2)
+    bt_tc_kernel(int N, int64_t batch, const cc* __restrict__ Vt, cc* __restrict__ Uio, int* __restrict__ status,
+                 int wait_limit) {
+    extern __shared__ __align__(1024) unsigned char bt_smem[];
+    __shared__ __align__(8) uint64_t bar_mma, bar_ops;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ volatile int abort_sh;
+    __shared__ cc G[BT8 * BT8];
+    __shared__ cc tau_b[BT8];
+    unsigned char* Bhi = reinterpret_cast<unsigned char*>(((uintptr_t)bt_smem + 127) & ~(uintptr_t)127);
+    unsigned char* Blo = Bhi + BT_B_BYTES;
+    unsigned char* Ahi = Blo + BT_B_BYTES;
+    unsigned char* Alo = Ahi + BT_A_BYTES;
+    cc* Vs = reinterpret_cast<cc*>(Alo + BT_A_BYTES);  // (128, 8) the block's reflectors
+    cc* zx = Vs + 128 * BT8;                          // (128, 4) half 1's share of z
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int q = warp & 3, h = warp >> 2;
+    const int c = 32 * q + lane;  // this thread's column of U (TMEM lane)
+    const size_t NN = (size_t)N * N, pe = ht_packed_elems(N);
+    const uint32_t sBhi = su32(Bhi), sBlo = su32(Blo), sAhi = su32(Ahi), sAlo = su32(Alo);
+    const int nblk = (N - 1 + BT8 - 1) / BT8;  // blocks of reflectors 0 .. N-2
+
+    if (tid == 0) {
+        mbar_init(&bar_mma, 1);
+        mbar_init(&bar_ops, 128);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base_sh)),
+                     "r"(HT_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+    const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16);
+    uint32_t done = 0;    // updates committed and waited for (thread 0)
+    uint32_t issued = 0;  // updates issued (thread 128)
+
+    for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+        const cc* Vm = Vt + (size_t)b * (pe + N);
+        cc* U = Uio + b * NN;
+        // ------------------------------------------ U^T -> TMEM (rows 64 h ..) --
+        for (int i0 = 64 * h; i0 < 64 * h + 64; i0 += 8) {
+            uint32_t r[16];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int i = i0 + k;
+                const cc u = (i < N && c < N) ? U[(size_t)i * N + c] : mk<float>(0.f, 0.f);
+                r[2 * k] = __float_as_uint(u.re);
+                r[2 * k + 1] = __float_as_uint(u.im);
+            }
+            tmem_st16(trow + (uint32_t)(2 * i0), r);
+        }
+        tmem_wait_st();
+        // this thread's reflector components of the first (last-applied-first) block:
+        // row i = tid & 127 of V, reflectors 4 h' .. 4 h' + 3 with h' = tid >> 7
+        const int vi = tid & 127, vh = tid >> 7;
+        auto load_v = [&](int j0, cc (&vr)[4]) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int j = j0 + 4 * vh + t;
+                vr[t] = (j <= N - 2 && vi > j && vi < N) ? Vm[ht_diag_off(N, j) + (size_t)(vi - j)]
+                                                          : mk<float>(0.f, 0.f);
+            }
+        };
+        cc vr[4];
+        load_v(BT8 * (nblk - 1), vr);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+
+        bool aborted = false;
+        for (int blk = nblk - 1; blk >= 0; --blk) {
+            const int j0 = BT8 * blk;
+            // ---------------- the previous block's update is complete: tiles and TMEM free --
+            if (tid == 0 && blk < nblk - 1) {
+                if (!mbar_wait(&bar_mma, done & 1u, &abort_sh, wait_limit)) abort_sh = 1;
+                ++done;
+            }
+            __syncthreads();
+            tc_fence_after();
+            if (abort_sh) {
+                aborted = true;
+                break;
+            }
+            // ------------------------------ this block's V: FP32 copy and the B tiles --
+            {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) Vs[vi * BT8 + 4 * vh + t] = vr[t];
+                uint4 rhi, rlo, ihi, ilo, jhi, jlo, khi, klo;
+                // row 2 i: [Re V(i, 4 vh ..) | ... ] at K group vh, [-Im V(i, 4 vh ..)] at K group 2 + vh
+                split4(vr[0].re, vr[1].re, vr[2].re, vr[3].re, rhi, rlo);
+                split4(-vr[0].im, -vr[1].im, -vr[2].im, -vr[3].im, ihi, ilo);
+                // row 2 i + 1: [Im V] at K group vh, [Re V] at K group 2 + vh
+                split4(vr[0].im, vr[1].im, vr[2].im, vr[3].im, jhi, jlo);
+                khi = rhi;
+                klo = rlo;
+                st_shared_v4(sBhi + bt_off(2 * vi, vh), rhi);
+                st_shared_v4(sBlo + bt_off(2 * vi, vh), rlo);
+                st_shared_v4(sBhi + bt_off(2 * vi, 2 + vh), ihi);
+                st_shared_v4(sBlo + bt_off(2 * vi, 2 + vh), ilo);
+                st_shared_v4(sBhi + bt_off(2 * vi + 1, vh), jhi);
+                st_shared_v4(sBlo + bt_off(2 * vi + 1, vh), jlo);
+                st_shared_v4(sBhi + bt_off(2 * vi + 1, 2 + vh), khi);
+                st_shared_v4(sBlo + bt_off(2 * vi + 1, 2 + vh), klo);
+                if (tid < BT8) tau_b[tid] = (j0 + tid <= N - 2) ? Vm[pe + j0 + tid] : mk<float>(0.f, 0.f);
+            }
+            __syncthreads();
+            // the next block's reflectors, read while this block is applied
+            if (blk > 0) load_v(j0 - BT8, vr);
+            // ---------------------------------------- Gram matrix G(l, m) = v_l^H v_m, l < m --
+            if (tid < 8 * 28) {
+                const int e = tid >> 3, p8 = tid & 7;
+                int l = 0, m = 1, cnt = e;
+                while (cnt >= BT8 - 1 - l) {
+                    cnt -= BT8 - 1 - l;
+                    ++l;
+                }
+                m = l + 1 + cnt;
+                cc g = mk<float>(0.f, 0.f);
+                for (int i = j0 + 1 + p8; i < N; i += 8) fma_cjx(g, Vs[i * BT8 + l], Vs[i * BT8 + m]);
+#pragma unroll
+                for (int o = 1; o < 8; o <<= 1) {
+                    g.re += __shfl_xor_sync(0xffffffffu, g.re, o);
+                    g.im += __shfl_xor_sync(0xffffffffu, g.im, o);
+                }
+                if (p8 == 0) G[l * BT8 + m] = g;
+            }
+            // ----------------- z = V^H U(:, c) for this half's 4 reflectors, from TMEM rows --
+            cc z[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) z[t] = mk<float>(0.f, 0.f);
+            {
+                // rows j0 + 1 .. N - 1 in chunks of 8 (16 TMEM columns), two chunks per wait
+                const int i_first = j0 & ~7, i_end = (N + 7) & ~7;
+                for (int i0 = i_first; i0 < i_end; i0 += 16) {
+                    const bool two = i0 + 8 < i_end;
+                    uint32_t r[2][16];
+                    tmem_ld16(trow + (uint32_t)(2 * i0), r[0]);
+                    if (two) tmem_ld16(trow + (uint32_t)(2 * i0 + 16), r[1]);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int g2 = 0; g2 < 2; ++g2) {
+                        if (g2 == 1 && !two) break;
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int i = i0 + 8 * g2 + k;
+                            const float ur = __uint_as_float(r[g2][2 * k]), ui = __uint_as_float(r[g2][2 * k + 1]);
+                            const float4 va = *reinterpret_cast<const float4*>(Vs + i * BT8 + 4 * h);
+                            const float4 vb = *reinterpret_cast<const float4*>(Vs + i * BT8 + 4 * h + 2);
+                            // z += conj(V(i, l)) U(i, c)
+                            z[0].re = fmaf(va.x, ur, z[0].re); z[0].re = fmaf(va.y, ui, z[0].re);
+                            z[0].im = fmaf(va.x, ui, z[0].im); z[0].im = fmaf(-va.y, ur, z[0].im);
+                            z[1].re = fmaf(va.z, ur, z[1].re); z[1].re = fmaf(va.w, ui, z[1].re);
+                            z[1].im = fmaf(va.z, ui, z[1].im); z[1].im = fmaf(-va.w, ur, z[1].im);
+                            z[2].re = fmaf(vb.x, ur, z[2].re); z[2].re = fmaf(vb.y, ui, z[2].re);
+                            z[2].im = fmaf(vb.x, ui, z[2].im); z[2].im = fmaf(-vb.y, ur, z[2].im);
+                            z[3].re = fmaf(vb.z, ur, z[3].re); z[3].re = fmaf(vb.w, ui, z[3].re);
+                            z[3].im = fmaf(vb.z, ui, z[3].im); z[3].im = fmaf(-vb.w, ur, z[3].im);
+                        }
+                    }
+                }
+            }
+            if (h == 1) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) zx[c * 4 + t] = z[t];
+            }
+            tc_fence_before();
+            __syncthreads();
+            // --------------------------------- y = T z, A operand row c = -[Re y | Im y] --
+            if (h == 0) {
+                cc zz[BT8], y[BT8];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    zz[t] = z[t];
+                    zz[4 + t] = zx[c * 4 + t];
+                }
+#pragma unroll
+                for (int l = BT8 - 1; l >= 0; --l) {
+                    cc sv = zz[l];
+#pragma unroll
+                    for (int m = l + 1; m < BT8; ++m) sv = sv - G[l * BT8 + m] * y[m];
+                    y[l] = tau_b[l] * sv;
+                }
+                uint4 h0, l0, h1, l1, h2, l2, h3, l3;
+                split4(-y[0].re, -y[1].re, -y[2].re, -y[3].re, h0, l0);
+                split4(-y[4].re, -y[5].re, -y[6].re, -y[7].re, h1, l1);
+                split4(-y[0].im, -y[1].im, -y[2].im, -y[3].im, h2, l2);
+                split4(-y[4].im, -y[5].im, -y[6].im, -y[7].im, h3, l3);
+                st_shared_v4(sAhi + bt_off(c, 0), h0);
+                st_shared_v4(sAhi + bt_off(c, 1), h1);
+                st_shared_v4(sAhi + bt_off(c, 2), h2);
+                st_shared_v4(sAhi + bt_off(c, 3), h3);
+                st_shared_v4(sAlo + bt_off(c, 0), l0);
+                st_shared_v4(sAlo + bt_off(c, 1), l1);
+                st_shared_v4(sAlo + bt_off(c, 2), l2);
+                st_shared_v4(sAlo + bt_off(c, 3), l3);
+                fence_async_smem();
+                mbar_arrive(&bar_ops);
+            } else if (tid == 128) {
+                if (!mbar_wait(&bar_ops, issued & 1u, &abort_sh, wait_limit)) {
+                    abort_sh = 1;
+                } else {
+                    tc_fence_after();
+                    // U rows from j0 on: D columns 2 j0 .., B rows 2 j0 .. (8-row groups of 512 bytes)
+                    const uint32_t id = idesc_tf32((uint32_t)(2 * (HT_NC - j0)));
+                    const uint32_t d = tmem + (uint32_t)(2 * j0), boff = 128u * (uint32_t)j0;
+#pragma unroll
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const uint64_t ah = smem_desc(sAhi + 256u * kk, 128, 512);
+                        const uint64_t al = smem_desc(sAlo + 256u * kk, 128, 512);
+                        const uint64_t bh = smem_desc(sBhi + boff + 256u * kk, 128, 512);
+                        const uint64_t bl = smem_desc(sBlo + boff + 256u * kk, 128, 512);
+                        umma_tf32(d, ah, bh, id);
+                        umma_tf32(d, al, bh, id);
+                        umma_tf32(d, ah, bl, id);
+                    }
+                    umma_commit(&bar_mma);
+                    ++issued;
+                }
+            }
+        }
+        if (aborted) break;
+        // ------------------------------------------------ TMEM -> U (rows 64 h ..) --
+        if (tid == 0) {
+            if (!mbar_wait(&bar_mma, done & 1u, &abort_sh, wait_limit)) abort_sh = 1;
+            ++done;
+        }
+        __syncthreads();
+        tc_fence_after();
+        if (abort_sh) break;
+        for (int i0 = 64 * h; i0 < 64 * h + 64; i0 += 16) {
+            uint32_t r[2][16];
+            tmem_ld16(trow + (uint32_t)(2 * i0), r[0]);
+            tmem_ld16(trow + (uint32_t)(2 * i0 + 16), r[1]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                const int i = i0 + k;
+                if (i < N && c < N)
+                    U[(size_t)i * N + c] = mk<float>(__uint_as_float(r[k >> 3][2 * (k & 7)]),
+                                                     __uint_as_float(r[k >> 3][2 * (k & 7) + 1]));
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (abort_sh) {
+        if (tid == 0) atomicOr(status, 2);  // bit 1: a bounded wait ran out
+        if (tid == 128 && issued > 0) mbar_wait_plain(&bar_mma, (issued - 1) & 1u);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(HT_TMEM_COLS)
+                     : "memory");
+    }
+}
+
 }  // namespace
 
 bool eig_tc_enabled() {
@@ -401,18 +697,25 @@ bool eig_tc_enabled() {
 
 bool hetrd_tc_fits(int N) { return N >= 2 && N <= HT_MAXN; }
 
+// The back-transformation on the tensor cores unless TBG_BT_TC=0 (then the
+// shared-memory blocked pass runs after the TMEM-resident reduction).
+bool bt_tc_enabled() {
+    static const bool on = [] {
+        const char* s = std::getenv("TBG_BT_TC");
+        return !(s && s[0] == '0');
+    }();
+    return on;
+}
+
 size_t hetrd_tc_de_bytes(int N, int64_t batch) { return sizeof(float) * 2 * (size_t)N * (size_t)batch; }
 
 int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
              int* status_d) {
     if (batch <= 0) return TBG_OK;
     if (!hetrd_tc_fits(N)) return set_error(TBG_E_UNSUPPORTED, "hetrd_tc: matrix order beyond 128");
-    static std::atomic<bool> attr_set{false};
-    if (!attr_set.load()) {
-        cudaError_t e = cudaFuncSetAttribute(hetrd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HT_SMEM);
-        if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(hetrd_tc)");
-        attr_set.store(true);
-    }
+    // a per-function attribute of the current device (set on every call: cheap, and right for every device)
+    cudaError_t e = cudaFuncSetAttribute(hetrd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HT_SMEM);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(hetrd_tc)");
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -420,6 +723,21 @@ int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const z
     KTimer kt(st, "hetrd_tc_kernel", 16.0 / 3.0 * (double)N * N * N * batch);
     hetrd_tc_kernel<<<(unsigned)grid, HT_THREADS, HT_SMEM, st>>>(N, batch, Hpair, H, Vt, de, status_d, tc_wait_limit());
     TBG_LAUNCHED("hetrd_tc_kernel");
+    return TBG_OK;
+}
+
+int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d) {
+    if (batch <= 0 || N < 2) return TBG_OK;
+    if (!hetrd_tc_fits(N)) return set_error(TBG_E_UNSUPPORTED, "bt_tc: matrix order beyond 128");
+    cudaError_t e = cudaFuncSetAttribute(bt_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(bt_tc)");
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>((int64_t)nsm * 2, batch);
+    KTimer kt(st, "bt_tc_kernel", 8.0 * (double)N * N * N * batch);
+    bt_tc_kernel<<<(unsigned)grid, HT_THREADS, BT_SMEM, st>>>(N, batch, Vt, U, status_d, tc_wait_limit());
+    TBG_LAUNCHED("bt_tc_kernel");
     return TBG_OK;
 }
 

@@ -356,6 +356,10 @@ bool hetrd_tc_fits(int N);
 size_t hetrd_tc_de_bytes(int N, int64_t batch);
 int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
              int* status_d);
+// Back-transformation U <- Q U of the same solver with U (eigenvectors of the
+// tridiagonal form, in columns) resident in TMEM and tcgen05 block updates.
+int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d);
+bool bt_tc_enabled();
 // FP32 eigensolve, refinement and rotation on the tensor cores: H, Vx, Vy as
 // float pairs (batch stride N*N) -> refined E (ascending) and Omega.
 size_t mixed_berry_workspace_bytes(int N, int64_t batch);
