@@ -149,10 +149,16 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
 
 
 # DRAM bytes (read + write) per k-point of each kernel family, from ncu captures over 512 k-points
-# of this workload: the FP32 solver's two passes, and the seven FP64-class tcgen05 products of one
-# k-point (refinement and rotation) together.
-DRAM_BYTES_PER_MATRIX = {"heev_kernel<float,smem>": 112.5e6 / 512, "heev_bt_kernel": 112.5e6 / 512,
-                         "ozaki_tc_kernel<high>": 2176.1e6 / 512}
+# of this workload: the FP32 solver's passes (TMEM-resident reduction, back-transformation), the
+# three HIGH products of the refinement and the four MID products of the rotation of one k-point.
+DRAM_BYTES_PER_MATRIX = {"hetrd_tc_kernel": 141.3e6 / 512, "heev_kernel<float,smem>": 112.5e6 / 512,
+                         "heev_bt_kernel": 112.5e6 / 512}
+
+
+def slice_products(name: str) -> int:
+    """BF16 digit products per FP64-class product of an exact-slice kernel
+    family: 21 (HIGH, six digits), 15 (MID, five), 6 (LOW, three)."""
+    return 6 if "low" in name else (15 if "mid" in name else 21)
 
 
 def kernel_roofline(timing: dict, peaks: dict, units: int = 0) -> dict | None:
@@ -166,12 +172,12 @@ def kernel_roofline(timing: dict, peaks: dict, units: int = 0) -> dict | None:
     traffic = None
     if name in DRAM_BYTES_PER_MATRIX and units and launches:
         traffic = DRAM_BYTES_PER_MATRIX[name] * units / launches
-    if name.startswith("heev_kernel<float") or name.startswith("fp32"):
+    if name.startswith(("heev_kernel<float", "hetrd_tc", "bt_tc", "fp32")):
         bound, peak, src = "fp32", peaks["fp32_tflops"], "FP32 FMA loop on this GPU (tbg_measure_fma_peaks)"
     elif name.startswith("ozaki"):
-        # FP64-class products from 21 BF16 digit products (6 for the low class):
-        # the attainable algorithmic rate is the BF16 peak divided by the pair count
-        pairs = 6 if "low" in name else 21
+        # FP64-class products from BF16 digit products: the attainable algorithmic
+        # rate is the BF16 peak divided by the digit products per product
+        pairs = slice_products(name)
         bound, peak = "tensor", (peaks.get("bf16_tflops") or 0.0) / pairs
         src = f"MEASURED_PEAKS.json bf16_tflops (burst) / {pairs} slice products"
     else:

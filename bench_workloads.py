@@ -611,12 +611,12 @@ def wilson_bench(args, rank, world, local):
     p32 = ctypes.c_double(0.0)
     lib.tbg_measure_fma_peaks(ctypes.byref(p64), ctypes.byref(p32))
     ach = work / (ms / 1e3) / 1e12 if work > 0 and ms > 0 else None
-    if name.startswith("heev_kernel<float"):
+    if name.startswith(("heev_kernel<float", "hetrd_tc", "bt_tc")):
         bound, peak, src = "fp32", p32.value, "FP32 FMA loop on this GPU (tbg_measure_fma_peaks); 14 N^3 per eigensolve"
     elif name.startswith("ozaki"):
         mp = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "MEASURED_PEAKS.json")
         bf16 = json.load(open(mp)).get("bf16_tflops", 1900.0) if os.path.exists(mp) else 1900.0
-        pairs = 6 if "low" in name else 21
+        pairs = 6 if "low" in name else (15 if "mid" in name else 21)
         bound, peak, src = "tensor", bf16 / pairs, f"MEASURED_PEAKS.json bf16_tflops / {pairs} slice products"
     else:
         bound, peak, src = "fp64", p64.value, "FP64 FMA loop on this GPU (tbg_measure_fma_peaks)"
