@@ -256,10 +256,36 @@ def batched(args, rank, world, local):
         tb = time.perf_counter() - t1
         fb = sum(j.k_count() * batch._work_per_k(j.model) for j in sub)
         per_bucket[str(b)] = {"models": len(sub), "seconds": tb, "tflops": fb / tb / 1e12}
+    # the per-k outputs of the batched workload (eigenvalues and Berry curvature at every k): models of
+    # equal band count stacked into one pipeline each (tbg_berry_curvature_multi)
+    def mesh_head(mesh, n):
+        idx = np.arange(min(n, int(np.prod(mesh))))
+        cols, rest = [], idx
+        for d in reversed(range(len(mesh))):  # gen_kmesh order: first dimension outermost
+            cols.append((rest % mesh[d]) / mesh[d])
+            rest = rest // mesh[d]
+        return np.ascontiguousarray(np.stack(cols[::-1], axis=1))
+    kper = [mesh_head(j.params.kmesh, j.k_count()) for j in jobs]
+    pb = {2: Parameters(kmesh=(1, 1), direction=np.eye(2), mu=[0.0]),
+          3: Parameters(kmesh=(1, 1, 1), direction=np.eye(3)[:2], mu=[0.0])}
+
+    def berry_all():
+        for dim in (2, 3):
+            sel = [i for i, j in enumerate(jobs) if j.model.dim == dim]
+            batch.berry_curvature_many([jobs[i].model for i in sel], [kper[i] for i in sel], pb[dim], Precision.MIXED)
+    berry_all()  # warm-up
+    t0 = time.perf_counter()
+    berry_all()
+    dtb = time.perf_counter() - t0
+    groups = len({(j.model.nsta, j.model.dim) for j in jobs})
     _line(args, world, "algorithmic GFLOP/s (batched uneven models)", flops / dt / 1e9, "GFLOP/s", dt * 1e3,
           "f32 eigensolve + exact-slice tensor products", cfg,
           {"k_pts_per_s": nk / dt, "plan": runner.stats["plan"], "items": runner.stats["items"],
-           "workers": runner.stats["workers"], "per_bucket": per_bucket})
+           "workers": runner.stats["workers"], "per_bucket": per_bucket,
+           "per_k_outputs": {"what": "eigenvalues and Berry curvature at every k-point (berry_curvature_many: "
+                                     "models of equal band count and dimension stacked into one pipeline)",
+                             "seconds": dtb, "gflops": flops / dtb / 1e9, "k_pts_per_s": nk / dtb,
+                             "stacked_groups": groups}})
     return 0
 
 

@@ -160,6 +160,20 @@ int tbg_berry_curvature(const tbg_model* m, int64_t nk, const double* k,
                         const double* dirs2, int spin, double eta,
                         int precision, double* Omega_out, double* E_out);
 
+/* The same for several models with the same nsta and dim at once: model i
+ * takes nk[i] k-points, k is their concatenation (sum nk, dim) and Omega_out,
+ * E_out (sum nk, nsta) are concatenated the same way.  The models' H and
+ * velocities come from their own hopping tables into one stacked buffer and
+ * the eigensolve, rotation and Omega run once over the stacked k-points, so
+ * many small models fill the GPU as one large one does; results equal those
+ * of tbg_berry_curvature model by model.  Replaces: a loop of
+ * berry_curvature_at (src/response/traits.rs:60-78) over models, as Rustb's
+ * users batch many models (rayon over models, src/response/linear/mod.rs:198-202). */
+int tbg_berry_curvature_multi(int64_t n_models, const tbg_model* const* models,
+                              const int64_t* nk, const double* k,
+                              const double* dirs2, int spin, double eta,
+                              int precision, double* Omega_out, double* E_out);
+
 /* Occupation-weighted Berry curvature sum_n Omega_n f(E_n, mu) per k-point.
  * T in kelvin (0 = step function with f(mu) = 1/2).
  * Replaces: BerryCurvature::occupied_berry_curvature_on

@@ -85,6 +85,9 @@ SIGNATURES = [
     ("tbg_berry_curvature", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                            _c_double_p, _c_double_p]),
+    ("tbg_berry_curvature_multi", ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), _c_int64_p,
+                                                 _c_double_p, _c_double_p, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_int, _c_double_p, _c_double_p]),
     ("tbg_occupied_berry_curvature", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_double_p, _c_double_p,
                                                     ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                     ctypes.c_double, ctypes.c_int, _c_double_p]),

@@ -215,6 +215,41 @@ class BatchRunner:
         return out
 
 
+def berry_curvature_many(models: list, k_lists: list, params: Parameters, precision=Precision.MIXED) -> list:
+    """Band-resolved Berry curvature and energies of many models, each at its
+    own k-points: ``berry_curvature_on`` per model, with the models of equal
+    band count and dimension (a bucket) stacked into one pipeline
+    (``tbg_berry_curvature_multi``): their H and velocities are formed from
+    each model's table and the eigensolve, rotation and Omega run once over
+    all of the bucket's k-points.  Returns [(Omega, E)] in input order."""
+    if len(models) != len(k_lists):
+        raise ValueError("one k-list per model")
+    lib = _lib.load()
+    out = [None] * len(models)
+    groups = {}
+    ks = []
+    for i, (m, k) in enumerate(zip(models, k_lists)):
+        kk = np.zeros((0, m.dim)) if np.size(k) == 0 else m._klist(k)
+        m._check_berry_params(params)
+        ks.append(kk)
+        groups.setdefault((m.nsta, m.dim), []).append(i)
+    d = _lib.as_f64(params.direction)
+    for (nsta, _dim), idxs in sorted(groups.items()):
+        handles = (ctypes.c_void_p * len(idxs))(*[models[i].device_handle() for i in idxs])
+        nk = np.array([ks[i].shape[0] for i in idxs], dtype=np.int64)
+        kcat = np.ascontiguousarray(np.concatenate([ks[i] for i in idxs], axis=0))
+        Om = np.empty((int(nk.sum()), nsta))
+        E = np.empty((int(nk.sum()), nsta))
+        _lib.check(lib.tbg_berry_curvature_multi(len(idxs), handles, _lib.iptr(nk), _lib.dptr(kcat), _lib.dptr(d),
+                                                 spin_code(params.spin), float(params.eta), int(precision),
+                                                 _lib.dptr(Om), _lib.dptr(E)), lib)
+        o = 0
+        for i, n in zip(idxs, nk):
+            out[i] = (Om[o:o + n], E[o:o + n])
+            o += int(n)
+    return out
+
+
 def _work_per_k(m: Model) -> float:
     N = m.nsta
     return 24.0 * m.nR * N * N + 46.0 * N ** 3

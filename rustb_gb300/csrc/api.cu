@@ -345,6 +345,8 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
     return ctx.rc;
 }
 
+int berry_tail(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d);
+
 int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
     ModelDev& m = *J.m;
     const int N = (int)m.nsta;
@@ -370,6 +372,27 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
             if ((rc = z_to_pairs(ctx.st, nkc, NN, J.V, 2 * NN, P + nkc * NN))) return rc;
             if ((rc = z_to_pairs(ctx.st, nkc, NN, J.V + NN, 2 * NN, P + 2 * nkc * NN))) return rc;
         }
+        return berry_tail(ctx, J, nkc, clusters_d);
+    }
+    rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
+    if (rc) return rc;
+    if (m.n_rmat > 0) {
+        rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
+        if (rc) return rc;
+    }
+    return berry_tail(ctx, J, nkc, clusters_d);
+}
+
+// The part of a chunk after H and the velocities are formed (J.pairs for the
+// mixed path, J.H / J.V for FP64): spin dressing, eigensolve, rotation, Omega.
+// It depends on the model only through N and norb.
+int berry_tail(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
+    ModelDev& m = *J.m;
+    const int N = (int)m.nsta;
+    const int64_t NN = (int64_t)N * N;
+    int rc;
+    if (J.precision == TBG_PREC_MIXED) {
+        float4* P = J.pairs;
         if (J.spin >= 0) {
             rc = spin_dress_pairs(ctx.st, N, m.norb, nkc, J.spin, P + nkc * NN, NN,
                                   reinterpret_cast<float4*>(J.scratch));
@@ -380,12 +403,6 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
                                J.work_bytes, J.status_d, clusters_d, nullptr, nullptr, J.occ);
         return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
                            J.status_d, clusters_d, J.Met);
-    }
-    rc = fourier_direct(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, NN, 2 * NN);
-    if (rc) return rc;
-    if (m.n_rmat > 0) {
-        rc = rmatrix_term(m, ctx.st, nkc, J.k_d, TBG_GAUGE_ATOM, 2, J.dirs_d, J.H, J.V, J.scratch);
-        if (rc) return rc;
     }
     if (J.spin >= 0) {
         rc = spin_dress(ctx.st, N, m.norb, nkc, J.spin, J.V, 2 * NN, J.scratch);
@@ -858,6 +875,137 @@ int tbg_occupied_berry_curvature(const tbg_model* m, int64_t nk, const double* k
         return set_error(TBG_E_INVALID_RESPONSE_PARAMETER, "T: all values must be finite and non-negative");
     if (!out && nk > 0) return set_error(TBG_E_INVALID_ARGUMENT, "null output");
     return berry_common(m, nk, k, dirs2, spin, eta, precision, nullptr, nullptr, 1, &mu, T, out);
+}
+
+int tbg_berry_curvature_multi(int64_t n_models, const tbg_model* const* models, const int64_t* nk, const double* k,
+                              const double* dirs2, int spin, double eta, int precision, double* Omega_out,
+                              double* E_out) {
+    if (n_models < 0) return set_error(TBG_E_INVALID_ARGUMENT, "tbg_berry_curvature_multi: negative model count");
+    if (n_models == 0) return TBG_OK;
+    if (!models || !nk) return set_error(TBG_E_INVALID_ARGUMENT, "tbg_berry_curvature_multi: null models or k counts");
+    int rc;
+    for (int64_t i = 0; i < n_models; ++i)
+        if ((rc = check_model(models[i]))) return rc;
+    const ModelDev& M0 = models[0]->d;
+    const int N = (int)M0.nsta, dim = M0.dim;
+    int64_t total = 0;
+    for (int64_t i = 0; i < n_models; ++i) {
+        const ModelDev& Mi = models[i]->d;
+        if (Mi.nsta != M0.nsta || Mi.dim != M0.dim)
+            return set_error(TBG_E_INVALID_ARGUMENT,
+                             "tbg_berry_curvature_multi: the models must have the same number of states and dimension");
+        if (nk[i] < 0) return set_error(TBG_E_INVALID_ARGUMENT, "tbg_berry_curvature_multi: negative k count");
+        total += nk[i];
+    }
+    if ((rc = check_k(k, total, dim))) return rc;
+    if ((rc = check_dirs(dirs2, 2, dim, 2))) return rc;
+    if ((rc = check_eta(eta))) return rc;
+    for (int64_t i = 0; i < n_models; ++i)
+        if ((rc = check_spin(models[i], spin))) return rc;
+    if (precision != TBG_PREC_FP64 && precision != TBG_PREC_MIXED)
+        return set_error(TBG_E_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (mixed)");
+    if (total == 0) return TBG_OK;
+    const int prec = effective_precision(M0, precision);  // depends on the number of states only
+    const int64_t NN = (int64_t)N * N;
+    std::vector<int64_t> off(n_models + 1, 0);
+    for (int64_t i = 0; i < n_models; ++i) off[i + 1] = off[i] + nk[i];
+    // Models outside the stacked form (the one-thread-per-k small-model kernel,
+    // position matrices, tables beyond the exact contraction) run alone.
+    std::vector<int64_t> sidx;
+    int64_t stotal = 0, max_nR = 0;
+    for (int64_t i = 0; i < n_models; ++i) {
+        const ModelDev& Mi = models[i]->d;
+        const bool stack = !use_small_fused(Mi) && Mi.n_rmat == 0 && (prec == TBG_PREC_FP64 || fourier_mixed_ok(Mi));
+        if (!stack) {
+            if (nk[i] > 0 && (rc = berry_common(models[i], nk[i], k + off[i] * dim, dirs2, spin, eta, precision,
+                                                Omega_out ? Omega_out + off[i] * N : nullptr,
+                                                E_out ? E_out + off[i] * N : nullptr, 0, nullptr, 0.0, nullptr)))
+                return rc;
+            continue;
+        }
+        if (nk[i] == 0) continue;
+        sidx.push_back(i);
+        stotal += nk[i];
+        max_nR = std::max<int64_t>(max_nR, Mi.nR);
+    }
+    if (stotal == 0) return TBG_OK;
+    // buffers sized for the stacked model with the largest table (the Fourier scratch grows with nR)
+    int64_t rep = sidx[0];
+    for (int64_t i : sidx)
+        if (models[i]->d.nR > models[rep]->d.nR) rep = i;
+    Ctx ctx;
+    BerryJob J;
+    J.m = const_cast<ModelDev*>(&models[rep]->d);
+    J.spin = spin;
+    J.eta = eta;
+    J.precision = prec;
+    J.want_metric = false;
+    J.chunk = choose_chunk(stotal, sizeof(zc) * NN * (prec == TBG_PREC_MIXED ? 15 : 5) + 64 * N +
+                                       (prec == TBG_PREC_MIXED ? 48 * max_nR : 0));
+    double* dirs_d = ctx.alloc<double>(2 * dim);
+    J.dirs_d = dirs_d;
+    if (ctx.rc) return ctx.rc;
+    if ((rc = alloc_berry(ctx, J))) return rc;
+    // models whose hop table is not packed (the mma.sync form) contract into a
+    // buffer of their own and are copied into the stacked one
+    bool unpacked = false;
+    if (prec == TBG_PREC_MIXED)
+        for (int64_t i : sidx) {
+            bool packed = true;
+            if ((rc = fourier_mixed_packed(const_cast<ModelDev&>(models[i]->d), ctx.st, &packed))) return rc;
+            unpacked = unpacked || !packed;
+        }
+    float4* Ptmp = unpacked ? ctx.alloc<float4>(3 * J.chunk * NN) : nullptr;
+    if (ctx.rc) return ctx.rc;
+    TBG_CUDA(cudaMemcpyAsync(dirs_d, dirs2, sizeof(double) * 2 * dim, cudaMemcpyHostToDevice, ctx.st));
+    struct Seg {
+        int64_t model, pos, n, at;  // k-points [pos, pos + n) of the model at chunk position at
+    };
+    size_t si = 0;
+    int64_t spos = 0;
+    for (int64_t done = 0; done < stotal;) {
+        const int64_t nkc = std::min(J.chunk, stotal - done);
+        std::vector<Seg> segs;
+        for (int64_t filled = 0; filled < nkc;) {
+            const int64_t i = sidx[si];
+            const int64_t n = std::min(nk[i] - spos, nkc - filled);
+            segs.push_back({i, spos, n, filled});
+            filled += n;
+            spos += n;
+            if (spos == nk[i]) {
+                ++si;
+                spos = 0;
+            }
+        }
+        // each segment's H and velocities from its own model, into the chunk's stacked buffers
+        for (const Seg& g : segs) {
+            double* kd = J.k_d + g.at * dim;
+            TBG_CUDA(cudaMemcpyAsync(kd, k + (off[g.model] + g.pos) * dim, sizeof(double) * g.n * dim,
+                                     cudaMemcpyHostToDevice, ctx.st));
+            ModelDev& Mi = const_cast<ModelDev&>(models[g.model]->d);
+            rc = (prec == TBG_PREC_MIXED)
+                     ? fourier_mixed_pairs(Mi, ctx.st, g.n, kd, dirs_d, Ptmp, J.fwork, J.fwork_bytes,
+                                           J.pairs + g.at * NN, nkc * NN)
+                     : fourier_direct(Mi, ctx.st, g.n, kd, TBG_GAUGE_ATOM, 2, dirs_d, J.H + g.at * NN,
+                                      J.V + g.at * 2 * NN, NN, 2 * NN);
+            if (rc) return rc;
+        }
+        // the rest once for the whole chunk
+        if ((rc = berry_tail(ctx, J, nkc, nullptr))) return rc;
+        for (const Seg& g : segs) {
+            const int64_t o = (off[g.model] + g.pos) * N;
+            if (Omega_out)
+                TBG_CUDA(cudaMemcpyAsync(Omega_out + o, J.Om + g.at * N, sizeof(double) * g.n * N,
+                                         cudaMemcpyDeviceToHost, ctx.st));
+            if (E_out)
+                TBG_CUDA(cudaMemcpyAsync(E_out + o, J.E + g.at * N, sizeof(double) * g.n * N, cudaMemcpyDeviceToHost,
+                                         ctx.st));
+        }
+        if (ctx.sync("berry multi")) return ctx.rc;
+        done += nkc;
+    }
+    if ((rc = check_status(J.status_d, ctx.st))) return rc;
+    return ctx.sync("berry multi");
 }
 
 static int hall_impl(const tbg_model* m, const int64_t* kmesh, int64_t k_begin, int64_t k_count, bool whole,

@@ -560,10 +560,10 @@ __global__ void tau_pairs_kernel(int64_t nk, int N, float4* __restrict__ C, cons
 }
 
 // Packed upper-triangle contraction output -> full float-pair H, V_0, V_1
-// (P: blocks [0, nk), [nk, 2nk), [2nk, 3nk) of N^2 elements) with the
+// (P: three blocks of nk N^2 elements, blk elements apart) with the
 // orbital-position term V_p += i (tau_p,n - tau_p,m) H, in float-pair arithmetic.
 __global__ void unpack_tau_kernel(int64_t nk, int N, const float4* __restrict__ Cp, const float2* __restrict__ tau2,
-                                  float4* __restrict__ P) {
+                                  float4* __restrict__ P, int64_t blk) {
     const int64_t NN = (int64_t)N * N;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= NN) return;
@@ -580,7 +580,7 @@ __global__ void unpack_tau_kernel(int64_t nk, int N, const float4* __restrict__ 
             const float4 v = c_elem(Cp, true, nk, N, 1 + p, kk, mrow, ncol);
             const float2 vr = df_add(make_float2(v.x, v.y), df_neg(df_mul(d[p], hi)));
             const float2 vi = df_add(make_float2(v.z, v.w), df_mul(d[p], hr));
-            P[((1 + p) * nk + kk) * NN + e] = make_float4(vr.x, vr.y, vi.x, vi.y);
+            P[(1 + p) * blk + kk * NN + e] = make_float4(vr.x, vr.y, vi.x, vi.y);
         }
     }
 }
@@ -890,13 +890,27 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
     return TBG_OK;
 }
 
+int fourier_mixed_packed(ModelDev& m, cudaStream_t st, bool* packed) {
+    std::lock_guard<std::mutex> lk(g_hop_mu);
+    if (!m.hop_slices) {
+        int rc = build_hop_table(m, st);
+        if (rc) return rc;
+    }
+    *packed = m.hop_packed;
+    return TBG_OK;
+}
+
 int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
-                        float4* C, void* scratch, size_t scratch_bytes) {
+                        float4* C, void* scratch, size_t scratch_bytes, float4* out, int64_t blk) {
     if (nk <= 0) return TBG_OK;
     if (!fourier_mixed_ok(m) || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
         return set_error(TBG_E_UNSUPPORTED, "fourier_mixed_pairs: nR beyond the exact contraction length");
     const int N = (int)m.nsta;
     const int64_t NN = (int64_t)N * N;
+    if (!out) {
+        out = C;
+        blk = nk * NN;
+    }
     zc* orbph;
     double* taup;
     float2* tau2;
@@ -906,11 +920,15 @@ int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* 
     KTimer kt(st, "tau_pairs_kernel");
     dim3 grid((unsigned)((NN + 255) / 256), (unsigned)std::min<int64_t>(nk, 65535));
     if (m.hop_packed) {
-        unpack_tau_kernel<<<grid, 256, 0, st>>>(nk, N, Cg, tau2, C);
+        unpack_tau_kernel<<<grid, 256, 0, st>>>(nk, N, Cg, tau2, out, blk);
         TBG_LAUNCHED("unpack_tau_kernel");
     } else {
         tau_pairs_kernel<<<grid, 256, 0, st>>>(nk, N, C, tau2);
         TBG_LAUNCHED("tau_pairs_kernel");
+        if (out != C)
+            for (int p = 0; p < 3; ++p)
+                TBG_CUDA(cudaMemcpyAsync(out + p * blk, C + p * nk * NN, sizeof(float4) * nk * NN,
+                                         cudaMemcpyDeviceToDevice, st));
     }
     return TBG_OK;
 }

@@ -248,9 +248,15 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
                   zc* V, float4* C, void* scratch, size_t scratch_bytes);
 // Same contraction, left in C as float pairs in the lattice gauge with the
 // orbital-position term added to V_0, V_1 (blocks [0,nk), [nk,2nk), [2nk,3nk)
-// of N^2 elements).  Requires fourier_mixed_ok(m).
+// of N^2 elements).  Requires fourier_mixed_ok(m).  With `out` the three
+// blocks go there instead, `blk` elements apart (k-points of several models
+// stacked in one buffer); C is then only needed when the hop table is not
+// packed (fourier_mixed_packed false).
 int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
-                        float4* C, void* scratch, size_t scratch_bytes);
+                        float4* C, void* scratch, size_t scratch_bytes, float4* out = nullptr, int64_t blk = 0);
+// Builds the model's hop table for the mixed contraction if needed; true when
+// its columns are the packed upper triangle (the tcgen05 form).
+int fourier_mixed_packed(ModelDev& m, cudaStream_t st, bool* packed);
 
 // Batched Hermitian eigensolver: A (batch, N, N) FP64 input (destroyed),
 // E (batch, N) ascending, U (batch, N, N) eigenvectors in columns (may be

@@ -123,3 +123,43 @@ def test_native_async_queue_matches_synchronous_calls():
     lib = batch._lib.load()
     st = batch.ctypes.c_int(0)
     assert lib.tbg_batch_wait(123456789, batch.ctypes.byref(st)) == 9  # unknown ticket
+
+
+@pytest.mark.parametrize("precision", [Precision.MIXED, Precision.FP64])
+def test_berry_curvature_many_matches_per_model(precision, monkeypatch):
+    """Models of one band count stacked into one pipeline
+    (tbg_berry_curvature_multi) give each model's berry_curvature_on results:
+    tables of different size, k-lists of different length (one empty), chunks
+    that end inside a model's k-list (TBG_MAX_CHUNK), a model of another
+    dimension (its own group) and a small model (the one-thread-per-k path,
+    run alone).  One model is also checked against the oracle."""
+    models = [W.random_model(3, 12, True, 1, seed=11), W.random_model(3, 12, True, 2, seed=12),
+              W.random_model(2, 12, True, 1, seed=13), W.random_model(3, 3, False, 1, seed=14),
+              W.random_model(3, 12, True, 1, seed=15), W.random_model(3, 12, True, 1, seed=16)]
+    rng = np.random.default_rng(7)
+    sizes = [37, 300, 50, 20, 0, 91]
+    ks = [rng.uniform(0, 1, (n, m.dim)) for n, m in zip(sizes, models)]
+    dirs3 = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])
+    p3 = Parameters.rank2((1, 1, 1), dirs3[0], dirs3[1], [0.0])
+    # the 2D model takes its own rank-2 directions: split by dimension
+    monkeypatch.setenv("TBG_MAX_CHUNK", "100")
+    idx3 = [0, 1, 3, 4, 5]
+    res = batch.berry_curvature_many([models[i] for i in idx3], [ks[i] for i in idx3], p3, precision)
+    for r, i in zip(res, idx3):
+        Om, E = r
+        Om1, E1 = models[i].berry_curvature_on(ks[i], p3, precision) if sizes[i] else (np.zeros((0, 1)),) * 2
+        assert Om.shape[0] == sizes[i]
+        if sizes[i] == 0:
+            continue
+        scale = max(np.abs(Om1).max(), 1e-300)
+        assert np.max(np.abs(Om - Om1)) <= 1e-12 * scale, i
+        assert np.max(np.abs(E - E1)) <= 1e-12 * max(np.abs(E1).max(), 1.0), i
+    Om, E = res[1]
+    Omr, Er = O.berry_on(models[1], ks[1][:4], dirs3)
+    tol = 1e-6 if precision == Precision.MIXED else 1e-8
+    assert np.max(np.abs(Om[:4] - Omr)) <= tol * np.abs(Omr).max()
+    assert np.max(np.abs(E[:4] - Er)) <= 1e-9 * np.abs(Er).max()
+    p2 = Parameters.rank2((1, 1), [1.0, 0.0], [0.0, 1.0], [0.0])
+    (Om2, E2), = batch.berry_curvature_many([models[2]], [ks[2]], p2, precision)
+    Om2r, E2r = models[2].berry_curvature_on(ks[2], p2, precision)
+    assert np.max(np.abs(Om2 - Om2r)) <= 1e-12 * np.abs(Om2r).max()
