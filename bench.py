@@ -151,8 +151,9 @@ def algorithmic_flops_per_k(N: int, nR: int) -> float:
 # DRAM bytes (read + write) per k-point of each kernel family, from ncu captures over 512 k-points
 # of this workload: the FP32 solver's passes (TMEM-resident reduction, back-transformation), the
 # three HIGH products of the refinement and the four MID products of the rotation of one k-point.
-DRAM_BYTES_PER_MATRIX = {"hetrd_tc_kernel": 141.3e6 / 512, "heev_kernel<float,smem>": 112.5e6 / 512,
-                         "heev_bt_kernel": 112.5e6 / 512}
+DRAM_BYTES_PER_MATRIX = {"hetrd_tc_kernel": 141.3e6 / 512, "bt_tc_kernel": 109.3e6 / 512,
+                         "heev_kernel<float,smem>": 112.5e6 / 512, "heev_bt_kernel": 112.5e6 / 512,
+                         "ozaki_tc_kernel<high>": 730.9e6 / 512, "ozaki_tc_kernel<mid>": 1466.6e6 / 512}
 
 
 def slice_products(name: str) -> int:
