@@ -280,10 +280,17 @@ __host__ __device__ inline size_t packed_elems(int N) {  // rounded to 16 bytes 
     return PACKED ? (((size_t)N * (N + 1) / 2 + 1) & ~(size_t)1) : (size_t)N * N;
 }
 
+// First packed element of the rows kept in shared memory in the hybrid layout
+// (rows below r0 in global memory), rounded down to an even index so the
+// buffers after the matrix stay 16-byte aligned; 0 without it.
+__host__ __device__ inline size_t hyb_smem_start(int N, int r0) {
+    return r0 > 0 ? diag_off<true>(N, 0, r0) & ~(size_t)1 : 0;
+}
+
 template <typename T>
-__host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB) {
+__host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int PB, int r0 = 0) {
     size_t b = 0;
-    if (a_smem) b += sizeof(cx<T>) * packed_elems<true>(N);  // packed upper triangle
+    if (a_smem) b += sizeof(cx<T>) * (packed_elems<true>(N) - hyb_smem_start(N, r0));  // packed upper triangle
     b += sizeof(T) * 4 * (size_t)N;
     b += sizeof(cx<T>) * 4 * (size_t)N;  // tau, v, v2, w
     b += sizeof(T) * 64;
@@ -304,19 +311,26 @@ __host__ __device__ inline size_t eig_smem_bytes(int N, bool a_smem, int G, int 
 // input matrix is reduced in place (destroyed).  U: (batch, N, N) cx<T>.
 // MINB = CTAs per SM the launch bounds are set for: 3 (320 threads) for the
 // packed matrices of up to about 130 bands, else 2 or 1 (512 threads).
-template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
+// HYB (with A_SMEM): the hybrid layout for matrices whose packed triangle
+// exceeds shared memory: rows below r0 (the longest, and the ones the first
+// r0 steps finish) in global memory, Aglob (per CTA, packed as in shared
+// memory), the rest in shared memory.
+template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1), bool HYB = false>
 __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N, int64_t batch, zc* __restrict__ Hin,
                                                    const float4* __restrict__ Hpair, double* __restrict__ Eout,
                                                    cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
                                                    int* __restrict__ status, int G, int PB,
-                                                   const float* __restrict__ tri_de) {
+                                                   const float* __restrict__ tri_de, cx<T>* __restrict__ Aglob,
+                                                   int r0) {
+    static_assert(!HYB || A_SMEM, "the hybrid layout extends the shared-memory one");
+    if (!HYB) r0 = 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     EigShared<T> sh;
     {
         unsigned char* p = smem_raw;
         if (A_SMEM) {
             sh.A = reinterpret_cast<cx<T>*>(p);
-            p += sizeof(cx<T>) * packed_elems<true>(N);
+            p += sizeof(cx<T>) * (packed_elems<true>(N) - hyb_smem_start(N, r0));
         }
         sh.tau = reinterpret_cast<cx<T>*>(p);
         p += sizeof(cx<T>) * N;
@@ -338,23 +352,31 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
         p += sizeof(T) * 64;
         sh.scratch = A_SMEM ? reinterpret_cast<T*>(sh.A) : reinterpret_cast<T*>(p);
         // flags close the layout that eig_smem_bytes sizes
-        sh.flags = reinterpret_cast<int*>(smem_raw + eig_smem_bytes<T>(N, A_SMEM, G, PB) - sizeof(int) * (4 + (size_t)N));
+        sh.flags =
+            reinterpret_cast<int*>(smem_raw + eig_smem_bytes<T>(N, A_SMEM, G, PB, r0) - sizeof(int) * (4 + (size_t)N));
     }
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
     const size_t NN = (size_t)N * N;
     const int LDA = N;  // row stride of the working matrix in global memory
     auto doff = [&](int i) { return diag_off<A_SMEM>(N, LDA, i); };
+    const size_t e0s = hyb_smem_start(N, r0), e0 = HYB ? diag_off<true>(N, 0, r0) : 0;
+    cx<T>* Ag = HYB ? Aglob + (size_t)blockIdx.x * e0 : nullptr;
 
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
         cx<T>* A;
         if (A_SMEM) {
-            A = sh.A;
+            A = sh.A;  // (hybrid: the shared-memory rows, element doff(r) at A[doff(r) - e0s])
         } else if (sizeof(T) == sizeof(double)) {
             A = reinterpret_cast<cx<T>*>(Hin + b * NN);
         } else {
             A = Awork + (size_t)blockIdx.x * NN;
         }
+        // A(r, r): row r of the working matrix from its diagonal on
+        auto rowp = [&](int r) -> cx<T>* {
+            if constexpr (HYB) return (r < r0) ? Ag + doff(r) : A + (doff(r) - e0s);
+            return A + doff(r);
+        };
         if (tri_de) {
             // tridiagonal form given (TMEM-resident reduction): d then e
             const float* src = tri_de + (size_t)b * 2 * N;
@@ -373,7 +395,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                 const int r = (int)(idx / N), c = (int)(idx % N);
                 if (A_SMEM && c < r) continue;  // upper triangle only
                 const float4 h = src[idx];
-                A[doff(r) + (c - r)] = mk<T>((T)(h.x + h.y), (T)(h.z + h.w));
+                rowp(r)[c - r] = mk<T>((T)(h.x + h.y), (T)(h.z + h.w));
             }
         } else if (A_SMEM || sizeof(T) != sizeof(double)) {
             const zc* src = Hin + b * NN;
@@ -381,7 +403,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                 const int r = (int)(idx / N), c = (int)(idx % N);
                 if (A_SMEM && c < r) continue;
                 zc h = src[idx];
-                A[doff(r) + (c - r)] = mk<T>((T)h.re, (T)h.im);
+                rowp(r)[c - r] = mk<T>((T)h.re, (T)h.im);
             }
         }
         if (tid == 0) sh.flags[0] = 0;
@@ -396,7 +418,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
         // reflector by warp 0 from row jr: H^H [alpha; x] = [beta; 0]
         auto make_reflector = [&](int jr, cx<T>* vout) {
             const int mr = N - 1 - jr;
-            cx<T>* rowj = A + doff(jr) + 1;  // row jr, columns jr+1.. = conj(column jr)
+            cx<T>* rowj = rowp(jr) + 1;  // row jr, columns jr+1.. = conj(column jr)
             T part = 0;
             for (int i = 1 + lane; i < mr; i += 32) part += abs2(rowj[i]);
             const T xnorm2 = warp_sum(part);
@@ -423,7 +445,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
             if (lane == 0) {
                 sh.tau[jr] = tau;
                 sh.e[jr] = beta;
-                sh.d[jr] = A[doff(jr)].re;
+                sh.d[jr] = rowp(jr)[0].re;
             }
         };
         if (N > 1 && warp == 0) make_reflector(0, sh.v);
@@ -433,7 +455,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
             const cx<T>* v = (j & 1) ? sh.v2 : sh.v;
             const cx<T> tau = sh.tau[j];
             // A22(i, l) = A(j+1+i, j+1+l); row22(i)[l] = A22(i, l) for l >= i
-            auto row22 = [&](int i) { return A + doff(j + 1 + i) - i; };
+            auto row22 = [&](int i) { return rowp(j + 1 + i) - i; };
             // w = tau * A22 v: four threads per row, two-level butterfly; partial of w^H v
             cx<T> dpart = mk<T>(0, 0);
             {
@@ -453,7 +475,15 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                     // element offsets advance by doff(r + 4) - doff(r) - 4 per 4 rows
                     // (4 LDA for full rows; 4 N - 4 r - 10 packed, r the global row)
                     l = q;
-                    {
+                    if constexpr (HYB) {
+                        // row by row (the rows below r0 are in global memory)
+                        const int col = j + 1 + i;
+                        for (; l + 4 < i; l += 8) {
+                            fma_cjx(acc, rowp(j + 1 + l)[col - (j + 1 + l)], v[l]);
+                            fma_cjx(acc2, rowp(j + 5 + l)[col - (j + 5 + l)], v[l + 4]);
+                        }
+                        if (l < i) fma_cjx(acc, rowp(j + 1 + l)[col - (j + 1 + l)], v[l]);
+                    } else {
                         int r = j + 1 + q;
                         int a = (int)doff(r) + (j + 1 + i) - r;
                         int s4 = A_SMEM ? 4 * N - 4 * r - 10 : 4 * LDA;
@@ -515,7 +545,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
             __syncthreads();
         }
         if (tid == 0) {
-            sh.d[N - 1] = A[doff(N - 1)].re;
+            sh.d[N - 1] = rowp(N - 1)[0].re;
             sh.e[N - 1] = 0;
         }
         __syncthreads();
@@ -535,7 +565,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
             if (Uout && !tri_de) {
                 const size_t pe = packed_elems<true>(N);
                 cx<T>* dst = Awork + (size_t)b * (pe + N);
-                for (size_t i = tid; i < pe; i += nthr) dst[i] = A[i];
+                for (size_t i = tid; i < pe; i += nthr) dst[i] = (HYB && i < e0) ? Ag[i] : A[i - e0s];
                 for (int i = tid; i < N; i += nthr) dst[pe + i] = sh.tau[i];
             }
         }
@@ -652,7 +682,8 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
         // (1) isolated eigenvalues: twisted factorisation, N scratch values
         //     each, at most one per thread at a time: all N in the freed matrix
         //     storage (N (N + 1) values) when it is in shared memory, else 4G
-        const int tw = A_SMEM ? min(N, nthr) : min(4 * G, nthr);
+        // (hybrid: the shared-memory rows hold 4 N G values, as in the global layout)
+        const int tw = (A_SMEM && !HYB) ? min(N, nthr) : min(4 * G, nthr);
         T* twx = A_SMEM ? reinterpret_cast<T*>(A) : sh.scratch;
         for (int g0 = 0; g0 < N; g0 += tw) {
             if (tid < tw && g0 + tid < N) {
@@ -824,7 +855,7 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
     cc* G = Y + (size_t)BT_NB * PB;             // BT_NB x BT_NB
     cc* tau = G + BT_NB * BT_NB;                // N4
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
-    constexpr int kPre = 8;  // tile elements per thread: BT_NB * N4 <= 8 * 512
+    constexpr int kPre = 8;  // tile elements per thread prefetched: all of BT_NB * N4 up to 256 bands
     if (N < 2) return;
     const int jtop = ((N - 2) / BT_NB) * BT_NB;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
@@ -978,7 +1009,8 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     }
                 }
             }
-            // the next block's tile into the other buffer
+            // the next block's tile into the other buffer (beyond kPre elements per thread,
+            // N above 256, the rest is read directly)
             if (j0 > 0) {
                 cc* nxt = Vbuf + (size_t)(buf ^ 1) * BT_NB * N4;
 #pragma unroll
@@ -986,6 +1018,7 @@ __global__ void __launch_bounds__(512, 1) heev_bt_tiled_kernel(int N, int64_t ba
                     const int e = tid + u * nthr;
                     if (e < BT_NB * N4) nxt[e] = pre[u];
                 }
+                for (int e = tid + kPre * nthr; e < BT_NB * N4; e += nthr) nxt[e] = bt_vb_elem(Vm, N, N4, j0 - BT_NB, e);
             }
             buf ^= 1;
             __syncthreads();
@@ -1050,12 +1083,12 @@ int allow_max_smem(K kern, size_t need) {
     return TBG_OK;
 }
 
-template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1)>
+template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1), bool HYB = false>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
                 size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr,
-                const float* tri_de = nullptr, bool skip_bt = false) {
-    const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB);
-    auto kern = heev_kernel<T, A_SMEM, MINB>;
+                const float* tri_de = nullptr, bool skip_bt = false, int r0 = 0) {
+    const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB, HYB ? r0 : 0);
+    auto kern = heev_kernel<T, A_SMEM, MINB, HYB>;
     if (int rc = allow_max_smem(kern, smem)) return rc;
     cudaError_t e;
     int dev = 0, nsm = 0, perSM = 0;
@@ -1072,17 +1105,26 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
         if (cap < 1) return set_error(TBG_E_OOM, "eigensolver workspace too small");
         grid = std::min(grid, cap);
     }
-    if (A_SMEM && U && work_bytes < sizeof(cx<T>) * (packed_elems<true>(N) + N) * (size_t)batch)
+    const size_t refl = sizeof(cx<T>) * (packed_elems<true>(N) + N) * (size_t)batch;
+    if (A_SMEM && U && work_bytes < refl)
         return set_error(TBG_E_OOM, "eigensolver workspace too small for the reflectors");
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
+    // hybrid layout: the global-memory rows of each CTA after the reflectors
+    cx<T>* Aglob = nullptr;
+    if (HYB) {
+        const size_t e0 = diag_off<true>(N, 0, r0);
+        if (work_bytes < refl + sizeof(cx<T>) * e0 * (size_t)grid)
+            return set_error(TBG_E_OOM, "eigensolver workspace too small for the hybrid layout");
+        Aglob = reinterpret_cast<cx<T>*>(static_cast<unsigned char*>(work) + refl);
+    }
     {
         // flops as LAPACK counts them: 16/3 N^3 (reduction) + 8 N^3 (back-transformation, a
         // separate pass when the matrix is in shared memory) + O(N^2) per matrix
         // (the tridiagonal stage alone, O(N^2) per matrix, is counted as no flops)
         KTimer kt(st, name, tri_de ? 0.0 : (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N * batch);
         kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work),
-                                                    status_d, G, PB, tri_de);
+                                                    status_d, G, PB, tri_de, Aglob, HYB ? r0 : 0);
         TBG_LAUNCHED(name);
     }
     if constexpr (A_SMEM) {
@@ -1121,6 +1163,30 @@ inline bool f32_in_smem(int N) {
     return f32_in_smem(N, G, PB);
 }
 
+// Hybrid layout for matrices whose packed triangle exceeds one CTA's shared
+// memory (from about 229 bands): the smallest r0 whose remaining rows fit with
+// room for the inverse-iteration / twisted-factorisation scratch of G >= 8
+// groups (4 N G values) and a back-transformation panel of at least 8
+// columns.  Up to TBG_F32_HYBRID_MAX bands (default 320; 0 = never).
+int f32_hybrid_max_n() {
+    static const int v = [] {
+        const char* s = std::getenv("TBG_F32_HYBRID_MAX");
+        return s ? std::max(0, std::atoi(s)) : 320;
+    }();
+    return v;
+}
+inline bool f32_hybrid_plan(int N, int& r0, int& G, int& PB) {
+    if (N > f32_hybrid_max_n() || f32_in_smem(N)) return false;
+    PB = bt_tiled_panel(N, kEigSmemOne);
+    if (PB < 8) return false;
+    for (r0 = 1; r0 < N; ++r0) {
+        const size_t part = sizeof(cc) * (packed_elems<true>(N) - hyb_smem_start(N, r0));
+        G = (int)std::min<size_t>(32, part / (sizeof(float) * 4 * (size_t)N));
+        if (G >= 8 && eig_smem_bytes<float>(N, true, G, PB, r0) <= kEigSmemOne) return true;
+    }
+    return false;
+}
+
 }  // namespace
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
@@ -1129,6 +1195,16 @@ size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (f32_in_smem(N))
         return (sizeof(cc) * (packed_elems<true>(N) + N) + sizeof(float) * 2 * (size_t)N) *
                (size_t)std::max<int64_t>(batch, 1);
+    int r0, G, PB;
+    if (f32_hybrid_plan(N, r0, G, PB)) {
+        // the reflectors, then each resident CTA's global-memory rows (at most two per SM)
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) nsm = 152;
+        const int64_t ctas = std::min<int64_t>(std::max<int64_t>(batch, 1), 2 * (int64_t)nsm);
+        return sizeof(cc) * (packed_elems<true>(N) + N) * (size_t)std::max<int64_t>(batch, 1) +
+               sizeof(cc) * diag_off<true>(N, 0, r0) * (size_t)ctas;
+    }
     return (size_t)sizeof(cc) * N * N * (size_t)std::min<int64_t>(batch, 152 * 4);
 }
 
@@ -1174,7 +1250,8 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem);
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
-    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB, nullptr);
+    kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB, nullptr,
+                                                nullptr, 0);
     TBG_LAUNCHED("heev_kernel<double> (static scratch)");
     return TBG_OK;
 }
@@ -1205,6 +1282,10 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
         return launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
                                         G, PB, Hpair);
     }
+    int r0 = 0;
+    if (f32_hybrid_plan(N, r0, G, PB))
+        return launch_heev<float, true, 2, true>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                 "heev_kernel<float,hybrid>", G, PB, Hpair, nullptr, false, r0);
     choose_g_pb<float>(N, false, 32, 64, G, PB);
     return launch_heev<float, false>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,global>",
                                      G, PB, Hpair);
