@@ -910,12 +910,14 @@ int tbg_berry_curvature_multi(int64_t n_models, const tbg_model* const* models, 
     std::vector<int64_t> off(n_models + 1, 0);
     for (int64_t i = 0; i < n_models; ++i) off[i + 1] = off[i] + nk[i];
     // Models outside the stacked form (the one-thread-per-k small-model kernel,
-    // position matrices, tables beyond the exact contraction) run alone.
+    // position matrices, tables beyond the exact contraction, another device
+    // than the first model's) run alone.
     std::vector<int64_t> sidx;
     int64_t stotal = 0, max_nR = 0;
     for (int64_t i = 0; i < n_models; ++i) {
         const ModelDev& Mi = models[i]->d;
-        const bool stack = !use_small_fused(Mi) && Mi.n_rmat == 0 && (prec == TBG_PREC_FP64 || fourier_mixed_ok(Mi));
+        const bool stack = !use_small_fused(Mi) && Mi.n_rmat == 0 && Mi.device == M0.device &&
+                           (prec == TBG_PREC_FP64 || fourier_mixed_ok(Mi));
         if (!stack) {
             if (nk[i] > 0 && (rc = berry_common(models[i], nk[i], k + off[i] * dim, dirs2, spin, eta, precision,
                                                 Omega_out ? Omega_out + off[i] * N : nullptr,
@@ -929,6 +931,7 @@ int tbg_berry_curvature_multi(int64_t n_models, const tbg_model* const* models, 
         max_nR = std::max<int64_t>(max_nR, Mi.nR);
     }
     if (stotal == 0) return TBG_OK;
+    if (cudaSetDevice(M0.device) != cudaSuccess) return set_error(TBG_E_CUDA, "cudaSetDevice failed");
     // buffers sized for the stacked model with the largest table (the Fourier scratch grows with nR)
     int64_t rep = sidx[0];
     for (int64_t i : sidx)

@@ -53,9 +53,11 @@ def quality(H, E, U):
 # of 4), one matrix per SM with the panel back-transformation (150, 200, 220),
 # the hybrid layout with the first rows in global memory (251, 300: rows below
 # 22 and 72), the matrix in global memory (330), the TMEM-resident reduction
-# (65-128), the small-matrix thread counts (9, 12, 17), and the edges of the
+# and back-transformation (65-128: both ends, and sizes that are not multiples
+# of the 8-column chunks), the small-matrix thread counts (9, 12, 17), and the
 # fused one-pass reduction (up to 129 bands: 129, 2, 3, 5).
-@pytest.mark.parametrize("n", [330, 300, 251, 220, 200, 150, 144, 131, 129, 128, 100, 64, 40, 17, 12, 9, 5, 3, 2])
+@pytest.mark.parametrize("n", [330, 300, 251, 220, 200, 150, 144, 131, 129, 128, 127, 100, 97, 65, 64, 40, 17, 12, 9, 5, 3,
+                               2])
 def test_fp32_eigenpairs_random_hermitian(n):
     rng = np.random.default_rng(n)
     X = rng.standard_normal((16, n, n)) + 1j * rng.standard_normal((16, n, n))
