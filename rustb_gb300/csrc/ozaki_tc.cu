@@ -384,19 +384,21 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                 const int kf = (it + 1) * TC_TK + 8 * g;
                 load8<FMTA>(A, idx0 + (int64_t)kf * kstride, kstride, rv ? n_valid(K, kf) : 0, nxt);
             }
+            // slice this stage while the MMAs of the two stages before it run; then
+            // wait only for the buffer and store
+            uint4 dre[S], dim[S];
+            item_planes<FMTA, 0, S>(cur, E, s1, s2, dre);
+            item_planes<FMTA, 1, S>(cur, E, s1, s2, dim);
             if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
                 abort_sh = 1;
                 break;
             }
             if (abort_sh) break;
             const uint32_t sa = sbase + bi * SB;
-            uint4 d[S];
-            item_planes<FMTA, 0, S>(cur, E, s1, s2, d);
 #pragma unroll
-            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_re, d[s]);
-            item_planes<FMTA, 1, S>(cur, E, s1, s2, d);
+            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_re, dre[s]);
 #pragma unroll
-            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(d[s]) : d[s]);
+            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(dim[s]) : dim[s]);
             fence_async_smem();  // make the generic-proxy writes visible to the tensor core
             mbar_arrive(&bar_full[bi]);
         }
@@ -446,24 +448,24 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     const int kf = (it + 1) * TC_TK + 8 * g;
                     load8<FB>(B, idx0 + (int64_t)kf * ldb, ldb, cv ? n_valid(K, kf) : 0, nxt);
                 }
+                uint4 dre[S], dim[S];
+                item_planes<FB, 0, S>(cur, E, s1, s2, dre);
+                item_planes<FB, 1, S>(cur, E, s1, s2, dim);
                 if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
                     abort_sh = 1;
                     break;
                 }
                 if (abort_sh) break;
                 const uint32_t sb = sbase + bi * SB + HS;
-                uint4 d[S];
-                item_planes<FB, 0, S>(cur, E, s1, s2, d);
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
-                    st_shared_v4(sb + s * PLANE + o_jre, d[s]);
-                    st_shared_v4(sb + s * PLANE + o_kim, d[s]);
+                    st_shared_v4(sb + s * PLANE + o_jre, dre[s]);
+                    st_shared_v4(sb + s * PLANE + o_kim, dre[s]);
                 }
-                item_planes<FB, 1, S>(cur, E, s1, s2, d);
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
-                    st_shared_v4(sb + s * PLANE + o_kre, d[s]);
-                    st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(d[s]));
+                    st_shared_v4(sb + s * PLANE + o_kre, dim[s]);
+                    st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(dim[s]));
                 }
                 fence_async_smem();
                 mbar_arrive(&bar_full[bi]);

@@ -196,3 +196,19 @@ def test_mixed_hall_fused_sums_many_mu(T):
     s = m.hall_conductivity(p, Precision.MIXED).conductivity
     ref = O.hall_conductivity(m, (3, 3, 2), XY3, mus, T)
     assert np.max(np.abs(s - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("norb", [251, 300])
+def test_large_model_band_resolved_omega_vs_oracle(norb):
+    """Models beyond one CTA's shared memory (the FP32 solver's hybrid layout,
+    the panel back-transformation, two row tiles of the exact-slice products
+    and, at 300 bands, contractions longer than one exact chunk): band-resolved
+    Omega and E of the mixed path at three k-points against the oracle."""
+    m = W.random_model(3, norb, False, 1, seed=norb)
+    k = np.random.default_rng(norb).uniform(0, 1, (3, 3))
+    p = Parameters.rank2((1, 1, 1), XY3[0], XY3[1], [0.0])
+    Om, E = m.berry_curvature_on(k, p, Precision.MIXED)
+    Omr, Er = O.berry_on(m, k, XY3)
+    nrm = np.abs(Er).max()
+    assert np.max(np.abs(E - Er)) <= 1e-9 * nrm
+    assert np.max(np.abs(Om - Omr)) <= 1e-6 * np.abs(Omr).max()
