@@ -321,7 +321,8 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                                                    cx<T>* __restrict__ Uout, cx<T>* __restrict__ Awork,
                                                    int* __restrict__ status, int G, int PB,
                                                    const float* __restrict__ tri_de, cx<T>* __restrict__ Aglob,
-                                                   int r0) {
+                                                   int r0, int stop, cx<T>* __restrict__ Tout,
+                                                   float* __restrict__ de_out) {
     static_assert(!HYB || A_SMEM, "the hybrid layout extends the shared-memory one");
     if (!HYB) r0 = 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -448,9 +449,13 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                 sh.d[jr] = rowp(jr)[0].re;
             }
         };
+        // stop > 0 (shared-memory layouts): only the first `stop` steps; the trailing
+        // block, the tridiagonal so far and the reflectors then go to global memory
+        // for the TMEM-resident reduction to finish
+        const int jend = (A_SMEM && stop > 0 && stop < N - 1) ? stop : N - 1;
         if (N > 1 && warp == 0) make_reflector(0, sh.v);
         __syncthreads();
-        for (int j = 0; j < N - 1; ++j) {
+        for (int j = 0; j < jend; ++j) {
             const int m = N - 1 - j;
             const cx<T>* v = (j & 1) ? sh.v2 : sh.v;
             const cx<T> tau = sh.tau[j];
@@ -537,12 +542,31 @@ __global__ void __launch_bounds__(MINB == 3 ? 320 : 512, MINB) heev_kernel(int N
                 if (nwarps == 1)
                     for (int i = 1; i < m; ++i) update_row(i);
                 __syncwarp();
-                if (m >= 2) make_reflector(j + 1, (j & 1) ? sh.v : sh.v2);
+                if (m >= 2 && j + 1 < jend) make_reflector(j + 1, (j & 1) ? sh.v : sh.v2);
             } else {
                 for (int i = warp; i < m; i += nwarps - 1) update_row(i);  // rows 1 .. m-1 over warps 1 ..
 
             }
             __syncthreads();
+        }
+        if (jend < N - 1) {
+            const int M = N - jend;
+            cx<T>* Tb = Tout + (size_t)b * M * M;
+            for (int idx = tid; idx < M * M; idx += nthr) {
+                const int i = idx / M, l = idx - i * M;
+                Tb[idx] = (i <= l) ? rowp(jend + i)[l - i] : conj(rowp(jend + l)[i - l]);
+            }
+            float* dd = de_out + (size_t)b * 2 * N;
+            for (int i = tid; i < jend; i += nthr) {
+                dd[i] = (float)sh.d[i];
+                dd[N + i] = (float)sh.e[i];
+            }
+            const size_t pe = packed_elems<true>(N);
+            cx<T>* dst = Awork + (size_t)b * (pe + N);  // rows from jend on are overwritten by the finish
+            for (size_t i = tid; i < pe; i += nthr) dst[i] = (HYB && i < e0) ? Ag[i] : A[i - e0s];
+            for (int i = tid; i < jend; i += nthr) dst[pe + i] = sh.tau[i];
+            __syncthreads();
+            continue;
         }
         if (tid == 0) {
             sh.d[N - 1] = rowp(N - 1)[0].re;
@@ -1086,7 +1110,8 @@ int allow_max_smem(K kern, size_t need) {
 template <typename T, bool A_SMEM, int MINB = (A_SMEM ? 2 : 1), bool HYB = false>
 int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* U, void* work,
                 size_t work_bytes, int* status_d, const char* name, int G, int PB, const float4* Hpair = nullptr,
-                const float* tri_de = nullptr, bool skip_bt = false, int r0 = 0) {
+                const float* tri_de = nullptr, bool skip_bt = false, int r0 = 0, int stop = 0,
+                cx<T>* Tout = nullptr, float* de_out = nullptr, size_t aglob_off = 0) {
     const size_t smem = eig_smem_bytes<T>(N, A_SMEM, G, PB, HYB ? r0 : 0);
     auto kern = heev_kernel<T, A_SMEM, MINB, HYB>;
     if (int rc = allow_max_smem(kern, smem)) return rc;
@@ -1110,25 +1135,30 @@ int launch_heev(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cx<T>* 
         return set_error(TBG_E_OOM, "eigensolver workspace too small for the reflectors");
     grid = std::min<int64_t>(grid, batch);
     if (grid < 1) return TBG_OK;
-    // hybrid layout: the global-memory rows of each CTA after the reflectors
+    // hybrid layout: the global-memory rows of each CTA, after the reflectors (or at aglob_off)
     cx<T>* Aglob = nullptr;
     if (HYB) {
         const size_t e0 = diag_off<true>(N, 0, r0);
-        if (work_bytes < refl + sizeof(cx<T>) * e0 * (size_t)grid)
+        const size_t off = aglob_off ? aglob_off : refl;
+        if (work_bytes < off + sizeof(cx<T>) * e0 * (size_t)grid)
             return set_error(TBG_E_OOM, "eigensolver workspace too small for the hybrid layout");
-        Aglob = reinterpret_cast<cx<T>*>(static_cast<unsigned char*>(work) + refl);
+        Aglob = reinterpret_cast<cx<T>*>(static_cast<unsigned char*>(work) + off);
     }
     {
         // flops as LAPACK counts them: 16/3 N^3 (reduction) + 8 N^3 (back-transformation, a
         // separate pass when the matrix is in shared memory) + O(N^2) per matrix
         // (the tridiagonal stage alone, O(N^2) per matrix, is counted as no flops)
-        KTimer kt(st, name, tri_de ? 0.0 : (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N * batch);
+        // (the partial reduction: 16/3 (N^3 - (N - stop)^3) flops)
+        const double fl = tri_de ? 0.0
+                          : stop > 0 ? 16.0 / 3.0 * ((double)N * N * N - (double)(N - stop) * (N - stop) * (N - stop))
+                                     : (A_SMEM && U ? 6.0 : 14.0) * (double)N * N * N;
+        KTimer kt(st, name, fl * batch);
         kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, H, Hpair, E, U, reinterpret_cast<cx<T>*>(work),
-                                                    status_d, G, PB, tri_de, Aglob, HYB ? r0 : 0);
+                                                    status_d, G, PB, tri_de, Aglob, HYB ? r0 : 0, stop, Tout, de_out);
         TBG_LAUNCHED(name);
     }
     if constexpr (A_SMEM) {
-        if (!U || skip_bt) return TBG_OK;
+        if (!U || skip_bt || stop > 0) return TBG_OK;
         static_assert(sizeof(T) == sizeof(float), "the shared-memory solver is the FP32 one");
         const size_t bsm = bt_tiled_smem_bytes(N, PB);
         auto bk = PB >= ((N + 3) & ~3) ? heev_bt_tiled_kernel<false> : heev_bt_tiled_kernel<true>;
@@ -1187,10 +1217,47 @@ inline bool f32_hybrid_plan(int N, int& r0, int& G, int& PB) {
     return false;
 }
 
+// Two-phase FP32 reduction for 129 .. f32_hybrid_max_n() bands: the
+// shared-memory (or hybrid) kernel does the first N - 128 steps and hands the
+// trailing 128 x 128 block to the TMEM-resident kernel, which finishes it;
+// the tridiagonal stage and the back-transformation then run on the whole
+// matrix.  Workspace: [reflectors + tau][d, e][trailing blocks][hybrid rows].
+struct TwoPhase {
+    bool on = false;
+    int ctas = 0, r0 = 0, G = 0, PB = 0;
+    size_t off_de = 0, off_tb = 0, off_ag = 0, total = 0;
+};
+inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+TwoPhase two_phase_plan(int N, int64_t batch) {
+    TwoPhase t;
+    if (!eig_tc_enabled() || N <= 128 || N > f32_hybrid_max_n()) return t;
+    int G = 0, PB = 0;
+    t.ctas = f32_smem_ctas(N, G, PB);
+    if (t.ctas == 0 && !f32_hybrid_plan(N, t.r0, G, PB)) return t;
+    t.G = G;
+    t.PB = PB;
+    const size_t b = (size_t)std::max<int64_t>(batch, 1);
+    t.off_de = al256(sizeof(cc) * (packed_elems<true>(N) + N) * b);
+    t.off_tb = t.off_de + al256(sizeof(float) * 2 * (size_t)N * b);
+    t.off_ag = t.off_tb + al256(sizeof(cc) * 128 * 128 * b);
+    size_t ag = 0;
+    if (t.r0 > 0) {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) nsm = 152;
+        ag = sizeof(cc) * diag_off<true>(N, 0, t.r0) * (size_t)std::min<int64_t>((int64_t)b, 2 * (int64_t)nsm);
+    }
+    t.total = t.off_ag + ag;
+    t.on = true;
+    return t;
+}
+
 }  // namespace
 
 size_t eig_workspace_bytes(int N, int64_t batch, int precision) {
     if (precision == 0) return 0;
+    const TwoPhase tp = two_phase_plan(N, batch);
+    if (tp.on) return tp.total;
     // reflectors (packed rows) and tau, then the tridiagonal forms of the TMEM-resident reduction
     if (f32_in_smem(N))
         return (sizeof(cc) * (packed_elems<true>(N) + N) + sizeof(float) * 2 * (size_t)N) *
@@ -1251,7 +1318,7 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
     if (e != cudaSuccess || perSM < 1) perSM = 1;
     const int64_t grid = std::min<int64_t>((int64_t)nsm * perSM, batch);
     kern<<<(unsigned)grid, threads, smem, st>>>(N, batch, A, nullptr, E, nullptr, nullptr, nullptr, G, PB, nullptr,
-                                                nullptr, 0);
+                                                nullptr, 0, 0, nullptr, nullptr);
     TBG_LAUNCHED("heev_kernel<double> (static scratch)");
     return TBG_OK;
 }
@@ -1274,6 +1341,44 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
                                                  "heev_tri_kernel<float>", G, PB, Hpair, de, bt_tc_enabled()))
             return rc;
         return (U && bt_tc_enabled()) ? bt_tc(st, N, batch, static_cast<const cc*>(work), U, status_d) : TBG_OK;
+    }
+    const TwoPhase tp = two_phase_plan(N, batch);
+    if (tp.on) {
+        if (work_bytes < tp.total) return set_error(TBG_E_OOM, "eigensolver workspace too small (two-phase reduction)");
+        unsigned char* w = static_cast<unsigned char*>(work);
+        float* de = reinterpret_cast<float*>(w + tp.off_de);
+        cc* Tb = reinterpret_cast<cc*>(w + tp.off_tb);
+        const int stop = N - 128;
+        int rc;
+        auto finish = [&]() {
+            return hetrd_tc(st, 128, batch, nullptr, nullptr, static_cast<cc*>(work), de, status_d, Tb, N, stop);
+        };
+        if (tp.r0 > 0) {
+            rc = launch_heev<float, true, 2, true>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                   "heev_kernel<float,hybrid>", tp.G, tp.PB, Hpair, nullptr, false,
+                                                   tp.r0, stop, Tb, de, tp.off_ag);
+            if (!rc) rc = finish();
+            if (!rc)
+                rc = launch_heev<float, true, 2, true>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                       "heev_tri_kernel<float>", tp.G, tp.PB, Hpair, de, false, tp.r0,
+                                                       0, nullptr, nullptr, tp.off_ag);
+        } else if (tp.ctas == 3) {
+            rc = launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                             "heev_kernel<float,smem>", tp.G, tp.PB, Hpair, nullptr, false, 0, stop, Tb,
+                                             de);
+            if (!rc) rc = finish();
+            if (!rc)
+                rc = launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                                 "heev_tri_kernel<float>", tp.G, tp.PB, Hpair, de);
+        } else {
+            rc = launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d, "heev_kernel<float,smem>",
+                                          tp.G, tp.PB, Hpair, nullptr, false, 0, stop, Tb, de);
+            if (!rc) rc = finish();
+            if (!rc)
+                rc = launch_heev<float, true>(st, N, batch, H, E, U, work, work_bytes, status_d,
+                                              "heev_tri_kernel<float>", tp.G, tp.PB, Hpair, de);
+        }
+        return rc;
     }
     if (ctas == 3)
         return launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,

@@ -107,11 +107,15 @@ __host__ __device__ __forceinline__ size_t ht_diag_off(int N, int i) {
 __host__ __device__ __forceinline__ size_t ht_packed_elems(int N) { return ((size_t)N * (N + 1) / 2 + 1) & ~(size_t)1; }
 
 // Hpair: float pairs {re_hi, re_lo, im_hi, im_lo} (batch, N, N), or Hz:
-// complex FP64.  Vt: (batch, packed + N) reflectors (packed rows) and tau;
-// de: (batch, 2 N) d then e.
+// complex FP64, or Hc: complex FP32.  Vt: (batch, packed + Nbig) reflectors
+// (packed rows) and tau; de: (batch, 2 Nbig) d then e.  The matrix may be the
+// trailing block (rows and columns off .. off + N - 1) of an Nbig-band one
+// whose first off steps another kernel has done: reflectors, tau, d and e
+// then go to rows off .. of the big matrix's layouts.
 __global__ void __launch_bounds__(HT_THREADS, 2)
     hetrd_tc_kernel(int N, int64_t batch, const float4* __restrict__ Hpair, const zc* __restrict__ Hz,
-                    cc* __restrict__ Vt, float* __restrict__ de, int* __restrict__ status, int wait_limit) {
+                    const cc* __restrict__ Hc, cc* __restrict__ Vt, float* __restrict__ de, int* __restrict__ status,
+                    int wait_limit, int Nbig, int off) {
     extern __shared__ __align__(1024) unsigned char ht_smem[];
     __shared__ __align__(8) uint64_t bar_mma, bar_ops;
     __shared__ uint32_t tmem_base_sh;
@@ -132,7 +136,7 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int q = warp & 3, h = warp >> 2;
     const int i = 32 * q + lane;  // this thread's row (TMEM lane)
-    const size_t NN = (size_t)N * N, pe = ht_packed_elems(N);
+    const size_t NN = (size_t)N * N, pe = ht_packed_elems(Nbig);
     const uint32_t sA = su32(opA), sB1 = su32(opB1), sB2 = su32(opB2);
 
     if (tid == 0) {
@@ -171,6 +175,10 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
                         const float4 p = Hpair[b * NN + (size_t)i * N + col];
                         xr = p.x + p.y;
                         xi = p.z + p.w;
+                    } else if (Hc) {
+                        const cc z = Hc[b * NN + (size_t)i * N + col];
+                        xr = z.re;
+                        xi = z.im;
                     } else {
                         const zc z = Hz[b * NN + (size_t)i * N + col];
                         xr = (float)z.re;
@@ -189,10 +197,10 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
         tc_fence_after();
 
         bool aborted = false;
-        cc* Vm = Vt + (size_t)b * (pe + N);
+        cc* Vm = Vt + (size_t)b * (pe + Nbig);
         cc wnext = mk<float>(0.f, 0.f);  // w of the previous step at the current column (row j)
-        size_t dj = 0;                   // packed offset of row j's diagonal
-        for (int j = 0; j < N - 1; dj += (size_t)(N - j), ++j) {
+        size_t dj = ht_diag_off(Nbig, off);  // packed offset of (big) row off + j's diagonal
+        for (int j = 0; j < N - 1; dj += (size_t)(Nbig - off - j), ++j) {
             const int jn = j + 1;
             // ------------------------------------- column j, reflector --
             cc a = mk<float>(0.f, 0.f);
@@ -235,7 +243,7 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
             }
             if (tid == 0) {
                 esm[j] = beta;
-                Vm[pe + j] = tau;
+                Vm[pe + off + j] = tau;
                 // step j-1's update must be in TMEM before the product below reads it
                 if (j > 0 && !mbar_wait(&bar_mma, (base + j - 1) & 1u, &abort_sh, wait_limit)) abort_sh = 1;
             }
@@ -367,12 +375,12 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
             esm[N - 1] = 0.f;
         }
         __syncthreads();
-        float* dout = de + (size_t)b * 2 * N;
+        float* dout = de + (size_t)b * 2 * Nbig + off;
         for (int k = tid; k < N; k += HT_THREADS) {
             dout[k] = dsm[k];
-            dout[N + k] = esm[k];
+            dout[Nbig + k] = esm[k];
         }
-        if (tid == 0) Vt[(size_t)b * (pe + N) + pe + (N - 1)] = mk<float>(0.f, 0.f);
+        if (tid == 0) Vt[(size_t)b * (pe + Nbig) + pe + (Nbig - 1)] = mk<float>(0.f, 0.f);
         __syncthreads();
     }
     tc_fence_before();
@@ -710,7 +718,8 @@ bool bt_tc_enabled() {
 size_t hetrd_tc_de_bytes(int N, int64_t batch) { return sizeof(float) * 2 * (size_t)N * (size_t)batch; }
 
 int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
-             int* status_d) {
+             int* status_d, const cc* Hc, int Nbig, int off) {
+    if (Nbig <= 0) Nbig = N;
     if (batch <= 0) return TBG_OK;
     if (!hetrd_tc_fits(N)) return set_error(TBG_E_UNSUPPORTED, "hetrd_tc: matrix order beyond 128");
     // a per-function attribute of the current device (set on every call: cheap, and right for every device)
@@ -721,7 +730,8 @@ int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const z
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = std::min<int64_t>((int64_t)nsm * 2, batch);
     KTimer kt(st, "hetrd_tc_kernel", 16.0 / 3.0 * (double)N * N * N * batch);
-    hetrd_tc_kernel<<<(unsigned)grid, HT_THREADS, HT_SMEM, st>>>(N, batch, Hpair, H, Vt, de, status_d, tc_wait_limit());
+    hetrd_tc_kernel<<<(unsigned)grid, HT_THREADS, HT_SMEM, st>>>(N, batch, Hpair, H, Hc, Vt, de, status_d,
+                                                                 tc_wait_limit(), Nbig, off);
     TBG_LAUNCHED("hetrd_tc_kernel");
     return TBG_OK;
 }

@@ -361,7 +361,7 @@ bool eig_tc_enabled();
 bool hetrd_tc_fits(int N);
 size_t hetrd_tc_de_bytes(int N, int64_t batch);
 int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const zc* H, cc* Vt, float* de,
-             int* status_d);
+             int* status_d, const cc* Hc = nullptr, int Nbig = 0, int off = 0);
 // Back-transformation U <- Q U of the same solver with U (eigenvectors of the
 // tridiagonal form, in columns) resident in TMEM and tcgen05 block updates.
 int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d);
