@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -596,7 +597,19 @@ int ozaki_build_hop_slices_real(cudaStream_t st, int Kc, int64_t Nc, const zc* T
 int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
                            int64_t ncols);
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
-                  const void* Bs, float4* C, int* err);
+                  const void* Bs, float4* C, int* err, int64_t high_rows);
+
+// Class of the velocity rows of the exact-slice Fourier sum: MID (five digits,
+// about 2^-35 of the row scale; the velocities only enter the rotation, which
+// is a MID product itself) unless TBG_FOURIER_V_HIGH=1.  The Hamiltonian rows
+// stay HIGH.
+static bool fourier_v_mid() {
+    static const bool mid = [] {
+        const char* e = std::getenv("TBG_FOURIER_V_HIGH");
+        return !(e && e[0] == '1');
+    }();
+    return mid;
+}
 
 bool fourier_mixed_ok(const ModelDev& m) { return m.nR <= ozaki_fourier_max_k(); }
 
@@ -858,8 +871,9 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     }
     int rc = cudaMemsetAsync(err, 0, sizeof(int), st) == cudaSuccess ? TBG_OK : set_error(TBG_E_CUDA, "memset");
     if (rc) return rc;
+    // rows [H | Vx | Vy] (nk each): H in the HIGH class, the velocities in MID
     rc = ozaki_fourier(st, 3 * nk, m.hop_packed ? NP : NN, m.hop_packed ? m.hop_K : nR, ph3, EA, m.hop_EB,
-                       m.hop_slices, Cg, err);
+                       m.hop_slices, Cg, err, fourier_v_mid() ? nk : -1);
     if (rc) return rc;
     *Cg_out = Cg;
     *orbph_out = orbph;

@@ -115,8 +115,18 @@ __device__ void jacobi_small(int c, zc* A, zc* W, double* w) {
 __device__ __forceinline__ zc pair_z(float4 v) { return mk((double)v.x + (double)v.y, (double)v.z + (double)v.w); }
 __device__ __forceinline__ zc widen(cc v) { return mk((double)v.re, (double)v.im); }
 
+// Offset (in doubles, even: 16-byte aligned) of the warps' cluster rotations in
+// oa_pairs_kernel's shared memory, after lam (N doubles) and three 4-byte arrays.
+__host__ __device__ constexpr size_t oa_wslot_off(int N) { return ((5 * (size_t)N + 1) / 2 + 1) & ~(size_t)1; }
+
 // One CTA per matrix.  XX = X^H X and S = X^H H X as float pairs -> refined
-// eigenvalues E (FP64) and the update F (FP32 complex).  The Rayleigh-Ritz
+// eigenvalues E (FP64) and the update F (FP32 complex).  E is the Rayleigh
+// quotient plus its second-order term: with F_tj the first-order coefficient
+// of X_t in eigenvector j, lambda_j += sum_t |F_tj|^2 (lambda_j - lambda_t)
+// over the separated t (for a cluster member, the same sum over the rotated
+// numerators).  The quotient alone is off by |r|^2 / gap for an FP32 residual
+// r, 1e-9 of ||H|| for pairs just outside the cluster threshold; the second-
+// order term leaves a third-order error.  The Rayleigh-Ritz
 // rotations of clusters (entries of order one) are not left in F: a product
 // X F whose operand columns hold them would be sliced on those columns'
 // exponents and lose the small first-order entries beside them.  They go to
@@ -124,7 +134,7 @@ __device__ __forceinline__ zc widen(cc v) { return mk((double)v.re, (double)v.im
 // matrix for member p of the cluster starting at i), with cinfo[j] =
 // (start << 4) | size for every member column j and -1 elsewhere, and their
 // block of F is zero.
-__global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, const float4* __restrict__ XX,
+__global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, const float4* __restrict__ XX,
                                                        const float4* __restrict__ S, double* __restrict__ E,
                                                        cc* __restrict__ F, int64_t* __restrict__ clusters,
                                                        int* __restrict__ cinfo, zc* __restrict__ Fcl) {
@@ -132,6 +142,10 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
     double* lam = smem;                                   // N
     float* lamf = reinterpret_cast<float*>(lam + N);      // N
     int* cstart = reinterpret_cast<int*>(lamf + N);       // N
+    float* corr = reinterpret_cast<float*>(cstart + N);   // N: second-order eigenvalue terms
+    // per warp: the rotation W and Ritz values of the cluster it is working on
+    zc* wslot = reinterpret_cast<zc*>(smem + oa_wslot_off(N));
+    double* wval = reinterpret_cast<double*>(wslot + (blockDim.x >> 5) * kMaxCluster * kMaxCluster);
     __shared__ double red[32];
     const int NN = N * N;
     for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
@@ -181,88 +195,159 @@ __global__ void __launch_bounds__(256) oa_pairs_kernel(int N, int64_t batch, con
         if (threadIdx.x == 0 && ncl && clusters)
             atomicAdd(reinterpret_cast<unsigned long long*>(clusters), (unsigned long long)ncl);
         __syncthreads();
-        // F for separated pairs (FP32); R/2 inside clusters and on the diagonal
-        for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
-            const int i = idx / N, j = idx - i * N;
-            const float4 x4 = XXb[idx];
-            float fr, fi;
-            if (cstart[i] == cstart[j]) {
-                fr = (i == j) ? 0.5f * ((1.f - x4.x) - x4.y) : -0.5f * (x4.x + x4.y);
-                fi = -0.5f * (x4.z + x4.w);
-            } else {
-                const float4 s4 = Sb[idx];
-                const float lj = lamf[j];
-                // |den| > 1e-3 max|lambda|: the fast reciprocal is accurate to a few ulp
-                const float rden = __frcp_rn((float)(lam[j] - lam[i]));
-                fr = ((s4.x + s4.y) - lj * (x4.x + x4.y)) * rden;
-                fi = ((s4.z + s4.w) - lj * (x4.z + x4.w)) * rden;
+        // F for separated pairs (FP32); R/2 inside clusters and on the diagonal.
+        // Thread (p, j) walks column j over the rows i = p (mod P) and sums the
+        // second-order terms of lambda_j in a fixed order (the result must not
+        // depend on scheduling: a matrix gives the same bits alone or in a batch).
+        const int P = max(1, (int)blockDim.x / N);
+        __shared__ float part[256];
+        for (int cj = threadIdx.x; cj < P * N; cj += blockDim.x) {
+            const int p = cj / N, j = cj - p * N;
+            const float lj = lamf[j];
+            float acc = 0.f;
+            for (int i = p; i < N; i += P) {
+                const int idx = i * N + j;
+                const float4 x4 = XXb[idx];
+                float fr, fi;
+                if (cstart[i] == cstart[j]) {
+                    fr = (i == j) ? 0.5f * ((1.f - x4.x) - x4.y) : -0.5f * (x4.x + x4.y);
+                    fi = -0.5f * (x4.z + x4.w);
+                } else {
+                    const float4 s4 = Sb[idx];
+                    // |den| > 1e-3 max|lambda|: the fast reciprocal is accurate to a few ulp
+                    const float den = (float)(lam[j] - lam[i]);
+                    const float rden = __frcp_rn(den);
+                    fr = ((s4.x + s4.y) - lj * (x4.x + x4.y)) * rden;
+                    fi = ((s4.z + s4.w) - lj * (x4.z + x4.w)) * rden;
+                    acc = fmaf(fr * fr + fi * fi, den, acc);
+                }
+                Fb[idx] = mk(fr, fi);
             }
-            Fb[idx] = mk(fr, fi);
+            if (P == 1)
+                corr[j] = acc;
+            else
+                part[cj] = acc;
+        }
+        if (P > 1) {
+            __syncthreads();
+            for (int j = threadIdx.x; j < N; j += blockDim.x) {
+                float acc = 0.f;
+                for (int p = 0; p < P; ++p) acc += part[p * N + j];
+                corr[j] = acc;
+            }
         }
         for (int i = threadIdx.x; i < N; i += blockDim.x) cinfo[b * N + i] = -1;
         __syncthreads();
-        // Rayleigh-Ritz on clusters (one thread per cluster, FP64)
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            if (cstart[i] != i) continue;
-            int c = 1;
-            while (i + c < N && cstart[i + c] == i) ++c;
-            if (c < 2 || c > kMaxCluster) continue;
-            zc A[kMaxCluster * kMaxCluster], W[kMaxCluster * kMaxCluster];
-            double w[kMaxCluster];
-            // S~ = S_c + (R_c S_c + S_c R_c)/2, with R_c = 2 F_c (F_c holds R_c/2 now)
-            for (int p = 0; p < c; ++p)
-                for (int q = 0; q < c; ++q) {
-                    zc acc = pair_z(Sb[(i + p) * N + (i + q)]);
-                    for (int t = 0; t < c; ++t) {
-                        const zc fpt = widen(Fb[(i + p) * N + (i + t)]);
-                        const zc stq = pair_z(Sb[(i + t) * N + (i + q)]);
-                        const zc spt = pair_z(Sb[(i + p) * N + (i + t)]);
-                        const zc ftq = widen(Fb[(i + t) * N + (i + q)]);
-                        acc = acc + fpt * stq + spt * ftq;
+        // Rayleigh-Ritz on clusters, one warp per cluster (dealt to the warps in
+        // index order).  Lane 0 diagonalises the projected block (FP64); the lanes
+        // then rotate the rows outside the cluster and sum the second-order terms
+        // of the Ritz values (a fixed-order warp reduction).
+        {
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+            zc* Ws = wslot + warp * kMaxCluster * kMaxCluster;
+            double* ws = wval + warp * kMaxCluster;
+            int k = 0;  // clusters seen so far (the same in every lane)
+            for (int base = 0; base < N; base += 32) {
+                const int il = base + lane;
+                int cl = 0;
+                if (il < N && cstart[il] == il) {
+                    cl = 1;
+                    while (il + cl < N && cstart[il + cl] == il) ++cl;
+                }
+                unsigned todo = __ballot_sync(0xffffffffu, cl >= 2 && cl <= kMaxCluster);
+                while (todo) {
+                    const int src = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const int c = __shfl_sync(0xffffffffu, cl, src);
+                    if ((k++ % nw) != warp) continue;
+                    const int i = base + src;
+                    if (lane == 0) {
+                        zc A[kMaxCluster * kMaxCluster], W[kMaxCluster * kMaxCluster];
+                        double w[kMaxCluster];
+                        // S~ = S_c + (R_c S_c + S_c R_c)/2, with R_c = 2 F_c (F_c holds R_c/2 now)
+                        for (int p = 0; p < c; ++p)
+                            for (int q = 0; q < c; ++q) {
+                                zc acc = pair_z(Sb[(i + p) * N + (i + q)]);
+                                for (int t = 0; t < c; ++t) {
+                                    const zc fpt = widen(Fb[(i + p) * N + (i + t)]);
+                                    const zc stq = pair_z(Sb[(i + t) * N + (i + q)]);
+                                    const zc spt = pair_z(Sb[(i + p) * N + (i + t)]);
+                                    const zc ftq = widen(Fb[(i + t) * N + (i + q)]);
+                                    acc = acc + fpt * stq + spt * ftq;
+                                }
+                                A[p * c + q] = acc;
+                            }
+                        for (int p = 0; p < c; ++p)  // Hermitise
+                            for (int q = p; q < c; ++q) {
+                                const zc a = A[p * c + q], bq = A[q * c + p];
+                                const zc h = mk(0.5 * (a.re + bq.re), 0.5 * (a.im - bq.im));
+                                A[p * c + q] = h;
+                                A[q * c + p] = conj(h);
+                            }
+                        jacobi_small(c, A, W, w);
+                        // F_c = (I + R_c/2) W - I
+                        zc Fn[kMaxCluster * kMaxCluster];
+                        for (int p = 0; p < c; ++p)
+                            for (int q = 0; q < c; ++q) {
+                                zc acc = W[p * c + q];
+                                for (int t = 0; t < c; ++t) acc = acc + widen(Fb[(i + p) * N + (i + t)]) * W[t * c + q];
+                                if (p == q) acc.re -= 1.0;
+                                Fn[p * c + q] = acc;
+                            }
+                        for (int p = 0; p < c; ++p) {
+                            for (int q = 0; q < c; ++q) {
+                                Fb[(i + p) * N + (i + q)] = mk(0.f, 0.f);
+                                Fcl[(b * N + i + p) * kMaxCluster + q] = Fn[p * c + q];
+                                Ws[p * c + q] = W[p * c + q];
+                            }
+                            cinfo[b * N + i + p] = (i << 4) | c;
+                            ws[p] = w[p];
+                            lam[i + p] = w[p];
+                        }
                     }
-                    A[p * c + q] = acc;
-                }
-            for (int p = 0; p < c; ++p)  // Hermitise
-                for (int q = p; q < c; ++q) {
-                    const zc a = A[p * c + q], bq = A[q * c + p];
-                    const zc h = mk(0.5 * (a.re + bq.re), 0.5 * (a.im - bq.im));
-                    A[p * c + q] = h;
-                    A[q * c + p] = conj(h);
-                }
-            jacobi_small(c, A, W, w);
-            // F_c = (I + R_c/2) W - I
-            zc Fn[kMaxCluster * kMaxCluster];
-            for (int p = 0; p < c; ++p)
-                for (int q = 0; q < c; ++q) {
-                    zc acc = W[p * c + q];
-                    for (int t = 0; t < c; ++t) acc = acc + widen(Fb[(i + p) * N + (i + t)]) * W[t * c + q];
-                    if (p == q) acc.re -= 1.0;
-                    Fn[p * c + q] = acc;
-                }
-            for (int p = 0; p < c; ++p) {
-                for (int q = 0; q < c; ++q) {
-                    Fb[(i + p) * N + (i + q)] = mk(0.f, 0.f);
-                    Fcl[(b * N + i + p) * kMaxCluster + q] = Fn[p * c + q];
-                }
-                cinfo[b * N + i + p] = (i << 4) | c;
-                lam[i + p] = w[p];
-            }
-            // rows outside the cluster: F_{t,c} <- F_{t,c} W
-            for (int t = 0; t < N; ++t) {
-                if (t >= i && t < i + c) continue;
-                zc row[kMaxCluster];
-                for (int q = 0; q < c; ++q) row[q] = widen(Fb[t * N + i + q]);
-                for (int q = 0; q < c; ++q) {
-                    zc acc = mk(0.0, 0.0);
-                    for (int u = 0; u < c; ++u) acc = acc + row[u] * W[u * c + q];
-                    Fb[t * N + i + q] = mk((float)acc.re, (float)acc.im);
+                    __syncwarp();
+                    // rows outside the cluster: F_{t,c} <- F_{t,c} W, and the second-order
+                    // terms from the rotated numerators n_tp = sum_q F_tq (lambda_q - lambda_t) W_qp
+                    // (lamf is never rewritten)
+                    double d2[kMaxCluster];
+                    for (int p = 0; p < c; ++p) d2[p] = 0.0;
+                    for (int t = lane; t < N; t += 32) {
+                        if (t >= i && t < i + c) continue;
+                        zc row[kMaxCluster], nrow[kMaxCluster];
+                        for (int q = 0; q < c; ++q) {
+                            row[q] = widen(Fb[t * N + i + q]);
+                            const double g = (double)lamf[i + q] - (double)lamf[t];
+                            nrow[q] = mk(row[q].re * g, row[q].im * g);
+                        }
+                        for (int q = 0; q < c; ++q) {
+                            zc acc = mk(0.0, 0.0), nacc = mk(0.0, 0.0);
+                            for (int u = 0; u < c; ++u) {
+                                acc = acc + row[u] * Ws[u * c + q];
+                                nacc = nacc + nrow[u] * Ws[u * c + q];
+                            }
+                            Fb[t * N + i + q] = mk((float)acc.re, (float)acc.im);
+                            d2[q] += (nacc.re * nacc.re + nacc.im * nacc.im) / (ws[q] - (double)lamf[t]);
+                        }
+                    }
+                    for (int q = 0; q < c; ++q) {
+                        double v = d2[q];
+                        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                        if (lane == 0) corr[i + q] = (float)v;
+                    }
+                    __syncwarp();
                 }
             }
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < N; i += blockDim.x) E[b * N + i] = lam[i];
+        for (int i = threadIdx.x; i < N; i += blockDim.x) E[b * N + i] = lam[i] + (double)corr[i];
         __syncthreads();
     }
+}
+
+// Dynamic shared memory of oa_pairs_kernel (256 threads): lam (double),
+// lamf, cstart, corr (4-byte, padded to 8) and each warp's cluster rotation.
+size_t oa_smem_bytes(int N) {
+    return sizeof(double) * oa_wslot_off(N) + 8 * (sizeof(zc) * kMaxCluster * kMaxCluster + sizeof(double) * kMaxCluster);
 }
 
 // X' = X + X F + X_c F_c as a float pair: hi = X (exact FP32 eigenvectors),
@@ -652,7 +737,9 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     // 3. Ogita-Aishima update F and refined eigenvalues
     {
         KTimer kt(st, "oa_kernel");
-        const size_t smem = sizeof(double) * N + sizeof(float) * N + sizeof(int) * N;
+        const size_t smem = oa_smem_bytes(N);
+        cudaError_t ea = cudaFuncSetAttribute(oa_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ea != cudaSuccess) return cuda_error(ea, "cudaFuncSetAttribute(oa_kernel)");
         oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, bC, E, F,
                                                                                         clusters_d, cinfo, Fcl);
         TBG_LAUNCHED("oa_kernel");

@@ -407,7 +407,8 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
         if (PRE) {
             // ------------------------- pre-sliced B: bulk copy of stage images
             if (q == 0) {
-                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HS;
+                // stage images hold TC_S planes; a class with fewer digits copies the leading S
+                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HALF_STAGE;
                 int last[2] = {-1, -1};
                 for (int it = 0; it < nstages; ++it) {
                     const int bi = it & 1;
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     }
                     if (abort_sh) break;
                     mbar_arrive_tx(&bar_bcopy[bi], HS);
-                    bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HS, HS, &bar_bcopy[bi]);
+                    bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HALF_STAGE, HS, &bar_bcopy[bi]);
                     last[bi] = it;
                 }
                 // every copy issued has landed before the CTA can leave
@@ -833,21 +834,34 @@ int ozaki_hop_image_real_launch(cudaStream_t st, int Kc, int64_t Nc, const zc* T
 }
 
 // Fourier contraction on tcgen05: C (M x Nc) = A (M x K FP64 phases) . hop
-// table (stage images); EA filled by the caller.  Row tiles vary fastest so
-// that the CTAs resident together share one column tile's images in L2.
-int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
-                     const void* img, float4* C, int* err) {
-    auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED, TC_S>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+// table (stage images); EA filled by the caller.  Rows [0, high_rows) use the
+// HIGH class, the rest the MID class (five of the images' six digit planes);
+// high_rows < 0 keeps every row HIGH.  Row tiles vary fastest so that the CTAs
+// resident together share one column tile's images in L2.
+template <int S>
+static int fourier_tc_launch(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA,
+                             const int* EB, const void* img, float4* C, int* err) {
+    if (M <= 0) return TBG_OK;
+    auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED, S>;
+    const int smem = tc_smem_bytes(S);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc fourier)");
+    KTimer kt(st, S == TC_S ? "ozaki_tc_fourier_kernel" : "ozaki_tc_fourier_kernel<mid>", 8.0 * (double)M * Nc * K);
+    dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
+    kern<<<grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0,
+                                         nullptr, tc_wait_limit());
+    TBG_LAUNCHED(S == TC_S ? "ozaki_tc_fourier_kernel" : "ozaki_tc_fourier_kernel<mid>");
+    return TBG_OK;
+}
+
+int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
+                     const void* img, float4* C, int* err, int64_t high_rows) {
     if ((Nc + TC_TN - 1) / TC_TN > 65535 || M > 0x7fffffff)
         return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier_tc: grid too large");
-    KTimer kt(st, "ozaki_tc_fourier_kernel", 8.0 * (double)M * Nc * K);
-    dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
-    kern<<<grid, TC_THREADS, TC_SMEM, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0,
-                                            nullptr, tc_wait_limit());
-    TBG_LAUNCHED("ozaki_tc_fourier_kernel");
-    return TBG_OK;
+    const int64_t mh = high_rows < 0 ? M : std::min<int64_t>(high_rows, M);
+    int rc = fourier_tc_launch<TC_S>(st, mh, Nc, K, A, EA, EB, img, C, err);
+    if (rc) return rc;
+    return fourier_tc_launch<5>(st, M - mh, Nc, K, A + mh * K, EA + mh, EB, img, C + mh * Nc, err);
 }
 
 }  // namespace tbg
