@@ -409,8 +409,8 @@ int tbg_kernel_timing_read(char* names, int64_t* launches, double* total_ms,
                            double* total_flops, int max_entries, int reset);
 
 /* Bytes of device scratch one call sizes its k-point chunks to at this
- * moment: TBG_CHUNK_BYTES when set, else an eighth of the free device memory
- * between 6 and 24 GB (no reference counterpart; for callers that admit
+ * moment: TBG_CHUNK_BYTES when set, else a sixth of the free device memory
+ * between 6 and 40 GB (no reference counterpart; for callers that admit
  * concurrent calls by device footprint). */
 int64_t tbg_chunk_budget_bytes(void);
 

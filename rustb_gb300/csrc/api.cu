@@ -102,11 +102,13 @@ struct Ctx {
     }
 };
 
-// Device scratch one call sizes its k-point chunks to: an eighth of the free
-// device memory, between 6 and 24 GB (so concurrent calls still leave memory
+// Device scratch one call sizes its k-point chunks to: a sixth of the free
+// device memory, between 6 and 40 GB (so concurrent calls still leave memory
 // free).  Larger chunks give each batched kernel more waves over which to
 // amortise its last, partly idle one: 8192 k-points of 128 bands took
-// 63.1 ms per step in 6 GB chunks, 60.7 in 12 GB and 59.9 in 24 GB.
+// 63.1 ms per step in 6 GB chunks, 60.7 in 12 GB and 59.9 in 24 GB (an
+// earlier build); with the current kernels 48.3 ms in three chunks, 47.2 in
+// two and 46.55 in one (33 GB).
 int64_t chunk_budget_bytes() {
     const char* s = std::getenv("TBG_CHUNK_BYTES");
     if (s) {
@@ -116,7 +118,7 @@ int64_t chunk_budget_bytes() {
     int64_t b = 6LL << 30;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-        b = std::max<int64_t>(b, std::min<int64_t>(24LL << 30, (int64_t)(free_b / 8)));
+        b = std::max<int64_t>(b, std::min<int64_t>(40LL << 30, (int64_t)(free_b / 6)));
     else
         cudaGetLastError();
     return b;
@@ -310,6 +312,8 @@ struct BerryJob {
     bool want_metric;
     double* Met;  // quantum metric (chunk, N) when want_metric
     const OccSums* occ = nullptr;  // mixed hall path: fused Omega + occupation k-sum
+    int* rexp = nullptr;           // mixed: row exponents of H, V_0, V_1 (3 chunk N) from the Fourier stage
+    bool rexp_ok = false;          // ... written for the current chunk
 };
 
 int alloc_berry(Ctx& ctx, BerryJob& J) {
@@ -337,6 +341,7 @@ int alloc_berry(Ctx& ctx, BerryJob& J) {
         J.fwork_bytes = fourier_mixed_scratch_bytes(*J.m, c);
         J.fwork = ctx.alloc<unsigned char>(J.fwork_bytes);
         J.pairs = ctx.alloc<float4>(3 * c * NN);
+        J.rexp = ctx.alloc<int>(3 * c * N);
     }
     if (ctx.rc == TBG_OK) {
         cudaError_t e = cudaMemsetAsync(J.status_d, 0, sizeof(int), ctx.st);
@@ -357,8 +362,10 @@ int run_berry_chunk(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
         // lattice gauge, or (position-matrix models, nR beyond the exact
         // contraction length) Atom-gauge FP64 converted to pairs
         float4* P = J.pairs;
+        J.rexp_ok = false;
         if (m.n_rmat == 0 && fourier_mixed_ok(m)) {
-            rc = fourier_mixed_pairs(m, ctx.st, nkc, J.k_d, J.dirs_d, P, J.fwork, J.fwork_bytes);
+            rc = fourier_mixed_pairs(m, ctx.st, nkc, J.k_d, J.dirs_d, P, J.fwork, J.fwork_bytes, nullptr, 0, J.rexp,
+                                     &J.rexp_ok);
             if (rc) return rc;
         } else {
             rc = fourier_mixed(m, ctx.st, nkc, J.k_d, J.dirs_d, J.H, J.V, P, J.fwork, J.fwork_bytes);
@@ -398,11 +405,16 @@ int berry_tail(Ctx& ctx, BerryJob& J, int64_t nkc, int64_t* clusters_d) {
                                   reinterpret_cast<float4*>(J.scratch));
             if (rc) return rc;
         }
+        // row exponents from the Fourier stage (the velocities' only when no
+        // spin dressing has changed them since)
+        const int* hr = J.rexp_ok ? J.rexp : nullptr;
+        const int* vr = (J.rexp_ok && J.spin < 0) ? J.rexp + nkc * N : nullptr;
+        J.rexp_ok = false;
         if (J.occ)
             return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, nullptr, J.work,
-                               J.work_bytes, J.status_d, clusters_d, nullptr, nullptr, J.occ);
+                               J.work_bytes, J.status_d, clusters_d, nullptr, nullptr, J.occ, hr, vr);
         return mixed_berry(ctx.st, N, nkc, P, P + nkc * NN, P + 2 * nkc * NN, J.eta, J.E, J.Om, J.work, J.work_bytes,
-                           J.status_d, clusters_d, J.Met);
+                           J.status_d, clusters_d, J.Met, nullptr, nullptr, hr, vr);
     }
     if (J.spin >= 0) {
         rc = spin_dress(ctx.st, N, m.norb, nkc, J.spin, J.V, 2 * NN, J.scratch);

@@ -563,25 +563,78 @@ __global__ void tau_pairs_kernel(int64_t nk, int N, float4* __restrict__ C, cons
 // Packed upper-triangle contraction output -> full float-pair H, V_0, V_1
 // (P: three blocks of nk N^2 elements, blk elements apart) with the
 // orbital-position term V_p += i (tau_p,n - tau_p,m) H, in float-pair arithmetic.
-__global__ void unpack_tau_kernel(int64_t nk, int N, const float4* __restrict__ Cp, const float2* __restrict__ tau2,
-                                  float4* __restrict__ P, int64_t blk) {
+// With rexp (three blocks of nk N ints) the row exponents of the three written
+// matrices come out too: when a block of 256 threads holds whole rows (N a
+// multiple of 32 dividing 256) each warp's maximum goes through shared memory
+// and the row's exponent is stored; otherwise rexp is preset below every
+// exponent and the maxima are folded in by atomicMax, one per warp when N is
+// a multiple of 32 (a warp then lies in one row), else per lane.
+constexpr int kUnpackThreads = 256;
+__host__ __device__ constexpr bool unpack_block_rows(int N) { return (N & 31) == 0 && kUnpackThreads % N == 0; }
+
+__global__ void __launch_bounds__(kUnpackThreads) unpack_tau_kernel(int64_t nk, int N, const float4* __restrict__ Cp,
+                                                                   const float2* __restrict__ tau2,
+                                                                   float4* __restrict__ P, int64_t blk,
+                                                                   int* __restrict__ rexp) {
     const int64_t NN = (int64_t)N * N;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= NN) return;
-    const int mrow = e / N, ncol = e - mrow * N;
+    const int e = blockIdx.x * kUnpackThreads + threadIdx.x;
+    const bool valid = e < NN;
+    const int mrow = valid ? e / N : 0, ncol = valid ? e - mrow * N : 0;
+    const bool warp_row = (N & 31) == 0, block_rows = unpack_block_rows(N);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int wmax[2][3][kUnpackThreads / 32];
     float2 d[2];
 #pragma unroll
     for (int p = 0; p < 2; ++p) d[p] = df_add(tau2[p * N + ncol], df_neg(tau2[p * N + mrow]));
-    for (int64_t kk = blockIdx.y; kk < nk; kk += gridDim.y) {
-        const float4 h = c_elem(Cp, true, nk, N, 0, kk, mrow, ncol);
-        P[kk * NN + e] = h;
-        const float2 hr = make_float2(h.x, h.y), hi = make_float2(h.z, h.w);
+    int par = 0;  // alternates per k-point of this block
+    for (int64_t kk = blockIdx.y; kk < nk; kk += gridDim.y, par ^= 1) {
+        float mag[3] = {0.f, 0.f, 0.f};
+        if (valid) {
+            const float4 h = c_elem(Cp, true, nk, N, 0, kk, mrow, ncol);
+            P[kk * NN + e] = h;
+            mag[0] = pair_mag(h);
+            const float2 hr = make_float2(h.x, h.y), hi = make_float2(h.z, h.w);
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
-            const float4 v = c_elem(Cp, true, nk, N, 1 + p, kk, mrow, ncol);
-            const float2 vr = df_add(make_float2(v.x, v.y), df_neg(df_mul(d[p], hi)));
-            const float2 vi = df_add(make_float2(v.z, v.w), df_mul(d[p], hr));
-            P[(1 + p) * blk + kk * NN + e] = make_float4(vr.x, vr.y, vi.x, vi.y);
+            for (int p = 0; p < 2; ++p) {
+                const float4 v = c_elem(Cp, true, nk, N, 1 + p, kk, mrow, ncol);
+                const float2 vr = df_add(make_float2(v.x, v.y), df_neg(df_mul(d[p], hi)));
+                const float2 vi = df_add(make_float2(v.z, v.w), df_mul(d[p], hr));
+                const float4 o = make_float4(vr.x, vr.y, vi.x, vi.y);
+                P[(1 + p) * blk + kk * NN + e] = o;
+                mag[1 + p] = pair_mag(o);
+            }
+        }
+        if (rexp) {
+            // magnitudes are >= 0 (NaN counts as 0, as fmaxf over a row would
+            // skip it), so their bit patterns order as integers
+#pragma unroll
+            for (int c = 0; c < 3; ++c) mag[c] = (mag[c] == mag[c]) ? mag[c] : 0.f;
+            if (block_rows) {
+                // every thread is valid (NN is a multiple of 256); the buffer
+                // alternates per k-point, so one barrier per k-point suffices
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const int v = __reduce_max_sync(0xffffffffu, __float_as_int(mag[c]));
+                    if (lane == 0) wmax[par][c][warp] = v;
+                }
+                __syncthreads();
+                const int rows = kUnpackThreads / N, wpr = N / 32;
+                if (threadIdx.x < 3 * rows) {
+                    const int c = threadIdx.x / rows, rr = threadIdx.x - c * rows;
+                    int v = 0;
+                    for (int w = rr * wpr; w < (rr + 1) * wpr; ++w) v = max(v, wmax[par][c][w]);
+                    rexp[(c * nk + kk) * N + blockIdx.x * rows + rr] = line_exp_of(__int_as_float(v));
+                }
+            } else if (warp_row) {  // NN and the warps' starts are multiples of 32: all lanes valid or none
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const int v = __reduce_max_sync(0xffffffffu, __float_as_int(mag[c]));
+                    if (valid && lane == 0) atomicMax(&rexp[(c * nk + kk) * N + mrow], line_exp_of(__int_as_float(v)));
+                }
+            } else if (valid) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) atomicMax(&rexp[(c * nk + kk) * N + mrow], line_exp_of(mag[c]));
+            }
         }
     }
 }
@@ -915,7 +968,9 @@ int fourier_mixed_packed(ModelDev& m, cudaStream_t st, bool* packed) {
 }
 
 int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
-                        float4* C, void* scratch, size_t scratch_bytes, float4* out, int64_t blk) {
+                        float4* C, void* scratch, size_t scratch_bytes, float4* out, int64_t blk, int* rexp,
+                        bool* rexp_filled) {
+    if (rexp_filled) *rexp_filled = false;
     if (nk <= 0) return TBG_OK;
     if (!fourier_mixed_ok(m) || scratch_bytes < fourier_mixed_scratch_bytes(m, nk))
         return set_error(TBG_E_UNSUPPORTED, "fourier_mixed_pairs: nR beyond the exact contraction length");
@@ -934,7 +989,13 @@ int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* 
     KTimer kt(st, "tau_pairs_kernel");
     dim3 grid((unsigned)((NN + 255) / 256), (unsigned)std::min<int64_t>(nk, 65535));
     if (m.hop_packed) {
-        unpack_tau_kernel<<<grid, 256, 0, st>>>(nk, N, Cg, tau2, out, blk);
+        if (rexp) {
+            // below every exponent (0x80808080), so each row's first atomicMax sets it
+            if (!unpack_block_rows(N))
+                TBG_CUDA(cudaMemsetAsync(rexp, 0x80, sizeof(int) * 3 * (size_t)nk * N, st));
+            if (rexp_filled) *rexp_filled = true;
+        }
+        unpack_tau_kernel<<<grid, kUnpackThreads, 0, st>>>(nk, N, Cg, tau2, out, blk, rexp);
         TBG_LAUNCHED("unpack_tau_kernel");
     } else {
         tau_pairs_kernel<<<grid, 256, 0, st>>>(nk, N, C, tau2);

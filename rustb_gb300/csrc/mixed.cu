@@ -116,8 +116,8 @@ __device__ __forceinline__ zc pair_z(float4 v) { return mk((double)v.x + (double
 __device__ __forceinline__ zc widen(cc v) { return mk((double)v.re, (double)v.im); }
 
 // Offset (in doubles, even: 16-byte aligned) of the warps' cluster rotations in
-// oa_pairs_kernel's shared memory, after lam (N doubles) and three 4-byte arrays.
-__host__ __device__ constexpr size_t oa_wslot_off(int N) { return ((5 * (size_t)N + 1) / 2 + 1) & ~(size_t)1; }
+// oa_pairs_kernel's shared memory, after lam (N doubles) and four 4-byte arrays.
+__host__ __device__ constexpr size_t oa_wslot_off(int N) { return (3 * (size_t)N + 1) & ~(size_t)1; }
 
 // One CTA per matrix.  XX = X^H X and S = X^H H X as float pairs -> refined
 // eigenvalues E (FP64) and the update F (FP32 complex).  E is the Rayleigh
@@ -137,12 +137,14 @@ __host__ __device__ constexpr size_t oa_wslot_off(int N) { return ((5 * (size_t)
 __global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, const float4* __restrict__ XX,
                                                        const float4* __restrict__ S, double* __restrict__ E,
                                                        cc* __restrict__ F, int64_t* __restrict__ clusters,
-                                                       int* __restrict__ cinfo, zc* __restrict__ Fcl) {
+                                                       int* __restrict__ cinfo, zc* __restrict__ Fcl,
+                                                       int* __restrict__ Fexp, unsigned long long* __restrict__ clist) {
     extern __shared__ double smem[];
     double* lam = smem;                                   // N
     float* lamf = reinterpret_cast<float*>(lam + N);      // N
     int* cstart = reinterpret_cast<int*>(lamf + N);       // N
     float* corr = reinterpret_cast<float*>(cstart + N);   // N: second-order eigenvalue terms
+    float* cmax = corr + N;                               // N: largest |F| entry of each column
     // per warp: the rotation W and Ritz values of the cluster it is working on
     zc* wslot = reinterpret_cast<zc*>(smem + oa_wslot_off(N));
     double* wval = reinterpret_cast<double*>(wslot + (blockDim.x >> 5) * kMaxCluster * kMaxCluster);
@@ -200,11 +202,11 @@ __global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, 
         // second-order terms of lambda_j in a fixed order (the result must not
         // depend on scheduling: a matrix gives the same bits alone or in a batch).
         const int P = max(1, (int)blockDim.x / N);
-        __shared__ float part[256];
+        __shared__ float part[256], partm[256];
         for (int cj = threadIdx.x; cj < P * N; cj += blockDim.x) {
             const int p = cj / N, j = cj - p * N;
             const float lj = lamf[j];
-            float acc = 0.f;
+            float acc = 0.f, mx = 0.f;
             for (int i = p; i < N; i += P) {
                 const int idx = i * N + j;
                 const float4 x4 = XXb[idx];
@@ -222,18 +224,26 @@ __global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, 
                     acc = fmaf(fr * fr + fi * fi, den, acc);
                 }
                 Fb[idx] = mk(fr, fi);
+                mx = fmaxf(mx, f32_mag(fr, fi));
             }
-            if (P == 1)
+            if (P == 1) {
                 corr[j] = acc;
-            else
+                cmax[j] = mx;
+            } else {
                 part[cj] = acc;
+                partm[cj] = mx;
+            }
         }
         if (P > 1) {
             __syncthreads();
             for (int j = threadIdx.x; j < N; j += blockDim.x) {
-                float acc = 0.f;
-                for (int p = 0; p < P; ++p) acc += part[p * N + j];
+                float acc = 0.f, mx = 0.f;
+                for (int p = 0; p < P; ++p) {
+                    acc += part[p * N + j];
+                    mx = fmaxf(mx, partm[p * N + j]);
+                }
                 corr[j] = acc;
+                cmax[j] = mx;
             }
         }
         for (int i = threadIdx.x; i < N; i += blockDim.x) cinfo[b * N + i] = -1;
@@ -304,13 +314,20 @@ __global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, 
                             ws[p] = w[p];
                             lam[i + p] = w[p];
                         }
+                        // the cluster's columns of X' are formed from this list
+                        const unsigned long long at = atomicAdd(&clist[0], 1ull);
+                        clist[1 + at] = ((unsigned long long)b << 20) | ((unsigned long long)i << 4) | (unsigned)c;
                     }
                     __syncwarp();
                     // rows outside the cluster: F_{t,c} <- F_{t,c} W, and the second-order
                     // terms from the rotated numerators n_tp = sum_q F_tq (lambda_q - lambda_t) W_qp
                     // (lamf is never rewritten)
                     double d2[kMaxCluster];
-                    for (int p = 0; p < c; ++p) d2[p] = 0.0;
+                    float mq[kMaxCluster];  // the rotated columns' largest entries (the block is zero)
+                    for (int p = 0; p < c; ++p) {
+                        d2[p] = 0.0;
+                        mq[p] = 0.f;
+                    }
                     for (int t = lane; t < N; t += 32) {
                         if (t >= i && t < i + c) continue;
                         zc row[kMaxCluster], nrow[kMaxCluster];
@@ -325,27 +342,39 @@ __global__ void __launch_bounds__(256, 5) oa_pairs_kernel(int N, int64_t batch, 
                                 acc = acc + row[u] * Ws[u * c + q];
                                 nacc = nacc + nrow[u] * Ws[u * c + q];
                             }
-                            Fb[t * N + i + q] = mk((float)acc.re, (float)acc.im);
+                            const float fre = (float)acc.re, fim = (float)acc.im;
+                            Fb[t * N + i + q] = mk(fre, fim);
+                            mq[q] = fmaxf(mq[q], f32_mag(fre, fim));
                             d2[q] += (nacc.re * nacc.re + nacc.im * nacc.im) / (ws[q] - (double)lamf[t]);
                         }
                     }
                     for (int q = 0; q < c; ++q) {
                         double v = d2[q];
-                        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                        if (lane == 0) corr[i + q] = (float)v;
+                        float mv = mq[q];
+                        for (int o = 16; o > 0; o >>= 1) {
+                            v += __shfl_xor_sync(0xffffffffu, v, o);
+                            mv = fmaxf(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+                        }
+                        if (lane == 0) {
+                            corr[i + q] = (float)v;
+                            cmax[i + q] = mv;
+                        }
                     }
                     __syncwarp();
                 }
             }
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < N; i += blockDim.x) E[b * N + i] = lam[i] + (double)corr[i];
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            E[b * N + i] = lam[i] + (double)corr[i];
+            if (Fexp) Fexp[b * N + i] = line_exp_of(cmax[i]);
+        }
         __syncthreads();
     }
 }
 
 // Dynamic shared memory of oa_pairs_kernel (256 threads): lam (double),
-// lamf, cstart, corr (4-byte, padded to 8) and each warp's cluster rotation.
+// lamf, cstart, corr, cmax (4-byte, padded to 8) and each warp's cluster rotation.
 size_t oa_smem_bytes(int N) {
     return sizeof(double) * oa_wslot_off(N) + 8 * (sizeof(zc) * kMaxCluster * kMaxCluster + sizeof(double) * kMaxCluster);
 }
@@ -355,32 +384,89 @@ size_t oa_smem_bytes(int N) {
 // of a cluster also gets the cluster's rotation, sum_p X[r, s + p] Fcl[s + p,
 // j - s] in FP64 (cinfo as oa_pairs_kernel writes it), and the pair is formed
 // from the FP64 sum.
-__global__ void xprime_kernel(int64_t n, int N, const cc* __restrict__ X, const float4* __restrict__ XF,
-                              const int* __restrict__ cinfo, const zc* __restrict__ Fcl, float4* __restrict__ Xp) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const cc x = X[i];
-        const float4 f = XF[i];
-        const int64_t b = i / ((int64_t)N * N);
-        const int j = (int)(i % N);
-        const int ci = cinfo[b * N + j];
-        if (ci < 0) {
-            Xp[i] = make_float4(x.re, f.x + f.y, x.im, f.z + f.w);
-            continue;
+// One thread per column walks its rows (a warp reads 32 consecutive entries
+// of a row), so with xpc the column exponents of X' (the conjugated operand of
+// the rotation) come out of the same pass.  Columns of clusters are left to
+// xprime_cluster_kernel.
+__global__ void __launch_bounds__(128, 16) xprime_kernel(int64_t batch, int N, const cc* __restrict__ X,
+                                                         const float4* __restrict__ XF, const int* __restrict__ cinfo,
+                                                         float4* __restrict__ Xp, int* __restrict__ xpc) {
+    const int nch = (N + 127) / 128;
+    const int64_t NN = (int64_t)N * N;
+    for (int64_t w = blockIdx.x; w < batch * nch; w += gridDim.x) {
+        const int64_t b = w / nch;
+        const int j = (int)(w % nch) * 128 + threadIdx.x;
+        if (j >= N || cinfo[b * N + j] >= 0) continue;
+        const cc* Xb = X + b * NN + j;
+        const float4* XFb = XF + b * NN + j;
+        float4* Xpb = Xp + b * NN + j;
+        float m = 0.f;
+#pragma unroll 4
+        for (int r = 0; r < N; ++r) {
+            const int64_t i = (int64_t)r * N;
+            const cc x = Xb[i];
+            const float4 f = XFb[i];
+            const float4 o = make_float4(x.re, f.x + f.y, x.im, f.z + f.w);
+            Xpb[i] = o;
+            m = fmaxf(m, pair_mag(o));
         }
-        const int st = ci >> 4, c = ci & 15;
-        const cc* xr = X + (i - j);  // row r of this matrix
-        const zc* fc = Fcl + (b * N + st) * kMaxCluster + (j - st);
-        double re = ((double)f.x + (double)f.y), im = ((double)f.z + (double)f.w);
-        for (int p = 0; p < c; ++p) {
-            const cc a = xr[st + p];
-            const zc w = fc[p * kMaxCluster];
-            re += (double)a.re * w.re - (double)a.im * w.im;
-            im += (double)a.re * w.im + (double)a.im * w.re;
+        if (xpc) xpc[b * N + j] = line_exp_of(m);
+    }
+}
+
+// The columns of clusters: X' in FP64 with the cluster's rotation
+// sum_p X[r, st + p] Fcl[st + p, j - st], then the pair.  One block per entry
+// of clist (count, then (b << 20 | st << 4 | c) per cluster, as
+// oa_pairs_kernel appends them), threads over the rows; the column maxima
+// are combined in integer order of their bits (the magnitudes are >= 0).
+__global__ void __launch_bounds__(128) xprime_cluster_kernel(int N, const cc* __restrict__ X,
+                                                             const float4* __restrict__ XF, const zc* __restrict__ Fcl,
+                                                             float4* __restrict__ Xp, int* __restrict__ xpc,
+                                                             const unsigned long long* __restrict__ clist) {
+    __shared__ int wm[4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long n = clist[0];
+    const int64_t NN = (int64_t)N * N;
+    for (unsigned long long e = blockIdx.x; e < n; e += gridDim.x) {
+        const unsigned long long v = clist[1 + e];
+        const int64_t b = (int64_t)(v >> 20);
+        const int st = (int)((v >> 4) & 0xFFFF), c = (int)(v & 15);
+        const cc* Xb = X + b * NN;
+        const float4* XFb = XF + b * NN;
+        float4* Xpb = Xp + b * NN;
+        for (int q = 0; q < c; ++q) {
+            const int j = st + q;
+            const zc* fc = Fcl + (b * N + st) * kMaxCluster + q;
+            float m = 0.f;
+            for (int r = threadIdx.x; r < N; r += blockDim.x) {
+                const int64_t i = (int64_t)r * N + j;
+                const cc x = Xb[i];
+                const float4 f = XFb[i];
+                const cc* xr = Xb + (int64_t)r * N;  // row r
+                double re = ((double)f.x + (double)f.y), im = ((double)f.z + (double)f.w);
+                for (int p = 0; p < c; ++p) {
+                    const cc a = xr[st + p];
+                    const zc wv = fc[p * kMaxCluster];
+                    re += (double)a.re * wv.re - (double)a.im * wv.im;
+                    im += (double)a.re * wv.im + (double)a.im * wv.re;
+                }
+                re += (double)x.re;
+                im += (double)x.im;
+                const float rh = (float)re, ih = (float)im;
+                const float4 o = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+                Xpb[i] = o;
+                m = fmaxf(m, pair_mag(o));
+            }
+            const int wv = __reduce_max_sync(0xffffffffu, __float_as_int(m));
+            if (lane == 0) wm[warp] = wv;
+            __syncthreads();
+            if (threadIdx.x == 0 && xpc) {
+                int mx = 0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = max(mx, wm[w]);
+                xpc[b * N + j] = line_exp_of(__int_as_float(mx));
+            }
+            __syncthreads();
         }
-        re += (double)x.re;
-        im += (double)x.im;
-        const float rh = (float)re, ih = (float)im;
-        Xp[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
     }
 }
 
@@ -668,14 +754,16 @@ size_t mixed_berry_workspace_bytes(int N, int64_t batch) {
     // X and F (cc) + 5 pair buffers + line exponents (10 operand sides) + FP32 solver workspace
     return (size_t)batch * NN * (2 * sizeof(cc) + 5 * sizeof(float4)) + sizeof(int) * 10 * (size_t)batch * N +
            ozaki_exp_bytes(batch, N, N) + eig_workspace_bytes(N, batch, 1) +
-           (size_t)batch * N * (sizeof(int) + kMaxCluster * sizeof(zc)) + 4096 + 512;
+           (size_t)batch * N * (sizeof(int) + kMaxCluster * sizeof(zc)) +
+           sizeof(unsigned long long) * ((size_t)batch * N / 2 + 1) + 4096 + 768;
 }
 
 // H, Vx, Vy as float pairs (batch stride N*N) -> E (refined, ascending), Omega and, when Met is
 // not null, the quantum metric.
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met, zc* Uout, const OccSums* occ) {
+                int64_t* clusters_d, double* Met, zc* Uout, const OccSums* occ, const int* h_rexp,
+                const int* v_rexp) {
     if (batch <= 0) return TBG_OK;
     const int64_t NN = (int64_t)N * N;
     if (work_bytes < mixed_berry_workspace_bytes(N, batch)) return set_error(TBG_E_OOM, "mixed workspace too small");
@@ -699,11 +787,26 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     int* ex = static_cast<int*>(take(sizeof(int) * 10 * (size_t)batch * N));
     int* cinfo = static_cast<int*>(take(sizeof(int) * (size_t)batch * N));
     zc* Fcl = static_cast<zc*>(take(sizeof(zc) * kMaxCluster * (size_t)batch * N));
-    auto slot = [&](int i) { return ex + (size_t)i * batch * N; };
-    enum { XC, HR, HXC, XR, FC, XPC, VXR, VYR, BXC, BYC };
+    // clusters found by the refinement: a count, then one entry per cluster
+    unsigned long long* clist =
+        static_cast<unsigned long long*>(take(sizeof(unsigned long long) * ((size_t)batch * N / 2 + 1)));
+    enum { XC, HR, HXC, XR, FC, XPC, VXR, VYR, BXC, BYC, NSLOT };
+    // slots whose exponents a kernel writing the operand has already produced
+    // (the caller's for H, Vx, Vy; the refinement kernel's for F; the X' pass's)
+    int* given[NSLOT] = {};
+    bool ready[NSLOT] = {};
+    auto slot = [&](int i) { return given[i] ? given[i] : ex + (size_t)i * batch * N; };
     const bool tc = ozaki_use_tc();
+    if (tc) {
+        given[HR] = const_cast<int*>(h_rexp);
+        given[VXR] = const_cast<int*>(v_rexp);
+        given[VYR] = v_rexp ? const_cast<int*>(v_rexp) + batch * N : nullptr;
+        ready[HR] = h_rexp != nullptr;
+        ready[VXR] = ready[VYR] = v_rexp != nullptr;
+    }
     auto exps = [&](int fmt, bool cols, const void* M, int s) -> int {
-        return tc ? ozaki_line_exps(st, fmt, cols, batch, N, N, M, N, NN, slot(s)) : TBG_OK;
+        if (!tc || ready[s]) return TBG_OK;
+        return ozaki_line_exps(st, fmt, cols, batch, N, N, M, N, NN, slot(s));
     };
     const size_t eigw_bytes = eig_workspace_bytes(N, batch, 1);
     void* eigw = take(eigw_bytes);
@@ -740,9 +843,11 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
         const size_t smem = oa_smem_bytes(N);
         cudaError_t ea = cudaFuncSetAttribute(oa_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (ea != cudaSuccess) return cuda_error(ea, "cudaFuncSetAttribute(oa_kernel)");
-        oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(N, batch, bA, bC, E, F,
-                                                                                        clusters_d, cinfo, Fcl);
+        TBG_CUDA(cudaMemsetAsync(clist, 0, sizeof(unsigned long long), st));
+        oa_pairs_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, smem, st>>>(
+            N, batch, bA, bC, E, F, clusters_d, cinfo, Fcl, tc ? slot(FC) : nullptr, clist);
         TBG_LAUNCHED("oa_kernel");
+        ready[FC] = tc;
     }
     auto energies_out = [&]() -> int {
         sort_e_om_kernel<<<(unsigned)std::min<int64_t>(batch, 152 * 8), 256, 3 * sizeof(double) * N, st>>>(
@@ -767,8 +872,13 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     if (rc) return rc;
     {
         KTimer kt(st, "xprime_kernel");
-        xprime_kernel<<<nblk(batch * NN), 256, 0, st>>>(batch * NN, N, X, bE, cinfo, Fcl, bA);
+        const int64_t work = batch * ((N + 127) / 128);
+        const unsigned g = (unsigned)std::min<int64_t>(work, 152 * 64);
+        xprime_kernel<<<g, 128, 0, st>>>(batch, N, X, bE, cinfo, bA, tc ? slot(XPC) : nullptr);
         TBG_LAUNCHED("xprime_kernel");
+        xprime_cluster_kernel<<<152 * 4, 128, 0, st>>>(N, X, bE, Fcl, bA, tc ? slot(XPC) : nullptr, clist);
+        TBG_LAUNCHED("xprime_cluster_kernel");
+        ready[XPC] = tc;
     }
     if (Uout) {  // eigenpairs only: refined E and X' in ascending order, no velocities
         const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)N;

@@ -43,12 +43,9 @@ constexpr int OZ_TM = 64;      // output rows per CTA
 constexpr int OZ_TN = 64;      // complex output columns per CTA (128 real)
 constexpr int OZ_TK = 16;      // complex k per stage (32 real)
 constexpr int OZ_PAD = 40;     // bf16 per smem row (32 + 8 pad, 80 bytes)
-constexpr int OZ_ZERO_EXP = -100000;
+constexpr int OZ_ZERO_EXP = kLineZeroExp;
 
-__device__ __forceinline__ int exp_of_max(float m) {
-    if (!(m > 0.f)) return OZ_ZERO_EXP;
-    return ilogbf(m) + 1;  // m < 2^E
-}
+__device__ __forceinline__ int exp_of_max(float m) { return line_exp_of(m); }  // m < 2^E
 
 // Signed fixed-point value trunc(x * 2^(42 - E)) of a double, |x| < 2^E.
 __device__ __forceinline__ long long fixed_f64(double x, int E) {
@@ -127,10 +124,9 @@ __device__ __forceinline__ float mag_of(const void* base, int64_t idx) {
         return (float)fmax(fabs(v.x), fabs(v.y)) * 1.0000002f;
     } else if (FMT == FMT_F32) {
         const float2 v = reinterpret_cast<const float2*>(base)[idx];
-        return fmaxf(fabsf(v.x), fabsf(v.y));
+        return f32_mag(v.x, v.y);
     } else if (FMT == FMT_PAIR) {
-        const float4 v = reinterpret_cast<const float4*>(base)[idx];
-        return fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w));
+        return pair_mag(reinterpret_cast<const float4*>(base)[idx]);
     }
     return 0.f;
 }

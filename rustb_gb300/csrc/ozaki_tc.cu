@@ -61,7 +61,7 @@ constexpr int TC_THREADS = 416;                 // 13 warps
 constexpr int MMA_WARP = 12;
 constexpr int A_PRODUCERS = 256;
 constexpr int B_PRODUCERS = 128;
-constexpr int ZERO_EXP = -100000;
+constexpr int ZERO_EXP = kLineZeroExp;
 // Longest contraction one launch keeps exact: 2K real terms of digit products
 // below 2^15 per level stay within FP32's 24-bit significand.
 constexpr int kTcMaxK = 256;

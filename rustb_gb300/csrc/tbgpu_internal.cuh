@@ -112,6 +112,19 @@ __device__ __forceinline__ float2 df_of(double x) {
 }
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
+// Line exponents of the exact-slice products: E with m < 2^E for a line's
+// largest magnitude m (kLineZeroExp for an all-zero line).  E is monotone in m,
+// so the exponent of a line's maximum is the maximum of its elements'
+// exponents: kernels that write an operand fold them in with integer atomicMax
+// in any order.  Magnitude of an element: max(|re|, |im|) (FP32 complex) or
+// max(|re_hi| + |re_lo|, |im_hi| + |im_lo|) (float pair).
+constexpr int kLineZeroExp = -100000;
+__device__ __forceinline__ int line_exp_of(float m) { return (m > 0.f) ? ilogbf(m) + 1 : kLineZeroExp; }
+__device__ __forceinline__ float f32_mag(float re, float im) { return fmaxf(fabsf(re), fabsf(im)); }
+__device__ __forceinline__ float pair_mag(float4 v) {
+    return fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w));
+}
+
 // Occupation (src/thermodynamics.rs:100-118): T = 0 step with 1/2 at E == mu,
 // else the Fermi function with its +-50 clamp; width = k_B T.
 __device__ __forceinline__ double occupation_f(double e, double mu, double width) {
@@ -251,9 +264,13 @@ int fourier_mixed(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, c
 // of N^2 elements).  Requires fourier_mixed_ok(m).  With `out` the three
 // blocks go there instead, `blk` elements apart (k-points of several models
 // stacked in one buffer); C is then only needed when the hop table is not
-// packed (fourier_mixed_packed false).
+// packed (fourier_mixed_packed false).  With rexp (3 nk N ints) the row
+// exponents of the three blocks (H, V_0, V_1; k-major, as the exact-slice
+// products take them) are written there as a by-product when the table is
+// packed; *rexp_filled says whether they were.
 int fourier_mixed_pairs(ModelDev& m, cudaStream_t st, int64_t nk, const double* k_d, const double* dirs_d,
-                        float4* C, void* scratch, size_t scratch_bytes, float4* out = nullptr, int64_t blk = 0);
+                        float4* C, void* scratch, size_t scratch_bytes, float4* out = nullptr, int64_t blk = 0,
+                        int* rexp = nullptr, bool* rexp_filled = nullptr);
 // Builds the model's hop table for the mixed contraction if needed; true when
 // its columns are the packed upper triangle (the tcgen05 form).
 int fourier_mixed_packed(ModelDev& m, cudaStream_t st, bool* packed);
@@ -385,13 +402,16 @@ bool occ_fused_ok(int N, int nmu);  // the fused kernel's band and shared-memory
 int occ_partials_add(cudaStream_t st, const OccSums& o, double* acc);
 int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const float4* Vx, const float4* Vy,
                 double eta, double* E, double* Om, void* work, size_t work_bytes, int* status_d,
-                int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr, const OccSums* occ = nullptr);
+                int64_t* clusters_d, double* Met = nullptr, zc* Uout = nullptr, const OccSums* occ = nullptr,
+                const int* h_rexp = nullptr, const int* v_rexp = nullptr);
 // With occ (and Om, Met null) the Berry stage is the fused Omega + occupation +
 // compensated k-sum kernel: per-band Omega is not stored and E is not sorted.
 // With Uout, mixed_berry stops after the refinement: refined E ascending and the
 // refined eigenvectors (columns, FP64) in Uout; Vx, Vy are not read.  With
 // neither Om nor Uout it stops after the eigenvalue refinement (refined E
-// ascending only).
+// ascending only).  h_rexp (batch N ints) and v_rexp (2 batch N: Vx then Vy),
+// when given, are the row exponents of H and of the velocities as the Fourier
+// stage wrote them (line_exp_of over each row), used instead of a scan.
 // Spin-current dressing of float-pair velocities (V_0 blocks, batch stride ldV).
 int spin_dress_pairs(cudaStream_t st, int N, int64_t norb, int64_t batch, int spin, float4* V, int64_t ldV,
                      float4* scratch);
