@@ -1325,7 +1325,9 @@ int eig_values_f64_inplace(cudaStream_t st, int N, int64_t batch, zc* A, double*
 
 // FP32 driver (mixed path): H preserved, U complex<float>.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d, const float4* Hpair) {
+                    size_t work_bytes, int* status_d, const float4* Hpair, int* urow_exp, int* ucol_exp,
+                    bool* exps_filled) {
+    if (exps_filled) *exps_filled = false;
     if (batch <= 0) return TBG_OK;
     int G, PB;
     const int ctas = f32_smem_ctas(N, G, PB);
@@ -1340,7 +1342,13 @@ int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc*
         if (int rc = launch_heev<float, true, 3>(st, N, batch, H, E, U, work, work_bytes, status_d,
                                                  "heev_tri_kernel<float>", G, PB, Hpair, de, bt_tc_enabled()))
             return rc;
-        return (U && bt_tc_enabled()) ? bt_tc(st, N, batch, static_cast<const cc*>(work), U, status_d) : TBG_OK;
+        if (!U || !bt_tc_enabled()) return TBG_OK;
+        const bool ex = urow_exp && ucol_exp;
+        if (int rc = bt_tc(st, N, batch, static_cast<const cc*>(work), U, status_d, ex ? urow_exp : nullptr,
+                           ex ? ucol_exp : nullptr))
+            return rc;
+        if (exps_filled) *exps_filled = ex;
+        return TBG_OK;
     }
     const TwoPhase tp = two_phase_plan(N, batch);
     if (tp.on) {

@@ -428,13 +428,14 @@ __device__ __forceinline__ uint32_t bt_off(int r, int kc) {
 
 __global__ void __launch_bounds__(HT_THREADS, 2)
     bt_tc_kernel(int N, int64_t batch, const cc* __restrict__ Vt, cc* __restrict__ Uio, int* __restrict__ status,
-                 int wait_limit) {
+                 int wait_limit, int* __restrict__ urow_exp, int* __restrict__ ucol_exp) {
     extern __shared__ __align__(1024) unsigned char bt_smem[];
     __shared__ __align__(8) uint64_t bar_mma, bar_ops;
     __shared__ uint32_t tmem_base_sh;
     __shared__ volatile int abort_sh;
     __shared__ cc G[BT8 * BT8];
     __shared__ cc tau_b[BT8];
+    __shared__ int rmax[4][128], cmax[2][128];  // line maxima of U (float bits) by lane quarter / row half
     unsigned char* Bhi = reinterpret_cast<unsigned char*>(((uintptr_t)bt_smem + 127) & ~(uintptr_t)127);
     unsigned char* Blo = Bhi + BT_B_BYTES;
     unsigned char* Ahi = Blo + BT_B_BYTES;
@@ -662,6 +663,12 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
         __syncthreads();
         tc_fence_after();
         if (abort_sh) break;
+        // with urow_exp / ucol_exp the line exponents of U come out too: the
+        // magnitudes (>= 0, NaN as 0) are combined as integers, rows over the
+        // lanes of a warp and then the four lane quarters, columns over the
+        // two row halves
+        const bool lines = urow_exp != nullptr;
+        float cm = 0.f;
         for (int i0 = 64 * h; i0 < 64 * h + 64; i0 += 16) {
             uint32_t r[2][16];
             tmem_ld16(trow + (uint32_t)(2 * i0), r[0]);
@@ -670,14 +677,33 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
 #pragma unroll
             for (int k = 0; k < 16; ++k) {
                 const int i = i0 + k;
-                if (i < N && c < N)
-                    U[(size_t)i * N + c] = mk<float>(__uint_as_float(r[k >> 3][2 * (k & 7)]),
-                                                     __uint_as_float(r[k >> 3][2 * (k & 7) + 1]));
+                const float ure = __uint_as_float(r[k >> 3][2 * (k & 7)]);
+                const float uim = __uint_as_float(r[k >> 3][2 * (k & 7) + 1]);
+                const bool in = i < N && c < N;
+                if (in) U[(size_t)i * N + c] = mk<float>(ure, uim);
+                if (lines) {
+                    float mg = in ? f32_mag(ure, uim) : 0.f;
+                    mg = (mg == mg) ? mg : 0.f;
+                    cm = fmaxf(cm, mg);
+                    const int rm = __reduce_max_sync(0xffffffffu, __float_as_int(mg));
+                    if (lane == 0) rmax[q][i] = rm;
+                }
             }
         }
+        if (lines) cmax[h][c] = __float_as_int(cm);
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
+        if (lines) {
+            if (tid < 128) {
+                if (tid < N)
+                    urow_exp[b * N + tid] = line_exp_of(__int_as_float(
+                        max(max(rmax[0][tid], rmax[1][tid]), max(rmax[2][tid], rmax[3][tid]))));
+            } else if (tid - 128 < N) {
+                ucol_exp[b * N + (tid - 128)] = line_exp_of(__int_as_float(max(cmax[0][tid - 128], cmax[1][tid - 128])));
+            }
+            __syncthreads();
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -736,7 +762,7 @@ int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const z
     return TBG_OK;
 }
 
-int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d) {
+int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d, int* urow_exp, int* ucol_exp) {
     if (batch <= 0 || N < 2) return TBG_OK;
     if (!hetrd_tc_fits(N)) return set_error(TBG_E_UNSUPPORTED, "bt_tc: matrix order beyond 128");
     cudaError_t e = cudaFuncSetAttribute(bt_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
@@ -746,7 +772,8 @@ int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* statu
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = std::min<int64_t>((int64_t)nsm * 2, batch);
     KTimer kt(st, "bt_tc_kernel", 8.0 * (double)N * N * N * batch);
-    bt_tc_kernel<<<(unsigned)grid, HT_THREADS, BT_SMEM, st>>>(N, batch, Vt, U, status_d, tc_wait_limit());
+    bt_tc_kernel<<<(unsigned)grid, HT_THREADS, BT_SMEM, st>>>(N, batch, Vt, U, status_d, tc_wait_limit(), urow_exp,
+                                                              ucol_exp);
     TBG_LAUNCHED("bt_tc_kernel");
     return TBG_OK;
 }

@@ -831,7 +831,13 @@ int mixed_berry(cudaStream_t st, int N, int64_t batch, const float4* H, const fl
     };
     int rc;
     // 1. FP32 eigenpairs of H
-    if ((rc = eig_batched_f32(st, N, batch, nullptr, E, X, eigw, eigw_bytes, status_d, H))) return rc;
+    {
+        bool xe = false;
+        if ((rc = eig_batched_f32(st, N, batch, nullptr, E, X, eigw, eigw_bytes, status_d, H, tc ? slot(XR) : nullptr,
+                                  tc ? slot(XC) : nullptr, &xe)))
+            return rc;
+        ready[XR] = ready[XC] = xe;
+    }
     // 2. X^H X and S = X^H (H X)   (FP64-class, tensor cores)
     if ((rc = exps(F32, true, X, XC)) || (rc = exps(PAIR, false, H, HR))) return rc;
     if ((rc = hp(true, F32, F32, X, X, bA, XC, XC))) return rc;

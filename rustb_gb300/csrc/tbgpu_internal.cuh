@@ -368,8 +368,12 @@ int dos_accumulate(cudaStream_t st, int64_t count, const double* ev, int64_t E_n
 // ------------------------------------------------------------- mixed path --
 // FP32 solver: H (FP64) or, when Hpair is given, float pairs
 // {re_hi, re_lo, im_hi, im_lo} (batch stride N*N); U32 eigenvectors in columns.
+// With urow_exp / ucol_exp the solver may also write the row and column line
+// exponents of U (when its last pass holds them: the TMEM-resident
+// back-transformation); *exps_filled says whether it did.
 int eig_batched_f32(cudaStream_t st, int N, int64_t batch, zc* H, double* E, cc* U, void* work,
-                    size_t work_bytes, int* status_d, const float4* Hpair = nullptr);
+                    size_t work_bytes, int* status_d, const float4* Hpair = nullptr, int* urow_exp = nullptr,
+                    int* ucol_exp = nullptr, bool* exps_filled = nullptr);
 // Householder reduction of up to 128-band matrices with the matrix resident
 // in TMEM and tcgen05 rank-2 updates (eig_tc.cu): Vt (batch, packed + N)
 // reflectors and tau, de (batch, 2 N) the tridiagonal d then e.  Used by
@@ -381,7 +385,10 @@ int hetrd_tc(cudaStream_t st, int N, int64_t batch, const float4* Hpair, const z
              int* status_d, const cc* Hc = nullptr, int Nbig = 0, int off = 0);
 // Back-transformation U <- Q U of the same solver with U (eigenvectors of the
 // tridiagonal form, in columns) resident in TMEM and tcgen05 block updates.
-int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d);
+// With urow_exp and ucol_exp (batch N ints each) the row and column line
+// exponents of the FP32 result come out of the same pass.
+int bt_tc(cudaStream_t st, int N, int64_t batch, const cc* Vt, cc* U, int* status_d, int* urow_exp = nullptr,
+          int* ucol_exp = nullptr);
 bool bt_tc_enabled();
 // FP32 eigensolve, refinement and rotation on the tensor cores: H, Vx, Vy as
 // float pairs (batch stride N*N) -> refined E (ascending) and Omega.
