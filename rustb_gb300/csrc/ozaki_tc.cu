@@ -57,6 +57,8 @@ template <> struct Class<5> { static constexpr int LMAX = 4, NLEV = 4, MIN_CTAS 
 template <> struct Class<3> { static constexpr int LMAX = 2, NLEV = 1, MIN_CTAS = 2; };
 constexpr int tc_smem_bytes(int S) { return 2 * 2 * S * PLANE + 1024; }  // two stages of A and B planes + slack
 constexpr int TC_SMEM = tc_smem_bytes(TC_S);
+// whether a class's two stage buffers can hold the 128 x 65 float-pair output tile
+constexpr bool tc_staged(int S) { return 2 * 2 * S * PLANE >= 128 * 65 * 16; }
 constexpr int TC_THREADS = 416;                 // 13 warps
 constexpr int MMA_WARP = 12;
 constexpr int A_PRODUCERS = 256;
@@ -279,12 +281,51 @@ __host__ __device__ __forceinline__ int plane_off(int row, int kp) {
 }
 __device__ __forceinline__ int n_valid(int K, int kfirst) { return max(0, min(8, K - kfirst)); }
 
+// One tile = 128 rows x 64 complex columns of one matrix.  Tiles are numbered
+// as the blocks of a (gx, gy, batch) grid, x fastest: x = row tile when
+// rows_fast, else column tile.
+struct TileId {
+    int rt, ct;
+    int64_t b;
+};
+__device__ __forceinline__ TileId tile_of(int64_t L, int gx, int gy, int rows_fast) {
+    const int x = (int)(L % gx);
+    const int64_t r = L / gx;
+    const int y = (int)(r % gy);
+    TileId t;
+    t.b = r / gy;
+    t.rt = rows_fast ? x : y;
+    t.ct = rows_fast ? y : x;
+    return t;
+}
+
+// OR of v over the eight epilogue warps (named barrier 1, 256 threads): every
+// participating thread gets the same verdict.
+__device__ __forceinline__ bool epilogue_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, 256, q;\n\tselp.u32 %0, 1, 0, "
+        "p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+// Persistent CTAs: each walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// Every role keeps the same tile order; a stage's buffer and barrier phase come
+// from the CTA's running stage count gs = (tiles before) * nstages + it.  The
+// epilogue warps (the A producers) drain the tile's accumulators from TMEM
+// (bar_tmem frees them for the next tile's MMAs), stage the tile of float
+// pairs in the idle stage buffers and write it out row by row, coalesced;
+// bar_stage then hands the buffers to the next tile's B stages.  The next
+// tile's first A and B stages are loaded into registers before the drain.
 template <bool CONJ_A, int FMTA, int FMTB, int S>
 __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     oz_tc_kernel(int M, int Nc, int K, const void* __restrict__ A, int64_t lda, int64_t sA, const void* __restrict__ B,
                  int64_t ldb, int64_t sB, const int* __restrict__ EA, const int* __restrict__ EB,
                  float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err,
-                 int accumulate, int* __restrict__ Ecol, int wait_limit) {
+                 int accumulate, int* __restrict__ Ecol, int wait_limit, int gx, int gy, int64_t ntiles) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
     constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
     constexpr int HS = S * PLANE;             // planes of one operand in a stage
@@ -292,16 +333,18 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     constexpr uint32_t TMEM_COLS = NLEV * 128;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t bar_full[2], bar_bcopy[2], bar_empty[2], bar_done;
+    __shared__ __align__(8) uint64_t bar_full[2], bar_bcopy[2], bar_empty[2], bar_done, bar_tmem, bar_stage;
     __shared__ uint32_t tmem_base_sh;
     __shared__ volatile int abort_sh;
+    __shared__ int emax[2][4][TC_TN];  // column maxima of a tile (float bits) by lane quarter
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t b = blockIdx.z;
-    const int rt = rows_fast ? (int)blockIdx.x : (int)blockIdx.y;
-    const int ct = rows_fast ? (int)blockIdx.y : (int)blockIdx.x;
-    const int row0 = rt * TC_TM, col0 = ct * TC_TN;
     const int nstages = (K + TC_TK - 1) / TC_TK;
     const uint32_t sbase = su32(base);
+    // With room in the stage buffers the 128 x 64 output tile is staged there
+    // (rows padded to 65 entries: no bank conflicts either way).
+    constexpr int TROW = TC_TN + 1;
+    constexpr bool STAGE = 2 * SB >= TC_TM * TROW * 16;
+    float4* tile = reinterpret_cast<float4*>(base);
 
     if (tid == 0) {
         const uint32_t nfull = PRE ? A_PRODUCERS : A_PRODUCERS + B_PRODUCERS;
@@ -312,6 +355,8 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
         mbar_init(&bar_empty[0], 1);
         mbar_init(&bar_empty[1], 1);
         mbar_init(&bar_done, 1);
+        mbar_init(&bar_tmem, 8);  // one arrival per epilogue warp
+        mbar_init(&bar_stage, 1);
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -325,248 +370,219 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
+    int ndone = 0;  // MMA thread: tiles committed to bar_done
 
     if (warp == MMA_WARP) {
         // ------------------------------------------------ MMA issuer (lane 0)
         if (lane == 0) {
-            for (int it = 0; it < nstages; ++it) {
-                const int bi = it & 1;
-                const uint32_t ph = (it >> 1) & 1;
-                if (!mbar_wait(&bar_full[bi], ph, &abort_sh, wait_limit) ||
-                    (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh, wait_limit))) {
+            int tn = 0;
+            for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x, ++tn) {
+                // the previous tile's accumulators have been read out
+                if (tn > 0 && !mbar_wait(&bar_tmem, (tn - 1) & 1, &abort_sh, wait_limit)) {
                     abort_sh = 1;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t sa = sbase + bi * SB;
-                const uint32_t sb = sa + HS;
+                bool stop = false;
+                for (int it = 0; it < nstages; ++it) {
+                    const int64_t gs = (int64_t)tn * nstages + it;
+                    const int bi = (int)(gs & 1);
+                    const uint32_t ph = (uint32_t)((gs >> 1) & 1);
+                    if (!mbar_wait(&bar_full[bi], ph, &abort_sh, wait_limit) ||
+                        (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh, wait_limit))) {
+                        abort_sh = 1;
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = sbase + bi * SB;
+                    const uint32_t sb = sa + HS;
 #pragma unroll
-                for (int ks = 0; ks < 2; ++ks) {
+                    for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
-                    for (int t = 0; t < S; ++t) {
+                        for (int t = 0; t < S; ++t) {
 #pragma unroll
-                        for (int s = 0; s < S; ++s) {
-                            if (s + t > LMAX) continue;
-                            const int lv = (s + t) < NLEV - 1 ? (s + t) : NLEV - 1;
-                            const uint64_t ad = smem_desc(sa + s * PLANE + ks * 256, 128, 512);
-                            const uint64_t bd = smem_desc(sb + t * PLANE + ks * 256, 128, 512);
-                            // the first product into each accumulator overwrites it
-                            const uint32_t acc = (it == 0 && ks == 0 && t == 0 && s <= NLEV - 1) ? 0u : 1u;
-                            umma(tmem + (uint32_t)(lv * 128), ad, bd, acc);
+                            for (int s = 0; s < S; ++s) {
+                                if (s + t > LMAX) continue;
+                                const int lv = (s + t) < NLEV - 1 ? (s + t) : NLEV - 1;
+                                const uint64_t ad = smem_desc(sa + s * PLANE + ks * 256, 128, 512);
+                                const uint64_t bd = smem_desc(sb + t * PLANE + ks * 256, 128, 512);
+                                // the first product into each accumulator overwrites it
+                                const uint32_t acc = (it == 0 && ks == 0 && t == 0 && s <= NLEV - 1) ? 0u : 1u;
+                                umma(tmem + (uint32_t)(lv * 128), ad, bd, acc);
+                            }
                         }
                     }
+                    umma_commit(&bar_empty[bi]);
                 }
-                umma_commit(&bar_empty[bi]);
+                umma_commit(&bar_done);  // this tile's MMAs (all issued so far)
+                ++ndone;
+                if (stop) break;
             }
-            umma_commit(&bar_done);  // tracks every MMA issued above
         }
         __syncwarp();
     } else if (tid < A_PRODUCERS) {
-        // ------------------------------------- A digit producers (row, 8 k)
+        // -------------------- A digit producers (row, 8 k), then the epilogue
         const int r = CONJ_A ? (tid & 127) : (tid >> 1);
         const int g = CONJ_A ? (tid >> 7) : (tid & 1);
-        const int gi = row0 + r;
-        const bool rv = gi < M;
-        const int E = rv ? EA[b * M + gi] : ZERO_EXP;
-        float s1, s2;
-        f32_scales(E, s1, s2);
         const int64_t kstride = CONJ_A ? lda : 1;
-        const int64_t idx0 = CONJ_A ? (b * sA + gi) : (b * sA + (int64_t)gi * lda);
         const uint32_t o_re = plane_off(r, 8 * g), o_im = plane_off(r, 16 + 8 * g);
+        const int q = warp & 3, h = warp >> 2;  // epilogue: TMEM lanes 32q .. 32q+31; complex columns 32h .. 32h+31
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+        // element index of (row gi of op(A), k = 0) for tile L, and whether the row exists
+        auto row_base = [&](int64_t L, bool& rv) -> int64_t {
+            const TileId t = tile_of(L, gx, gy, rows_fast);
+            const int gi = t.rt * TC_TM + r;
+            rv = gi < M;
+            return CONJ_A ? (t.b * sA + gi) : (t.b * sA + (int64_t)gi * lda);
+        };
         int4 nxt[8];
-        load8<FMTA>(A, idx0 + (int64_t)(8 * g) * kstride, kstride, rv ? n_valid(K, 8 * g) : 0, nxt);
-        for (int it = 0; it < nstages; ++it) {
-            const int bi = it & 1;
-            int4 cur[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
-            if (it + 1 < nstages) {
-                const int kf = (it + 1) * TC_TK + 8 * g;
-                load8<FMTA>(A, idx0 + (int64_t)kf * kstride, kstride, rv ? n_valid(K, kf) : 0, nxt);
-            }
-            // slice this stage while the MMAs of the two stages before it run; then
-            // wait only for the buffer and store
-            uint4 dre[S], dim[S];
-            item_planes<FMTA, 0, S>(cur, E, s1, s2, dre);
-            item_planes<FMTA, 1, S>(cur, E, s1, s2, dim);
-            if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
-                abort_sh = 1;
-                break;
-            }
-            if (abort_sh) break;
-            const uint32_t sa = sbase + bi * SB;
-#pragma unroll
-            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_re, dre[s]);
-#pragma unroll
-            for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(dim[s]) : dim[s]);
-            fence_async_smem();  // make the generic-proxy writes visible to the tensor core
-            mbar_arrive(&bar_full[bi]);
+        {
+            bool rv0;
+            const int64_t i0 = row_base(blockIdx.x, rv0);
+            if (blockIdx.x < ntiles)
+                load8<FMTA>(A, i0 + (int64_t)(8 * g) * kstride, kstride, rv0 ? n_valid(K, 8 * g) : 0, nxt);
         }
-    } else if (tid < A_PRODUCERS + B_PRODUCERS) {
-        const int q = tid - A_PRODUCERS;
-        if (PRE) {
-            // ------------------------- pre-sliced B: bulk copy of stage images
-            if (q == 0) {
-                // stage images hold TC_S planes; a class with fewer digits copies the leading S
-                const unsigned char* src = static_cast<const unsigned char*>(B) + (int64_t)ct * nstages * HALF_STAGE;
-                int last[2] = {-1, -1};
-                for (int it = 0; it < nstages; ++it) {
-                    const int bi = it & 1;
-                    if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
-                        abort_sh = 1;
-                        break;
-                    }
-                    if (abort_sh) break;
-                    mbar_arrive_tx(&bar_bcopy[bi], HS);
-                    bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HALF_STAGE, HS, &bar_bcopy[bi]);
-                    last[bi] = it;
-                }
-                // every copy issued has landed before the CTA can leave
-                for (int bi = 0; bi < 2; ++bi)
-                    if (last[bi] >= 0) mbar_wait_plain(&bar_bcopy[bi], (last[bi] >> 1) & 1);
-            }
-        } else {
-            // ---------------------------------- B digit producers (col, 8 k)
-            // real embedding: row j = [Re B | -Im B], row 64 + j = [Im B | Re B]
-            const int j = q & 63, g = q >> 6;
-            const int gj = col0 + j;
-            const bool cv = gj < Nc;
-            const int E = cv ? EB[b * Nc + gj] : ZERO_EXP;
+        int tn = 0;
+        for (int64_t L = blockIdx.x; L < ntiles; L += gridDim.x, ++tn) {
+            const TileId t = tile_of(L, gx, gy, rows_fast);
+            const int row0 = t.rt * TC_TM, col0 = t.ct * TC_TN;
+            const int gi = row0 + r;
+            const bool rv = gi < M;
+            const int E = rv ? EA[t.b * M + gi] : ZERO_EXP;
             float s1, s2;
             f32_scales(E, s1, s2);
-            const int64_t idx0 = b * sB + gj;
-            const uint32_t o_jre = plane_off(j, 8 * g), o_jim = plane_off(j, 16 + 8 * g);
-            const uint32_t o_kre = plane_off(64 + j, 8 * g), o_kim = plane_off(64 + j, 16 + 8 * g);
-            constexpr int FB = PRE ? FMT_F64 : FMTB;
-            int4 nxt[8];
-            load8<FB>(B, idx0 + (int64_t)(8 * g) * ldb, ldb, cv ? n_valid(K, 8 * g) : 0, nxt);
+            const int64_t idx0 = CONJ_A ? (t.b * sA + gi) : (t.b * sA + (int64_t)gi * lda);
             for (int it = 0; it < nstages; ++it) {
-                const int bi = it & 1;
+                const int64_t gs = (int64_t)tn * nstages + it;
+                const int bi = (int)(gs & 1);
                 int4 cur[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
                 if (it + 1 < nstages) {
                     const int kf = (it + 1) * TC_TK + 8 * g;
-                    load8<FB>(B, idx0 + (int64_t)kf * ldb, ldb, cv ? n_valid(K, kf) : 0, nxt);
+                    load8<FMTA>(A, idx0 + (int64_t)kf * kstride, kstride, rv ? n_valid(K, kf) : 0, nxt);
+                } else if (L + gridDim.x < ntiles) {
+                    // the next tile's first stage, in flight during this tile's epilogue
+                    bool rvn;
+                    const int64_t in = row_base(L + gridDim.x, rvn);
+                    load8<FMTA>(A, in + (int64_t)(8 * g) * kstride, kstride, rvn ? n_valid(K, 8 * g) : 0, nxt);
                 }
+                // slice this stage while the MMAs of the two stages before it run; then
+                // wait only for the buffer and store
                 uint4 dre[S], dim[S];
-                item_planes<FB, 0, S>(cur, E, s1, s2, dre);
-                item_planes<FB, 1, S>(cur, E, s1, s2, dim);
-                if (it >= 2 && !mbar_wait(&bar_empty[bi], ((it >> 1) - 1) & 1, &abort_sh, wait_limit)) {
+                item_planes<FMTA, 0, S>(cur, E, s1, s2, dre);
+                item_planes<FMTA, 1, S>(cur, E, s1, s2, dim);
+                if (gs >= 2 && !mbar_wait(&bar_empty[bi], (uint32_t)(((gs >> 1) - 1) & 1), &abort_sh, wait_limit)) {
                     abort_sh = 1;
                     break;
                 }
                 if (abort_sh) break;
-                const uint32_t sb = sbase + bi * SB + HS;
+                const uint32_t sa = sbase + bi * SB;
 #pragma unroll
-                for (int s = 0; s < S; ++s) {
-                    st_shared_v4(sb + s * PLANE + o_jre, dre[s]);
-                    st_shared_v4(sb + s * PLANE + o_kim, dre[s]);
-                }
+                for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_re, dre[s]);
 #pragma unroll
-                for (int s = 0; s < S; ++s) {
-                    st_shared_v4(sb + s * PLANE + o_kre, dim[s]);
-                    st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(dim[s]));
-                }
-                fence_async_smem();
+                for (int s = 0; s < S; ++s) st_shared_v4(sa + s * PLANE + o_im, CONJ_A ? neg_bf16x8(dim[s]) : dim[s]);
+                fence_async_smem();  // make the generic-proxy writes visible to the tensor core
                 mbar_arrive(&bar_full[bi]);
             }
-        }
-    }
-
-    // ---------------------------------------------------------- epilogue
-    // With room in the (now idle) stage buffers the 128 x 64 tile of float
-    // pairs is staged in shared memory (rows padded to 65 entries: no bank
-    // conflicts either way) and written out row by row, coalesced.
-    constexpr int TROW = TC_TN + 1;
-    constexpr bool STAGE = 2 * SB >= TC_TM * TROW * 16;
-    float4* tile = reinterpret_cast<float4*>(base);
-    if (warp < 8) {
-        // A time-out here is an abort too; after the named barrier every
-        // epilogue warp sees the same flag (nothing sets it once every MMA has
-        // completed), so either the whole tile is written or none of it.
-        if (!mbar_wait(&bar_done, 0, &abort_sh, wait_limit)) abort_sh = 1;
-        asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
-        const bool ok = !abort_sh;
-        tc_fence_after();
-        const int q = warp & 3, h = warp >> 2;  // TMEM lanes 32q .. 32q+31; complex columns 32h .. 32h+31
-        const int r = row0 + 32 * q + lane;
-        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-        if (ok) {
-            const int ea = (r < M) ? EA[b * M + r] : ZERO_EXP;
+            // ------------------------------------------------------ epilogue
+            // A time-out here is an abort too; either the whole tile is written
+            // or none of it
+            // (the verdict is one barrier reduction: roles still running may set
+            // abort_sh at any time, and the eight warps must agree)
+            bool bad = abort_sh != 0;
+            if (!bad && !mbar_wait(&bar_done, tn & 1, &abort_sh, wait_limit)) {
+                abort_sh = 1;
+                bad = true;
+            }
+            if (epilogue_any(bad)) break;
+            tc_fence_after();
+            const int re_ = row0 + 32 * q + lane;
+            const int ea = (re_ < M) ? EA[t.b * M + re_] : ZERO_EXP;
+            const int par = tn & 1;
             for (int cc = 0; cc < 4; ++cc) {
                 const int c0 = 32 * h + 8 * cc;
                 uint32_t v[2 * NLEV][8];  // [2 * level + (0 re, 1 im)][column]
 #pragma unroll
-                for (int L = 0; L < NLEV; ++L) {
-                    tmem_ld8(lane_addr + (uint32_t)(L * 128 + c0), v[2 * L]);
-                    tmem_ld8(lane_addr + (uint32_t)(L * 128 + TC_TN + c0), v[2 * L + 1]);
+                for (int Lv = 0; Lv < NLEV; ++Lv) {
+                    tmem_ld8(lane_addr + (uint32_t)(Lv * 128 + c0), v[2 * Lv]);
+                    tmem_ld8(lane_addr + (uint32_t)(Lv * 128 + TC_TN + c0), v[2 * Lv + 1]);
                 }
                 tmem_wait_ld();
-                if (STAGE || r < M) {
+                if (cc == 3) {
+                    // every accumulator of this warp's lanes and columns is in registers
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&bar_tmem);
+                }
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) {
-                        const int j = col0 + c0 + c;
-                        if (!STAGE && j >= Nc) continue;
-                        float hl[4];
+                for (int c = 0; c < 8; ++c) {
+                    const int j = col0 + c0 + c;
+                    float hl[4];
 #pragma unroll
-                        for (int part = 0; part < 2; ++part) {
-                            if (NLEV == 1) {
-                                hl[2 * part] = __uint_as_float(v[part][c]);
-                                hl[2 * part + 1] = 0.f;
-                                continue;
-                            }
-                            const float a0 = __uint_as_float(v[0 + part][c]), a1 = __uint_as_float(v[2 + part][c]);
-                            const float a2 = __uint_as_float(v[4 + part][c]), a3 = __uint_as_float(v[6 + part][c]);
-                            const float s1 = a0 + a1;
-                            const float t1 = s1 - a0;
-                            const float e1 = (a0 - (s1 - t1)) + (a1 - t1);
-                            const float hi = s1 + a2;
-                            const float t2 = hi - s1;
-                            const float e2 = (s1 - (hi - t2)) + (a2 - t2);
-                            hl[2 * part] = hi;
-                            hl[2 * part + 1] = (e1 + e2) + a3;
-                        }
-                        const int eb = (j < Nc) ? EB[b * Nc + j] : ZERO_EXP;
-                        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (ea != ZERO_EXP && eb != ZERO_EXP) {
-                            const int n = max(-126, min(127, ea + eb - 14));
-                            const float sc = pow2f(n);
-                            out = make_float4(hl[0] * sc, hl[1] * sc, hl[2] * sc, hl[3] * sc);
-                        }
-                        if (STAGE) {
-                            tile[(32 * q + lane) * TROW + c0 + c] = out;
+                    for (int part = 0; part < 2; ++part) {
+                        if (NLEV == 1) {
+                            hl[2 * part] = __uint_as_float(v[part][c]);
+                            hl[2 * part + 1] = 0.f;
                             continue;
                         }
-                        float4* cp = C + b * sC + (int64_t)r * ldc + j;
+                        const float a0 = __uint_as_float(v[0 + part][c]), a1 = __uint_as_float(v[2 + part][c]);
+                        const float a2 = __uint_as_float(v[4 + part][c]), a3 = __uint_as_float(v[6 + part][c]);
+                        const float s1_ = a0 + a1;
+                        const float t1 = s1_ - a0;
+                        const float e1 = (a0 - (s1_ - t1)) + (a1 - t1);
+                        const float hi = s1_ + a2;
+                        const float t2 = hi - s1_;
+                        const float e2 = (s1_ - (hi - t2)) + (a2 - t2);
+                        hl[2 * part] = hi;
+                        hl[2 * part + 1] = (e1 + e2) + a3;
+                    }
+                    const int eb = (j < Nc) ? EB[t.b * Nc + j] : ZERO_EXP;
+                    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (ea != ZERO_EXP && eb != ZERO_EXP) {
+                        const int n = max(-126, min(127, ea + eb - 14));
+                        const float sc = pow2f(n);
+                        out = make_float4(hl[0] * sc, hl[1] * sc, hl[2] * sc, hl[3] * sc);
+                    }
+                    if (STAGE) {
+                        tile[(32 * q + lane) * TROW + c0 + c] = out;
+                        continue;
+                    }
+                    const bool in = re_ < M && j < Nc;
+                    if (in) {
+                        float4* cp = C + t.b * sC + (int64_t)re_ * ldc + j;
                         if (accumulate) {  // a later K chunk: add to the stored pair
                             const float4 prev = *cp;
-                            const float2 re = pair_add(prev.x, prev.y, out.x, out.y);
-                            const float2 im = pair_add(prev.z, prev.w, out.z, out.w);
-                            out = make_float4(re.x, re.y, im.x, im.y);
+                            const float2 pre = pair_add(prev.x, prev.y, out.x, out.y);
+                            const float2 pim = pair_add(prev.z, prev.w, out.z, out.w);
+                            out = make_float4(pre.x, pre.y, pim.x, pim.y);
                         }
                         *cp = out;
                     }
-                }
-            }
-        }
-        if (STAGE) {
-            asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
-            if (ok && Ecol) {
-                // exponents of the output's columns, as the line scan would take
-                // them (one row tile holds all rows): warp w, columns w, w + 8, ...
-                for (int cl = warp; cl < TC_TN; cl += 8) {
-                    float m = 0.f;
-                    for (int rl = lane; rl < TC_TM; rl += 32) {
-                        const float4 v = tile[rl * TROW + cl];
-                        m = fmaxf(m, fmaxf(fabsf(v.x) + fabsf(v.y), fabsf(v.z) + fabsf(v.w)));
+                    if (Ecol) {
+                        // the column's largest magnitude over this warp's rows (>= 0,
+                        // NaN as 0: ordered as integers)
+                        float mg = in ? pair_mag(out) : 0.f;
+                        mg = (mg == mg) ? mg : 0.f;
+                        const int mv = __reduce_max_sync(0xffffffffu, __float_as_int(mg));
+                        if (lane == 0) emax[par][q][c0 + c] = mv;
                     }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-                    if (lane == 0 && col0 + cl < Nc) Ecol[b * Nc + col0 + cl] = (m > 0.f) ? ilogbf(m) + 1 : ZERO_EXP;
                 }
             }
-            if (ok) {
+            if (STAGE) {
+                asm volatile("bar.sync 1, 256;" ::: "memory");  // the tile is staged
+                if (Ecol) {
+                    // exponents of the output's columns, as the line scan would take
+                    // them (one row tile holds all rows): warp w, columns w, w + 8, ...
+                    for (int cl = warp; cl < TC_TN; cl += 8) {
+                        float m = 0.f;
+                        for (int rl = lane; rl < TC_TM; rl += 32) m = fmaxf(m, pair_mag(tile[rl * TROW + cl]));
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                        if (lane == 0 && col0 + cl < Nc) Ecol[t.b * Nc + col0 + cl] = line_exp_of(m);
+                    }
+                }
                 // warp w writes rows w, w + 8, ...; lanes over the 64 columns
                 for (int rl = warp; rl < TC_TM; rl += 8) {
                     const int rr = row0 + rl;
@@ -576,15 +592,135 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                         const int jl = lane + 32 * half, j = col0 + jl;
                         if (j >= Nc) continue;
                         float4 out = tile[rl * TROW + jl];
-                        float4* cp = C + b * sC + (int64_t)rr * ldc + j;
+                        float4* cp = C + t.b * sC + (int64_t)rr * ldc + j;
                         if (accumulate) {  // a later K chunk: add to the stored pair
                             const float4 prev = *cp;
-                            const float2 re = pair_add(prev.x, prev.y, out.x, out.y);
-                            const float2 im = pair_add(prev.z, prev.w, out.z, out.w);
-                            out = make_float4(re.x, re.y, im.x, im.y);
+                            const float2 pre = pair_add(prev.x, prev.y, out.x, out.y);
+                            const float2 pim = pair_add(prev.z, prev.w, out.z, out.w);
+                            out = make_float4(pre.x, pre.y, pim.x, pim.y);
                         }
                         *cp = out;
                     }
+                }
+                asm volatile("bar.sync 1, 256;" ::: "memory");  // every read of the staged tile done
+                if (tid == 0) mbar_arrive(&bar_stage);
+            } else if (Ecol) {
+                // one row tile holds every row: the tile's column maxima are the columns'
+                asm volatile("bar.sync 1, 256;" ::: "memory");
+                if (tid < TC_TN && col0 + tid < Nc) {
+                    const int mx = max(max(emax[par][0][tid], emax[par][1][tid]), max(emax[par][2][tid], emax[par][3][tid]));
+                    Ecol[t.b * Nc + col0 + tid] = line_exp_of(__int_as_float(mx));
+                }
+            }
+        }
+    } else if (tid < A_PRODUCERS + B_PRODUCERS) {
+        const int qb = tid - A_PRODUCERS;
+        if (PRE) {
+            // ------------------------- pre-sliced B: bulk copy of stage images
+            if (qb == 0) {
+                int64_t last[2] = {-1, -1};
+                int tn = 0;
+                bool stop = false;
+                for (int64_t L = blockIdx.x; L < ntiles && !stop; L += gridDim.x, ++tn) {
+                    const TileId t = tile_of(L, gx, gy, rows_fast);
+                    // stage images hold TC_S planes; a class with fewer digits copies the leading S
+                    const unsigned char* src =
+                        static_cast<const unsigned char*>(B) + (int64_t)t.ct * nstages * HALF_STAGE;
+                    for (int it = 0; it < nstages; ++it) {
+                        const int64_t gs = (int64_t)tn * nstages + it;
+                        const int bi = (int)(gs & 1);
+                        if ((gs >= 2 &&
+                             !mbar_wait(&bar_empty[bi], (uint32_t)(((gs >> 1) - 1) & 1), &abort_sh, wait_limit)) ||
+                            (STAGE && tn > 0 && it < 2 &&
+                             !mbar_wait(&bar_stage, (uint32_t)((tn - 1) & 1), &abort_sh, wait_limit))) {
+                            abort_sh = 1;
+                            stop = true;
+                            break;
+                        }
+                        if (abort_sh) {
+                            stop = true;
+                            break;
+                        }
+                        mbar_arrive_tx(&bar_bcopy[bi], HS);
+                        bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HALF_STAGE, HS, &bar_bcopy[bi]);
+                        last[bi] = gs;
+                    }
+                }
+                // every copy issued has landed before the CTA can leave
+                for (int bi = 0; bi < 2; ++bi)
+                    if (last[bi] >= 0) mbar_wait_plain(&bar_bcopy[bi], (uint32_t)((last[bi] >> 1) & 1));
+            }
+        } else {
+            // ---------------------------------- B digit producers (col, 8 k)
+            // real embedding: row j = [Re B | -Im B], row 64 + j = [Im B | Re B]
+            const int j = qb & 63, g = qb >> 6;
+            const uint32_t o_jre = plane_off(j, 8 * g), o_jim = plane_off(j, 16 + 8 * g);
+            const uint32_t o_kre = plane_off(64 + j, 8 * g), o_kim = plane_off(64 + j, 16 + 8 * g);
+            constexpr int FB = PRE ? FMT_F64 : FMTB;
+            auto col_base = [&](int64_t L, bool& cv) -> int64_t {
+                const TileId t = tile_of(L, gx, gy, rows_fast);
+                const int gj = t.ct * TC_TN + j;
+                cv = gj < Nc;
+                return t.b * sB + gj;
+            };
+            int4 nxt[8];
+            {
+                bool cv0;
+                const int64_t i0 = col_base(blockIdx.x, cv0);
+                if (blockIdx.x < ntiles) load8<FB>(B, i0 + (int64_t)(8 * g) * ldb, ldb, cv0 ? n_valid(K, 8 * g) : 0, nxt);
+            }
+            int tn = 0;
+            bool stop = false;
+            for (int64_t L = blockIdx.x; L < ntiles && !stop; L += gridDim.x, ++tn) {
+                const TileId t = tile_of(L, gx, gy, rows_fast);
+                const int gj = t.ct * TC_TN + j;
+                const bool cv = gj < Nc;
+                const int E = cv ? EB[t.b * Nc + gj] : ZERO_EXP;
+                float s1, s2;
+                f32_scales(E, s1, s2);
+                const int64_t idx0 = t.b * sB + gj;
+                for (int it = 0; it < nstages; ++it) {
+                    const int64_t gs = (int64_t)tn * nstages + it;
+                    const int bi = (int)(gs & 1);
+                    int4 cur[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) cur[i] = nxt[i];
+                    if (it + 1 < nstages) {
+                        const int kf = (it + 1) * TC_TK + 8 * g;
+                        load8<FB>(B, idx0 + (int64_t)kf * ldb, ldb, cv ? n_valid(K, kf) : 0, nxt);
+                    } else if (L + gridDim.x < ntiles) {
+                        bool cvn;
+                        const int64_t in = col_base(L + gridDim.x, cvn);
+                        load8<FB>(B, in + (int64_t)(8 * g) * ldb, ldb, cvn ? n_valid(K, 8 * g) : 0, nxt);
+                    }
+                    uint4 dre[S], dim[S];
+                    item_planes<FB, 0, S>(cur, E, s1, s2, dre);
+                    item_planes<FB, 1, S>(cur, E, s1, s2, dim);
+                    if ((gs >= 2 &&
+                         !mbar_wait(&bar_empty[bi], (uint32_t)(((gs >> 1) - 1) & 1), &abort_sh, wait_limit)) ||
+                        (STAGE && tn > 0 && it < 2 &&
+                         !mbar_wait(&bar_stage, (uint32_t)((tn - 1) & 1), &abort_sh, wait_limit))) {
+                        abort_sh = 1;
+                        stop = true;
+                        break;
+                    }
+                    if (abort_sh) {
+                        stop = true;
+                        break;
+                    }
+                    const uint32_t sb = sbase + bi * SB + HS;
+#pragma unroll
+                    for (int s = 0; s < S; ++s) {
+                        st_shared_v4(sb + s * PLANE + o_jre, dre[s]);
+                        st_shared_v4(sb + s * PLANE + o_kim, dre[s]);
+                    }
+#pragma unroll
+                    for (int s = 0; s < S; ++s) {
+                        st_shared_v4(sb + s * PLANE + o_kre, dim[s]);
+                        st_shared_v4(sb + s * PLANE + o_jim, neg_bf16x8(dim[s]));
+                    }
+                    fence_async_smem();
+                    mbar_arrive(&bar_full[bi]);
                 }
             }
         }
@@ -593,7 +729,8 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
     __syncthreads();
     if (abort_sh && tid == 0) atomicOr(err, 2);  // bit 1: a bounded wait ran out
     if (warp == MMA_WARP) {
-        if (lane == 0) mbar_wait_plain(&bar_done, 0);  // every committed MMA has finished
+        // every committed MMA has finished (the last commit tracks all of them)
+        if (lane == 0 && ndone > 0) mbar_wait_plain(&bar_done, (uint32_t)((ndone - 1) & 1));
         __syncwarp();
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -692,6 +829,17 @@ __global__ void hop_image_real_kernel(int Kc, int64_t Nc, const zc* __restrict__
 
 int tc_wait_limit() { return g_tc_wait_limit.load(std::memory_order_relaxed); }
 
+// Multiprocessors of the current device (the persistent kernels' grid).
+static int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n;
+}
+
 int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t batch, int M, int Nc, int K,
                      const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, int* EA, int* EB);
 
@@ -705,17 +853,17 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc)");
     KTimer kt(st, name, work);
-    for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
-        const int64_t nb = std::min<int64_t>(65535, batch - b0);
-        dim3 grid((Nc + TC_TN - 1) / TC_TN, (M + TC_TM - 1) / TC_TM, (unsigned)nb);
-        const size_t ea = FA == FMT_F32 ? 8 : 16;
-        const size_t eb = FB == FMT_F32 ? 8 : 16;
-        kern<<<grid, TC_THREADS, smem, st>>>(M, Nc, K, static_cast<const char*>(A) + b0 * sA * ea, lda, sA,
-                                                static_cast<const char*>(B) + b0 * sB * eb, ldb, sB, EA + b0 * M,
-                                                EB + b0 * Nc, C + b0 * sC, ldc, sC, 0, err, accumulate,
-                                                Ecol ? Ecol + b0 * Nc : nullptr, tc_wait_limit());
-        TBG_LAUNCHED(name);
-    }
+    // tiles (column tile, row tile, matrix), column tiles fastest; persistent
+    // CTAs where the output is staged in shared memory (HIGH, MID: the
+    // per-CTA set-up and launch gap were ~12 % of a 128^3 tile), one tile per
+    // CTA for the LOW class (two CTAs per SM already overlap its epilogues)
+    const int gx = (Nc + TC_TN - 1) / TC_TN, gy = (M + TC_TM - 1) / TC_TM;
+    const int64_t ntiles = (int64_t)gx * gy * batch;
+    const int64_t grid = tc_staged(S) ? std::min<int64_t>(ntiles, (int64_t)sm_count() * Class<S>::MIN_CTAS)
+                                      : std::min<int64_t>(ntiles, 0x7fffffff);
+    kern<<<(unsigned)grid, TC_THREADS, smem, st>>>(M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB, C, ldc, sC, 0, err,
+                                                   accumulate, Ecol, tc_wait_limit(), gx, gy, ntiles);
+    TBG_LAUNCHED(name);
     return TBG_OK;
 }
 
@@ -847,9 +995,12 @@ static int fourier_tc_launch(cudaStream_t st, int64_t M, int64_t Nc, int K, cons
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc fourier)");
     KTimer kt(st, S == TC_S ? "ozaki_tc_fourier_kernel" : "ozaki_tc_fourier_kernel<mid>", 8.0 * (double)M * Nc * K);
-    dim3 grid((unsigned)((M + TC_TM - 1) / TC_TM), (unsigned)((Nc + TC_TN - 1) / TC_TN), 1);
-    kern<<<grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err, 0,
-                                         nullptr, tc_wait_limit());
+    // persistent CTAs over (row tile, column tile), row tiles fastest
+    const int gx = (int)((M + TC_TM - 1) / TC_TM), gy = (int)((Nc + TC_TN - 1) / TC_TN);
+    const int64_t ntiles = (int64_t)gx * gy;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * Class<S>::MIN_CTAS);
+    kern<<<(unsigned)grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err,
+                                                   0, nullptr, tc_wait_limit(), gx, gy, ntiles);
     TBG_LAUNCHED(S == TC_S ? "ozaki_tc_fourier_kernel" : "ozaki_tc_fourier_kernel<mid>");
     return TBG_OK;
 }
