@@ -84,12 +84,24 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                  : "memory");
 }
 
+// One MMA; COL selects the use of the A collector buffer across consecutive
+// MMAs with the same A: 0 none, 1 fill, 2 use, 3 last use.
+template <int COL>
 __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-            d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
-        : "memory");
+#define TBG_UMMA(Q)                                                                                             \
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16" Q        \
+                 " [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),                                                     \
+                 "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)                                            \
+                 : "memory")
+    if constexpr (COL == 1)
+        TBG_UMMA(".collector::a::fill");
+    else if constexpr (COL == 2)
+        TBG_UMMA(".collector::a::use");
+    else if constexpr (COL == 3)
+        TBG_UMMA(".collector::a::lastuse");
+    else
+        TBG_UMMA("");
+#undef TBG_UMMA
 }
 // ---- digit extraction ----
 // Fixed-point value trunc(x * 2^(42 - E)) of a double with |x| < 2^E.
@@ -397,19 +409,30 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     tc_fence_after();
                     const uint32_t sa = sbase + bi * SB;
                     const uint32_t sb = sa + HS;
+                    // A digit s outer, B digit t inner: the A tile of a group of
+                    // products stays in the collector buffer
 #pragma unroll
                     for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
-                        for (int t = 0; t < S; ++t) {
+                        for (int s = 0; s < S; ++s) {
+                            const int tmax = LMAX - s < S - 1 ? LMAX - s : S - 1;
 #pragma unroll
-                            for (int s = 0; s < S; ++s) {
-                                if (s + t > LMAX) continue;
+                            for (int t = 0; t <= tmax; ++t) {
                                 const int lv = (s + t) < NLEV - 1 ? (s + t) : NLEV - 1;
                                 const uint64_t ad = smem_desc(sa + s * PLANE + ks * 256, 128, 512);
                                 const uint64_t bd = smem_desc(sb + t * PLANE + ks * 256, 128, 512);
                                 // the first product into each accumulator overwrites it
-                                const uint32_t acc = (it == 0 && ks == 0 && t == 0 && s <= NLEV - 1) ? 0u : 1u;
-                                umma(tmem + (uint32_t)(lv * 128), ad, bd, acc);
+                                // (level l first gets digit pair (0, l); levels >= NLEV - 1 (0, NLEV - 1))
+                                const uint32_t acc = (it == 0 && ks == 0 && s == 0 && t <= NLEV - 1) ? 0u : 1u;
+                                const uint32_t dst = tmem + (uint32_t)(lv * 128);
+                                if (tmax == 0)
+                                    umma<0>(dst, ad, bd, acc);
+                                else if (t == 0)
+                                    umma<1>(dst, ad, bd, acc);
+                                else if (t == tmax)
+                                    umma<3>(dst, ad, bd, acc);
+                                else
+                                    umma<2>(dst, ad, bd, acc);
                             }
                         }
                     }
