@@ -67,12 +67,22 @@ constexpr int OPA_BYTES = 128 * 32, OPB_BYTES = 2 * HT_NC * 32;
 constexpr uint32_t IDESC_TF32_M128 = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 4) << 24);
 __device__ __forceinline__ uint32_t idesc_tf32(uint32_t n) { return IDESC_TF32_M128 | ((n >> 3) << 17); }
 
+// COL: use of the A collector buffer across consecutive MMAs with the same A
+// (0 none, 1 fill, 3 last use).
+template <int COL = 0>
 __device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-            d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc)
-        : "memory");
+#define TBG_UMMA32(Q)                                                                                            \
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32" Q            \
+                 " [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),                                                       \
+                 "l"(adesc), "l"(bdesc), "r"(idesc)                                                              \
+                 : "memory")
+    if constexpr (COL == 1)
+        TBG_UMMA32(".collector::a::fill");
+    else if constexpr (COL == 3)
+        TBG_UMMA32(".collector::a::lastuse");
+    else
+        TBG_UMMA32("");
+#undef TBG_UMMA32
 }
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -355,8 +365,8 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
                     const int c0 = jn & ~7;
                     const uint32_t id = idesc_tf32((uint32_t)(2 * (HT_NC - c0)));
                     const uint64_t ad = smem_desc(sA, 128, 256);
-                    umma_tf32(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB1 + 64u * (uint32_t)c0, 128, 256), id);
-                    umma_tf32(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB2 + 64u * (uint32_t)c0, 128, 256), id);
+                    umma_tf32<1>(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB1 + 64u * (uint32_t)c0, 128, 256), id);
+                    umma_tf32<3>(tmem + (uint32_t)(2 * c0), ad, smem_desc(sB2 + 64u * (uint32_t)c0, 128, 256), id);
                     umma_commit(&bar_mma);
                     ++issued;
                 }
@@ -645,9 +655,10 @@ __global__ void __launch_bounds__(HT_THREADS, 2)
                         const uint64_t al = smem_desc(sAlo + 256u * kk, 128, 512);
                         const uint64_t bh = smem_desc(sBhi + boff + 256u * kk, 128, 512);
                         const uint64_t bl = smem_desc(sBlo + boff + 256u * kk, 128, 512);
-                        umma_tf32(d, ah, bh, id);
+                        // the two products with A_hi back to back, A_hi kept in the collector
+                        umma_tf32<1>(d, ah, bh, id);
+                        umma_tf32<3>(d, ah, bl, id);
                         umma_tf32(d, al, bh, id);
-                        umma_tf32(d, ah, bl, id);
                     }
                     umma_commit(&bar_mma);
                     ++issued;
