@@ -882,6 +882,8 @@ static int launch_tc(cudaStream_t st, int64_t batch, int M, int Nc, int K, const
     // CTA for the LOW class (two CTAs per SM already overlap its epilogues)
     const int gx = (Nc + TC_TN - 1) / TC_TN, gy = (M + TC_TM - 1) / TC_TM;
     const int64_t ntiles = (int64_t)gx * gy * batch;
+    if (ntiles <= 0) return TBG_OK;  // nothing to compute
+    if (K <= 0) return set_error(TBG_E_INVALID_ARGUMENT, "ozaki_zgemm_tc: empty contraction");
     const int64_t grid = tc_staged(S) ? std::min<int64_t>(ntiles, (int64_t)sm_count() * Class<S>::MIN_CTAS)
                                       : std::min<int64_t>(ntiles, 0x7fffffff);
     kern<<<(unsigned)grid, TC_THREADS, smem, st>>>(M, Nc, K, A, lda, sA, B, ldb, sB, EA, EB, C, ldc, sC, 0, err,
@@ -1021,6 +1023,8 @@ static int fourier_tc_launch(cudaStream_t st, int64_t M, int64_t Nc, int K, cons
     // persistent CTAs over (row tile, column tile), row tiles fastest
     const int gx = (int)((M + TC_TM - 1) / TC_TM), gy = (int)((Nc + TC_TN - 1) / TC_TN);
     const int64_t ntiles = (int64_t)gx * gy;
+    if (ntiles <= 0) return TBG_OK;
+    if (K <= 0) return set_error(TBG_E_INVALID_ARGUMENT, "ozaki_fourier_tc: empty contraction");
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * Class<S>::MIN_CTAS);
     kern<<<(unsigned)grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err,
                                                    0, nullptr, tc_wait_limit(), gx, gy, ntiles);
