@@ -616,7 +616,6 @@ int tbg_model_destroy(tbg_model* m) {
     cudaFree(M.tau_d);
     cudaFree(M.taucart_d);
     cudaFree(M.rmatrix);
-    cudaFree(M.box);
     cudaFree(M.hop_slices);
     cudaFree(M.hop_EB);
     cudaFree(M.hop_pair_d);

@@ -182,10 +182,6 @@ struct ModelDev {
     double* taucart_d = nullptr; // device (nsta, 3) Cartesian
     int64_t n_rmat = 0;
     zc* rmatrix = nullptr;       // device (n_rmat, dim, nsta, nsta)
-    // separable-mesh table: dense box copy of ham (built lazily)
-    int box_lo[3] = {0, 0, 0}, box_len[3] = {1, 1, 1};
-    zc* box = nullptr;           // device (L0, L1, L2, nsta, nsta)
-    bool box_ready = false;
     int device = 0;
     // digit planes of the hop table for the tensor-core Fourier sum (built lazily)
     void* hop_slices = nullptr;
