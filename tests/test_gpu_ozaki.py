@@ -146,3 +146,23 @@ def test_ozaki_tc_mid_precision(conj_a, M, Nc, K):
     err = (np.abs(C - ref) / scale).max()
     print(f"MID class {M}x{Nc}x{K}: {err:.2e}")
     assert err < 1e-10, err
+
+
+@pytest.mark.parametrize("conj_a", [False, True])
+def test_ozaki_tc_mid_many_tiles_long_contraction(conj_a):
+    """MID class, more tiles than SMs and a contraction of two exact chunks:
+    the persistent CTAs run several tiles each and the second chunk adds its
+    float pairs to the first chunk's output (bound 1e-10)."""
+    lib = _lib.load()
+    rng = np.random.default_rng(91 + conj_a)
+    batch, M, Nc, K = 120, 200, 130, 300
+    shapeA = (batch, K, M) if conj_a else (batch, M, K)
+    A = rng.standard_normal(shapeA) + 1j * rng.standard_normal(shapeA)
+    B = rng.standard_normal((batch, K, Nc)) + 1j * rng.standard_normal((batch, K, Nc))
+    B *= 10.0 ** rng.uniform(-3, 3, (batch, 1, Nc))
+    opA = np.conj(np.transpose(A, (0, 2, 1))) if conj_a else A
+    ref = opA @ B
+    C = ozaki(lib, A, B, conj_a, 2, 1)
+    scale = (np.abs(opA).max(axis=2)[:, :, None] * np.abs(B).max(axis=1)[:, None, :]) * K
+    err = (np.abs(C - ref) / scale).max()
+    assert err < 1e-10, err
