@@ -650,7 +650,8 @@ int ozaki_build_hop_slices_real(cudaStream_t st, int Kc, int64_t Nc, const zc* T
 int ozaki_build_hop_slices(cudaStream_t st, int K, int64_t Nc, const zc* ham, int* EB, void* Bs, const int* colmap,
                            int64_t ncols);
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
-                  const void* Bs, float4* C, int* err, int64_t high_rows);
+                  const void* Bs, float4* C, int* err, int64_t high_rows, void* aimg);
+size_t ozaki_fourier_img_bytes(int64_t M, int K);
 
 // Class of the velocity rows of the exact-slice Fourier sum: MID (five digits,
 // about 2^-35 of the row scale; the velocities only enter the rotation, which
@@ -668,10 +669,12 @@ bool fourier_mixed_ok(const ModelDev& m) { return m.nR <= ozaki_fourier_max_k();
 
 size_t fourier_mixed_scratch_bytes(const ModelDev& m, int64_t nk) {
     const size_t N = (size_t)m.nsta, nR = (size_t)m.nR;
-    // phases, orbital phases, exponents; the packed (upper-triangle) contraction output
+    // phases, orbital phases, exponents; the packed (upper-triangle) contraction
+    // output; the phases' stage images
     return (size_t)nk * (3 * (nR + 1) * sizeof(zc) + N * sizeof(zc) + 3 * sizeof(int) +
                          3 * (N * (N + 1) / 2) * sizeof(float4)) +
-           2 * nR * sizeof(double) + 2 * N * sizeof(double) + 2 * N * sizeof(float2) + 10 * 256;
+           ozaki_fourier_img_bytes(3 * nk, (int)nR + 1) + 2 * nR * sizeof(double) + 2 * N * sizeof(double) +
+           2 * N * sizeof(float2) + 11 * 256;
 }
 
 namespace {
@@ -895,6 +898,7 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     int* EA = static_cast<int*>(take(sizeof(int) * 3 * nk));
     int* err = static_cast<int*>(take(sizeof(int)));
     float4* Cpk = static_cast<float4*>(take(sizeof(float4) * 3 * nk * NP));
+    void* aimg = take(ozaki_fourier_img_bytes(3 * nk, m.hop_packed ? m.hop_K : nR));
     float4* Cg = m.hop_packed ? Cpk : C;
     {
         KTimer kt(st, "phases_kernel");
@@ -926,7 +930,7 @@ int fourier_mixed_gemm(ModelDev& m, cudaStream_t st, int64_t nk, const double* k
     if (rc) return rc;
     // rows [H | Vx | Vy] (nk each): H in the HIGH class, the velocities in MID
     rc = ozaki_fourier(st, 3 * nk, m.hop_packed ? NP : NN, m.hop_packed ? m.hop_K : nR, ph3, EA, m.hop_EB,
-                       m.hop_slices, Cg, err, fourier_v_mid() ? nk : -1);
+                       m.hop_slices, Cg, err, fourier_v_mid() ? nk : -1, aimg);
     if (rc) return rc;
     *Cg_out = Cg;
     *orbph_out = orbph;

@@ -427,7 +427,7 @@ int ozaki_exp_launch(cudaStream_t st, bool conj_a, int fmt_a, int fmt_b, int64_t
 }
 
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
-                     const void* Bs, float4* C, int* err, int64_t high_rows);
+                     const void* Bs, float4* C, int* err, int64_t high_rows, void* aimg);
 int ozaki_zgemm_tc_low(cudaStream_t st, int64_t batch, int M, int Nc, int K, const void* A, int64_t lda, int64_t sA,
                        const void* B, int64_t ldb, int64_t sB, float4* C, int64_t ldc, int64_t sC, int* EA, int* EB,
                        int* err, bool exps_ready = false);
@@ -544,11 +544,11 @@ int ozaki_build_hop_slices_real(cudaStream_t st, int Kc, int64_t Nc, const zc* T
 
 // C (M x Nc, float pairs) = A (M x K, complex double) . hop (digit planes).
 int ozaki_fourier(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, int* EA, const int* EB,
-                  const void* Bs, float4* C, int* err, int64_t high_rows) {
+                  const void* Bs, float4* C, int* err, int64_t high_rows, void* aimg) {
     if (K > ozaki_fourier_max_k()) return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier: nR > 408");
     row_exp_kernel<<<(unsigned)std::min<int64_t>((M * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(M, K, A, K, EA);
     TBG_LAUNCHED("row_exp_kernel");
-    if (ozaki_use_tc() && err) return ozaki_fourier_tc(st, M, Nc, K, A, EA, EB, Bs, C, err, high_rows);
+    if (ozaki_use_tc() && err && aimg) return ozaki_fourier_tc(st, M, Nc, K, A, EA, EB, Bs, C, err, high_rows, aimg);
     constexpr int SA = 6, SB = 6, LMAX = 5;
     const size_t smem = sizeof(__nv_bfloat16) * OZ_PAD * (SA * OZ_TM + SB * 2 * OZ_TN);
     auto kern = oz_gemm_kernel<SA, SB, LMAX, false, FMT_F64, FMT_PRESLICED>;

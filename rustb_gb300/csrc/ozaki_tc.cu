@@ -339,6 +339,11 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                  float4* __restrict__ C, int64_t ldc, int64_t sC, int rows_fast, int* __restrict__ err,
                  int accumulate, int* __restrict__ Ecol, int wait_limit, int gx, int gy, int64_t ntiles) {
     constexpr bool PRE = FMTB == FMT_PRESLICED;
+    // A pre-sliced too (stage images of S planes per row tile, the Fourier
+    // sum's phases): the copy thread brings both operands, the A warps only run
+    // the epilogue
+    constexpr bool PRE_A = FMTA == FMT_PRESLICED;
+    static_assert(!PRE_A || (PRE && !CONJ_A), "pre-sliced A goes with pre-sliced B, not conjugated");
     constexpr int LMAX = Class<S>::LMAX, NLEV = Class<S>::NLEV;
     constexpr int HS = S * PLANE;             // planes of one operand in a stage
     constexpr int SB = 2 * HS;                // stage bytes
@@ -400,7 +405,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     const int64_t gs = (int64_t)tn * nstages + it;
                     const int bi = (int)(gs & 1);
                     const uint32_t ph = (uint32_t)((gs >> 1) & 1);
-                    if (!mbar_wait(&bar_full[bi], ph, &abort_sh, wait_limit) ||
+                    if ((!PRE_A && !mbar_wait(&bar_full[bi], ph, &abort_sh, wait_limit)) ||
                         (PRE && !mbar_wait(&bar_bcopy[bi], ph, &abort_sh, wait_limit))) {
                         abort_sh = 1;
                         stop = true;
@@ -460,7 +465,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
             return CONJ_A ? (t.b * sA + gi) : (t.b * sA + (int64_t)gi * lda);
         };
         int4 nxt[8];
-        {
+        if constexpr (!PRE_A) {
             bool rv0;
             const int64_t i0 = row_base(blockIdx.x, rv0);
             if (blockIdx.x < ntiles)
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
             float s1, s2;
             f32_scales(E, s1, s2);
             const int64_t idx0 = CONJ_A ? (t.b * sA + gi) : (t.b * sA + (int64_t)gi * lda);
-            for (int it = 0; it < nstages; ++it) {
+            if constexpr (!PRE_A) for (int it = 0; it < nstages; ++it) {
                 const int64_t gs = (int64_t)tn * nstages + it;
                 const int bi = (int)(gs & 1);
                 int4 cur[8];
@@ -649,6 +654,9 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                     // stage images hold TC_S planes; a class with fewer digits copies the leading S
                     const unsigned char* src =
                         static_cast<const unsigned char*>(B) + (int64_t)t.ct * nstages * HALF_STAGE;
+                    // the A images of this row tile (S planes per stage)
+                    const unsigned char* srca =
+                        PRE_A ? static_cast<const unsigned char*>(A) + (int64_t)t.rt * nstages * HS : nullptr;
                     for (int it = 0; it < nstages; ++it) {
                         const int64_t gs = (int64_t)tn * nstages + it;
                         const int bi = (int)(gs & 1);
@@ -664,7 +672,8 @@ __global__ void __launch_bounds__(TC_THREADS, Class<S>::MIN_CTAS)
                             stop = true;
                             break;
                         }
-                        mbar_arrive_tx(&bar_bcopy[bi], HS);
+                        mbar_arrive_tx(&bar_bcopy[bi], PRE_A ? 2 * HS : HS);
+                        if (PRE_A) bulk_g2s(sbase + bi * SB, srca + (int64_t)it * HS, HS, &bar_bcopy[bi]);
                         bulk_g2s(sbase + bi * SB + HS, src + (int64_t)it * HALF_STAGE, HS, &bar_bcopy[bi]);
                         last[bi] = gs;
                     }
@@ -1006,6 +1015,44 @@ int ozaki_hop_image_real_launch(cudaStream_t st, int Kc, int64_t Nc, const zc* T
     return TBG_OK;
 }
 
+// Stage images of the phases (A operand of the Fourier contraction, M x K
+// FP64, row exponents EA): for row tile rt and stage it, the S digit planes
+// exactly as the A producers would store them in shared memory (S * PLANE
+// bytes at (rt * nstages + it) * S * PLANE).  One thread per (row, 8
+// consecutive k) of a stage, as the producers.
+template <int S>
+__global__ void phase_image_kernel(int64_t M, int K, const zc* __restrict__ A, const int* __restrict__ EA,
+                                   unsigned char* __restrict__ img) {
+    const int nst = (K + TC_TK - 1) / TC_TK;
+    const int64_t nrt = (M + TC_TM - 1) / TC_TM;
+    const int64_t total = nrt * nst * A_PRODUCERS;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(idx % A_PRODUCERS);
+        const int64_t blk = idx / A_PRODUCERS;  // rt * nst + it
+        const int it = (int)(blk % nst);
+        const int64_t rt = blk / nst;
+        const int r = q >> 1, g = q & 1;
+        const int64_t gi = rt * TC_TM + r;
+        const bool rv = gi < M;
+        const int E = rv ? EA[gi] : ZERO_EXP;
+        float s1, s2;
+        f32_scales(E, s1, s2);
+        const int kf = it * TC_TK + 8 * g;
+        int4 cur[8];
+        load8<FMT_F64>(A, gi * K + kf, 1, rv ? n_valid(K, kf) : 0, cur);
+        uint4 dre[S], dim[S];
+        item_planes<FMT_F64, 0, S>(cur, E, s1, s2, dre);
+        item_planes<FMT_F64, 1, S>(cur, E, s1, s2, dim);
+        unsigned char* dst = img + blk * (int64_t)(S * PLANE);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(r, 8 * g)) = dre[s];
+            *reinterpret_cast<uint4*>(dst + s * PLANE + plane_off(r, 16 + 8 * g)) = dim[s];
+        }
+    }
+}
+
 // Fourier contraction on tcgen05: C (M x Nc) = A (M x K FP64 phases) . hop
 // table (stage images); EA filled by the caller.  Rows [0, high_rows) use the
 // HIGH class, the rest the MID class (five of the images' six digit planes);
@@ -1013,9 +1060,18 @@ int ozaki_hop_image_real_launch(cudaStream_t st, int Kc, int64_t Nc, const zc* T
 // resident together share one column tile's images in L2.
 template <int S>
 static int fourier_tc_launch(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA,
-                             const int* EB, const void* img, float4* C, int* err) {
+                             const int* EB, const void* img, float4* C, int* err, unsigned char* aimg) {
     if (M <= 0) return TBG_OK;
-    auto kern = oz_tc_kernel<false, FMT_F64, FMT_PRESLICED, S>;
+    if (K <= 0) return set_error(TBG_E_INVALID_ARGUMENT, "ozaki_fourier_tc: empty contraction");
+    {
+        // the phases cut into stage images once, not once per column tile
+        const int64_t total = (M + TC_TM - 1) / TC_TM * ((K + TC_TK - 1) / TC_TK) * A_PRODUCERS;
+        KTimer kt(st, "phase_image_kernel");
+        phase_image_kernel<S><<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 64), 256, 0, st>>>(M, K, A, EA,
+                                                                                                        aimg);
+        TBG_LAUNCHED("phase_image_kernel");
+    }
+    auto kern = oz_tc_kernel<false, FMT_PRESLICED, FMT_PRESLICED, S>;
     const int smem = tc_smem_bytes(S);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(oz_tc fourier)");
@@ -1026,20 +1082,27 @@ static int fourier_tc_launch(cudaStream_t st, int64_t M, int64_t Nc, int K, cons
     if (ntiles <= 0) return TBG_OK;
     if (K <= 0) return set_error(TBG_E_INVALID_ARGUMENT, "ozaki_fourier_tc: empty contraction");
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * Class<S>::MIN_CTAS);
-    kern<<<(unsigned)grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, A, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1, err,
-                                                   0, nullptr, tc_wait_limit(), gx, gy, ntiles);
+    kern<<<(unsigned)grid, TC_THREADS, smem, st>>>((int)M, (int)Nc, K, aimg, K, 0, img, Nc, 0, EA, EB, C, Nc, 0, 1,
+                                                   err, 0, nullptr, tc_wait_limit(), gx, gy, ntiles);
     TBG_LAUNCHED(S == TC_S ? "ozaki_tc_fourier_kernel" : "ozaki_tc_fourier_kernel<mid>");
     return TBG_OK;
 }
 
+// Bytes of the phase images for up to M rows of a K-long contraction (either
+// class; the two row ranges of one contraction reuse the buffer in turn).
+size_t ozaki_fourier_img_bytes(int64_t M, int K) {
+    return (size_t)((M + TC_TM - 1) / TC_TM) * (size_t)((K + TC_TK - 1) / TC_TK) * HALF_STAGE;
+}
+
 int ozaki_fourier_tc(cudaStream_t st, int64_t M, int64_t Nc, int K, const zc* A, const int* EA, const int* EB,
-                     const void* img, float4* C, int* err, int64_t high_rows) {
+                     const void* img, float4* C, int* err, int64_t high_rows, void* aimg) {
     if ((Nc + TC_TN - 1) / TC_TN > 65535 || M > 0x7fffffff)
         return set_error(TBG_E_UNSUPPORTED, "ozaki_fourier_tc: grid too large");
     const int64_t mh = high_rows < 0 ? M : std::min<int64_t>(high_rows, M);
-    int rc = fourier_tc_launch<TC_S>(st, mh, Nc, K, A, EA, EB, img, C, err);
+    unsigned char* ai = static_cast<unsigned char*>(aimg);
+    int rc = fourier_tc_launch<TC_S>(st, mh, Nc, K, A, EA, EB, img, C, err, ai);
     if (rc) return rc;
-    return fourier_tc_launch<5>(st, M - mh, Nc, K, A + mh * K, EA + mh, EB, img, C + mh * Nc, err);
+    return fourier_tc_launch<5>(st, M - mh, Nc, K, A + mh * K, EA + mh, EB, img, C + mh * Nc, err, ai);
 }
 
 }  // namespace tbg
